@@ -1,0 +1,171 @@
+// Device view of a Layout (layout.h): raw pointers into one HBM-resident table
+// allocation plus scalar sizes, passed by value to every kernel.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace imsrg {
+
+struct DevLayout {
+  int N, A, P, JM, NJ, nblocks, ncc, n_ob, sj_nh;
+  int64_t off_fhh, off_fpp, off_fph, slab, n_unique, cc_size, wcc_size;
+  // per orbit
+  const int* jj;
+  const int* ll;
+  const int* tz;
+  const int* con;
+  const int* loc;
+  const int* holes;
+  const int* parts;
+  const int* same_start;
+  const int* same_count;
+  const int* same_list;
+  // sq_op channels
+  const int* lamJ;
+  const int* ncls;      // [q*3+c]
+  const int* pair_off;  // [q*3+c]
+  const int16_t* pair_a;
+  const int16_t* pair_b;
+  const int* pairpos;   // [(a*N+b)*NJ+J/2]
+  const int64_t* goff;  // [q*6+g]
+  const int* gn1;
+  const int* gn2;
+  const int64_t* uoff;  // [q*6+g], nblocks*6+1 entries
+  // cross-coupled
+  const int* cc_rlen;
+  const int* cc_nph;
+  const int* cc_J;
+  const int64_t* cc_off;   // ncc+1
+  const int64_t* wcc_off;  // ncc+1
+  const int* cc_row_off;
+  const int* cc_col_off;
+  const int16_t* cc_ra;
+  const int16_t* cc_rb;
+  const int16_t* cc_cp;
+  const int16_t* cc_ch;
+  const int* ccr;       // [(a*N+b)*NJ+JC/2]
+  // one-body output list
+  const int* ob_kind;
+  const int* ob_p;
+  const int* ob_q;
+  const int* ob_pk;
+  const int* ob_qk;
+  int n_ai;
+  const int* ai_a;
+  const int* ai_i;
+  // 6j
+  const int* sj_off;
+  const int* sj_j3min;
+  const int* sj_j6min;
+  const int* sj_n6;
+  const double* sj_val;
+};
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ bool d_tri(int a, int b, int J) { return J <= a + b && J >= abs(a - b); }
+__device__ __forceinline__ double d_sgn(int n) { return (n & 1) ? -1.0 : 1.0; }
+
+// 6j symbol {j1 j2 j3; j4 j5 j6} (j1,j2,j4,j5 odd, j3,j6 even; doubled units)
+__device__ __forceinline__ double d_sixj(const DevLayout& D, int j1, int j2, int j3, int j4, int j5, int j6) {
+  if (!(d_tri(j1, j2, j3) && d_tri(j4, j5, j3) && d_tri(j1, j5, j6) && d_tri(j4, j2, j6))) return 0.0;
+  const int nh = D.sj_nh;
+  const int k = (((j1 >> 1) * nh + (j2 >> 1)) * nh + (j4 >> 1)) * nh + (j5 >> 1);
+  return __ldg(D.sj_val + D.sj_off[k] + ((j3 - D.sj_j3min[k]) >> 1) * D.sj_n6[k] + ((j6 - D.sj_j6min[k]) >> 1));
+}
+
+// f_elem (src/basic_IMSRG.f90:1191-1221)
+__device__ __forceinline__ double d_f_elem(const DevLayout& D, const double* op, int herm, int a, int b) {
+  const int c1 = D.con[a], c2 = D.con[b];
+  if (c1 + c2 == 0) return op[D.off_fpp + D.loc[a] + (int64_t)D.loc[b] * D.P];
+  if (c1 + c2 == 2) return op[D.off_fhh + D.loc[a] + (int64_t)D.loc[b] * D.A];
+  if (c1 > c2) return op[D.off_fph + D.loc[b] + (int64_t)D.loc[a] * D.P] * herm;
+  return op[D.off_fph + D.loc[a] + (int64_t)D.loc[b] * D.P];
+}
+
+// Position of the element v_elem(a,b,c,d,J) would read (src/basic_IMSRG.f90:1314-1429):
+// returns false when the element vanishes by symmetry, otherwise the slab index, the
+// prefactor (swap phases, sqrt(2) for identical orbits) and whether herm applies.
+struct VRef {
+  int64_t idx;
+  double pre;
+  bool herm;
+};
+__device__ __forceinline__ bool d_vref(const DevLayout& D, int a, int b, int c, int d, int J, VRef& r) {
+  const int ja = D.jj[a], jb = D.jj[b], jc = D.jj[c], jd = D.jj[d];
+  if (!(d_tri(ja, jb, J) && d_tri(jc, jd, J))) return false;
+  const int P = (D.ll[a] + D.ll[b]) & 1;
+  if (((D.ll[c] + D.ll[d]) & 1) != P) return false;
+  const int tab = D.tz[a] + D.tz[b];
+  if (D.tz[c] + D.tz[d] != tab) return false;
+  const int q = 3 * J + (tab + 2) + P;  // block_index with 2*(Tz+1) = tab+2
+  const int C1 = D.con[a] + D.con[b], C2 = D.con[c] + D.con[d];
+  // (C1,C2) -> g : pp,pp 0 | pp,ph 1 | pp,hh 2 | ph,ph 3 | hh,hh 4 | ph,hh 5
+  const int lo = C1 < C2 ? C1 : C2, hi = C1 < C2 ? C2 : C1;
+  const int g = (lo == 0) ? hi : (lo == 1 ? (hi == 1 ? 3 : 5) : 4);
+  const int NJ = D.NJ, N = D.N;
+  double pre = 1.0;
+  int i1, i2;
+  if (a > b) {
+    i1 = D.pairpos[(b * N + a) * NJ + (J >> 1)];
+    pre = d_sgn(1 + ((ja + jb - J) >> 1));
+  } else {
+    if (a == b) pre = 1.4142135623730951;
+    i1 = D.pairpos[(a * N + b) * NJ + (J >> 1)];
+  }
+  if (c > d) {
+    i2 = D.pairpos[(d * N + c) * NJ + (J >> 1)];
+    pre *= d_sgn(1 + ((jc + jd - J) >> 1));
+  } else {
+    if (c == d) pre *= 1.4142135623730951;
+    i2 = D.pairpos[(c * N + d) * NJ + (J >> 1)];
+  }
+  const int k = q * 6 + g;
+  const int n1 = D.gn1[k];
+  if (C1 > C2) {
+    r.idx = D.goff[k] + i2 + (int64_t)i1 * n1;
+    r.herm = true;
+  } else {
+    r.idx = D.goff[k] + i1 + (int64_t)i2 * n1;
+    r.herm = false;
+  }
+  r.pre = pre;
+  return true;
+}
+
+__device__ __forceinline__ double d_v_elem(const DevLayout& D, const double* op, int herm, int a, int b, int c, int d,
+                                           int J) {
+  VRef r;
+  if (!d_vref(D, a, b, c, d, J, r)) return 0.0;
+  return op[r.idx] * (r.herm ? herm * r.pre : r.pre);
+}
+
+// (q, g, IX, JX) of unique 2b element u (upper triangle incl. diagonal for square arrays,
+// column-major order within each array).
+__device__ __forceinline__ void d_unique_decode(const DevLayout& D, int64_t u, int& q, int& g, int& IX, int& JX) {
+  int lo = 0, hi = D.nblocks * 6;  // find k with uoff[k] <= u < uoff[k+1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (D.uoff[mid] <= u) lo = mid; else hi = mid;
+  }
+  // skip empty arrays sharing the same start
+  while (D.uoff[lo + 1] <= u) ++lo;
+  q = lo / 6;
+  g = lo - q * 6;
+  const int64_t e = u - D.uoff[lo];
+  const int n1 = D.gn1[lo];
+  if (g == 0 || g == 3 || g == 4) {
+    // column JX holds JX+1 elements (IX = 0..JX)
+    int j = (int)((sqrt(8.0 * (double)e + 1.0) - 1.0) * 0.5);
+    while ((int64_t)(j + 1) * (j + 2) / 2 <= e) ++j;
+    while ((int64_t)j * (j + 1) / 2 > e) --j;
+    JX = j;
+    IX = (int)(e - (int64_t)j * (j + 1) / 2);
+  } else {
+    JX = (int)(e / n1);
+    IX = (int)(e - (int64_t)JX * n1);
+  }
+}
+
+#endif  // __CUDACC__
+
+}  // namespace imsrg

@@ -1,0 +1,90 @@
+// Engine state behind the opaque C-ABI handles.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/imsrg_gb300.h"
+#include "dev.cuh"
+#include "gemm.h"
+#include "layout.h"
+
+namespace imsrg {
+struct TcState;
+}
+
+struct Ctx {
+  imsrg::Layout L;
+  imsrg::DevLayout D{};
+  int device = 0;
+  int precision = IMSRG_PREC_FP64;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  void* d_tables = nullptr;
+  std::vector<imsrg::GemmProb> pphh_probs, wcc_probs;
+  std::vector<imsrg::GemmTile> pphh_tiles, wcc_tiles;
+  const imsrg::GemmProb* d_pphh_probs = nullptr;
+  const imsrg::GemmTile* d_pphh_tiles = nullptr;
+  const imsrg::GemmProb* d_wcc_probs = nullptr;
+  const imsrg::GemmTile* d_wcc_tiles = nullptr;
+  const int64_t* d_seg_start = nullptr;
+  const int* d_seg_len = nullptr;
+  const int8_t* d_seg_w = nullptr;
+  int nseg = 0;
+  double* d_partial = nullptr;
+  double* d_scalars = nullptr;
+  double* h_scalars = nullptr;
+  double* d_mono = nullptr;
+  // commutator workspaces (w1, w2: sq_op shaped; LCC/RCC: CCX; WCC: rlen x rlen blocks)
+  double *d_w1 = nullptr, *d_w2 = nullptr, *d_lcc = nullptr, *d_rcc = nullptr, *d_wcc = nullptr;
+  // Magnus / BCH intermediates
+  double *d_int1 = nullptr, *d_int2 = nullptr, *d_ad = nullptr;
+  imsrg::TcState* tc = nullptr;
+
+  ~Ctx();
+  imsrg_status fail(imsrg_status code, const std::string& msg);
+  imsrg_status cuda(cudaError_t e, const char* what);
+  imsrg_status launched(const char* what);
+  imsrg_status upload_tables();
+  imsrg_status ensure_workspace();
+  imsrg_status ensure_flow_workspace();
+
+  imsrg_status pandya(const double* op, int herm, double* cc);
+  imsrg_status e0(const double* L, int hL, const double* R, int hR, double* RES, double* out);
+  imsrg_status c111(const double* L, int hL, const double* R, int hR, double* RES);
+  imsrg_status c121(const double* L, int hL, const double* R, int hR, double* RES, int hRES);
+  imsrg_status c122(const double* L, int hL, const double* R, int hR, double* RES, int hRES);
+  imsrg_status pphh(const double* L, int hL, const double* R, int hR, double* RES, double* w1, double* w2);
+  imsrg_status c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2);
+  imsrg_status ph(const double* lcc, int hL, const double* rcc, int hR, double* RES, int hRES, double* wcc);
+  imsrg_status commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
+  imsrg_status axpby(const double* A, double ax, const double* B, double bx, double* C);
+  imsrg_status frob_async(const double* op, double scale, int slot);
+  imsrg_status read_scalars(int n);
+  imsrg_status white(const double* H, int hH, double* ETA);
+  imsrg_status magnus_expand(double* DG, int hDG, const double* G, int hG, int* used);
+  imsrg_status bch_expand(double* HS, const double* G, int hG, const double* H, int hH, int max_terms, double conv,
+                          int* terms);
+
+  // tensor-core (split-BF16, tcgen05) path, gemm_tc.cu
+  imsrg_status tc_prepare(int mode);
+  imsrg_status tc_pphh(const double* L, int hL, const double* R, int hR, double* w1, double* w2);
+  imsrg_status tc_wcc(const double* lcc, const double* rcc, double* wcc);
+  void tc_release();
+};
+
+struct imsrg_op {
+  double* d = nullptr;
+  int herm = 1;
+  Ctx* owner = nullptr;
+};
+
+struct imsrg_cc {
+  double* d = nullptr;
+  int64_t n = 0;
+  int kind = 0;
+  int herm = 1;
+  Ctx* owner = nullptr;
+};

@@ -1,0 +1,31 @@
+// Kernel declarations shared by the engine translation unit.
+#pragma once
+#include <cstdint>
+
+#include "dev.cuh"
+#include "gemm.h"
+
+namespace imsrg {
+
+__global__ void k_pandya(DevLayout D, const double* op, int herm, double* cc);
+__global__ void k_comm122(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
+__global__ void k_pphh_update(DevLayout D, double* RES, const double* w1, const double* w2, double pm);
+__global__ void k_comm222ph(DevLayout D, const double* WCC, int hL, int hR, double* RES, int hRES);
+__global__ void k_comm111(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_comm121(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
+__global__ void k_comm221(DevLayout D, int pm, double* RES, int hRES, const double* w1, const double* w2);
+__global__ void k_e0(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, double* out);
+
+__global__ void k_monopole(DevLayout D, const double* H, int hH, double* mono);
+__global__ void k_white_1b(DevLayout D, const double* H, int hH, double* ETA);
+__global__ void k_white_2b(DevLayout D, const double* H, int hH, const double* mono, double* ETA);
+__global__ void k_axpby(int64_t n, const double* A, double ax, const double* B, double bx, double* C);
+__global__ void k_frob_partial(const double* op, const int64_t* seg_start, const int* seg_len, const int8_t* seg_w,
+                               double* partial);
+__global__ void k_sum_sqrt(const double* partial, int n, double scale, double* out);
+__global__ void k_mbpt2_partial(DevLayout D, const double* H, int hH, double* partial);
+__global__ void k_sum(const double* partial, int n, double* out);
+
+__global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOperands ops);
+
+}  // namespace imsrg

@@ -1,0 +1,263 @@
+"""Python mirror of the reference's commutator interface, on the GB300 engine.
+
+Names, argument order and assign / accumulate semantics follow the Fortran routines
+(src/commutators.f90, src/cross_coupled.f90, src/generators.f90, src/IMSRG_MAGNUS.f90);
+every call goes through the C ABI of libimsrg_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .basis import Basis
+
+# reference default-real literal for the BCH / Magnus convergence tests
+CONV = float(np.float32(1e-6))
+
+
+class SqOp:
+    """A device-resident type(sq_op) (handle owned by an Engine)."""
+
+    def __init__(self, eng: "Engine", herm: int = 1):
+        self.eng = eng
+        h = C.c_void_p()
+        eng._ck(eng.L.imsrg_op_create(eng.h, int(herm), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.eng.L.imsrg_op_destroy(self.eng.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def herm(self) -> int:
+        v = C.c_int32()
+        self.eng._ck(self.eng.L.imsrg_op_get_herm(self.eng.h, self.h, C.byref(v)))
+        return v.value
+
+    @herm.setter
+    def herm(self, v: int):
+        self.eng._ck(self.eng.L.imsrg_op_set_herm(self.eng.h, self.h, int(v)))
+
+    def upload(self, slab: np.ndarray):
+        slab = np.ascontiguousarray(slab, dtype=np.float64)
+        if slab.size != self.eng.slab:
+            raise ValueError(f"slab has {slab.size} elements, layout needs {self.eng.slab}")
+        self.eng._ck(self.eng.L.imsrg_op_upload_slab(self.eng.h, self.h, slab.ctypes.data))
+        self.eng.synchronize()
+        return self
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.eng.slab, np.float64)
+        self.eng._ck(self.eng.L.imsrg_op_download_slab(self.eng.h, self.h, out.ctypes.data))
+        return out
+
+    def device_ptr(self) -> int:
+        p = C.c_void_p()
+        self.eng._ck(self.eng.L.imsrg_op_device_slab(self.eng.h, self.h, C.byref(p)))
+        return p.value
+
+    @property
+    def E0(self) -> float:
+        v = C.c_double()
+        self.eng._ck(self.eng.L.imsrg_op_get_e0(self.eng.h, self.h, C.byref(v)))
+        return v.value
+
+
+class CCMat:
+    """A device-resident type(cc_mat): kind 0 = CCX storage, kind 1 = WCC workspace."""
+
+    def __init__(self, eng: "Engine", kind: int = 0):
+        self.eng = eng
+        self.kind = kind
+        h = C.c_void_p()
+        eng._ck(eng.L.imsrg_cc_create(eng.h, int(kind), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.eng.L.imsrg_cc_destroy(self.eng.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def download(self) -> np.ndarray:
+        n = self.eng.wcc_size if self.kind else self.eng.cc_size
+        out = np.empty(n, np.float64)
+        if n:
+            self.eng._ck(self.eng.L.imsrg_cc_download(self.eng.h, self.h, out.ctypes.data))
+        return out
+
+
+class Engine:
+    """One basis (jbas + channel layout + 6j table) on one GPU."""
+
+    def __init__(self, basis: Basis, device: int = 0, precision: str = "fp64"):
+        self.L = _lib.load()
+        self.basis = basis
+        arrs = basis.arrays()
+        self._keep = arrs
+        P = C.POINTER(C.c_int32)
+        b = _lib.Basis_t(basis.norbits, *[a.ctypes.data_as(P) for a in arrs], basis.eMax, basis.lMax,
+                         float(basis.hw), basis.Aprot, basis.Aneut)
+        h = C.c_void_p()
+        st = self.L.imsrg_ctx_create(C.byref(b), int(device), C.byref(h))
+        if st != 0:
+            raise _lib.ImsrgError(st, "imsrg_ctx_create failed")
+        self.h = h
+        slab, cc, wcc = C.c_int64(), C.c_int64(), C.c_int64()
+        nb, ncc = C.c_int32(), C.c_int32()
+        self._ck(self.L.imsrg_ctx_sizes(self.h, C.byref(slab), C.byref(cc), C.byref(wcc), C.byref(nb), C.byref(ncc)))
+        self.slab, self.cc_size, self.wcc_size = slab.value, cc.value, wcc.value
+        self.nblocks, self.ncc = nb.value, ncc.value
+        self.precision = "fp64"
+        if precision != "fp64":
+            self.set_precision(precision)
+
+    def _ck(self, st: int):
+        if st != 0:
+            msg = self.L.imsrg_last_error(self.h)
+            raise _lib.ImsrgError(st, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.imsrg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- layout
+    def block_info(self):
+        arrs = [np.zeros(self.nblocks, np.int32) for _ in range(6)]
+        P = C.POINTER(C.c_int32)
+        self._ck(self.L.imsrg_block_info(self.h, *[a.ctypes.data_as(P) for a in arrs]))
+        return dict(zip(("lamJ", "lamP", "lamT", "npp", "nph", "nhh"), arrs))
+
+    def block_pairs(self, q: int, cls: int) -> np.ndarray:
+        info = self.block_info()
+        n = int((info["npp"], info["nph"], info["nhh"])[cls][q])
+        out = np.zeros(2 * max(n, 1), np.int32)
+        self._ck(self.L.imsrg_block_pairs(self.h, q, cls, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out[: 2 * n].reshape(n, 2)
+
+    def cc_info(self):
+        arrs = [np.zeros(self.ncc, np.int32) for _ in range(3)]
+        P = C.POINTER(C.c_int32)
+        self._ck(self.L.imsrg_cc_info(self.h, *[a.ctypes.data_as(P) for a in arrs]))
+        return dict(zip(("rlen", "nph", "J"), arrs))
+
+    def set_precision(self, mode: str):
+        self._ck(self.L.imsrg_set_precision(self.h, _lib.PREC[mode]))
+        self.precision = mode
+
+    def synchronize(self):
+        self._ck(self.L.imsrg_synchronize(self.h))
+
+    # ---------------------------------------------------------------- objects
+    def new_op(self, herm: int = 1, slab: np.ndarray | None = None) -> SqOp:
+        op = SqOp(self, herm)
+        if slab is not None:
+            op.upload(slab)
+        return op
+
+    def new_cc(self, kind: int = 0) -> CCMat:
+        return CCMat(self, kind)
+
+    def synthetic_hamiltonian(self, seed: int = 1, v_scale: float = 1.0) -> np.ndarray:
+        out = np.zeros(self.slab, np.float64)
+        self._ck(self.L.imsrg_synthetic_hamiltonian(self.h, C.c_uint64(seed), float(v_scale), out.ctypes.data))
+        return out
+
+    # ---------------------------------------------------------------- algebra
+    def copy_sq_op(self, H: SqOp, op: SqOp):
+        self._ck(self.L.imsrg_copy_sq_op(self.h, H.h, op.h))
+
+    def clear_sq_op(self, op: SqOp):
+        self._ck(self.L.imsrg_clear_sq_op(self.h, op.h))
+
+    def add_sq_op(self, A: SqOp, ax: float, B: SqOp, bx: float, Cop: SqOp):
+        self._ck(self.L.imsrg_add_sq_op(self.h, A.h, float(ax), B.h, float(bx), Cop.h))
+
+    def scale_sq_op(self, A: SqOp, ax: float):
+        self._ck(self.L.imsrg_scale_sq_op(self.h, A.h, float(ax)))
+
+    def mat_frob_norm(self, op: SqOp) -> float:
+        v = C.c_double()
+        self._ck(self.L.imsrg_mat_frob_norm(self.h, op.h, C.byref(v)))
+        return v.value
+
+    def mbpt2(self, H: SqOp) -> float:
+        v = C.c_double()
+        self._ck(self.L.imsrg_mbpt2(self.h, H.h, C.byref(v)))
+        return v.value
+
+    # ---------------------------------------------------------------- commutator pieces
+    def calculate_cross_coupled(self, HS: SqOp, CCME: CCMat):
+        self._ck(self.L.imsrg_calculate_cross_coupled(self.h, HS.h, CCME.h))
+
+    def commutator_110(self, L: SqOp, R: SqOp) -> float:
+        v = C.c_double()
+        self._ck(self.L.imsrg_commutator_110(self.h, L.h, R.h, C.byref(v)))
+        return v.value
+
+    def commutator_220(self, L: SqOp, R: SqOp) -> float:
+        v = C.c_double()
+        self._ck(self.L.imsrg_commutator_220(self.h, L.h, R.h, C.byref(v)))
+        return v.value
+
+    def commutator_111(self, L: SqOp, R: SqOp, RES: SqOp):
+        self._ck(self.L.imsrg_commutator_111(self.h, L.h, R.h, RES.h))
+
+    def commutator_121(self, L: SqOp, R: SqOp, RES: SqOp):
+        self._ck(self.L.imsrg_commutator_121(self.h, L.h, R.h, RES.h))
+
+    def commutator_122(self, L: SqOp, R: SqOp, RES: SqOp):
+        self._ck(self.L.imsrg_commutator_122(self.h, L.h, R.h, RES.h))
+
+    def commutator_222_pp_hh(self, L: SqOp, R: SqOp, RES: SqOp, w1: SqOp, w2: SqOp):
+        self._ck(self.L.imsrg_commutator_222_pp_hh(self.h, L.h, R.h, RES.h, w1.h, w2.h))
+
+    def commutator_221(self, L: SqOp, R: SqOp, RES: SqOp, w1: SqOp, w2: SqOp):
+        self._ck(self.L.imsrg_commutator_221(self.h, L.h, R.h, RES.h, w1.h, w2.h))
+
+    def commutator_222_ph(self, LCC: CCMat, RCC: CCMat, RES: SqOp, WCC: CCMat):
+        self._ck(self.L.imsrg_commutator_222_ph(self.h, LCC.h, RCC.h, RES.h, WCC.h))
+
+    def commutator(self, L: SqOp, R: SqOp, RES: SqOp, e0: bool = True):
+        self._ck(self.L.imsrg_commutator(self.h, L.h, R.h, RES.h, _lib.COMM_E0 if e0 else 0))
+
+    # ---------------------------------------------------------------- generator / flow
+    def build_gs_white(self, H: SqOp, ETA: SqOp):
+        self._ck(self.L.imsrg_build_gs_white(self.h, H.h, ETA.h))
+
+    def magnus_expand(self, DG: SqOp, G: SqOp) -> int:
+        n = C.c_int32()
+        self._ck(self.L.imsrg_magnus_expand(self.h, DG.h, G.h, C.byref(n)))
+        return n.value
+
+    def euler_step(self, G: SqOp, DG: SqOp, s: float, stp: float) -> float:
+        sv = C.c_double(s)
+        self._ck(self.L.imsrg_euler_step(self.h, G.h, DG.h, C.byref(sv), float(stp)))
+        return sv.value
+
+    def bch_expand(self, HS: SqOp, G: SqOp, H: SqOp, max_terms: int = 40, conv: float = CONV) -> int:
+        n = C.c_int32()
+        self._ck(self.L.imsrg_bch_expand(self.h, HS.h, G.h, H.h, int(max_terms), float(conv), C.byref(n)))
+        return n.value

@@ -1,0 +1,164 @@
+/*
+ * imsrg_gb300.h -- C ABI of the GB300 IMSRG(2) commutator engine.
+ *
+ * Drop-in for the hot path of EOM-IMSRG: the two-body-truncated commutator
+ * (src/commutators.f90, src/cross_coupled.f90), the White generator
+ * (src/generators.f90) and the Magnus / BCH loop (src/IMSRG_MAGNUS.f90).
+ * Each entry point below names the Fortran routine it replaces.
+ *
+ * Conventions
+ *  - Every function returns an imsrg_status (0 = IMSRG_OK); none aborts the process.
+ *    imsrg_last_error() describes the last failure on a context.
+ *  - Operators live in device memory, owned by the library.  Their content is the
+ *    reference's type(sq_op) flattened as the "sq_op slab" (FP64, column-major,
+ *    full square storage):
+ *        [E0][fhh A*A][fpp P*P][fph P*A][for q=1..nblocks, g=1..6: gam(g) of block q]
+ *    with gam(1..6) = pppp, ppph, pphh, phph, hhhh, phhh.  Block q, its pair lists
+ *    and the pair order are those of allocate_blocks (src/basic_IMSRG.f90:521-685).
+ *  - Orbit indices in this header are 0-based (Fortran index - 1).
+ *  - All work on one context is ordered on that context's CUDA stream; calls that
+ *    return host values synchronize it.  A context is thread-compatible, not
+ *    thread-safe: serialize calls on one context.
+ */
+#ifndef IMSRG_GB300_H
+#define IMSRG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t imsrg_status;
+#define IMSRG_OK 0
+#define IMSRG_ERR_INVALID_ARGUMENT 1
+#define IMSRG_ERR_CUDA 2
+#define IMSRG_ERR_OUT_OF_MEMORY 3
+#define IMSRG_ERR_NOT_CONVERGED 4
+#define IMSRG_ERR_MISMATCH 5
+#define IMSRG_ERR_UNSUPPORTED 6
+
+/* arithmetic of the channel contractions (pp/hh ladders and cross-coupled GEMM) */
+#define IMSRG_PREC_FP64 0    /* plain FP64 (DFMA) */
+#define IMSRG_PREC_BF16X3 1  /* 2-slice split-BF16 operands, 3 products, FP32 accumulate (tcgen05) */
+#define IMSRG_PREC_BF16X6 2  /* 3-slice split-BF16 operands, 6 products, FP32 accumulate (tcgen05) */
+
+/* flags of imsrg_commutator */
+#define IMSRG_COMM_E0 1      /* also assign RES%E0 = commutator_110 + commutator_220 */
+
+typedef struct imsrg_ctx imsrg_ctx;
+typedef struct imsrg_op imsrg_op;
+typedef struct imsrg_cc imsrg_cc;
+
+/* The fields of type(spd) the engine needs (src/basic_IMSRG.f90:25-37). */
+typedef struct imsrg_basis {
+  int32_t norbits;
+  const int32_t* nn;
+  const int32_t* ll;
+  const int32_t* jj;   /* 2j */
+  const int32_t* itzp; /* 2tz */
+  const int32_t* con;  /* 1 hole, 0 particle */
+  int32_t eMax, lMax;
+  double hw;
+  int32_t Aprot, Aneut;
+} imsrg_basis;
+
+/* ---- context: basis, channel layout, index maps, 6j table (read_sp_basis + store_6j +
+ *      allocate_blocks + allocate_CCMAT, src/basic_IMSRG.f90:192-382, 521-685, 2227-2332;
+ *      src/cross_coupled.f90:61-177).  device < 0 makes a host-only context that answers
+ *      the layout queries and imsrg_synthetic_hamiltonian without touching a GPU; every
+ *      other call on it returns IMSRG_ERR_UNSUPPORTED. */
+imsrg_status imsrg_ctx_create(const imsrg_basis* basis, int32_t device, imsrg_ctx** out);
+imsrg_status imsrg_ctx_destroy(imsrg_ctx* ctx);
+const char* imsrg_last_error(const imsrg_ctx* ctx);
+imsrg_status imsrg_ctx_sizes(const imsrg_ctx* ctx, int64_t* slab, int64_t* cc, int64_t* wcc, int32_t* nblocks,
+                             int32_t* ncc);
+/* per block: 2J, parity, Tz, npp, nph, nhh (sq_block%lam, %npp, %nph, %nhh) */
+imsrg_status imsrg_block_info(const imsrg_ctx* ctx, int32_t* lamJ, int32_t* lamP, int32_t* lamT, int32_t* npp,
+                              int32_t* nph, int32_t* nhh);
+/* pair list qn(cls+1)%Y of block q as 0-based orbit pairs out[2k], out[2k+1] */
+imsrg_status imsrg_block_pairs(const imsrg_ctx* ctx, int32_t q, int32_t cls, int32_t* out);
+/* per cross-coupled block: rlen, nph, 2J (cc_mat%rlen, %nph, %Jval) */
+imsrg_status imsrg_cc_info(const imsrg_ctx* ctx, int32_t* rlen, int32_t* nph, int32_t* J);
+imsrg_status imsrg_set_precision(imsrg_ctx* ctx, int32_t mode);
+imsrg_status imsrg_synchronize(imsrg_ctx* ctx);
+
+/* ---- operators: allocate_blocks / duplicate_sq_op (src/basic_IMSRG.f90:521, 2797) */
+imsrg_status imsrg_op_create(imsrg_ctx* ctx, int32_t herm, imsrg_op** out);
+imsrg_status imsrg_op_destroy(imsrg_ctx* ctx, imsrg_op* op);
+imsrg_status imsrg_op_set_herm(imsrg_ctx* ctx, imsrg_op* op, int32_t herm);
+imsrg_status imsrg_op_get_herm(imsrg_ctx* ctx, const imsrg_op* op, int32_t* herm);
+/* Per-array transfer: gam[q*6+g] points at the contiguous column-major array
+ * op%mat(q+1)%gam(g+1)%X (c_loc in Fortran); NULL is allowed for empty arrays. */
+imsrg_status imsrg_op_upload(imsrg_ctx* ctx, imsrg_op* op, const double* const* gam, const double* fhh,
+                             const double* fph, const double* fpp, double E0);
+imsrg_status imsrg_op_download(imsrg_ctx* ctx, const imsrg_op* op, double* const* gam, double* fhh, double* fph,
+                               double* fpp, double* E0);
+/* whole-slab transfer from / to host memory (pinned memory gives full bandwidth) */
+imsrg_status imsrg_op_upload_slab(imsrg_ctx* ctx, imsrg_op* op, const double* host_slab);
+imsrg_status imsrg_op_download_slab(imsrg_ctx* ctx, const imsrg_op* op, double* host_slab);
+/* device-resident slab (for device-to-device interop, e.g. torch tensors) */
+imsrg_status imsrg_op_device_slab(imsrg_ctx* ctx, imsrg_op* op, double** dev_slab);
+imsrg_status imsrg_op_get_e0(imsrg_ctx* ctx, const imsrg_op* op, double* E0);
+imsrg_status imsrg_pinned_alloc(int64_t bytes, void** host_ptr);
+imsrg_status imsrg_pinned_free(void* host_ptr);
+
+/* ---- operator algebra (src/basic_IMSRG.f90) */
+imsrg_status imsrg_copy_sq_op(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* op);                       /* :3005 */
+imsrg_status imsrg_clear_sq_op(imsrg_ctx* ctx, imsrg_op* C);                                          /* :3638 */
+imsrg_status imsrg_add_sq_op(imsrg_ctx* ctx, const imsrg_op* A, double ax, const imsrg_op* B, double bx,
+                             imsrg_op* C);                                                            /* :3551 */
+imsrg_status imsrg_scale_sq_op(imsrg_ctx* ctx, imsrg_op* A, double ax);                               /* :3610 */
+imsrg_status imsrg_mat_frob_norm(imsrg_ctx* ctx, const imsrg_op* op, double* out);                    /* :4056 */
+imsrg_status imsrg_mbpt2(imsrg_ctx* ctx, const imsrg_op* H, double* out);                             /* :4165 */
+
+/* ---- cross-coupled matrices: type(cc_mat) (src/cross_coupled.f90:11-15)
+ * kind 0 = CCX storage (rlen x nph per block, init_ph_mat), kind 1 = WCC workspace
+ * (rlen x rlen per block, init_ph_wkspc / allocate_CC_wkspc :1075-1096) */
+imsrg_status imsrg_cc_create(imsrg_ctx* ctx, int32_t kind, imsrg_cc** out);
+imsrg_status imsrg_cc_destroy(imsrg_ctx* ctx, imsrg_cc* cc);
+imsrg_status imsrg_cc_download(imsrg_ctx* ctx, const imsrg_cc* cc, double* host);
+/* calculate_cross_coupled(HS, CCME, jbas)  src/cross_coupled.f90:1190 */
+imsrg_status imsrg_calculate_cross_coupled(imsrg_ctx* ctx, const imsrg_op* HS, imsrg_cc* CCME);
+
+/* ---- commutator pieces, src/commutators.f90 (same argument meaning and
+ *      assign / accumulate semantics as the Fortran) */
+imsrg_status imsrg_commutator_110(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, double* out);  /* :10  */
+imsrg_status imsrg_commutator_111(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES); /* :36 */
+imsrg_status imsrg_commutator_121(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES); /* :83 */
+imsrg_status imsrg_commutator_122(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES); /* :283 */
+imsrg_status imsrg_commutator_220(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, double* out);  /* :399 */
+imsrg_status imsrg_commutator_221(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES,
+                                  const imsrg_op* w1, const imsrg_op* w2);                            /* :435 */
+imsrg_status imsrg_commutator_222_pp_hh(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES,
+                                        imsrg_op* w1, imsrg_op* w2);                                  /* :581 */
+imsrg_status imsrg_commutator_222_ph(imsrg_ctx* ctx, const imsrg_cc* LCC, const imsrg_cc* RCC, imsrg_op* RES,
+                                     imsrg_cc* WCC);                                                  /* :771 */
+/* The whole two-body-truncated [L,R] in the order of src/IMSRG_MAGNUS.f90:207-219:
+ * both Pandya transforms, (110+220 when IMSRG_COMM_E0), 111, 121, 122, 222_pp_hh,
+ * 221, 222_ph.  Uses the context's workspaces and its precision mode. */
+imsrg_status imsrg_commutator(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES, int32_t flags);
+
+/* ---- generator and flow (src/generators.f90, src/IMSRG_MAGNUS.f90) */
+imsrg_status imsrg_build_gs_white(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* ETA);   /* generators.f90:4 */
+/* MAGNUS_EXPAND(DG, G, AD, jbas) :620 -- DG holds eta on entry and dOmega on exit */
+imsrg_status imsrg_magnus_expand(imsrg_ctx* ctx, imsrg_op* DG, const imsrg_op* G, int32_t* commutators_used);
+/* euler_step(G, DG, s, stp) :754 -- G += stp*DG; *s += stp */
+imsrg_status imsrg_euler_step(imsrg_ctx* ctx, imsrg_op* G, const imsrg_op* DG, double* s, double stp);
+/* BCH_EXPAND(HS, G, H, jbas, quads) :149 -- HS = e^G H e^-G; stops when a term's norm
+ * times its coefficient drops below conv, or returns IMSRG_ERR_NOT_CONVERGED after
+ * max_terms (the reference STOPs after 40). */
+imsrg_status imsrg_bch_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H, int32_t max_terms,
+                              double conv, int32_t* terms_used);
+
+/* ---- input preparation (host, FP64): seeded synthetic Hamiltonian in the reference's
+ * me2j -> pn J-scheme layout (read_me2j_interaction, src/interaction_IO.f90:282-557) plus the
+ * harmonic-oscillator kinetic energy (calculate_h0_harm_osc, src/basic_IMSRG.f90:2093-2191),
+ * normal ordered w.r.t. the reference state (normal_order, src/basic_IMSRG.f90:2419-2550).
+ * Writes one host slab (herm = +1). */
+imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* host_slab);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMSRG_GB300_H */

@@ -1,0 +1,223 @@
+"""ctypes binding of the CPU oracle (oracle/oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the checker
+and by bench.py's cpu_baseline leg.  The product never imports this module.
+
+Operators are numpy float64 "slabs" in the sq_op flattening described at the top of
+oracle.cpp, paired with their hermiticity flag.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    L = C.CDLL(LIB_PATH)
+    vp, i, d, i64, u64 = C.c_void_p, C.c_int, C.c_double, C.c_int64, C.c_uint64
+    sig = {
+        "orc_basis_create": (vp, [i, _ip, _ip, _ip, _ip, _ip, i, d, i, i]),
+        "orc_basis_destroy": (None, [vp]),
+        "orc_slab_size": (i64, [vp]),
+        "orc_nblocks": (i, [vp]),
+        "orc_ncc": (i, [vp]),
+        "orc_cc_size": (i64, [vp]),
+        "orc_wcc_size": (i64, [vp]),
+        "orc_block_info": (None, [vp, _ip, _ip, _ip, _ip, _ip, _ip]),
+        "orc_block_pairs": (None, [vp, i, i, _ip]),
+        "orc_cc_info": (None, [vp, _ip, _ip, _ip]),
+        "orc_set_num_threads": (None, [i]),
+        "orc_get_max_threads": (i, []),
+        "orc_set_dgemm": (None, [vp, i]),
+        "orc_sixj": (d, [i] * 6),
+        "orc_ninej": (d, [i] * 9),
+        "orc_v_elem": (d, [vp, _dp, i, i, i, i, i, i]),
+        "orc_f_elem": (d, [vp, _dp, i, i, i]),
+        "orc_random_op": (None, [vp, u64, i, _dp]),
+        "orc_commutator_110": (d, [vp, _dp, i, _dp, i]),
+        "orc_commutator_220": (d, [vp, _dp, i, _dp, i]),
+        "orc_commutator_111": (None, [vp, _dp, i, _dp, i, _dp, i]),
+        "orc_commutator_121": (None, [vp, _dp, i, _dp, i, _dp, i]),
+        "orc_commutator_122": (None, [vp, _dp, i, _dp, i, _dp, i]),
+        "orc_commutator_222_pp_hh": (None, [vp, _dp, i, _dp, i, _dp, i, _dp, _dp]),
+        "orc_commutator_221": (None, [vp, _dp, i, _dp, i, _dp, i, _dp, _dp]),
+        "orc_calculate_cross_coupled": (None, [vp, _dp, i, _dp]),
+        "orc_commutator_222_ph": (None, [vp, _dp, i, _dp, i, _dp, i, _dp]),
+        "orc_full_commutator": (None, [vp, _dp, i, _dp, i, _dp, i]),
+        "orc_build_gs_white": (None, [vp, _dp, i, _dp]),
+        "orc_mat_frob_norm": (d, [vp, _dp]),
+        "orc_mbpt2": (d, [vp, _dp, i]),
+        "orc_add_sq_op": (None, [vp, _dp, d, _dp, d, _dp]),
+        "orc_magnus_expand": (i, [vp, _dp, _dp]),
+        "orc_bch_expand": (i, [vp, _dp, _dp, _dp, i, d]),
+        "orc_bf_0body": (d, [vp, _dp, i, _dp, i]),
+        "orc_bf_1body": (d, [vp, _dp, i, _dp, i, i, i]),
+        "orc_bf_2body": (d, [vp, _dp, i, _dp, i, i, i, i, i, i]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_num_threads(int(n))
+
+
+def use_blas_dgemm(addr: int, ilp64: bool) -> None:
+    lib().orc_set_dgemm(C.c_void_p(addr), 1 if ilp64 else 0)
+
+
+# reference default-real literal 1e-6 (src/IMSRG_MAGNUS.f90:152)
+BCH_CONV = float(np.float32(1e-6))
+
+
+class Oracle:
+    """One basis (the reference's jbas + channel layout) on the CPU."""
+
+    def __init__(self, basis):
+        self.basis = basis
+        L = lib()
+        nn, ll, jj, tz, con = basis.arrays()
+        self._keep = (nn, ll, jj, tz, con)
+        self.h = L.orc_basis_create(nn.size, nn, ll, jj, tz, con, basis.eMax, basis.hw,
+                                    basis.Aprot, basis.Aneut)
+        self.L = L
+        self.slab = int(L.orc_slab_size(self.h))
+        self.nblocks = int(L.orc_nblocks(self.h))
+        self.ncc = int(L.orc_ncc(self.h))
+        self.cc_size = int(L.orc_cc_size(self.h))
+        self.wcc_size = int(L.orc_wcc_size(self.h))
+
+    def __del__(self):
+        try:
+            self.L.orc_basis_destroy(self.h)
+        except Exception:
+            pass
+
+    # layout -------------------------------------------------------------
+    def block_info(self):
+        n = self.nblocks
+        arrs = [np.zeros(n, np.int32) for _ in range(6)]
+        self.L.orc_block_info(self.h, *arrs)
+        return dict(zip(("lamJ", "lamP", "lamT", "npp", "nph", "nhh"), arrs))
+
+    def block_pairs(self, q: int, cls: int) -> np.ndarray:
+        info = self.block_info()
+        n = int((info["npp"], info["nph"], info["nhh"])[cls][q])
+        out = np.zeros(2 * n, np.int32)
+        if n:
+            self.L.orc_block_pairs(self.h, q, cls, out)
+        return out.reshape(n, 2)
+
+    def cc_info(self):
+        arrs = [np.zeros(self.ncc, np.int32) for _ in range(3)]
+        self.L.orc_cc_info(self.h, *arrs)
+        return dict(zip(("rlen", "nph", "J"), arrs))
+
+    def new(self) -> np.ndarray:
+        return np.zeros(self.slab, np.float64)
+
+    def random(self, seed: int, herm: int) -> np.ndarray:
+        x = self.new()
+        self.L.orc_random_op(self.h, seed, herm, x)
+        return x
+
+    # pieces ---------------------------------------------------------------
+    def v_elem(self, op, herm, a, b, c, d, J):
+        return self.L.orc_v_elem(self.h, op, herm, a, b, c, d, J)
+
+    def f_elem(self, op, herm, a, b):
+        return self.L.orc_f_elem(self.h, op, herm, a, b)
+
+    def commutator_110(self, L, hL, R, hR):
+        return self.L.orc_commutator_110(self.h, L, hL, R, hR)
+
+    def commutator_220(self, L, hL, R, hR):
+        return self.L.orc_commutator_220(self.h, L, hL, R, hR)
+
+    def commutator_111(self, L, hL, R, hR, RES, hRES):
+        self.L.orc_commutator_111(self.h, L, hL, R, hR, RES, hRES)
+
+    def commutator_121(self, L, hL, R, hR, RES, hRES):
+        self.L.orc_commutator_121(self.h, L, hL, R, hR, RES, hRES)
+
+    def commutator_122(self, L, hL, R, hR, RES, hRES):
+        self.L.orc_commutator_122(self.h, L, hL, R, hR, RES, hRES)
+
+    def commutator_222_pp_hh(self, L, hL, R, hR, RES, hRES, w1, w2):
+        self.L.orc_commutator_222_pp_hh(self.h, L, hL, R, hR, RES, hRES, w1, w2)
+
+    def commutator_221(self, L, hL, R, hR, RES, hRES, w1, w2):
+        self.L.orc_commutator_221(self.h, L, hL, R, hR, RES, hRES, w1, w2)
+
+    def calculate_cross_coupled(self, op, herm):
+        cc = np.zeros(self.cc_size, np.float64)
+        self.L.orc_calculate_cross_coupled(self.h, op, herm, cc)
+        return cc
+
+    def commutator_222_ph(self, LCC, hL, RCC, hR, RES, hRES, WCC=None):
+        if WCC is None:
+            WCC = np.zeros(self.wcc_size, np.float64)
+        self.L.orc_commutator_222_ph(self.h, LCC, hL, RCC, hR, RES, hRES, WCC)
+        return WCC
+
+    def commutator(self, L, hL, R, hR, hRES=None):
+        """Full [L,R] in the reference's order; E0 assigned."""
+        if hRES is None:
+            hRES = -hL * hR
+        RES = self.new()
+        self.L.orc_full_commutator(self.h, L, hL, R, hR, RES, hRES)
+        return RES
+
+    def white(self, H, hH=1):
+        ETA = self.new()
+        self.L.orc_build_gs_white(self.h, H, hH, ETA)
+        return ETA
+
+    def frob(self, op):
+        return self.L.orc_mat_frob_norm(self.h, op)
+
+    def mbpt2(self, H, hH=1):
+        return self.L.orc_mbpt2(self.h, H, hH)
+
+    def magnus_expand(self, DG, G):
+        """In place: DG (eta on entry) becomes dOmega.  Returns commutators used."""
+        return self.L.orc_magnus_expand(self.h, DG, G)
+
+    def bch_expand(self, G, H, max_terms=40, conv=BCH_CONV):
+        HS = self.new()
+        n = self.L.orc_bch_expand(self.h, HS, G, H, max_terms, conv)
+        return HS, n
+
+    # brute force ---------------------------------------------------------
+    def bf_0body(self, A, hA, B, hB):
+        return self.L.orc_bf_0body(self.h, A, hA, B, hB)
+
+    def bf_1body(self, A, hA, B, hB, a, b):
+        return self.L.orc_bf_1body(self.h, A, hA, B, hB, a, b)
+
+    def bf_2body(self, A, hA, B, hB, a, b, c, d, J):
+        return self.L.orc_bf_2body(self.h, A, hA, B, hB, a, b, c, d, J)
