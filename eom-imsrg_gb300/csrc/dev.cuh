@@ -59,6 +59,7 @@ struct DevLayout {
   const int* sj_j6min;
   const int* sj_n6;
   const double* sj_val;
+  const float* sj_valf;
 };
 
 #if defined(__CUDACC__)

@@ -92,6 +92,8 @@ imsrg_status Ctx::upload_tables() {
   pk.add(l.ai_a, &d.ai_a); pk.add(l.ai_i, &d.ai_i);
   pk.add(l.sj_off, &d.sj_off); pk.add(l.sj_j3min, &d.sj_j3min); pk.add(l.sj_j6min, &d.sj_j6min);
   pk.add(l.sj_n6, &d.sj_n6); pk.add(l.sj_val, &d.sj_val);
+  std::vector<float> sjf(l.sj_val.begin(), l.sj_val.end());
+  pk.add(sjf, &d.sj_valf);
   // GEMM plans
   pphh_probs = build_pphh_problems(l.nblocks, l.ncls, l.goff);
   pphh_tiles = build_tiles(pphh_probs, 64, 64);
@@ -216,9 +218,9 @@ imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, 
 }
 
 imsrg_status Ctx::ph(const double* lcc, int hL, const double* rcc, int hR, double* RES, int hRES, double* wcc) {
-  if (precision != IMSRG_PREC_FP64) {
-    CK(tc_wcc(lcc, rcc, wcc));
-  } else if (!wcc_tiles.empty()) {
+  // the piecewise entry point keeps the reference's FP64 WCC; the mixed-precision full
+  // commutator (tc_commutator) uses the fused split-BF16 path instead
+  if (!wcc_tiles.empty()) {
     GemmOperands ops{};
     ops.in[kOpLCC] = lcc; ops.in[kOpRCC] = rcc;
     ops.out[kOpWCC] = wcc;
@@ -233,6 +235,7 @@ imsrg_status Ctx::ph(const double* lcc, int hL, const double* rcc, int hR, doubl
 
 imsrg_status Ctx::commutator(const double* Lp, int hL, const double* Rp, int hR, double* RES, int hRES, bool with_e0) {
   CK(ensure_workspace());
+  if (precision != IMSRG_PREC_FP64) return tc_commutator(Lp, hL, Rp, hR, RES, hRES, with_e0);
   CK(pandya(Rp, hR, d_rcc));
   CK(pandya(Lp, hL, d_lcc));
   if (with_e0) CK(e0(Lp, hL, Rp, hR, RES, nullptr));
@@ -469,7 +472,8 @@ imsrg_status imsrg_set_precision(imsrg_ctx* ctx, int32_t mode) {
 
 imsrg_status imsrg_synchronize(imsrg_ctx* ctx) {
   CTX(ctx);
-  return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  CK(c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"));
+  return c->tc_error();
 }
 
 imsrg_status imsrg_op_create(imsrg_ctx* ctx, int32_t herm, imsrg_op** out) {

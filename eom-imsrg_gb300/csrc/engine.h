@@ -9,6 +9,7 @@
 #include "dev.cuh"
 #include "gemm.h"
 #include "layout.h"
+#include "tc.h"
 
 namespace imsrg {
 struct TcState;
@@ -72,8 +73,18 @@ struct Ctx {
   imsrg_status tc_prepare(int mode);
   imsrg_status tc_pphh(const double* L, int hL, const double* R, int hR, double* w1, double* w2);
   imsrg_status tc_wcc(const double* lcc, const double* rcc, double* wcc);
+  imsrg_status tc_gemm(const imsrg::TcProb* probs, const imsrg::TcTile* tiles, int ntiles, imsrg::TcOut out, int hL,
+                       int hR);
+  imsrg_status tc_error();
+  imsrg_status tc_commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
   void tc_release();
 };
+
+#define CK_TC(expr)              \
+  do {                           \
+    imsrg_status _s = (expr);    \
+    if (_s != IMSRG_OK) return _s; \
+  } while (0)
 
 struct imsrg_op {
   double* d = nullptr;

@@ -1,5 +1,7 @@
 // Kernel declarations shared by the engine translation unit.
 #pragma once
+#include <cuda_bf16.h>
+
 #include <cstdint>
 
 #include "dev.cuh"
@@ -27,5 +29,11 @@ __global__ void k_mbpt2_partial(DevLayout D, const double* H, int hH, double* pa
 __global__ void k_sum(const double* partial, int n, double* out);
 
 __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOperands ops);
+
+// mixed-precision companions (kernels_mixed.cu)
+void launch_pandya_tc(int S, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
+                      __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* nkb);
+__global__ void k_comm122f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
+__global__ void k_comm222ph_z(DevLayout D, const float* Z, double* RES, int hRES);
 
 }  // namespace imsrg

@@ -1,0 +1,40 @@
+// Plans of the tensor-core (split-BF16 tcgen05) path.
+#pragma once
+#include <cstdint>
+
+namespace imsrg {
+
+// term sign: bit 0 times herm(L), bit 1 times herm(R), bit 2 negative
+enum TcSign : int { kSignHL = 1, kSignHR = 2, kSignNeg = 4 };
+
+// one FP64 array whose columns become K-major rows of the split operand buffer
+struct TcSplitOp {
+  int64_t src_off;
+  int src;       // 0 = L, 1 = R
+  int rows, K;   // rows = columns of the stored array, K = its leading dimension
+  int nkb;       // K blocks of 64
+  int tile_base;
+};
+
+struct TcTermDesc {
+  int a_tile, b_tile;  // first tile of the A / B operand (row block 0, K block 0)
+  int sign;            // TcSign
+};
+
+struct TcProb {
+  int64_t c_off;
+  int M, N, nkb, nterm;
+  int out_f32, c_id, ldc, pad;
+  TcTermDesc t[2];
+};
+
+struct TcTile {
+  int prob, m0, n0, pad;
+};
+
+struct TcOut {
+  double* f64[8];
+  float* f32;
+};
+
+}  // namespace imsrg
