@@ -38,7 +38,24 @@ imsrg_status Ctx::cuda(cudaError_t e, const char* what) {
   err = std::string(what) + ": " + cudaGetErrorString(e);
   return e == cudaErrorMemoryAllocation ? IMSRG_ERR_OUT_OF_MEMORY : IMSRG_ERR_CUDA;
 }
-imsrg_status Ctx::launched(const char* what) { return cuda(cudaGetLastError(), what); }
+imsrg_status Ctx::launched(const char* what) {
+  ++launches;
+  return cuda(cudaGetLastError(), what);
+}
+
+// Records the end of a phase on the stream when per-phase timing is enabled.
+void Ctx::mark(int phase) {
+  if (!prof) return;
+  cudaEvent_t e;
+  if (!prof_pool.empty()) {
+    e = prof_pool.back();
+    prof_pool.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    return;
+  }
+  cudaEventRecord(e, stream);
+  prof_marks.push_back({phase, e});
+}
 
 #define CK(expr)                                 \
   do {                                           \
@@ -159,6 +176,10 @@ Ctx::~Ctx() {
                   (void*)d_lcc, (void*)d_rcc, (void*)d_wcc, (void*)d_int1, (void*)d_int2, (void*)d_ad})
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
+  for (auto& m : prof_marks) cudaEventDestroy(m.second);
+  for (auto e : prof_pool) cudaEventDestroy(e);
+  if (ev_begin) cudaEventDestroy(ev_begin);
+  if (ev_end) cudaEventDestroy(ev_end);
   tc_release();
   if (stream) cudaStreamDestroy(stream);
 }
@@ -207,8 +228,11 @@ imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, doubl
     k_gemm_fp64<<<(int)pphh_tiles.size(), 256, 0, stream>>>(d_pphh_probs, d_pphh_tiles, ops);
     CK(launched("k_gemm_fp64(pphh)"));
   }
+  mark(kPhasePphhGemm);
   k_pphh_update<<<grid_for(L.slab - L.goff[0]), kThreads, 0, stream>>>(D, RES, w1, w2, (double)(hL * hR));
-  return launched("k_pphh_update");
+  CK(launched("k_pphh_update"));
+  mark(kPhasePphhUpdate);
+  return IMSRG_OK;
 }
 
 imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2) {
@@ -228,22 +252,30 @@ imsrg_status Ctx::ph(const double* lcc, int hL, const double* rcc, int hR, doubl
     k_gemm_fp64<<<(int)wcc_tiles.size(), 256, 0, stream>>>(d_wcc_probs, d_wcc_tiles, ops);
     CK(launched("k_gemm_fp64(wcc)"));
   }
+  mark(kPhasePhGemm);
   if (L.n_unique == 0) return IMSRG_OK;
   k_comm222ph<<<grid_for(L.n_unique), kThreads, 0, stream>>>(D, wcc, hL, hR, RES, hRES);
-  return launched("k_comm222ph");
+  CK(launched("k_comm222ph"));
+  mark(kPhaseRecouple);
+  return IMSRG_OK;
 }
 
 imsrg_status Ctx::commutator(const double* Lp, int hL, const double* Rp, int hR, double* RES, int hRES, bool with_e0) {
   CK(ensure_workspace());
   if (precision != IMSRG_PREC_FP64) return tc_commutator(Lp, hL, Rp, hR, RES, hRES, with_e0);
+  mark(kPhaseStart);
   CK(pandya(Rp, hR, d_rcc));
   CK(pandya(Lp, hL, d_lcc));
+  mark(kPhasePandya);
   if (with_e0) CK(e0(Lp, hL, Rp, hR, RES, nullptr));
   CK(c111(Lp, hL, Rp, hR, RES));
   CK(c121(Lp, hL, Rp, hR, RES, hRES));
+  mark(kPhaseOneBody);
   CK(c122(Lp, hL, Rp, hR, RES, hRES));
+  mark(kPhase122);
   CK(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2));
   CK(c221(hL, hR, RES, hRES, d_w1, d_w2));
+  mark(kPhase221);
   CK(ph(d_lcc, hL, d_rcc, hR, RES, hRES, d_wcc));
   return IMSRG_OK;
 }
@@ -474,6 +506,55 @@ imsrg_status imsrg_synchronize(imsrg_ctx* ctx) {
   CTX(ctx);
   CK(c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"));
   return c->tc_error();
+}
+
+imsrg_status imsrg_launch_count(imsrg_ctx* ctx, int64_t* count) {
+  if (!ctx || !count) return IMSRG_ERR_INVALID_ARGUMENT;
+  *count = reinterpret_cast<Ctx*>(ctx)->launches;
+  return IMSRG_OK;
+}
+
+imsrg_status imsrg_timer_begin(imsrg_ctx* ctx) {
+  CTX(ctx);
+  if (!c->ev_begin) CK(c->cuda(cudaEventCreate(&c->ev_begin), "cudaEventCreate"));
+  if (!c->ev_end) CK(c->cuda(cudaEventCreate(&c->ev_end), "cudaEventCreate"));
+  return c->cuda(cudaEventRecord(c->ev_begin, c->stream), "cudaEventRecord");
+}
+
+imsrg_status imsrg_timer_end(imsrg_ctx* ctx, float* ms) {
+  CTX(ctx);
+  if (!ms || !c->ev_begin) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_timer_begin was not called");
+  CK(c->cuda(cudaEventRecord(c->ev_end, c->stream), "cudaEventRecord"));
+  CK(c->cuda(cudaEventSynchronize(c->ev_end), "cudaEventSynchronize"));
+  return c->cuda(cudaEventElapsedTime(ms, c->ev_begin, c->ev_end), "cudaEventElapsedTime");
+}
+
+imsrg_status imsrg_profile_phases(imsrg_ctx* ctx, int32_t enable) {
+  CTX(ctx);
+  CK(c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"));
+  for (auto& m : c->prof_marks) c->prof_pool.push_back(m.second);
+  c->prof_marks.clear();
+  c->prof = enable != 0;
+  return IMSRG_OK;
+}
+
+imsrg_status imsrg_profile_read(imsrg_ctx* ctx, float* ms_per_phase, int32_t* count_per_phase) {
+  CTX(ctx);
+  if (!ms_per_phase || !count_per_phase) return IMSRG_ERR_INVALID_ARGUMENT;
+  CK(c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"));
+  for (int p = 0; p < IMSRG_NUM_PHASES; ++p) {
+    ms_per_phase[p] = 0.f;
+    count_per_phase[p] = 0;
+  }
+  for (size_t i = 1; i < c->prof_marks.size(); ++i) {
+    const int p = c->prof_marks[i].first;
+    if (p == kPhaseStart || p < 0 || p >= IMSRG_NUM_PHASES) continue;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->prof_marks[i - 1].second, c->prof_marks[i].second);
+    ms_per_phase[p] += ms;
+    count_per_phase[p] += 1;
+  }
+  return IMSRG_OK;
 }
 
 imsrg_status imsrg_op_create(imsrg_ctx* ctx, int32_t herm, imsrg_op** out) {

@@ -15,6 +15,21 @@ namespace imsrg {
 struct TcState;
 }
 
+// phases of one commutator for per-phase event timing (imsrg_profile_read)
+enum Phase : int {
+  kPhaseStart = 0,
+  kPhasePandya = 1,
+  kPhaseOneBody = 2,
+  kPhase122 = 3,
+  kPhasePphhSplit = 4,
+  kPhasePphhGemm = 5,
+  kPhasePphhSmall = 6,
+  kPhasePphhUpdate = 7,
+  kPhase221 = 8,
+  kPhasePhGemm = 9,
+  kPhaseRecouple = 10,
+};
+
 struct Ctx {
   imsrg::Layout L;
   imsrg::DevLayout D{};
@@ -43,6 +58,13 @@ struct Ctx {
   // Magnus / BCH intermediates
   double *d_int1 = nullptr, *d_int2 = nullptr, *d_ad = nullptr;
   imsrg::TcState* tc = nullptr;
+  // kernel launches issued (cumulative) and optional per-phase CUDA-event timing
+  int64_t launches = 0;
+  bool prof = false;
+  std::vector<std::pair<int, cudaEvent_t>> prof_marks;
+  std::vector<cudaEvent_t> prof_pool;
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  void mark(int phase);
 
   ~Ctx();
   imsrg_status fail(imsrg_status code, const std::string& msg);

@@ -666,10 +666,12 @@ imsrg_status Ctx::tc_pphh(const double* Lp, int hL, const double* Rp, int hR, do
       k_split_cols<3><<<grid, 256, 0, stream>>>(tc->d_split_ops, tc->d_split_prefix, nops, Lp, Rp, tc->buf, tc->slice_elems);
     CK_TC(launched("k_split_cols"));
   }
+  mark(kPhasePphhSplit);
   TcOut out{};
   out.f64[kOpW1] = w1;
   out.f64[kOpW2] = w2;
   CK_TC(tc_gemm(tc->d_pphh_probs, tc->d_pphh_tiles, (int)tc->pphh_tiles.size(), out, hL, hR));
+  mark(kPhasePphhGemm);
   if (!tc->small_tiles.empty()) {
     GemmOperands ops{};
     ops.in[kOpL] = Lp; ops.in[kOpR] = Rp;
@@ -678,6 +680,7 @@ imsrg_status Ctx::tc_pphh(const double* Lp, int hL, const double* Rp, int hR, do
     k_gemm_f32<<<(int)tc->small_tiles.size(), 256, 0, stream>>>(tc->d_small_probs, tc->d_small_tiles, ops);
     CK_TC(launched("k_gemm_f32"));
   }
+  mark(kPhasePphhSmall);
   return IMSRG_OK;
 }
 
@@ -702,29 +705,36 @@ imsrg_status Ctx::tc_wcc(const double*, const double*, double*) {
 imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int hR, double* RES, int hRES,
                                 bool with_e0) {
   const int64_t ncc = L.cc_size;
+  mark(kPhaseStart);
   if (ncc) {
     const int grid = (int)std::min<int64_t>((ncc + 255) / 256, 152 * 16);
     launch_pandya_tc(tc->S, grid, stream, D, Rp, hR, tc->buf, tc->slice_elems, tc->d_cc_tile_R, tc->d_cc_nkb);
     launch_pandya_tc(tc->S, grid, stream, D, Lp, hL, tc->buf, tc->slice_elems, tc->d_cc_tile_L, tc->d_cc_nkb);
     CK_TC(launched("k_pandya_tc"));
   }
+  mark(kPhasePandya);
   if (with_e0) CK_TC(e0(Lp, hL, Rp, hR, RES, nullptr));
   CK_TC(c111(Lp, hL, Rp, hR, RES));
   CK_TC(c121(Lp, hL, Rp, hR, RES, hRES));
+  mark(kPhaseOneBody);
   if (L.n_unique) {
     const int grid = (int)std::min<int64_t>((L.n_unique + 255) / 256, 152 * 16);
     k_comm122f<<<grid, 256, 0, stream>>>(D, Lp, hL, Rp, hR, RES, hRES);
     CK_TC(launched("k_comm122f"));
   }
+  mark(kPhase122);
   CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2));
   CK_TC(c221(hL, hR, RES, hRES, d_w1, d_w2));
+  mark(kPhase221);
   TcOut zo{};
   zo.f32 = tc->zbuf;
   CK_TC(tc_gemm(tc->d_z_probs, tc->d_z_tiles, (int)tc->z_tiles.size(), zo, hL, hR));
+  mark(kPhasePhGemm);
   if (L.n_unique) {
     const int grid = (int)std::min<int64_t>((L.n_unique + 255) / 256, 152 * 16);
     k_comm222ph_z<<<grid, 256, 0, stream>>>(D, tc->zbuf, RES, hRES);
     CK_TC(launched("k_comm222ph_z"));
   }
+  mark(kPhaseRecouple);
   return IMSRG_OK;
 }

@@ -81,7 +81,14 @@ SIGNATURES = {
     "imsrg_euler_step": [_vp, _vp, _vp, _pd, _d],
     "imsrg_bch_expand": [_vp, _vp, _vp, _vp, _i32, _d, _pi32],
     "imsrg_synthetic_hamiltonian": [_vp, _u64, _d, _vp],
+    "imsrg_launch_count": [_vp, _pi64],
+    "imsrg_timer_begin": [_vp],
+    "imsrg_timer_end": [_vp, C.POINTER(C.c_float)],
+    "imsrg_profile_phases": [_vp, _i32],
+    "imsrg_profile_read": [_vp, C.POINTER(C.c_float), _pi32],
 }
+PHASES = ["start", "pandya", "one_body", "c122", "pphh_split", "pphh_gemm", "pphh_small", "pphh_update", "c221",
+          "ph_gemm", "recouple"]
 
 _lib = None
 

@@ -170,6 +170,31 @@ class Engine:
     def synchronize(self):
         self._ck(self.L.imsrg_synchronize(self.h))
 
+    # ---------------------------------------------------------------- instrumentation
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        self._ck(self.L.imsrg_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def timer_begin(self):
+        self._ck(self.L.imsrg_timer_begin(self.h))
+
+    def timer_end(self) -> float:
+        """Elapsed ms on the context's stream since timer_begin (synchronizes)."""
+        v = C.c_float()
+        self._ck(self.L.imsrg_timer_end(self.h, C.byref(v)))
+        return v.value
+
+    def profile_phases(self, enable: bool):
+        self._ck(self.L.imsrg_profile_phases(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        n = len(_lib.PHASES)
+        ms = (C.c_float * n)()
+        cnt = (C.c_int32 * n)()
+        self._ck(self.L.imsrg_profile_read(self.h, ms, cnt))
+        return {name: (ms[i], cnt[i]) for i, name in enumerate(_lib.PHASES) if i > 0}
+
     # ---------------------------------------------------------------- objects
     def new_op(self, herm: int = 1, slab: np.ndarray | None = None) -> SqOp:
         op = SqOp(self, herm)

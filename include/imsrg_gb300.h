@@ -83,6 +83,20 @@ imsrg_status imsrg_cc_info(const imsrg_ctx* ctx, int32_t* rlen, int32_t* nph, in
 imsrg_status imsrg_set_precision(imsrg_ctx* ctx, int32_t mode);
 imsrg_status imsrg_synchronize(imsrg_ctx* ctx);
 
+/* ---- instrumentation (no reference counterpart: the reference only prints wall time,
+ *      print_time, src/basic_IMSRG.f90:152-169) */
+/* kernel launches issued on this context so far */
+imsrg_status imsrg_launch_count(imsrg_ctx* ctx, int64_t* count);
+/* CUDA-event timer on the context's stream: begin, then end returns elapsed ms */
+imsrg_status imsrg_timer_begin(imsrg_ctx* ctx);
+imsrg_status imsrg_timer_end(imsrg_ctx* ctx, float* ms);
+/* per-phase event timing of imsrg_commutator; phases: 1 Pandya, 2 one-body (110/220,
+ * 111, 121), 3 122, 4 ladder operand split, 5 ladder GEMM, 6 small-K ladder GEMM,
+ * 7 ladder accumulation, 8 221, 9 cross-coupled GEMM, 10 6j recoupling */
+#define IMSRG_NUM_PHASES 11
+imsrg_status imsrg_profile_phases(imsrg_ctx* ctx, int32_t enable);
+imsrg_status imsrg_profile_read(imsrg_ctx* ctx, float* ms_per_phase, int32_t* count_per_phase);
+
 /* ---- operators: allocate_blocks / duplicate_sq_op (src/basic_IMSRG.f90:521, 2797) */
 imsrg_status imsrg_op_create(imsrg_ctx* ctx, int32_t herm, imsrg_op** out);
 imsrg_status imsrg_op_destroy(imsrg_ctx* ctx, imsrg_op* op);
