@@ -133,6 +133,80 @@ __device__ __forceinline__ bool d_vref(const DevLayout& D, int a, int b, int c, 
   return true;
 }
 
+// FP32 flavour of d_vref: the same element position with a float prefactor, so the
+// FP32 kernels issue no FP64 instruction (GB300 runs FP64 at ~1/64 of the FP32 rate).
+struct VRefF {
+  int64_t idx;
+  float pre;  // swap phases and sqrt(2) factors
+  bool tr;    // element read from the transposed storage: multiply by the operator's herm
+  __device__ __forceinline__ float scale(int herm) const { return (tr && herm < 0) ? -pre : pre; }
+};
+__device__ __forceinline__ bool d_vref_f(const DevLayout& D, int a, int b, int c, int d, int J, VRefF& r) {
+  const int ja = D.jj[a], jb = D.jj[b], jc = D.jj[c], jd = D.jj[d];
+  if (!(d_tri(ja, jb, J) && d_tri(jc, jd, J))) return false;
+  const int P = (D.ll[a] + D.ll[b]) & 1;
+  if (((D.ll[c] + D.ll[d]) & 1) != P) return false;
+  const int tab = D.tz[a] + D.tz[b];
+  if (D.tz[c] + D.tz[d] != tab) return false;
+  const int q = 3 * J + (tab + 2) + P;
+  const int C1 = D.con[a] + D.con[b], C2 = D.con[c] + D.con[d];
+  const int lo = C1 < C2 ? C1 : C2, hi = C1 < C2 ? C2 : C1;
+  const int g = (lo == 0) ? hi : (lo == 1 ? (hi == 1 ? 3 : 5) : 4);
+  const int NJ = D.NJ, N = D.N;
+  int neg = 0, nsq = 0;
+  int i1, i2;
+  if (a > b) {
+    i1 = D.pairpos[(b * N + a) * NJ + (J >> 1)];
+    neg ^= (1 + ((ja + jb - J) >> 1)) & 1;
+  } else {
+    nsq += (a == b);
+    i1 = D.pairpos[(a * N + b) * NJ + (J >> 1)];
+  }
+  if (c > d) {
+    i2 = D.pairpos[(d * N + c) * NJ + (J >> 1)];
+    neg ^= (1 + ((jc + jd - J) >> 1)) & 1;
+  } else {
+    nsq += (c == d);
+    i2 = D.pairpos[(c * N + d) * NJ + (J >> 1)];
+  }
+  const int k = q * 6 + g;
+  const int n1 = D.gn1[k];
+  if (C1 > C2) {
+    r.idx = D.goff[k] + i2 + (int64_t)i1 * n1;
+    r.tr = true;
+  } else {
+    r.idx = D.goff[k] + i1 + (int64_t)i2 * n1;
+    r.tr = false;
+  }
+  const float m = nsq == 0 ? 1.0f : (nsq == 1 ? 1.41421356f : 2.0f);
+  r.pre = neg ? -m : m;
+  return true;
+}
+
+// FP64 -> FP32 by truncation with integer instructions only (no FP64 pipe); values below
+// FP32's normal range flush to zero.  The discarded bits are below FP32 precision, which
+// is the precision the mixed kernels work in.
+__device__ __forceinline__ float f64_to_f32(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e < 1023 - 126) return 0.0f;
+  const unsigned int sign = (unsigned int)(b >> 63) << 31;
+  const unsigned int fe = (unsigned int)(e - 1023 + 127);
+  const unsigned int mant = (unsigned int)((b >> 29) & 0x7FFFFF);
+  return __uint_as_float(sign | (fe << 23) | mant);
+}
+
+__device__ __forceinline__ float d_f_elem_f(const DevLayout& D, const double* op, int herm, int a, int b) {
+  const int c1 = D.con[a], c2 = D.con[b];
+  if (c1 + c2 == 0) return f64_to_f32(op[D.off_fpp + D.loc[a] + (int64_t)D.loc[b] * D.P]);
+  if (c1 + c2 == 2) return f64_to_f32(op[D.off_fhh + D.loc[a] + (int64_t)D.loc[b] * D.A]);
+  if (c1 > c2) {
+    const float v = f64_to_f32(op[D.off_fph + D.loc[b] + (int64_t)D.loc[a] * D.P]);
+    return herm < 0 ? -v : v;
+  }
+  return f64_to_f32(op[D.off_fph + D.loc[a] + (int64_t)D.loc[b] * D.P]);
+}
+
 __device__ __forceinline__ double d_v_elem(const DevLayout& D, const double* op, int herm, int a, int b, int c, int d,
                                            int J) {
   VRef r;

@@ -19,6 +19,7 @@
 #include <cstring>
 #include <vector>
 
+#include "dev.cuh"
 #include "engine.h"
 #include "kernels.h"
 #include "tc.h"
@@ -336,14 +337,46 @@ __global__ void k_split_cols(const TcSplitOp* __restrict__ ops, const int64_t* _
     const TcSplitOp& o = ops[lo];
     const int64_t loc = e - prefix[lo];
     const int r = (int)(loc / o.K), k = (int)(loc - (int64_t)r * o.K);
-    const double x = (o.src == 0 ? L : R)[o.src_off + k + (int64_t)r * o.K];
+    const float x = f64_to_f32((o.src == 0 ? L : R)[o.src_off + k + (int64_t)r * o.K]);
     const int64_t dst = ((int64_t)(o.tile_base + (r / BM) * o.nkb + k / BK) * BM + (r % BM)) * BK + (k % BK);
-    double rem = x;
+    float rem = x;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      const __nv_bfloat16 h = __double2bfloat16(rem);
+      const __nv_bfloat16 h = __float2bfloat16_rn(rem);
       buf[s * slice_elems + dst] = h;
-      rem -= (double)__bfloat162float(h);
+      rem -= __bfloat162float(h);
+    }
+  }
+}
+
+// Chunked split: one block per run of rows of one operand, each thread converts 8
+// consecutive k of one row and writes 16-byte bf16 vectors into every slice.
+template <int S>
+__global__ void __launch_bounds__(256) k_split_chunks(const TcSplitOp* __restrict__ ops,
+                                                      const SplitChunk* __restrict__ chunks,
+                                                      const double* __restrict__ L, const double* __restrict__ R,
+                                                      __nv_bfloat16* __restrict__ buf, int64_t slice_elems) {
+  const SplitChunk ch = chunks[blockIdx.x];
+  const TcSplitOp o = ops[ch.op];
+  const double* src = (o.src == 0 ? L : R) + o.src_off;
+  const int nvec = (o.K + 7) >> 3;
+  const int total = (ch.r1 - ch.r0) * nvec;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int r = ch.r0 + t / nvec;
+    const int k0 = (t - (r - ch.r0) * nvec) << 3;
+    float x[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) x[u] = (k0 + u < o.K) ? f64_to_f32(src[k0 + u + (int64_t)r * o.K]) : 0.0f;
+    const int64_t dst = ((int64_t)(o.tile_base + (r / BM) * o.nkb + k0 / BK) * BM + (r % BM)) * BK + (k0 % BK);
+#pragma unroll
+    for (int sl = 0; sl < S; ++sl) {
+      __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        h[u] = __float2bfloat16_rn(x[u]);
+        x[u] -= __bfloat162float(h[u]);
+      }
+      *reinterpret_cast<uint4*>(buf + sl * slice_elems + dst) = *reinterpret_cast<const uint4*>(h);
     }
   }
 }
@@ -447,6 +480,17 @@ struct TcState {
   const int* d_cc_nkb = nullptr;
   float* zbuf = nullptr;
   int* d_err = nullptr;
+  // orbit quadruples (i<=j, k<=l) of the particle-hole recoupling, j fastest
+  std::vector<uint64_t> quads;
+  const uint64_t* d_quads = nullptr;
+  std::vector<SplitChunk> chunks;
+  const SplitChunk* d_chunks = nullptr;
+  // commutator_122 neighbour lists, indexed by the global pair-list index
+  std::vector<int> nb_start;
+  std::vector<NbEntry> nb;
+  const int* d_nb_start = nullptr;
+  const NbEntry* d_nb = nullptr;
+  float* d_ft = nullptr;
   int num_sms = 148;
 };
 
@@ -491,6 +535,7 @@ void Ctx::tc_release() {
   if (tc->d_mem) cudaFree(tc->d_mem);
   if (tc->zbuf) cudaFree(tc->zbuf);
   if (tc->d_err) cudaFree(tc->d_err);
+  if (tc->d_ft) cudaFree(tc->d_ft);
   delete tc;
   tc = nullptr;
 }
@@ -528,6 +573,11 @@ imsrg_status Ctx::tc_prepare(int mode) {
         tiles += ceil_div(cols, BM) * o.nkb;
         tc->split_ops.push_back(o);
       }
+  }
+  for (int op = 0; op < (int)tc->split_ops.size(); ++op) {
+    const TcSplitOp& o = tc->split_ops[op];
+    const int rows_per = std::max(1, 4096 / std::max(o.K, 1));
+    for (int r0 = 0; r0 < o.rows; r0 += rows_per) tc->chunks.push_back(SplitChunk{op, r0, std::min(o.rows, r0 + rows_per)});
   }
   tc->split_prefix.push_back(0);
   for (auto& o : tc->split_ops) tc->split_prefix.push_back(tc->split_prefix.back() + (int64_t)o.rows * o.K);
@@ -593,6 +643,68 @@ imsrg_status Ctx::tc_prepare(int mode) {
   }
   tc->z_tiles = make_tiles(tc->z_probs);
   tc->total_tiles = tiles;
+  if (l.JM + 1 > 26) return fail(IMSRG_ERR_UNSUPPORTED, "mixed recoupling supports 2j <= 25 (eMax <= 12)");
+  // ---- commutator_122 neighbour lists (one list per channel pair, a-side then b-side)
+  {
+    const int N = l.N, NJ = l.NJ;
+    const int npairs = l.pair_off[l.nblocks * 3];
+    tc->nb_start.assign(npairs + 1, 0);
+    for (int q = 0; q < l.nblocks; ++q) {
+      const int J = l.lamJ[q];
+      for (int c = 0; c < 3; ++c)
+        for (int p = 0; p < l.ncls[q][c]; ++p) {
+          const int o = l.pair_off[q * 3 + c] + p;
+          const int a = l.pair_a[o], b = l.pair_b[o];
+          tc->nb_start[o] = (int)tc->nb.size();
+          for (int side = 0; side < 2; ++side) {
+            const int x = side == 0 ? a : b, other = side == 0 ? b : a;
+            for (int t = 0; t < l.same_count[x]; ++t) {
+              const int i = l.same_list[l.same_start[x] + t];
+              // replaced pair: side 0 -> (i, b), side 1 -> (a, i)
+              const int first = side == 0 ? i : other, second = side == 0 ? other : i;
+              const int u = std::min(first, second), v = std::max(first, second);
+              NbEntry e{};
+              e.pos = (int16_t)l.pairpos[((size_t)u * N + v) * NJ + J / 2];
+              e.cls = (int8_t)(l.con[u] + l.con[v]);
+              int flags = side;
+              if (first > second && ((1 + (l.jj[first] + l.jj[second] - J) / 2) & 1)) flags |= 2;
+              if (first == second) flags |= 4;
+              e.flags = (int8_t)flags;
+              e.fkey = (int16_t)(l.same_start[x] + t);
+              if (e.pos < 0) return fail(IMSRG_ERR_MISMATCH, "122 neighbour outside its channel");
+              tc->nb.push_back(e);
+            }
+          }
+        }
+    }
+    tc->nb_start[npairs] = (int)tc->nb.size();
+  }
+  // ---- recoupling quadruples: bra (i<=j) of class c1, ket (k<=l) of class c2, with
+  //      c1 < c2, or c1 == c2 and (i,j) <= (k,l) (the unique stored elements), matching
+  //      2Tz and parity and sharing at least one J
+  {
+    const int N = l.N;
+    std::vector<std::vector<int>> by_tp(4);  // orbits grouped by (tz, l parity)
+    for (int o = 0; o < N; ++o) by_tp[((l.tz[o] + 1) / 2) * 2 + (l.ll[o] & 1)].push_back(o);
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < N; ++k)
+        for (int ll2 = k; ll2 < N; ++ll2) {
+          const int tzj = l.tz[k] + l.tz[ll2] - l.tz[i];
+          if (tzj != -1 && tzj != 1) continue;
+          const int par = ((l.ll[k] + l.ll[ll2] - l.ll[i]) % 2 + 2) % 2;
+          const int c2 = l.con[k] + l.con[ll2];
+          const int kl_lo = std::abs(l.jj[k] - l.jj[ll2]), kl_hi = l.jj[k] + l.jj[ll2];
+          for (int j : by_tp[((tzj + 1) / 2) * 2 + par]) {
+            if (j < i) continue;
+            const int c1 = l.con[i] + l.con[j];
+            if (c1 > c2) continue;
+            if (c1 == c2 && (i > k || (i == k && j > ll2))) continue;
+            const int lo = std::max(std::abs(l.jj[i] - l.jj[j]), kl_lo), hi = std::min(l.jj[i] + l.jj[j], kl_hi);
+            if (lo > hi) continue;
+            tc->quads.push_back((uint64_t)i | ((uint64_t)j << 16) | ((uint64_t)k << 32) | ((uint64_t)ll2 << 48));
+          }
+        }
+  }
   tc->slice_rows = (int64_t)tiles * BM;
   tc->slice_elems = tc->slice_rows * BK;
   if ((int64_t)S * tc->slice_rows >= (int64_t)1 << 31) return fail(IMSRG_ERR_UNSUPPORTED, "operand buffer too large for 32-bit TMA rows");
@@ -603,6 +715,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   CK_TC(cuda(cudaMalloc(&tc->zbuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(Z)"));
   CK_TC(cuda(cudaMemset(tc->zbuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(Z)"));
   CK_TC(cuda(cudaMalloc(&tc->d_err, sizeof(int)), "cudaMalloc(err)"));
+  CK_TC(cuda(cudaMalloc(&tc->d_ft, sizeof(float) * 4 * std::max<size_t>(l.same_list.size(), 1)), "cudaMalloc(ft)"));
   CK_TC(cuda(cudaMemset(tc->d_err, 0, sizeof(int)), "memset(err)"));
   DevPacker pk;
   pk.add(tc->split_ops, &tc->d_split_ops);
@@ -616,6 +729,10 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->cc_tile_L, &tc->d_cc_tile_L);
   pk.add(tc->cc_tile_R, &tc->d_cc_tile_R);
   pk.add(tc->cc_nkb, &tc->d_cc_nkb);
+  pk.add(tc->quads, &tc->d_quads);
+  pk.add(tc->chunks, &tc->d_chunks);
+  pk.add(tc->nb_start, &tc->d_nb_start);
+  pk.add(tc->nb, &tc->d_nb);
   CK_TC(cuda(cudaMalloc(&tc->d_mem, pk.buf.size()), "cudaMalloc(tc tables)"));
   CK_TC(cuda(cudaMemcpy(tc->d_mem, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tc tables)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(tc->d_mem) + f.first;
@@ -656,15 +773,13 @@ imsrg_status Ctx::tc_gemm(const TcProb* probs, const TcTile* tiles, int ntiles, 
 }
 
 imsrg_status Ctx::tc_pphh(const double* Lp, int hL, const double* Rp, int hR, double* w1, double* w2) {
-  const int nops = (int)tc->split_ops.size();
-  if (nops) {
-    const int64_t n = tc->split_prefix.back();
-    const int grid = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+  if (!tc->chunks.empty()) {
+    const int grid = (int)tc->chunks.size();
     if (tc->S == 2)
-      k_split_cols<2><<<grid, 256, 0, stream>>>(tc->d_split_ops, tc->d_split_prefix, nops, Lp, Rp, tc->buf, tc->slice_elems);
+      k_split_chunks<2><<<grid, 256, 0, stream>>>(tc->d_split_ops, tc->d_chunks, Lp, Rp, tc->buf, tc->slice_elems);
     else
-      k_split_cols<3><<<grid, 256, 0, stream>>>(tc->d_split_ops, tc->d_split_prefix, nops, Lp, Rp, tc->buf, tc->slice_elems);
-    CK_TC(launched("k_split_cols"));
+      k_split_chunks<3><<<grid, 256, 0, stream>>>(tc->d_split_ops, tc->d_chunks, Lp, Rp, tc->buf, tc->slice_elems);
+    CK_TC(launched("k_split_chunks"));
   }
   mark(kPhasePphhSplit);
   TcOut out{};
@@ -718,9 +833,11 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   CK_TC(c121(Lp, hL, Rp, hR, RES, hRES));
   mark(kPhaseOneBody);
   if (L.n_unique) {
+    k_ft122<<<(L.N + 127) / 128, 128, 0, stream>>>(D, Lp, hL, Rp, hR, tc->d_ft);
+    CK_TC(launched("k_ft122"));
     const int grid = (int)std::min<int64_t>((L.n_unique + 255) / 256, 152 * 16);
-    k_comm122f<<<grid, 256, 0, stream>>>(D, Lp, hL, Rp, hR, RES, hRES);
-    CK_TC(launched("k_comm122f"));
+    k_comm122_nb<<<grid, 256, 0, stream>>>(D, tc->d_nb_start, tc->d_nb, tc->d_ft, Lp, hL, Rp, hR, RES, hRES);
+    CK_TC(launched("k_comm122_nb"));
   }
   mark(kPhase122);
   CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2));
@@ -730,10 +847,11 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   zo.f32 = tc->zbuf;
   CK_TC(tc_gemm(tc->d_z_probs, tc->d_z_tiles, (int)tc->z_tiles.size(), zo, hL, hR));
   mark(kPhasePhGemm);
-  if (L.n_unique) {
-    const int grid = (int)std::min<int64_t>((L.n_unique + 255) / 256, 152 * 16);
-    k_comm222ph_z<<<grid, 256, 0, stream>>>(D, tc->zbuf, RES, hRES);
-    CK_TC(launched("k_comm222ph_z"));
+  if (!tc->quads.empty()) {
+    const int64_t nq = (int64_t)tc->quads.size();
+    const int grid = (int)std::min<int64_t>((nq + 127) / 128, 152 * 32);
+    k_recouple_quad<<<grid, 128, 0, stream>>>(D, tc->d_quads, nq, tc->zbuf, RES, hRES);
+    CK_TC(launched("k_recouple_quad"));
   }
   mark(kPhaseRecouple);
   return IMSRG_OK;

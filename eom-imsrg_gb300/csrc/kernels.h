@@ -6,6 +6,7 @@
 
 #include "dev.cuh"
 #include "gemm.h"
+#include "tc.h"
 
 namespace imsrg {
 
@@ -34,6 +35,10 @@ __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOp
 void launch_pandya_tc(int S, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
                       __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* nkb);
 __global__ void k_comm122f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
+__global__ void k_ft122(DevLayout D, const double* L, int hL, const double* R, int hR, float* ft);
+__global__ void k_comm122_nb(DevLayout D, const int* nb_start, const NbEntry* nb, const float* ft, const double* L,
+                             int hL, const double* R, int hR, double* RES, int hRES);
 __global__ void k_comm222ph_z(DevLayout D, const float* Z, double* RES, int hRES);
+__global__ void k_recouple_quad(DevLayout D, const uint64_t* quads, int64_t nquads, const float* Z, double* RES, int hRES);
 
 }  // namespace imsrg

@@ -43,10 +43,10 @@ __global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm
     if (((D.ll[a] + D.ll[h]) & 1) == ((D.ll[b] + D.ll[p]) & 1) && D.tz[a] + D.tz[h] == D.tz[b] + D.tz[p]) {
       const int Jmin = max(abs(jp - jb), abs(ja - jh)), Jmax = min(jp + jb, ja + jh);
       float sm = 0.0f;
-      VRef rf;
+      VRefF rf;
       for (int JT = Jmin; JT <= Jmax; JT += 2) {
-        if (!d_vref(D, h, a, p, b, JT, rf)) continue;
-        const float v = (float)op[rf.idx] * (float)(rf.herm ? herm * rf.pre : rf.pre);
+        if (!d_vref_f(D, h, a, p, b, JT, rf)) continue;
+        const float v = f64_to_f32(op[rf.idx]) * rf.scale(herm);
         sm += ((JT & 2) ? -1.0f : 1.0f) * (float)(JT + 1) * d_sixjf(D, jp, jh, JC, ja, jb, JT) * v;
       }
       val = sm * (((jh + jb + JC) & 2) ? -1.0f : 1.0f) * sqrtf((float)(JC + 1));
@@ -82,7 +82,7 @@ __global__ void k_comm122f(DevLayout D, const double* __restrict__ L, int hL, co
     const int a = D.pair_a[o1], b = D.pair_b[o1], c = D.pair_a[o2], d = D.pair_b[o2];
     const int JT = D.lamJ[q];
     float sm = 0.0f;
-    VRef r;
+    VRefF r;
     const int who[4] = {a, b, c, d};
 #pragma unroll
     for (int slot = 0; slot < 4; ++slot) {
@@ -91,17 +91,17 @@ __global__ void k_comm122f(DevLayout D, const double* __restrict__ L, int hL, co
       for (int t = 0; t < n; ++t) {
         const int i = D.same_list[s0 + t];
         bool ok;
-        if (slot == 0) ok = d_vref(D, i, b, c, d, JT, r);
-        else if (slot == 1) ok = d_vref(D, a, i, c, d, JT, r);
-        else if (slot == 2) ok = d_vref(D, a, b, i, d, JT, r);
-        else ok = d_vref(D, a, b, c, i, JT, r);
+        if (slot == 0) ok = d_vref_f(D, i, b, c, d, JT, r);
+        else if (slot == 1) ok = d_vref_f(D, a, i, c, d, JT, r);
+        else if (slot == 2) ok = d_vref_f(D, a, b, i, d, JT, r);
+        else ok = d_vref_f(D, a, b, c, i, JT, r);
         if (!ok) continue;
-        const float vR = (float)R[r.idx] * (float)(r.herm ? hR * r.pre : r.pre);
-        const float vL = (float)L[r.idx] * (float)(r.herm ? hL * r.pre : r.pre);
+        const float vR = f64_to_f32(R[r.idx]) * r.scale(hR);
+        const float vL = f64_to_f32(L[r.idx]) * r.scale(hL);
         if (slot < 2) {
-          sm += (float)d_f_elem(D, L, hL, x, i) * vR - (float)d_f_elem(D, R, hR, x, i) * vL;
+          sm += d_f_elem_f(D, L, hL, x, i) * vR - d_f_elem_f(D, R, hR, x, i) * vL;
         } else {
-          sm += -(float)d_f_elem(D, L, hL, i, x) * vR + (float)d_f_elem(D, R, hR, i, x) * vL;
+          sm += -d_f_elem_f(D, L, hL, i, x) * vR + d_f_elem_f(D, R, hR, i, x) * vL;
         }
       }
     }
@@ -116,10 +116,98 @@ __global__ void k_comm122f(DevLayout D, const double* __restrict__ L, int hL, co
   }
 }
 
+// One-body coefficients of commutator_122 for every (x, i) with i of the same (l,j,tz):
+// ft[4*key + 0..3] = fL(x,i), fR(x,i), fL(i,x), fR(i,x)
+__global__ void k_ft122(DevLayout D, const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
+                        float* __restrict__ ft) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= D.N) return;
+  const int s0 = D.same_start[x], n = D.same_count[x];
+  for (int t = 0; t < n; ++t) {
+    const int i = D.same_list[s0 + t];
+    float* o = ft + 4 * (s0 + t);
+    o[0] = d_f_elem_f(D, L, hL, x, i);
+    o[1] = d_f_elem_f(D, R, hR, x, i);
+    o[2] = d_f_elem_f(D, L, hL, i, x);
+    o[3] = d_f_elem_f(D, R, hR, i, x);
+  }
+}
+
+// commutator_122 (src/commutators.f90:283-396) with precomputed neighbour lists:
+// bra neighbours of pair IX give the a- and b-replaced terms, ket neighbours of pair JX
+// the c- and d-replaced terms.  FP32 arithmetic, ASSIGNS every 2b element.
+__global__ void k_comm122_nb(DevLayout D, const int* __restrict__ nb_start, const NbEntry* __restrict__ nb,
+                             const float* __restrict__ ft, const double* __restrict__ L, int hL,
+                             const double* __restrict__ R, int hR, double* __restrict__ RES, int hRES) {
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < D.n_unique; u += (int64_t)gridDim.x * blockDim.x) {
+    int q, g, IX, JX;
+    d_unique_decode(D, u, q, g, IX, JX);
+    const int c1 = (g < 3) ? 0 : (g == 4 ? 2 : 1);
+    const int c2 = (g == 0) ? 0 : ((g == 1 || g == 3) ? 1 : 2);
+    const int o1 = D.pair_off[q * 3 + c1] + IX, o2 = D.pair_off[q * 3 + c2] + JX;
+    const int a = D.pair_a[o1], b = D.pair_b[o1], c = D.pair_a[o2], d = D.pair_b[o2];
+    const int64_t* go = D.goff + q * 6;
+    const int* gn = D.gn1 + q * 6;
+    float bra = 0.0f, ket = 0.0f;
+    // bra side: sum_i f(x,i) V(target, cd)
+    for (int e = nb_start[o1]; e < nb_start[o1 + 1]; ++e) {
+      const NbEntry n = nb[e];
+      const int ct = n.cls;
+      int64_t idx;
+      bool tr;
+      if (ct <= c2) {
+        const int gg = (ct == 0) ? c2 : (ct == 1 ? (c2 == 1 ? 3 : 5) : 4);
+        idx = go[gg] + n.pos + (int64_t)JX * gn[gg];
+        tr = false;
+      } else {
+        const int gg = (c2 == 0) ? ct : (c2 == 1 ? (ct == 1 ? 3 : 5) : 4);
+        idx = go[gg] + JX + (int64_t)n.pos * gn[gg];
+        tr = true;
+      }
+      float s = (n.flags & 4) ? 1.41421356f : 1.0f;
+      if (n.flags & 2) s = -s;
+      const float vR = f64_to_f32(R[idx]) * ((tr && hR < 0) ? -s : s);
+      const float vL = f64_to_f32(L[idx]) * ((tr && hL < 0) ? -s : s);
+      const float4 f = *reinterpret_cast<const float4*>(ft + 4 * n.fkey);
+      bra += f.x * vR - f.y * vL;
+    }
+    // ket side: sum_i -f(i,x) V(ab, target)
+    for (int e = nb_start[o2]; e < nb_start[o2 + 1]; ++e) {
+      const NbEntry n = nb[e];
+      const int ct = n.cls;
+      int64_t idx;
+      bool tr;
+      if (c1 <= ct) {
+        const int gg = (c1 == 0) ? ct : (c1 == 1 ? (ct == 1 ? 3 : 5) : 4);
+        idx = go[gg] + IX + (int64_t)n.pos * gn[gg];
+        tr = false;
+      } else {
+        const int gg = (ct == 0) ? c1 : (ct == 1 ? (c1 == 1 ? 3 : 5) : 4);
+        idx = go[gg] + n.pos + (int64_t)IX * gn[gg];
+        tr = true;
+      }
+      float s = (n.flags & 4) ? 1.41421356f : 1.0f;
+      if (n.flags & 2) s = -s;
+      const float vR = f64_to_f32(R[idx]) * ((tr && hR < 0) ? -s : s);
+      const float vL = f64_to_f32(L[idx]) * ((tr && hL < 0) ? -s : s);
+      const float4 f = *reinterpret_cast<const float4*>(ft + 4 * n.fkey);
+      ket += -f.z * vR + f.w * vL;
+    }
+    // v_elem carries sqrt(2) for the untouched identical pair; 122 divides by both
+    const float sm = bra * ((a == b) ? 0.70710678f : 1.0f) + ket * ((c == d) ? 0.70710678f : 1.0f);
+    const int k = q * 6 + g;
+    double* X = RES + D.goff[k];
+    const int n1 = D.gn1[k];
+    X[IX + (int64_t)JX * n1] = (double)sm;
+    if (g == 0 || g == 3 || g == 4) X[JX + (int64_t)IX * n1] = (double)sm * hRES;
+  }
+}
+
 // commutator_222_ph recoupling (src/commutators.f90:804-921) reading the antisymmetrised
 // cross-coupled product Z(q) = hL LCC RCC^T - hR RCC LCC^T (FP32), which folds the
 // reference's four WCC reads per J' into two.  ACCUMULATES into RES.
 __global__ void k_comm222ph_z(DevLayout D, const float* __restrict__ Z, double* __restrict__ RES, int hRES) {
+  // element-by-element form of the same recoupling (kept for reference and tests)
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < D.n_unique; u += (int64_t)gridDim.x * blockDim.x) {
     int q, g, IX, JX;
     d_unique_decode(D, u, q, g, IX, JX);
@@ -173,6 +261,93 @@ __global__ void k_comm222ph_z(DevLayout D, const float* __restrict__ Z, double* 
     const double nv = X[IX + (int64_t)JX * n1] + v;
     X[IX + (int64_t)JX * n1] = nv;
     if (g == 0 || g == 3 || g == 4) X[JX + (int64_t)IX * n1] = nv * hRES;
+  }
+}
+
+// commutator_222_ph recoupling organised by orbit quadruple: one thread per (i<=j, k<=l)
+// with matching Tz and parity.  The J'-sums of the direct and exchange terms do not
+// depend on the output J, so each Z(J') pair is read once and reused for every J the two
+// pairs share (the reference re-reads them for each J).  Quadruples are ordered with j
+// fastest so the reads Z[(l,j),(i,k)] and Z[(k,j),(i,l)] are consecutive across a warp.
+// ACCUMULATES into RES (and refreshes the mirrored element of square arrays).
+constexpr int kMaxJp = 26;  // J' values per term: at most jmax+1 (2j <= 25 for eMax <= 12)
+__global__ void k_recouple_quad(DevLayout D, const uint64_t* __restrict__ quads, int64_t nquads,
+                                const float* __restrict__ Z, double* __restrict__ RES, int hRES) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nquads; t += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t qd = quads[t];
+    const int i = (int)(qd & 0xFFFF), j = (int)((qd >> 16) & 0xFFFF), k = (int)((qd >> 32) & 0xFFFF),
+              l = (int)((qd >> 48) & 0xFFFF);
+    const int ji = D.jj[i], jj = D.jj[j], jk = D.jj[k], jl = D.jj[l];
+    const int N = D.N, NJ = D.NJ;
+    const float phase = ((ji + jj + jk + jl) & 2) ? -1.0f : 1.0f;
+    // direct term inputs: zd(J') = Z[(k,i),(j,l)] + phase Z[(l,j),(i,k)]
+    float zd[kMaxJp], ze[kMaxJp];
+    const int dlo = max(abs(jj - jl), abs(ji - jk)), dhi = min(jj + jl, ji + jk);
+    {
+      const int Tz = abs(D.tz[i] - D.tz[k]) >> 1, PAR = (D.ll[i] + D.ll[k]) & 1;
+      for (int JP = dlo, n = 0; JP <= dhi && n < kMaxJp; JP += 2, ++n) {
+        const int qx = (JP >> 1) + Tz * (D.JM + 1) + PAR * 2 * (D.JM + 1);
+        const float* W = Z + D.wcc_off[qx];
+        const int64_t rl = D.cc_rlen[qx];
+        const int h = JP >> 1;
+        const int64_t rjl = D.ccr[(j * N + l) * NJ + h], rik = D.ccr[(i * N + k) * NJ + h];
+        const int64_t gjl = D.ccr[(l * N + j) * NJ + h], gik = D.ccr[(k * N + i) * NJ + h];
+        zd[n] = ((rjl | rik | gjl | gik) < 0) ? 0.0f : W[gik + rjl * rl] + phase * W[gjl + rik * rl];
+      }
+    }
+    // exchange term inputs: ze(J') = Z[(l,i),(j,k)] + phase Z[(k,j),(i,l)]
+    const int elo = max(abs(ji - jl), abs(jj - jk)), ehi = min(ji + jl, jj + jk);
+    {
+      const int Tz = abs(D.tz[i] - D.tz[l]) >> 1, PAR = (D.ll[i] + D.ll[l]) & 1;
+      for (int JP = elo, n = 0; JP <= ehi && n < kMaxJp; JP += 2, ++n) {
+        const int qx = (JP >> 1) + Tz * (D.JM + 1) + PAR * 2 * (D.JM + 1);
+        const float* W = Z + D.wcc_off[qx];
+        const int64_t rl = D.cc_rlen[qx];
+        const int h = JP >> 1;
+        const int64_t ril = D.ccr[(i * N + l) * NJ + h], rjk = D.ccr[(j * N + k) * NJ + h];
+        const int64_t gil = D.ccr[(l * N + i) * NJ + h], gjk = D.ccr[(k * N + j) * NJ + h];
+        ze[n] = ((ril | rjk | gil | gjk) < 0) ? 0.0f : W[gil + rjk * rl] + phase * W[gjk + ril * rl];
+      }
+    }
+    // 6j blocks {ji jj J; jl jk J'} (direct) and {ji jj J; jk jl J'} (exchange)
+    const int nh = D.sj_nh;
+    const int kd = (((ji >> 1) * nh + (jj >> 1)) * nh + (jl >> 1)) * nh + (jk >> 1);
+    const int ke = (((ji >> 1) * nh + (jj >> 1)) * nh + (jk >> 1)) * nh + (jl >> 1);
+    const float* sjd = D.sj_valf + D.sj_off[kd];
+    const float* sje = D.sj_valf + D.sj_off[ke];
+    const int d3 = D.sj_j3min[kd], d6 = D.sj_j6min[kd], dn6 = D.sj_n6[kd];
+    const int e3 = D.sj_j3min[ke], e6 = D.sj_j6min[ke], en6 = D.sj_n6[ke];
+    const int C1 = D.con[i] + D.con[j], C2 = D.con[k] + D.con[l];
+    const int g = (C1 == 0) ? C2 : (C1 == 1 ? (C2 == 1 ? 3 : 5) : 4);
+    const bool square = (C1 == C2);
+    const int T = D.tz[i] + D.tz[j], P = (D.ll[i] + D.ll[j]) & 1;
+    const float pre = ((i == j) ? .70710678118f : 1.0f) * ((k == l) ? .70710678118f : 1.0f);
+    const int Jlo = max(abs(ji - jj), abs(jk - jl)), Jhi = min(ji + jj, jk + jl);
+    for (int J = Jlo; J <= Jhi; J += 2) {
+      float sd = 0.0f, se = 0.0f;
+      {
+        // valid J' for this J: triangles (ji,jj,J) hold; (jl,jk,J) and the J' range of zd
+        // every (J, J') here satisfies the four triangles: J lies in both pair ranges and
+        // J' in the direct range, whose lower ends are this 6j block's j3min / j6min
+        const float* row = sjd + ((J - d3) >> 1) * dn6 + ((dlo - d6) >> 1);
+        const int n = min((dhi - dlo) / 2 + 1, kMaxJp);
+        for (int m = 0; m < n; ++m) sd += row[m] * zd[m];
+      }
+      {
+        const float* row = sje + ((J - e3) >> 1) * en6 + ((elo - e6) >> 1);
+        const int n = min((ehi - elo) / 2 + 1, kMaxJp);
+        for (int m = 0; m < n; ++m) se += row[m] * ze[m];
+      }
+      const float sm = -(((jl + jk + J) & 2) ? -1.0f : 1.0f) * sd + se;
+      const int q = 3 * J + (T + 2) + P;
+      const int kk = q * 6 + g;
+      const int IX = D.pairpos[(i * N + j) * NJ + (J >> 1)], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
+      double* X = RES + D.goff[kk];
+      const int n1 = D.gn1[kk];
+      const double nv = X[IX + (int64_t)JX * n1] + (double)(sm * pre);
+      X[IX + (int64_t)JX * n1] = nv;
+      if (square) X[JX + (int64_t)IX * n1] = nv * hRES;
+    }
   }
 }
 
