@@ -132,17 +132,32 @@ imsrg_status Ctx::upload_tables() {
   add_seg(l.off_fpp, (int64_t)l.P * l.P, 1);
   for (int k = 0; k < l.nblocks * 6; ++k) add_seg(l.goff[k], (int64_t)l.gn1[k] * l.gn2[k], kSquare[k % 6] ? 1 : 2);
   nseg = (int)s_start.size();
+  // 222_pp_hh accumulation tiles: (array, row0, col0, square); square arrays by tile pairs
+  for (int k = 0; k < l.nblocks * 6; ++k) {
+    const int n1 = l.gn1[k], n2 = l.gn2[k];
+    if ((int64_t)n1 * n2 == 0) continue;
+    if (kSquare[k % 6]) {
+      for (int i0 = 0; i0 < n1; i0 += 32)
+        for (int j0 = i0; j0 < n1; j0 += 32) upd_tiles.push_back(make_int4(k, i0, j0, 1));
+    } else {
+      for (int j0 = 0; j0 < n2; j0 += 32)
+        for (int i0 = 0; i0 < n1; i0 += 32) upd_tiles.push_back(make_int4(k, i0, j0, 0));
+    }
+  }
   const GemmProb* pp_p = nullptr; const GemmTile* pp_t = nullptr;
   const GemmProb* wc_p = nullptr; const GemmTile* wc_t = nullptr;
   const int64_t* seg_s = nullptr; const int* seg_l = nullptr; const int8_t* seg_w = nullptr;
   pk.add(pphh_probs, &pp_p); pk.add(pphh_tiles, &pp_t); pk.add(wcc_probs, &wc_p); pk.add(wcc_tiles, &wc_t);
   pk.add(s_start, &seg_s); pk.add(s_len, &seg_l); pk.add(s_w, &seg_w);
+  const int4* ut = nullptr;
+  pk.add(upd_tiles, &ut);
 
   CK(cuda(cudaMalloc(&d_tables, pk.buf.size()), "cudaMalloc(tables)"));
   CK(cuda(cudaMemcpy(d_tables, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tables)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(d_tables) + f.first;
   d_pphh_probs = pp_p; d_pphh_tiles = pp_t; d_wcc_probs = wc_p; d_wcc_tiles = wc_t;
   d_seg_start = seg_s; d_seg_len = seg_l; d_seg_w = seg_w;
+  d_upd_tiles = ut;
   CK(cuda(cudaMalloc(&d_partial, sizeof(double) * (std::max(nseg, l.nblocks) + 64)), "cudaMalloc(partials)"));
   CK(cuda(cudaMalloc(&d_scalars, sizeof(double) * 64), "cudaMalloc(scalars)"));
   CK(cuda(cudaMallocHost(&h_scalars, sizeof(double) * 64), "cudaMallocHost(scalars)"));
@@ -157,6 +172,12 @@ imsrg_status Ctx::ensure_workspace() {
   CK(cuda(cudaMalloc(&d_w2, sb), "cudaMalloc(w2)"));
   CK(cuda(cudaMalloc(&d_lcc, sizeof(double) * std::max<int64_t>(L.cc_size, 1)), "cudaMalloc(LCC)"));
   CK(cuda(cudaMalloc(&d_rcc, sizeof(double) * std::max<int64_t>(L.cc_size, 1)), "cudaMalloc(RCC)"));
+  return IMSRG_OK;
+}
+
+// FP64 WCC workspace of the plain path (1.46 GiB at eMax=10), allocated on first use
+imsrg_status Ctx::ensure_wcc() {
+  if (d_wcc) return IMSRG_OK;
   CK(cuda(cudaMalloc(&d_wcc, sizeof(double) * std::max<int64_t>(L.wcc_size, 1)), "cudaMalloc(WCC)"));
   CK(cuda(cudaMemsetAsync(d_wcc, 0, sizeof(double) * std::max<int64_t>(L.wcc_size, 1), stream), "memset(WCC)"));
   return IMSRG_OK;
@@ -192,13 +213,15 @@ imsrg_status Ctx::pandya(const double* op, int herm, double* cc) {
 }
 
 imsrg_status Ctx::e0(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* out) {
-  k_e0<<<1, 1024, 0, stream>>>(D, Lp, hL, Rp, hR, RES, out);
-  return launched("k_e0");
+  k_e0_partial<<<L.nblocks + 1, 256, 0, stream>>>(D, Lp, hL, Rp, hR, d_partial);
+  CK(launched("k_e0_partial"));
+  k_e0_final<<<1, 32, 0, stream>>>(D, d_partial, RES, out);
+  return launched("k_e0_final");
 }
 
 imsrg_status Ctx::c111(const double* Lp, int hL, const double* Rp, int hR, double* RES) {
   const int64_t n = (int64_t)L.A * L.A + (int64_t)L.P * L.A + (int64_t)L.P * L.P;
-  k_comm111<<<grid_for(n), kThreads, 0, stream>>>(D, Lp, hL, Rp, hR, RES);
+  k_comm111<<<grid_for(n * 32), kThreads, 0, stream>>>(D, Lp, hL, Rp, hR, RES);
   return launched("k_comm111");
 }
 
@@ -229,14 +252,20 @@ imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, doubl
     CK(launched("k_gemm_fp64(pphh)"));
   }
   mark(kPhasePphhGemm);
-  k_pphh_update<<<grid_for(L.slab - L.goff[0]), kThreads, 0, stream>>>(D, RES, w1, w2, (double)(hL * hR));
-  CK(launched("k_pphh_update"));
+  if (!upd_tiles.empty()) {
+    k_pphh_update_tiled<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (double)(hL * hR));
+    CK(launched("k_pphh_update_tiled"));
+  }
   mark(kPhasePphhUpdate);
   return IMSRG_OK;
 }
 
-imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2) {
+imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2, bool f32) {
   if (D.n_ob == 0) return IMSRG_OK;
+  if (f32) {
+    k_comm221f<<<(D.n_ob * 32 + kThreads - 1) / kThreads, kThreads, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);
+    return launched("k_comm221f");
+  }
   k_comm221<<<(D.n_ob * 32 + kThreads - 1) / kThreads, kThreads, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);
   return launched("k_comm221");
 }
@@ -274,8 +303,9 @@ imsrg_status Ctx::commutator(const double* Lp, int hL, const double* Rp, int hR,
   CK(c122(Lp, hL, Rp, hR, RES, hRES));
   mark(kPhase122);
   CK(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2));
-  CK(c221(hL, hR, RES, hRES, d_w1, d_w2));
+  CK(c221(hL, hR, RES, hRES, d_w1, d_w2, false));
   mark(kPhase221);
+  CK(ensure_wcc());
   CK(ph(d_lcc, hL, d_rcc, hR, RES, hRES, d_wcc));
   return IMSRG_OK;
 }
@@ -848,7 +878,7 @@ imsrg_status imsrg_commutator_221(imsrg_ctx* ctx, const imsrg_op* L, const imsrg
   THREE_OPS("imsrg_commutator_221");
   CK(check_op(c, w1, "imsrg_commutator_221"));
   CK(check_op(c, w2, "imsrg_commutator_221"));
-  return c->c221(L->herm, R->herm, RES->d, RES->herm, w1->d, w2->d);
+  return c->c221(L->herm, R->herm, RES->d, RES->herm, w1->d, w2->d, false);
 }
 
 imsrg_status imsrg_commutator_222_ph(imsrg_ctx* ctx, const imsrg_cc* LCC, const imsrg_cc* RCC, imsrg_op* RES,

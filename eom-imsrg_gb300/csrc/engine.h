@@ -53,6 +53,8 @@ struct Ctx {
   double* d_scalars = nullptr;
   double* h_scalars = nullptr;
   double* d_mono = nullptr;
+  std::vector<int4> upd_tiles;
+  const int4* d_upd_tiles = nullptr;
   // commutator workspaces (w1, w2: sq_op shaped; LCC/RCC: CCX; WCC: rlen x rlen blocks)
   double *d_w1 = nullptr, *d_w2 = nullptr, *d_lcc = nullptr, *d_rcc = nullptr, *d_wcc = nullptr;
   // Magnus / BCH intermediates
@@ -80,7 +82,8 @@ struct Ctx {
   imsrg_status c121(const double* L, int hL, const double* R, int hR, double* RES, int hRES);
   imsrg_status c122(const double* L, int hL, const double* R, int hR, double* RES, int hRES);
   imsrg_status pphh(const double* L, int hL, const double* R, int hR, double* RES, double* w1, double* w2);
-  imsrg_status c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2);
+  imsrg_status c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2, bool f32);
+  imsrg_status ensure_wcc();
   imsrg_status ph(const double* lcc, int hL, const double* rcc, int hR, double* RES, int hRES, double* wcc);
   imsrg_status commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
   imsrg_status axpby(const double* A, double ax, const double* B, double bx, double* C);

@@ -841,7 +841,7 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   }
   mark(kPhase122);
   CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2));
-  CK_TC(c221(hL, hR, RES, hRES, d_w1, d_w2));
+  CK_TC(c221(hL, hR, RES, hRES, d_w1, d_w2, true));
   mark(kPhase221);
   TcOut zo{};
   zo.f32 = tc->zbuf;

@@ -17,7 +17,11 @@ __global__ void k_comm222ph(DevLayout D, const double* WCC, int hL, int hR, doub
 __global__ void k_comm111(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES);
 __global__ void k_comm121(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
 __global__ void k_comm221(DevLayout D, int pm, double* RES, int hRES, const double* w1, const double* w2);
-__global__ void k_e0(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, double* out);
+__global__ void k_e0_partial(DevLayout D, const double* L, int hL, const double* R, int hR, double* partial);
+__global__ void k_e0_final(DevLayout D, const double* partial, double* RES, double* out);
+__global__ void k_pphh_update_tiled(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
+                                    double pm);
+__global__ void k_comm221f(DevLayout D, int pm, double* RES, int hRES, const double* w1, const double* w2);
 
 __global__ void k_monopole(DevLayout D, const double* H, int hH, double* mono);
 __global__ void k_white_1b(DevLayout D, const double* H, int hH, double* ETA);

@@ -130,6 +130,55 @@ __global__ void k_pphh_update(DevLayout D, double* __restrict__ RES, const doubl
   }
 }
 
+// Tiled form of k_pphh_update: a block owns a 32x32 tile of one array (and, for square
+// arrays, its mirror tile), so both the direct and the transposed W reads are coalesced
+// through shared memory.  Same arithmetic per element as k_pphh_update.
+__global__ void __launch_bounds__(256) k_pphh_update_tiled(DevLayout D, const int4* __restrict__ tiles,
+                                                           double* __restrict__ RES, const double* __restrict__ w1,
+                                                           const double* __restrict__ w2, double pm) {
+  __shared__ double Xa[32][33];
+  __shared__ double Xb[32][33];
+  const int4 t = tiles[blockIdx.x];  // (array k, row0, col0, square flag)
+  const int k = t.x, i0 = t.y, j0 = t.z;
+  const int64_t base = D.goff[k];
+  const int n1 = D.gn1[k], n2 = D.gn2[k];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  if (!t.w) {
+    for (int r = ty; r < 32; r += 8) {
+      const int i = i0 + tx, j = j0 + r;
+      if (i < n1 && j < n2) {
+        const int64_t e = base + i + (int64_t)j * n1;
+        RES[e] = RES[e] + w1[e] - w2[e];
+      }
+    }
+    return;
+  }
+  // square: tiles A = (i0, j0) and B = (j0, i0) (the same tile on the diagonal)
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, j = j0 + r;
+    Xa[r][tx] = (i < n1 && j < n1) ? w1[base + i + (int64_t)j * n1] - w2[base + i + (int64_t)j * n1] : 0.0;
+    const int ib = j0 + tx, jb = i0 + r;
+    Xb[r][tx] = (ib < n1 && jb < n1) ? w1[base + ib + (int64_t)jb * n1] - w2[base + ib + (int64_t)jb * n1] : 0.0;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    {  // element (i0+tx, j0+r): its transpose is (j0+r, i0+tx) = Xb[tx][r]
+      const int i = i0 + tx, j = j0 + r;
+      if (i < n1 && j < n1) {
+        const int64_t e = base + i + (int64_t)j * n1;
+        RES[e] = RES[e] + Xa[r][tx] - Xb[tx][r] * pm;
+      }
+    }
+    if (i0 != j0) {  // element (j0+tx, i0+r): transpose (i0+r, j0+tx) = Xa[tx][r]
+      const int i = j0 + tx, j = i0 + r;
+      if (i < n1 && j < n1) {
+        const int64_t e = base + i + (int64_t)j * n1;
+        RES[e] = RES[e] + Xb[r][tx] - Xa[tx][r] * pm;
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------- 222_ph recoupling
 // src/commutators.f90:804-921: for each unique 2b element, sum over the cross-coupled J'
 // of 6j-weighted WCC gathers (direct and exchange terms); ACCUMULATES into RES.
@@ -194,59 +243,64 @@ __global__ void k_comm222ph(DevLayout D, const double* __restrict__ WCC, int hL,
 }
 
 // ---------------------------------------------------------------- one-body pieces
-// commutator_111 (src/commutators.f90:36-80), one thread per output of fhh, fph, fpp (ASSIGN)
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// commutator_111 (src/commutators.f90:36-80): one warp per output of fhh, fph, fpp
+// (lanes split the contractions), ASSIGNS the one-body part
 __global__ void k_comm111(DevLayout D, const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
                           double* __restrict__ RES) {
   const int A = D.A, P = D.P;
   const int total = A * A + P * A + P * P;
+  const int lane = threadIdx.x & 31;
   const double *Lhh = L + D.off_fhh, *Rhh = R + D.off_fhh, *Lph = L + D.off_fph, *Rph = R + D.off_fph;
   const double *Lpp = L + D.off_fpp, *Rpp = R + D.off_fpp;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < total; t += (gridDim.x * blockDim.x) >> 5) {
     if (t < A * A) {
       const int i = t % A, j = t / A;
       double th1 = 0, th2 = 0, th1t = 0, th2t = 0;
-      for (int k = 0; k < A; ++k) {
+      for (int k = lane; k < A; k += 32) {
         th1 += Lhh[i + k * A] * Rhh[k + j * A];
         th1t += Lhh[j + k * A] * Rhh[k + i * A];
       }
-      for (int p = 0; p < P; ++p) {
+      for (int p = lane; p < P; p += 32) {
         th2 += Lph[p + i * P] * Rph[p + j * P];
         th2t += Lph[p + j * P] * Rph[p + i * P];
       }
-      RES[D.off_fhh + t] = th1 + th2 * hL - (th1t * hL + th2t) * hR;
+      th1 = warp_sum(th1); th2 = warp_sum(th2); th1t = warp_sum(th1t); th2t = warp_sum(th2t);
+      if (lane == 0) RES[D.off_fhh + t] = th1 + th2 * hL - (th1t * hL + th2t) * hR;
     } else if (t < A * A + P * A) {
       const int s = t - A * A;
       const int p = s % P, i = s / P;
       double a1 = 0, a2 = 0, b1 = 0, b2 = 0;
-      for (int k = 0; k < A; ++k) {
+      for (int k = lane; k < A; k += 32) {
         a1 += Lph[p + k * P] * Rhh[k + i * A];
         b1 += Rph[p + k * P] * Lhh[k + i * A];
       }
-      for (int r = 0; r < P; ++r) {
+      for (int r = lane; r < P; r += 32) {
         a2 += Lpp[p + (int64_t)r * P] * Rph[r + i * P];
         b2 += Rpp[p + (int64_t)r * P] * Lph[r + i * P];
       }
-      RES[D.off_fph + s] = (a1 + a2) - b1 - b2;
+      a1 = warp_sum(a1); a2 = warp_sum(a2); b1 = warp_sum(b1); b2 = warp_sum(b2);
+      if (lane == 0) RES[D.off_fph + s] = (a1 + a2) - b1 - b2;
     } else {
       const int s = t - A * A - P * A;
       const int p = s % P, r = s / P;
       double tp1 = 0, tp2 = 0, tp1t = 0, tp2t = 0;
-      for (int k = 0; k < A; ++k) {
+      for (int k = lane; k < A; k += 32) {
         tp1 += Lph[p + k * P] * Rph[r + k * P];
         tp1t += Lph[r + k * P] * Rph[p + k * P];
       }
-      for (int m = 0; m < P; ++m) {
+      for (int m = lane; m < P; m += 32) {
         tp2 += Lpp[p + (int64_t)m * P] * Rpp[m + (int64_t)r * P];
         tp2t += Lpp[r + (int64_t)m * P] * Rpp[m + (int64_t)p * P];
       }
-      RES[D.off_fpp + s] = tp1 * hR + tp2 - (tp1t + tp2t * hR) * hL;
+      tp1 = warp_sum(tp1); tp2 = warp_sum(tp2); tp1t = warp_sum(tp1t); tp2t = warp_sum(tp2t);
+      if (lane == 0) RES[D.off_fpp + s] = tp1 * hR + tp2 - (tp1t + tp2t * hR) * hL;
     }
   }
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
 }
 
 __device__ __forceinline__ double* ob_ptr(const DevLayout& D, double* op, int kind, int p, int q) {
@@ -318,45 +372,45 @@ __global__ void k_comm221(DevLayout D, int pm, double* __restrict__ RES, int hRE
   }
 }
 
-// commutator_110 + commutator_220 (src/commutators.f90:10-33, 399-432).  One block with a
-// fixed reduction order (deterministic): out[0] = 110, out[1] = 220 and, when RES is given,
-// RES%E0 = 110 + 220 (ASSIGN).
-__global__ void k_e0(DevLayout D, const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
-                     double* __restrict__ RES, double* __restrict__ out) {
-  __shared__ double r1[1024], r2[1024];
-  double s110 = 0.0, s220 = 0.0;
-  const int A = D.A, P = D.P;
-  for (int t = threadIdx.x; t < A * P; t += blockDim.x) {
-    const int i = t / P;
-    const double lv = L[D.off_fph + t], rv = R[D.off_fph + t];
-    s110 += (lv * rv * hL - rv * lv * hR) * (D.jj[D.holes[i]] + 1);
-  }
-  if (hR * hL == -1) {
-    for (int q = 0; q < D.nblocks; ++q) {
-      const int np = D.ncls[q * 3], nh = D.ncls[q * 3 + 2];
-      const int64_t n = (int64_t)np * nh;
-      const double* XL = L + D.goff[q * 6 + 2];
-      const double* XR = R + D.goff[q * 6 + 2];
-      double s = 0.0;
-      for (int64_t t = threadIdx.x; t < n; t += blockDim.x) s -= XL[t] * XR[t] * hR;
-      s220 += s * (D.lamJ[q] + 1);
+// commutator_110 + commutator_220 (src/commutators.f90:10-33, 399-432), stage 1: block q
+// sums the 220 contribution of channel q, block nblocks the 110 sum (fixed order).
+__global__ void k_e0_partial(DevLayout D, const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
+                             double* __restrict__ partial) {
+  __shared__ double red[256];
+  const int q = blockIdx.x;
+  double acc = 0.0;
+  if (q == D.nblocks) {
+    const int A = D.A, P = D.P;
+    for (int t = threadIdx.x; t < A * P; t += blockDim.x) {
+      const int i = t / P;
+      const double lv = L[D.off_fph + t], rv = R[D.off_fph + t];
+      acc += (lv * rv * hL - rv * lv * hR) * (D.jj[D.holes[i]] + 1);
     }
+  } else if (hR * hL == -1) {
+    const int np = D.ncls[q * 3], nh = D.ncls[q * 3 + 2];
+    const int64_t n = (int64_t)np * nh;
+    const double* XL = L + D.goff[q * 6 + 2];
+    const double* XR = R + D.goff[q * 6 + 2];
+    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) acc -= XL[t] * XR[t] * hR;
   }
-  r1[threadIdx.x] = s110;
-  r2[threadIdx.x] = s220;
+  red[threadIdx.x] = acc;
   __syncthreads();
   for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      r1[threadIdx.x] += r1[threadIdx.x + s];
-      r2[threadIdx.x] += r2[threadIdx.x + s];
-    }
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    const double e110 = r1[0], e220 = r2[0] * 2.0;
-    if (out) { out[0] = e110; out[1] = e220; }
-    if (RES) RES[0] = e110 + e220;
-  }
+  if (threadIdx.x == 0) partial[q] = (q == D.nblocks) ? red[0] : red[0] * (D.lamJ[q] + 1);
+}
+
+// stage 2: out[0] = 110, out[1] = 220 and, when RES is given, RES%E0 = 110 + 220 (ASSIGN)
+__global__ void k_e0_final(DevLayout D, const double* __restrict__ partial, double* __restrict__ RES,
+                           double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s220 = 0.0;
+  for (int q = 0; q < D.nblocks; ++q) s220 += partial[q];
+  const double e110 = partial[D.nblocks], e220 = s220 * 2.0;
+  if (out) { out[0] = e110; out[1] = e220; }
+  if (RES) RES[0] = e110 + e220;
 }
 
 }  // namespace imsrg

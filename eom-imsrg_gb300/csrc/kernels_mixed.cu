@@ -116,6 +116,38 @@ __global__ void k_comm122f(DevLayout D, const double* __restrict__ L, int hL, co
   }
 }
 
+// commutator_221 (src/commutators.f90:435-578) with FP32 arithmetic: one warp per
+// one-body output, ACCUMULATES into RES (FP64)
+__global__ void k_comm221f(DevLayout D, int pm, double* __restrict__ RES, int hRES, const double* __restrict__ w1,
+                           const double* __restrict__ w2) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= D.n_ob) return;
+  const int kind = D.ob_kind[warp], p = D.ob_p[warp], q = D.ob_q[warp], ik = D.ob_pk[warp], jk = D.ob_qk[warp];
+  const int ji = D.jj[ik];
+  float sm = 0.0f;
+  VRefF r;
+  for (int ck = lane; ck < D.N; ck += 32) {
+    const double* w = D.con[ck] ? w1 : w2;
+    const int jc = D.jj[ck];
+    for (int JT = abs(jc - ji); JT <= jc + ji; JT += 2) {
+      float v = d_vref_f(D, ck, ik, ck, jk, JT, r) ? f64_to_f32(w[r.idx]) * r.pre : 0.0f;
+      if (kind < 2 && d_vref_f(D, ck, jk, ck, ik, JT, r)) v -= (float)pm * f64_to_f32(w[r.idx]) * r.pre;
+      sm += v * (float)(JT + 1);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
+  if (lane == 0) {
+    double* f = (kind == 0) ? RES + D.off_fhh + p + (int64_t)q * D.A
+                            : (kind == 1 ? RES + D.off_fpp + p + (int64_t)q * D.P : RES + D.off_fph + p + (int64_t)q * D.P);
+    const double v = *f + (double)(sm / (float)(ji + 1));
+    *f = v;
+    if (kind < 2) {
+      double* g = (kind == 0) ? RES + D.off_fhh + q + (int64_t)p * D.A : RES + D.off_fpp + q + (int64_t)p * D.P;
+      *g = v * hRES;
+    }
+  }
+}
+
 // One-body coefficients of commutator_122 for every (x, i) with i of the same (l,j,tz):
 // ft[4*key + 0..3] = fL(x,i), fR(x,i), fL(i,x), fR(i,x)
 __global__ void k_ft122(DevLayout D, const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
