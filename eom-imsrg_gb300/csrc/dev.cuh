@@ -196,6 +196,16 @@ __device__ __forceinline__ float f64_to_f32(double x) {
   return __uint_as_float(sign | (fe << 23) | mant);
 }
 
+// FP32 -> FP64 (exact) with integer instructions only; zero and subnormals map to zero
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xFF;
+  if (e == 0) return 0.0;
+  const unsigned long long b = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)(e + 1023 - 127) << 52) |
+                               ((unsigned long long)(u & 0x7FFFFF) << 29);
+  return __longlong_as_double((long long)b);
+}
+
 __device__ __forceinline__ float d_f_elem_f(const DevLayout& D, const double* op, int herm, int a, int b) {
   const int c1 = D.con[a], c2 = D.con[b];
   if (c1 + c2 == 0) return f64_to_f32(op[D.off_fpp + D.loc[a] + (int64_t)D.loc[b] * D.P]);
@@ -230,7 +240,7 @@ __device__ __forceinline__ void d_unique_decode(const DevLayout& D, int64_t u, i
   const int n1 = D.gn1[lo];
   if (g == 0 || g == 3 || g == 4) {
     // column JX holds JX+1 elements (IX = 0..JX)
-    int j = (int)((sqrt(8.0 * (double)e + 1.0) - 1.0) * 0.5);
+    int j = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);  // corrected below
     while ((int64_t)(j + 1) * (j + 2) / 2 <= e) ++j;
     while ((int64_t)j * (j + 1) / 2 > e) --j;
     JX = j;

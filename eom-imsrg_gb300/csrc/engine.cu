@@ -237,7 +237,8 @@ imsrg_status Ctx::c122(const double* Lp, int hL, const double* Rp, int hR, doubl
   return launched("k_comm122");
 }
 
-imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* w1, double* w2) {
+imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* w1, double* w2,
+                       bool upper_f32) {
   const size_t sb = sizeof(double) * (size_t)L.slab;
   CK(cuda(cudaMemsetAsync(w1, 0, sb, stream), "memset(w1)"));
   CK(cuda(cudaMemsetAsync(w2, 0, sb, stream), "memset(w2)"));
@@ -253,8 +254,13 @@ imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, doubl
   }
   mark(kPhasePphhGemm);
   if (!upd_tiles.empty()) {
-    k_pphh_update_tiled<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (double)(hL * hR));
-    CK(launched("k_pphh_update_tiled"));
+    if (upper_f32) {
+      k_pphh_update_f<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (float)(hL * hR));
+      CK(launched("k_pphh_update_f"));
+    } else {
+      k_pphh_update_tiled<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (double)(hL * hR));
+      CK(launched("k_pphh_update_tiled"));
+    }
   }
   mark(kPhasePphhUpdate);
   return IMSRG_OK;

@@ -81,7 +81,8 @@ struct Ctx {
   imsrg_status c111(const double* L, int hL, const double* R, int hR, double* RES);
   imsrg_status c121(const double* L, int hL, const double* R, int hR, double* RES, int hRES);
   imsrg_status c122(const double* L, int hL, const double* R, int hR, double* RES, int hRES);
-  imsrg_status pphh(const double* L, int hL, const double* R, int hR, double* RES, double* w1, double* w2);
+  imsrg_status pphh(const double* L, int hL, const double* R, int hR, double* RES, double* w1, double* w2,
+                    bool upper_f32 = false);
   imsrg_status c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2, bool f32);
   imsrg_status ensure_wcc();
   imsrg_status ph(const double* lcc, int hL, const double* rcc, int hR, double* RES, int hRES, double* wcc);

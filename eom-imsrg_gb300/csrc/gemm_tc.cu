@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         tmem_ld32(tmem_base + (uint32_t)(acc * BN + c0) + ((uint32_t)(quad * 32) << 16), r);
         if (m < P.M) {
           if (P.out_f32) {
-            float* C = out.f32 + P.c_off;
+            float* C = (P.out_f32 == 1 ? out.f32 : out.f32b) + P.c_off;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const int n = tile.n0 + c0 + j;
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const int n = tile.n0 + c0 + j;
-              if (n < P.N) C[m + (int64_t)n * P.ldc] = (double)__uint_as_float(r[j]);
+              if (n < P.N) C[m + (int64_t)n * P.ldc] = f32_to_f64(__uint_as_float(r[j]));
             }
           }
         }
@@ -463,7 +463,7 @@ struct TcState {
   std::vector<GemmProb> small_probs;
   std::vector<GemmTile> small_tiles;
   // particle-hole: Z(q) = hL LCC RCC^T - hR RCC LCC^T
-  std::vector<int> cc_tile_L, cc_tile_R, cc_nkb;
+  std::vector<int> cc_tile_L, cc_tile_R, cc_tile_Ls, cc_tile_Rs, cc_nkb, swap_row;
   std::vector<TcProb> z_probs;
   std::vector<TcTile> z_tiles;
   void* d_mem = nullptr;
@@ -478,7 +478,11 @@ struct TcState {
   const int* d_cc_tile_L = nullptr;
   const int* d_cc_tile_R = nullptr;
   const int* d_cc_nkb = nullptr;
+  const int* d_cc_tile_Ls = nullptr;
+  const int* d_cc_tile_Rs = nullptr;
+  const int* d_swap_row = nullptr;
   float* zbuf = nullptr;
+  float* ybuf = nullptr;
   int* d_err = nullptr;
   // orbit quadruples (i<=j, k<=l) of the particle-hole recoupling, j fastest
   std::vector<uint64_t> quads;
@@ -534,6 +538,7 @@ void Ctx::tc_release() {
   if (tc->buf) cudaFree(tc->buf);
   if (tc->d_mem) cudaFree(tc->d_mem);
   if (tc->zbuf) cudaFree(tc->zbuf);
+  if (tc->ybuf) cudaFree(tc->ybuf);
   if (tc->d_err) cudaFree(tc->d_err);
   if (tc->d_ft) cudaFree(tc->d_ft);
   delete tc;
@@ -621,25 +626,43 @@ imsrg_status Ctx::tc_prepare(int mode) {
     if (p.c_id == kOpW2) tc->small_probs.push_back(p);
   tc->small_tiles = build_tiles(tc->small_probs, 64, 64);
 
-  // ---- particle-hole: LCC / RCC rows r, K = nph
+  // ---- particle-hole: LCC / RCC rows r, K = nph, each also with its rows swapped
+  //      (row r(a,b) holding row r(b,a)); Z(q) = hL LCC RCC^T - hR RCC LCC^T and its
+  //      row-swapped copy Y(q) = hL LCCs RCC^T - hR RCCs LCC^T
   tc->cc_tile_L.assign(l.ncc, 0);
   tc->cc_tile_R.assign(l.ncc, 0);
+  tc->cc_tile_Ls.assign(l.ncc, 0);
+  tc->cc_tile_Rs.assign(l.ncc, 0);
   tc->cc_nkb.assign(l.ncc, 0);
+  tc->swap_row.assign(std::max<size_t>(l.cc_ra.size(), 1), 0);
+  for (int q = 0; q < l.ncc; ++q)
+    for (int r = 0; r < l.cc_rlen[q]; ++r) {
+      const int a = l.cc_ra[l.cc_row_off[q] + r], b = l.cc_rb[l.cc_row_off[q] + r];
+      const int rs = l.ccr[((size_t)b * l.N + a) * l.NJ + l.cc_J[q] / 2];
+      if (rs < 0) return fail(IMSRG_ERR_MISMATCH, "swapped pair outside its cross-coupled channel");
+      tc->swap_row[l.cc_row_off[q] + r] = rs;
+    }
   for (int q = 0; q < l.ncc; ++q) {
     const int r = l.cc_rlen[q], nb = l.cc_nph[q];
     if (r == 0 || nb == 0) continue;
     const int nkb = ceil_div(nb, BK);
+    const int blk = ceil_div(r, BM) * nkb;
     tc->cc_nkb[q] = nkb;
-    tc->cc_tile_L[q] = tiles;
-    tiles += ceil_div(r, BM) * nkb;
-    tc->cc_tile_R[q] = tiles;
-    tiles += ceil_div(r, BM) * nkb;
-    TcProb p{};
-    p.M = r; p.N = r; p.nkb = nkb; p.nterm = 2;
-    p.t[0] = TcTermDesc{tc->cc_tile_L[q], tc->cc_tile_R[q], hl};
-    p.t[1] = TcTermDesc{tc->cc_tile_R[q], tc->cc_tile_L[q], ng | hr};
-    p.out_f32 = 1; p.c_id = 0; p.c_off = l.wcc_off[q]; p.ldc = r;
-    tc->z_probs.push_back(p);
+    tc->cc_tile_L[q] = tiles; tiles += blk;
+    tc->cc_tile_R[q] = tiles; tiles += blk;
+    tc->cc_tile_Ls[q] = tiles; tiles += blk;
+    tc->cc_tile_Rs[q] = tiles; tiles += blk;
+    for (int which = 0; which < 2; ++which) {
+      TcProb p{};
+      p.M = r; p.N = r; p.nkb = nkb; p.nterm = 2;
+      const int aL = which ? tc->cc_tile_Ls[q] : tc->cc_tile_L[q];
+      const int aR = which ? tc->cc_tile_Rs[q] : tc->cc_tile_R[q];
+      p.t[0] = TcTermDesc{aL, tc->cc_tile_R[q], hl};
+      p.t[1] = TcTermDesc{aR, tc->cc_tile_L[q], ng | hr};
+      p.out_f32 = 1 + which;  // 1 -> Z, 2 -> Y
+      p.c_id = 0; p.c_off = l.wcc_off[q]; p.ldc = r;
+      tc->z_probs.push_back(p);
+    }
   }
   tc->z_tiles = make_tiles(tc->z_probs);
   tc->total_tiles = tiles;
@@ -714,6 +737,8 @@ imsrg_status Ctx::tc_prepare(int mode) {
   CK_TC(cuda(cudaMemset(tc->buf, 0, std::max<size_t>(bytes, 256)), "memset(tc operands)"));
   CK_TC(cuda(cudaMalloc(&tc->zbuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(Z)"));
   CK_TC(cuda(cudaMemset(tc->zbuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(Z)"));
+  CK_TC(cuda(cudaMalloc(&tc->ybuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(Y)"));
+  CK_TC(cuda(cudaMemset(tc->ybuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(Y)"));
   CK_TC(cuda(cudaMalloc(&tc->d_err, sizeof(int)), "cudaMalloc(err)"));
   CK_TC(cuda(cudaMalloc(&tc->d_ft, sizeof(float) * 4 * std::max<size_t>(l.same_list.size(), 1)), "cudaMalloc(ft)"));
   CK_TC(cuda(cudaMemset(tc->d_err, 0, sizeof(int)), "memset(err)"));
@@ -729,6 +754,9 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->cc_tile_L, &tc->d_cc_tile_L);
   pk.add(tc->cc_tile_R, &tc->d_cc_tile_R);
   pk.add(tc->cc_nkb, &tc->d_cc_nkb);
+  pk.add(tc->cc_tile_Ls, &tc->d_cc_tile_Ls);
+  pk.add(tc->cc_tile_Rs, &tc->d_cc_tile_Rs);
+  pk.add(tc->swap_row, &tc->d_swap_row);
   pk.add(tc->quads, &tc->d_quads);
   pk.add(tc->chunks, &tc->d_chunks);
   pk.add(tc->nb_start, &tc->d_nb_start);
@@ -823,8 +851,10 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   mark(kPhaseStart);
   if (ncc) {
     const int grid = (int)std::min<int64_t>((ncc + 255) / 256, 152 * 16);
-    launch_pandya_tc(tc->S, grid, stream, D, Rp, hR, tc->buf, tc->slice_elems, tc->d_cc_tile_R, tc->d_cc_nkb);
-    launch_pandya_tc(tc->S, grid, stream, D, Lp, hL, tc->buf, tc->slice_elems, tc->d_cc_tile_L, tc->d_cc_nkb);
+    launch_pandya_tc(tc->S, grid, stream, D, Rp, hR, tc->buf, tc->slice_elems, tc->d_cc_tile_R, tc->d_cc_tile_Rs,
+                     tc->d_cc_nkb, tc->d_swap_row);
+    launch_pandya_tc(tc->S, grid, stream, D, Lp, hL, tc->buf, tc->slice_elems, tc->d_cc_tile_L, tc->d_cc_tile_Ls,
+                     tc->d_cc_nkb, tc->d_swap_row);
     CK_TC(launched("k_pandya_tc"));
   }
   mark(kPhasePandya);
@@ -836,22 +866,27 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     k_ft122<<<(L.N + 127) / 128, 128, 0, stream>>>(D, Lp, hL, Rp, hR, tc->d_ft);
     CK_TC(launched("k_ft122"));
     const int grid = (int)std::min<int64_t>((L.n_unique + 255) / 256, 152 * 16);
-    k_comm122_nb<<<grid, 256, 0, stream>>>(D, tc->d_nb_start, tc->d_nb, tc->d_ft, Lp, hL, Rp, hR, RES, hRES);
+    k_comm122_nb<<<grid, 256, 0, stream>>>(D, tc->d_nb_start, tc->d_nb, tc->d_ft, Lp, hL, Rp, hR, RES, hRES, 0);
     CK_TC(launched("k_comm122_nb"));
   }
   mark(kPhase122);
-  CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2));
+  CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2, true));
   CK_TC(c221(hL, hR, RES, hRES, d_w1, d_w2, true));
   mark(kPhase221);
   TcOut zo{};
   zo.f32 = tc->zbuf;
+  zo.f32b = tc->ybuf;
   CK_TC(tc_gemm(tc->d_z_probs, tc->d_z_tiles, (int)tc->z_tiles.size(), zo, hL, hR));
   mark(kPhasePhGemm);
   if (!tc->quads.empty()) {
     const int64_t nq = (int64_t)tc->quads.size();
-    const int grid = (int)std::min<int64_t>((nq + 127) / 128, 152 * 32);
-    k_recouple_quad<<<grid, 128, 0, stream>>>(D, tc->d_quads, nq, tc->zbuf, RES, hRES);
-    CK_TC(launched("k_recouple_quad"));
+    const int grid = (int)std::min<int64_t>((nq + 255) / 256, 152 * 16);
+    k_recouple_y<<<grid, 256, 0, stream>>>(D, tc->d_quads, nq, tc->zbuf, tc->ybuf, RES, hL * hR);
+    CK_TC(launched("k_recouple_y"));
+  }
+  if (!upd_tiles.empty()) {
+    k_mirror_square<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, hRES);
+    CK_TC(launched("k_mirror_square"));
   }
   mark(kPhaseRecouple);
   return IMSRG_OK;

@@ -37,11 +37,17 @@ __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOp
 
 // mixed-precision companions (kernels_mixed.cu)
 void launch_pandya_tc(int S, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
-                      __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* nkb);
+                      __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s,
+                      const int* nkb, const int* swap_row);
 __global__ void k_comm122f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
 __global__ void k_ft122(DevLayout D, const double* L, int hL, const double* R, int hR, float* ft);
 __global__ void k_comm122_nb(DevLayout D, const int* nb_start, const NbEntry* nb, const float* ft, const double* L,
-                             int hL, const double* R, int hR, double* RES, int hRES);
+                             int hL, const double* R, int hR, double* RES, int hRES, int mirror);
+__global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
+                                float pm);
+__global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);
+__global__ void k_recouple_y(DevLayout D, const uint64_t* quads, int64_t nquads, const float* Z, const float* Y,
+                             double* RES, int pm);
 __global__ void k_comm222ph_z(DevLayout D, const float* Z, double* RES, int hRES);
 __global__ void k_recouple_quad(DevLayout D, const uint64_t* quads, int64_t nquads, const float* Z, double* RES, int hRES);
 

@@ -19,9 +19,12 @@ __device__ __forceinline__ float d_sixjf(const DevLayout& D, int j1, int j2, int
 // written straight into the K-major split-BF16 operand tiles of the cross-coupled GEMM:
 // row r of the tile block of channel q, column ph.  Threads run along ph so the writes
 // into each 128-byte tile row are contiguous.
+// Each element is written twice: at row r of the operand tiles and at row s(r) of the
+// row-swapped copy, s(r(a,b)) = r(b,a), which feeds the row-swapped product Y.
 template <int S>
 __global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm, __nv_bfloat16* __restrict__ buf,
-                            int64_t slice_elems, const int* __restrict__ tile_base, const int* __restrict__ nkb) {
+                            int64_t slice_elems, const int* __restrict__ tile_base, const int* __restrict__ tile_base_s,
+                            const int* __restrict__ nkb, const int* __restrict__ swap_row) {
   const int64_t total = D.cc_size;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = D.ncc;
@@ -51,23 +54,28 @@ __global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm
       }
       val = sm * (((jh + jb + JC) & 2) ? -1.0f : 1.0f) * sqrtf((float)(JC + 1));
     }
+    const int rs = swap_row[D.cc_row_off[q] + r];
     const int64_t dst =
         ((int64_t)(tile_base[q] + (r >> 7) * nkb[q] + (nbx >> 6)) * 128 + (r & 127)) * 64 + (nbx & 63);
+    const int64_t dsts =
+        ((int64_t)(tile_base_s[q] + (rs >> 7) * nkb[q] + (nbx >> 6)) * 128 + (rs & 127)) * 64 + (nbx & 63);
     float rem = val;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const __nv_bfloat16 hv = __float2bfloat16_rn(rem);
       buf[s * slice_elems + dst] = hv;
+      buf[s * slice_elems + dsts] = hv;
       rem -= __bfloat162float(hv);
     }
   }
 }
 void launch_pandya_tc(int S, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
-                      __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* nkb) {
+                      __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s,
+                      const int* nkb, const int* swap_row) {
   if (S == 2)
-    k_pandya_tc<2><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, nkb);
+    k_pandya_tc<2><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s, nkb, swap_row);
   else
-    k_pandya_tc<3><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, nkb);
+    k_pandya_tc<3><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s, nkb, swap_row);
 }
 
 // commutator_122 (src/commutators.f90:283-396), FP32 arithmetic -- ASSIGNS every 2b element
@@ -170,7 +178,7 @@ __global__ void k_ft122(DevLayout D, const double* __restrict__ L, int hL, const
 // the c- and d-replaced terms.  FP32 arithmetic, ASSIGNS every 2b element.
 __global__ void k_comm122_nb(DevLayout D, const int* __restrict__ nb_start, const NbEntry* __restrict__ nb,
                              const float* __restrict__ ft, const double* __restrict__ L, int hL,
-                             const double* __restrict__ R, int hR, double* __restrict__ RES, int hRES) {
+                             const double* __restrict__ R, int hR, double* __restrict__ RES, int hRES, int mirror) {
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < D.n_unique; u += (int64_t)gridDim.x * blockDim.x) {
     int q, g, IX, JX;
     d_unique_decode(D, u, q, g, IX, JX);
@@ -230,8 +238,75 @@ __global__ void k_comm122_nb(DevLayout D, const int* __restrict__ nb_start, cons
     const int k = q * 6 + g;
     double* X = RES + D.goff[k];
     const int n1 = D.gn1[k];
-    X[IX + (int64_t)JX * n1] = (double)sm;
-    if (g == 0 || g == 3 || g == 4) X[JX + (int64_t)IX * n1] = (double)sm * hRES;
+    X[IX + (int64_t)JX * n1] = f32_to_f64(sm);
+    if (mirror && (g == 0 || g == 3 || g == 4)) X[JX + (int64_t)IX * n1] = f32_to_f64(hRES < 0 ? -sm : sm);
+  }
+}
+
+// 222_pp_hh accumulation for the mixed path: FP32 arithmetic, upper triangles of the
+// square arrays only (a final mirror pass restores the lower triangles).
+__global__ void __launch_bounds__(256) k_pphh_update_f(DevLayout D, const int4* __restrict__ tiles,
+                                                       double* __restrict__ RES, const double* __restrict__ w1,
+                                                       const double* __restrict__ w2, float pm) {
+  __shared__ float Xa[32][33];
+  __shared__ float Xb[32][33];
+  const int4 t = tiles[blockIdx.x];
+  const int k = t.x, i0 = t.y, j0 = t.z;
+  const int64_t base = D.goff[k];
+  const int n1 = D.gn1[k], n2 = D.gn2[k];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  if (!t.w) {
+    for (int r = ty; r < 32; r += 8) {
+      const int i = i0 + tx, j = j0 + r;
+      if (i < n1 && j < n2) {
+        const int64_t e = base + i + (int64_t)j * n1;
+        RES[e] = f32_to_f64(f64_to_f32(RES[e]) + (f64_to_f32(w1[e]) - f64_to_f32(w2[e])));
+      }
+    }
+    return;
+  }
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, j = j0 + r;
+    Xa[r][tx] = (i < n1 && j < n1) ? f64_to_f32(w1[base + i + (int64_t)j * n1]) - f64_to_f32(w2[base + i + (int64_t)j * n1])
+                                   : 0.0f;
+    const int ib = j0 + tx, jb = i0 + r;
+    Xb[r][tx] = (ib < n1 && jb < n1) ? f64_to_f32(w1[base + ib + (int64_t)jb * n1]) -
+                                           f64_to_f32(w2[base + ib + (int64_t)jb * n1])
+                                     : 0.0f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, j = j0 + r;
+    if (i < n1 && j < n1 && i <= j) {
+      const int64_t e = base + i + (int64_t)j * n1;
+      RES[e] = f32_to_f64(f64_to_f32(RES[e]) + (Xa[r][tx] - Xb[tx][r] * pm));
+    }
+  }
+}
+
+// lower triangle of every square array (pppp, phph, hhhh) = herm * upper triangle
+__global__ void __launch_bounds__(256) k_mirror_square(DevLayout D, const int4* __restrict__ tiles,
+                                                       double* __restrict__ RES, int herm) {
+  __shared__ double T[32][33];
+  const int4 t = tiles[blockIdx.x];
+  if (!t.w) return;
+  const int k = t.x, i0 = t.y, j0 = t.z;  // i0 <= j0: source tile (upper), destination (j0, i0)
+  const int64_t base = D.goff[k];
+  const int n1 = D.gn1[k];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const unsigned long long flip = herm < 0 ? (1ull << 63) : 0ull;
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, j = j0 + r;
+    T[r][tx] = (i < n1 && j < n1) ? RES[base + i + (int64_t)j * n1] : 0.0;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    // destination element (j0 + tx, i0 + r) = herm * source (i0 + r, j0 + tx) = T[tx][r]
+    const int i = j0 + tx, j = i0 + r;
+    if (i < n1 && j < n1 && i > j) {
+      const double v = T[tx][r];
+      RES[base + i + (int64_t)j * n1] = __longlong_as_double(__double_as_longlong(v) ^ (long long)flip);
+    }
   }
 }
 
@@ -379,6 +454,95 @@ __global__ void k_recouple_quad(DevLayout D, const uint64_t* __restrict__ quads,
       const double nv = X[IX + (int64_t)JX * n1] + (double)(sm * pre);
       X[IX + (int64_t)JX * n1] = nv;
       if (square) X[JX + (int64_t)IX * n1] = nv * hRES;
+    }
+  }
+}
+
+// Recoupling with the row-swapped copy Y(r(a,b), c) = Z(r(b,a), c).  Using the
+// antisymmetry Z(x,y) = -pm Z(y,x), the four reads per J' become
+//   direct   : -pm Y[(l,j),(k,i)] + phase Z[(l,j),(i,k)]
+//   exchange : -pm Y[(k,j),(l,i)] + phase Z[(k,j),(i,l)]
+// whose rows advance with j; quadruples are ordered j fastest and the J' and J loops are
+// warp-uniform, so each warp reads consecutive rows of one channel matrix and writes
+// consecutive rows of one RES column.  Upper triangles only (mirror pass afterwards).
+__global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t* __restrict__ quads, int64_t nquads,
+                                                    const float* __restrict__ Z, const float* __restrict__ Y,
+                                                    double* __restrict__ RES, int pm) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int N = D.N, NJ = D.NJ, JM = D.JM;
+  const float fpm = (float)pm;
+  for (int64_t w = gw; w * 32 < nquads; w += nw) {
+    const int64_t t = w * 32 + lane;
+    const bool act = t < nquads;
+    const uint64_t qd = act ? quads[t] : 0ull;
+    const int i = (int)(qd & 0xFFFF), j = (int)((qd >> 16) & 0xFFFF), k = (int)((qd >> 32) & 0xFFFF),
+              l = (int)((qd >> 48) & 0xFFFF);
+    const int ji = D.jj[i], jj = D.jj[j], jk = D.jj[k], jl = D.jj[l];
+    const float phase = ((ji + jj + jk + jl) & 2) ? -1.0f : 1.0f;
+    const int dlo = act ? max(abs(jj - jl), abs(ji - jk)) : 1 << 20, dhi = act ? min(jj + jl, ji + jk) : -1;
+    const int elo = act ? max(abs(ji - jl), abs(jj - jk)) : 1 << 20, ehi = act ? min(ji + jl, jj + jk) : -1;
+    float zd[kMaxJp], ze[kMaxJp];
+    {
+      const int Tz = abs(D.tz[i] - D.tz[k]) >> 1, PAR = (D.ll[i] + D.ll[k]) & 1;
+      const int wlo = __reduce_min_sync(0xffffffffu, dlo), whi = __reduce_max_sync(0xffffffffu, dhi);
+      for (int JP = wlo; JP <= whi; JP += 2) {
+        if (JP < dlo || JP > dhi) continue;
+        const int qx = (JP >> 1) + Tz * (JM + 1) + PAR * 2 * (JM + 1);
+        const int64_t off = D.wcc_off[qx];
+        const int64_t rl = D.cc_rlen[qx];
+        const int h = JP >> 1;
+        const int64_t rlj = D.ccr[(l * N + j) * NJ + h], rki = D.ccr[(k * N + i) * NJ + h];
+        const int64_t rik = D.ccr[(i * N + k) * NJ + h];
+        zd[(JP - dlo) >> 1] = -fpm * Y[off + rlj + rki * rl] + phase * Z[off + rlj + rik * rl];
+      }
+    }
+    {
+      const int Tz = abs(D.tz[i] - D.tz[l]) >> 1, PAR = (D.ll[i] + D.ll[l]) & 1;
+      const int wlo = __reduce_min_sync(0xffffffffu, elo), whi = __reduce_max_sync(0xffffffffu, ehi);
+      for (int JP = wlo; JP <= whi; JP += 2) {
+        if (JP < elo || JP > ehi) continue;
+        const int qx = (JP >> 1) + Tz * (JM + 1) + PAR * 2 * (JM + 1);
+        const int64_t off = D.wcc_off[qx];
+        const int64_t rl = D.cc_rlen[qx];
+        const int h = JP >> 1;
+        const int64_t rkj = D.ccr[(k * N + j) * NJ + h], rli = D.ccr[(l * N + i) * NJ + h];
+        const int64_t ril = D.ccr[(i * N + l) * NJ + h];
+        ze[(JP - elo) >> 1] = -fpm * Y[off + rkj + rli * rl] + phase * Z[off + rkj + ril * rl];
+      }
+    }
+    const int nh = D.sj_nh;
+    const int kd = (((ji >> 1) * nh + (jj >> 1)) * nh + (jl >> 1)) * nh + (jk >> 1);
+    const int ke = (((ji >> 1) * nh + (jj >> 1)) * nh + (jk >> 1)) * nh + (jl >> 1);
+    const float* sjd = D.sj_valf + D.sj_off[kd];
+    const float* sje = D.sj_valf + D.sj_off[ke];
+    const int d3 = D.sj_j3min[kd], d6 = D.sj_j6min[kd], dn6 = D.sj_n6[kd];
+    const int e3 = D.sj_j3min[ke], e6 = D.sj_j6min[ke], en6 = D.sj_n6[ke];
+    const int C1 = D.con[i] + D.con[j], C2 = D.con[k] + D.con[l];
+    const int g = (C1 == 0) ? C2 : (C1 == 1 ? (C2 == 1 ? 3 : 5) : 4);
+    const int T = D.tz[i] + D.tz[j], P = (D.ll[i] + D.ll[j]) & 1;
+    const float pre = ((i == j) ? .70710678118f : 1.0f) * ((k == l) ? .70710678118f : 1.0f);
+    const int Jlo = act ? max(abs(ji - jj), abs(jk - jl)) : 1 << 20, Jhi = act ? min(ji + jj, jk + jl) : -1;
+    const int wJlo = __reduce_min_sync(0xffffffffu, Jlo), wJhi = __reduce_max_sync(0xffffffffu, Jhi);
+    const int nd = (dhi - dlo) / 2 + 1, ne = (ehi - elo) / 2 + 1;
+    for (int J = wJlo; J <= wJhi; J += 2) {
+      if (J < Jlo || J > Jhi) continue;
+      float sd = 0.0f, se = 0.0f;
+      {
+        const float* row = sjd + ((J - d3) >> 1) * dn6 + ((dlo - d6) >> 1);
+        for (int m = 0; m < nd; ++m) sd += row[m] * zd[m];
+      }
+      {
+        const float* row = sje + ((J - e3) >> 1) * en6 + ((elo - e6) >> 1);
+        for (int m = 0; m < ne; ++m) se += row[m] * ze[m];
+      }
+      const float sm = (-(((jl + jk + J) & 2) ? -1.0f : 1.0f) * sd + se) * pre;
+      const int q = 3 * J + (T + 2) + P;
+      const int kk = q * 6 + g;
+      const int IX = D.pairpos[(i * N + j) * NJ + (J >> 1)], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
+      double* X = RES + D.goff[kk] + IX + (int64_t)JX * D.gn1[kk];
+      *X = f32_to_f64(f64_to_f32(*X) + sm);
     }
   }
 }

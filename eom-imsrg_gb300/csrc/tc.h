@@ -50,7 +50,8 @@ struct SplitChunk {
 
 struct TcOut {
   double* f64[8];
-  float* f32;
+  float* f32;   // out_f32 == 1
+  float* f32b;  // out_f32 == 2
 };
 
 }  // namespace imsrg
