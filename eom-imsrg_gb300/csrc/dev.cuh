@@ -44,6 +44,8 @@ struct DevLayout {
   const int16_t* cc_cp;
   const int16_t* cc_ch;
   const int* ccr;       // [(a*N+b)*NJ+JC/2]
+  const int* ccr_t;     // same table, [(a*NJ+JC/2)*N+b]: consecutive b adjacent
+  const int* pairpos_t; // pairpos as [(a*NJ+J/2)*N+b]
   // one-body output list
   const int* ob_kind;
   const int* ob_p;

@@ -104,6 +104,16 @@ imsrg_status Ctx::upload_tables() {
   pk.add(l.cc_row_off, &d.cc_row_off); pk.add(l.cc_col_off, &d.cc_col_off);
   pk.add(l.cc_ra, &d.cc_ra); pk.add(l.cc_rb, &d.cc_rb); pk.add(l.cc_cp, &d.cc_cp); pk.add(l.cc_ch, &d.cc_ch);
   pk.add(l.ccr, &d.ccr);
+  // transposed copies (b fastest) for warps whose lanes vary the second orbit
+  std::vector<int> ccr_t(l.ccr.size()), ppos_t(l.pairpos.size());
+  for (int a = 0; a < l.N; ++a)
+    for (int b = 0; b < l.N; ++b)
+      for (int h = 0; h < l.NJ; ++h) {
+        ccr_t[((size_t)a * l.NJ + h) * l.N + b] = l.ccr[((size_t)a * l.N + b) * l.NJ + h];
+        ppos_t[((size_t)a * l.NJ + h) * l.N + b] = l.pairpos[((size_t)a * l.N + b) * l.NJ + h];
+      }
+  pk.add(ccr_t, &d.ccr_t);
+  pk.add(ppos_t, &d.pairpos_t);
   pk.add(l.ob_kind, &d.ob_kind); pk.add(l.ob_p, &d.ob_p); pk.add(l.ob_q, &d.ob_q);
   pk.add(l.ob_pk, &d.ob_pk); pk.add(l.ob_qk, &d.ob_qk);
   pk.add(l.ai_a, &d.ai_a); pk.add(l.ai_i, &d.ai_i);

@@ -30,7 +30,7 @@ namespace {
 
 constexpr int BM = 128, BN = 128, BK = 64;
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KiB, identical for A and B tiles
-constexpr int NUM_THREADS = 192;
+constexpr int NUM_THREADS = 320;  // TMA warp, MMA warp, 8 epilogue warps
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     for (int a = 0; a < 2; ++a) {
       mbar_init(&tfull[a], 1);
-      mbar_init(&tempty[a], 4);
+      mbar_init(&tempty[a], 8);
     }
     *abort_flag = 0;
     *consumed = 0;
@@ -275,8 +275,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
     }
   } else {
-    // ------------------------------------------------------------ epilogue (warps 2..5)
-    const int quad = warp & 3;  // TMEM lanes 32*quad .. 32*quad+31
+    // ------------------------------------------------------------ epilogue (warps 2..9)
+    const int quad = warp & 3;          // TMEM lanes 32*quad .. 32*quad+31
+    const int half = (warp - 2) >> 2;   // accumulator columns 64*half .. 64*half+63
     int local = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++local) {
       const TcTile tile = tiles[t];
@@ -285,7 +286,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (!mbar_wait(&tfull[acc], (local >> 1) & 1, abort_flag, err, 4)) break;
       tc_fence_after();
       const int m = tile.m0 + quad * 32 + lane;
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
         uint32_t r[32];
         tmem_ld32(tmem_base + (uint32_t)(acc * BN + c0) + ((uint32_t)(quad * 32) << 16), r);
         if (m < P.M) {
@@ -495,6 +496,9 @@ struct TcState {
   const int* d_nb_start = nullptr;
   const NbEntry* d_nb = nullptr;
   float* d_ft = nullptr;
+  float4* d_coef = nullptr;
+  std::vector<int4> u_chunks;  // 122 work: (array, first unique element, count, 0)
+  const int4* d_u_chunks = nullptr;
   int num_sms = 148;
 };
 
@@ -541,6 +545,7 @@ void Ctx::tc_release() {
   if (tc->ybuf) cudaFree(tc->ybuf);
   if (tc->d_err) cudaFree(tc->d_err);
   if (tc->d_ft) cudaFree(tc->d_ft);
+  if (tc->d_coef) cudaFree(tc->d_coef);
   delete tc;
   tc = nullptr;
 }
@@ -701,6 +706,11 @@ imsrg_status Ctx::tc_prepare(int mode) {
         }
     }
     tc->nb_start[npairs] = (int)tc->nb.size();
+    for (int k = 0; k < l.nblocks * 6; ++k) {
+      const int64_t n = l.uoff[k + 1] - l.uoff[k];
+      for (int64_t e0 = 0; e0 < n; e0 += 2048)
+        tc->u_chunks.push_back(make_int4(k, (int)e0, (int)std::min<int64_t>(2048, n - e0), 0));
+    }
   }
   // ---- recoupling quadruples: bra (i<=j) of class c1, ket (k<=l) of class c2, with
   //      c1 < c2, or c1 == c2 and (i,j) <= (k,l) (the unique stored elements), matching
@@ -741,6 +751,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   CK_TC(cuda(cudaMemset(tc->ybuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(Y)"));
   CK_TC(cuda(cudaMalloc(&tc->d_err, sizeof(int)), "cudaMalloc(err)"));
   CK_TC(cuda(cudaMalloc(&tc->d_ft, sizeof(float) * 4 * std::max<size_t>(l.same_list.size(), 1)), "cudaMalloc(ft)"));
+  CK_TC(cuda(cudaMalloc(&tc->d_coef, sizeof(float4) * std::max<size_t>(tc->nb.size(), 1)), "cudaMalloc(coef)"));
   CK_TC(cuda(cudaMemset(tc->d_err, 0, sizeof(int)), "memset(err)"));
   DevPacker pk;
   pk.add(tc->split_ops, &tc->d_split_ops);
@@ -761,6 +772,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->chunks, &tc->d_chunks);
   pk.add(tc->nb_start, &tc->d_nb_start);
   pk.add(tc->nb, &tc->d_nb);
+  pk.add(tc->u_chunks, &tc->d_u_chunks);
   CK_TC(cuda(cudaMalloc(&tc->d_mem, pk.buf.size()), "cudaMalloc(tc tables)"));
   CK_TC(cuda(cudaMemcpy(tc->d_mem, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tc tables)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(tc->d_mem) + f.first;
@@ -865,9 +877,12 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   if (L.n_unique) {
     k_ft122<<<(L.N + 127) / 128, 128, 0, stream>>>(D, Lp, hL, Rp, hR, tc->d_ft);
     CK_TC(launched("k_ft122"));
-    const int grid = (int)std::min<int64_t>((L.n_unique + 255) / 256, 152 * 16);
-    k_comm122_nb<<<grid, 256, 0, stream>>>(D, tc->d_nb_start, tc->d_nb, tc->d_ft, Lp, hL, Rp, hR, RES, hRES, 0);
-    CK_TC(launched("k_comm122_nb"));
+    const int nnb = (int)tc->nb.size();
+    k_coef122<<<(nnb + 255) / 256, 256, 0, stream>>>(tc->d_nb, nnb, tc->d_ft, tc->d_coef);
+    CK_TC(launched("k_coef122"));
+    k_comm122_chunks<<<(int)tc->u_chunks.size(), 256, 0, stream>>>(D, tc->d_u_chunks, tc->d_nb_start, tc->d_nb,
+                                                                   tc->d_coef, Lp, hL, Rp, hR, RES);
+    CK_TC(launched("k_comm122_chunks"));
   }
   mark(kPhase122);
   CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2, true));

@@ -43,6 +43,9 @@ __global__ void k_comm122f(DevLayout D, const double* L, int hL, const double* R
 __global__ void k_ft122(DevLayout D, const double* L, int hL, const double* R, int hR, float* ft);
 __global__ void k_comm122_nb(DevLayout D, const int* nb_start, const NbEntry* nb, const float* ft, const double* L,
                              int hL, const double* R, int hR, double* RES, int hRES, int mirror);
+__global__ void k_coef122(const NbEntry* nb, int n, const float* ft, float4* coef);
+__global__ void k_comm122_chunks(DevLayout D, const int4* chunks, const int* nb_start, const NbEntry* nb,
+                                 const float4* coef, const double* L, int hL, const double* R, int hR, double* RES);
 __global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
                                 float pm);
 __global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);

@@ -173,6 +173,99 @@ __global__ void k_ft122(DevLayout D, const double* __restrict__ L, int hL, const
   }
 }
 
+// Per-call coefficients of the 122 neighbour entries: the one-body element times the
+// entry's swap phase / sqrt(2): (bra fL, bra fR, ket fL, ket fR)
+__global__ void k_coef122(const NbEntry* __restrict__ nb, int n, const float* __restrict__ ft,
+                          float4* __restrict__ coef) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const NbEntry x = nb[e];
+  float s = (x.flags & 4) ? 1.41421356f : 1.0f;
+  if (x.flags & 2) s = -s;
+  const float4 f = *reinterpret_cast<const float4*>(ft + 4 * x.fkey);
+  coef[e] = make_float4(f.x * s, f.y * s, -f.z * s, -f.w * s);
+}
+
+// commutator_122 over a chunk list (one block = a run of unique elements of one array,
+// no search), with premultiplied neighbour coefficients.  FP32, ASSIGNS, upper triangle.
+__global__ void __launch_bounds__(256) k_comm122_chunks(DevLayout D, const int4* __restrict__ chunks,
+                                                        const int* __restrict__ nb_start,
+                                                        const NbEntry* __restrict__ nb, const float4* __restrict__ coef,
+                                                        const double* __restrict__ L, int hL,
+                                                        const double* __restrict__ R, int hR,
+                                                        double* __restrict__ RES) {
+  const int4 ch = chunks[blockIdx.x];  // (array k, first local element, count, 0)
+  const int k = ch.x;
+  const int q = k / 6, g = k - q * 6;
+  const bool square = (g == 0 || g == 3 || g == 4);
+  const int c1 = (g < 3) ? 0 : (g == 4 ? 2 : 1);
+  const int c2 = (g == 0) ? 0 : ((g == 1 || g == 3) ? 1 : 2);
+  const int n1 = D.gn1[k];
+  const int64_t* go = D.goff + q * 6;
+  const int* gn = D.gn1 + q * 6;
+  const int po1 = D.pair_off[q * 3 + c1], po2 = D.pair_off[q * 3 + c2];
+  const bool hLn = hL < 0, hRn = hR < 0;
+  for (int t = threadIdx.x; t < ch.z; t += blockDim.x) {
+    const int64_t e = (int64_t)ch.y + t;
+    int IX, JX;
+    if (square) {
+      int j = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+      while ((int64_t)(j + 1) * (j + 2) / 2 <= e) ++j;
+      while ((int64_t)j * (j + 1) / 2 > e) --j;
+      JX = j;
+      IX = (int)(e - (int64_t)j * (j + 1) / 2);
+    } else {
+      JX = (int)(e / n1);
+      IX = (int)(e - (int64_t)JX * n1);
+    }
+    const int o1 = po1 + IX, o2 = po2 + JX;
+    float bra = 0.0f, ket = 0.0f;
+    for (int x = nb_start[o1], xe = nb_start[o1 + 1]; x < xe; ++x) {
+      const NbEntry n = nb[x];
+      const float4 cf = coef[x];
+      const int ct = n.cls;
+      int64_t idx;
+      bool tr;
+      if (ct <= c2) {
+        const int gg = (ct == 0) ? c2 : (ct == 1 ? (c2 == 1 ? 3 : 5) : 4);
+        idx = go[gg] + n.pos + (int64_t)JX * gn[gg];
+        tr = false;
+      } else {
+        const int gg = (c2 == 0) ? ct : (c2 == 1 ? (ct == 1 ? 3 : 5) : 4);
+        idx = go[gg] + JX + (int64_t)n.pos * gn[gg];
+        tr = true;
+      }
+      float vR = f64_to_f32(R[idx]), vL = f64_to_f32(L[idx]);
+      if (tr && hRn) vR = -vR;
+      if (tr && hLn) vL = -vL;
+      bra += cf.x * vR - cf.y * vL;
+    }
+    for (int x = nb_start[o2], xe = nb_start[o2 + 1]; x < xe; ++x) {
+      const NbEntry n = nb[x];
+      const float4 cf = coef[x];
+      const int ct = n.cls;
+      int64_t idx;
+      bool tr;
+      if (c1 <= ct) {
+        const int gg = (c1 == 0) ? ct : (c1 == 1 ? (ct == 1 ? 3 : 5) : 4);
+        idx = go[gg] + IX + (int64_t)n.pos * gn[gg];
+        tr = false;
+      } else {
+        const int gg = (ct == 0) ? c1 : (ct == 1 ? (c1 == 1 ? 3 : 5) : 4);
+        idx = go[gg] + n.pos + (int64_t)IX * gn[gg];
+        tr = true;
+      }
+      float vR = f64_to_f32(R[idx]), vL = f64_to_f32(L[idx]);
+      if (tr && hRn) vR = -vR;
+      if (tr && hLn) vL = -vL;
+      ket += cf.z * vR - cf.w * vL;
+    }
+    const int a = D.pair_a[o1], b = D.pair_b[o1], c = D.pair_a[o2], d = D.pair_b[o2];
+    const float sm = bra * ((a == b) ? 0.70710678f : 1.0f) + ket * ((c == d) ? 0.70710678f : 1.0f);
+    RES[D.goff[k] + IX + (int64_t)JX * n1] = f32_to_f64(sm);
+  }
+}
+
 // commutator_122 (src/commutators.f90:283-396) with precomputed neighbour lists:
 // bra neighbours of pair IX give the a- and b-replaced terms, ket neighbours of pair JX
 // the c- and d-replaced terms.  FP32 arithmetic, ASSIGNS every 2b element.
@@ -493,7 +586,7 @@ __global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t*
         const int64_t off = D.wcc_off[qx];
         const int64_t rl = D.cc_rlen[qx];
         const int h = JP >> 1;
-        const int64_t rlj = D.ccr[(l * N + j) * NJ + h], rki = D.ccr[(k * N + i) * NJ + h];
+        const int64_t rlj = D.ccr_t[(l * NJ + h) * N + j], rki = D.ccr[(k * N + i) * NJ + h];
         const int64_t rik = D.ccr[(i * N + k) * NJ + h];
         zd[(JP - dlo) >> 1] = -fpm * Y[off + rlj + rki * rl] + phase * Z[off + rlj + rik * rl];
       }
@@ -507,7 +600,7 @@ __global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t*
         const int64_t off = D.wcc_off[qx];
         const int64_t rl = D.cc_rlen[qx];
         const int h = JP >> 1;
-        const int64_t rkj = D.ccr[(k * N + j) * NJ + h], rli = D.ccr[(l * N + i) * NJ + h];
+        const int64_t rkj = D.ccr_t[(k * NJ + h) * N + j], rli = D.ccr[(l * N + i) * NJ + h];
         const int64_t ril = D.ccr[(i * N + l) * NJ + h];
         ze[(JP - elo) >> 1] = -fpm * Y[off + rkj + rli * rl] + phase * Z[off + rkj + ril * rl];
       }
@@ -540,7 +633,7 @@ __global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t*
       const float sm = (-(((jl + jk + J) & 2) ? -1.0f : 1.0f) * sd + se) * pre;
       const int q = 3 * J + (T + 2) + P;
       const int kk = q * 6 + g;
-      const int IX = D.pairpos[(i * N + j) * NJ + (J >> 1)], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
+      const int IX = D.pairpos_t[(i * NJ + (J >> 1)) * N + j], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
       double* X = RES + D.goff[kk] + IX + (int64_t)JX * D.gn1[kk];
       *X = f32_to_f64(f64_to_f32(*X) + sm);
     }
