@@ -86,6 +86,7 @@ SIGNATURES = {
     "imsrg_timer_end": [_vp, C.POINTER(C.c_float)],
     "imsrg_profile_phases": [_vp, _i32],
     "imsrg_profile_read": [_vp, C.POINTER(C.c_float), _pi32],
+    "imsrg_mat_frob_norm_noalloc": [_vp, _vp, _vp, _vp],
 }
 PHASES = ["start", "pandya", "one_body", "c122", "pphh_split", "pphh_gemm", "pphh_small", "pphh_update", "c221",
           "ph_gemm", "recouple"]

@@ -126,6 +126,22 @@ imsrg_status imsrg_scale_sq_op(imsrg_ctx* ctx, imsrg_op* A, double ax);         
 imsrg_status imsrg_mat_frob_norm(imsrg_ctx* ctx, const imsrg_op* op, double* out);                    /* :4056 */
 imsrg_status imsrg_mbpt2(imsrg_ctx* ctx, const imsrg_op* H, double* out);                             /* :4165 */
 
+/* Frobenius norm for callers that cannot allocate GPU memory.  No counterpart in the
+ * reference.  Same value as imsrg_mat_frob_norm, but for code that must not call
+ * cudaMalloc when it needs the norm (an allocator that owns all device memory, a
+ * callback or pool that forbids new allocations, a host driver that only passes its own
+ * buffers): the call allocates nothing and frees nothing.  dev_slab is any device sq_op
+ * slab of this context's layout, dev_out one device double, stream a cudaStream_t
+ * (NULL = legacy default stream); the call is asynchronous on that stream.
+ * Scratch is one static device array of IMSRG_NOALLOC_MAX_SEGMENTS doubles (64 KiB) that
+ * every GPU loading the library keeps until exit; operators with more norm segments
+ * (one per 65536 elements of each array) get IMSRG_ERR_UNSUPPORTED.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU
+ * (different streams, no ordering between them) race on it. */
+#define IMSRG_NOALLOC_MAX_SEGMENTS 8192
+imsrg_status imsrg_mat_frob_norm_noalloc(imsrg_ctx* ctx, const double* dev_slab, double* dev_out, void* stream);
+
 /* ---- cross-coupled matrices: type(cc_mat) (src/cross_coupled.f90:11-15)
  * kind 0 = CCX storage (rlen x nph per block, init_ph_mat), kind 1 = WCC workspace
  * (rlen x rlen per block, init_ph_wkspc / allocate_CC_wkspc :1075-1096) */
