@@ -1,16 +1,19 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 IMSRG(2) commutator engine.
 
-Workload (one "step"): one full two-body-truncated commutator [eta, H] at eMax=10
-(132 j-orbits, 16O-like reference, 132 (J,parity,Tz) channels, 88 cross-coupled
-channels), eta the White generator of a seeded synthetic Hamiltonian -- the unit of
-the reference's Magnus/BCH loop (src/IMSRG_MAGNUS.f90:207-219).
+Workload: the Magnus flow of a seeded synthetic Hamiltonian at eMax=10 (132 j-orbits,
+16O-like reference, 132 (J,parity,Tz) channels, 88 cross-coupled channels) with the White
+generator.  One "step" is one Magnus step of magnus_decouple (src/IMSRG_MAGNUS.f90:47-110):
+MAGNUS_EXPAND, euler_step, BCH_EXPAND truncated at 10 nested commutators or a term norm
+below 1e-8, the generator and MBPT(2) -- replayed from one CUDA graph.  The metric counts
+the full two-body-truncated commutators [X, Y] those steps execute (counted on the device).
 
-Prints one JSON line.  `value` is mixed-precision (split-BF16 tcgen05) commutators/s
-with operators resident in HBM; `e2e` is the same metric through the C ABI with the
-operators uploaded from / downloaded to pinned host memory every step.  With
---impl reference the CPU restatement of the reference algorithm (FP64, OpenMP on all
-host cores, BLAS dgemm) is timed on the same workload instead.
+Prints one JSON line.  `value`: mixed-precision (split-BF16 tcgen05) commutators/s with
+the operators resident in HBM.  `e2e`: the same metric with the flow's operators kept in
+pinned host memory and copied in and out around every imsrg_magnus_step call.  The plain
+FP64 GPU path runs the same steps for the speed-up and the |dE0| / ||dH(s)|| comparison.
+With --impl reference the CPU restatement of the reference algorithm (FP64, OpenMP on all
+host cores, BLAS dgemm) is timed on the same commutators instead.
 """
 from __future__ import annotations
 
@@ -70,9 +73,11 @@ def allreduce_sum(pg, x: float) -> float:
 
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi sampled every 100 ms in the background; stop() keeps the samples inside [t0, t1]."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
     def __init__(self, gpu: int):
         self.gpu = gpu
@@ -83,35 +88,46 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
-    def stop(self) -> dict:
+    @staticmethod
+    def _stamp(s: str) -> float:
+        import datetime
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+            try:
+                return datetime.datetime.strptime(s, fmt).timestamp()
+            except ValueError:
+                pass
+        return float("nan")
+
+    def stop(self, t0: float, t1: float) -> dict:
+        """Summary of the samples taken between wall-clock times t0 and t1 (time.time())."""
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in open(self.path):
             p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sm.append(float(p[1]))
-                smax.append(float(p[2]))
+                rows.append((self._stamp(p[0]), float(p[2]), float(p[3]), p[6:10]))
             except ValueError:
                 continue
-            for k, v in zip(names, p[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(k)
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        inside = [r for r in rows if t0 - 0.05 <= r[0] <= t1 + 0.05]
+        sm = [r[1] for r in inside]
+        reasons = sorted({k for r in inside for k, v in zip(self.NAMES, r[3]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(r[2] for r in rows) if rows else None,
+                "reasons": reasons, "samples": len(sm), "window_s": round(t1 - t0, 3)}
 
 
 # ---------------------------------------------------------------- CPU side
@@ -166,7 +182,12 @@ def cpu_commutators(emax: int, n_warm: int, n_steps: int, seed: int = 1):
 
 # ---------------------------------------------------------------- roofline bookkeeping
 def algorithmic_work(eng, mode: str, phase: str):
-    """Algorithmic bytes (or FLOPs) of one launch of a phase at this basis."""
+    """Algorithmic bytes (or FLOPs) of one launch of a phase at this basis.
+
+    Bytes count each array the phase must touch once: FP64 operators (8 B), the FP32
+    particle-hole products Z and Y (4 B each, wcc_size elements), the split-BF16 operand
+    slices (2 B per slice).  FLOPs are 2 M N K of the reference's dgemm calls times the
+    number of slice products."""
     S = {"bf16x3": 3, "bf16x6": 6, "fp64": 1}[mode]          # slice products per GEMM
     slices = {"bf16x3": 2, "bf16x6": 3, "fp64": 1}[mode]
     info = eng.block_info()
@@ -174,12 +195,12 @@ def algorithmic_work(eng, mode: str, phase: str):
     P = eng.basis.norbits - A
     n2b = eng.slab - (1 + A * A + P * P + P * A)
     cc = eng.cc_info()
-    if phase == "recouple":   # read Z once (FP32) + read and write the 2b part of RES (FP64)
-        return "hbm", eng.wcc_size * 4 + 2 * 8 * n2b
+    if phase == "recouple":   # read Z and Y once, read and write the 2b part of RES
+        return "hbm", 2 * 4 * eng.wcc_size + 2 * 8 * n2b
     if phase == "c122":       # read L and R once, write the 2b part of RES
         return "hbm", 2 * 8 * eng.slab + 8 * n2b
-    if phase == "ph_gemm":    # Z written once in FP32 (the product itself is K<=90)
-        return "hbm", eng.wcc_size * 4
+    if phase == "ph_gemm":    # Z and Y written once in FP32 (the products have K <= nph)
+        return "hbm", 2 * 4 * eng.wcc_size
     if phase == "pphh_gemm":  # sum 2 M N K over the K = npp products, times slice products
         f = 0
         for q in range(eng.nblocks):
@@ -189,119 +210,172 @@ def algorithmic_work(eng, mode: str, phase: str):
             f += 2 * np_ * np_ * np_ + 2 * nh * nh * np_ + 2 * 2 * np_ * nh * np_
             f += 2 * nb * nb * np_ + 2 * 2 * np_ * nb * np_ + 2 * 2 * nb * nh * np_
         return "tensor", f * S
-    if phase == "pandya":     # two operators read, LCC and RCC written once
-        return "hbm", 2 * 8 * eng.slab + 2 * 2 * slices * int((cc["rlen"] * cc["nph"]).sum())
+    if phase == "pandya":     # two operators read, their CC slices written (standard and row-swapped)
+        return "hbm", 2 * 8 * eng.slab + 2 * 2 * 2 * slices * int((cc["rlen"] * cc["nph"]).sum())
     return None, None
+
+
+def flow_state(eng, H):
+    """(HS, G, DG, H) on the device at s = 0: HS = H, Omega = 0, DG = eta(H)."""
+    dH = eng.new_op(1, H)
+    HS = eng.new_op(1, H)
+    G = eng.new_op(-1)
+    DG = eng.new_op(-1)
+    eng.build_gs_white(HS, DG)
+    return HS, G, DG, dH
+
+
+def reference_arm(args):
+    """The CPU restatement of the reference (FP64, OpenMP on all host cores, BLAS dgemm)."""
+    dt, cores, blas, _ = cpu_commutators(args.emax, args.warmup, args.steps)
+    v = args.steps / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"[eta,H] IMSRG(2) commutators, eMax={args.emax}", "emax": args.emax,
+                   "path": "CPU restatement of the reference (FP64, OpenMP)", "blas": blas,
+                   "step": "one full commutator (the unit of the reference's Magnus/BCH loop)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full commutators at eMax={args.emax}"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20, help="timed Magnus steps")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--emax", type=int, default=10)
     ap.add_argument("--mode", default="bf16x6", choices=["bf16x3", "bf16x6"])
-    ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--flow-steps", type=int, default=3)
+    ap.add_argument("--ds", type=float, default=0.5)
+    ap.add_argument("--bch-max-terms", type=int, default=11, help="BCH_EXPAND max_terms (10 nested commutators)")
+    ap.add_argument("--bch-conv", type=float, default=1e-8)
+    ap.add_argument("--fp64-steps", type=int, default=3, help="FP64 graph steps (rate and |dE0|); 0 skips")
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        dt, cores, blas, _ = cpu_commutators(args.emax, args.warmup, args.steps)
-        v = args.steps / dt
-        print(json.dumps({
-            "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"one [eta,H] IMSRG(2) commutator, eMax={args.emax}", "emax": args.emax,
-                       "path": "CPU restatement of the reference (FP64, OpenMP)", "blas": blas},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} full commutators at eMax={args.emax}"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }), flush=True)
+        if rank == 0:
+            reference_arm(args)
         return
 
     from imsrg_gb300 import Engine, make_basis
-    from imsrg_gb300.flow import magnus_decouple
     import numpy as np
 
+    W = max(args.warmup, 3)
+    K = args.steps
+    step_kw = dict(max_terms=args.bch_max_terms, conv=args.bch_conv, graph=True)
     b = make_basis(args.emax)
     eng = Engine(b, device=local, precision=args.mode)
     H = eng.synthetic_hamiltonian(seed=1)
+
+    # ---- timed: K Magnus steps of the flow, each one CUDA-graph replay (after W warm-up steps)
+    st = flow_state(eng, H)
+    e0_steps = []
+    for _ in range(W):
+        e0_steps.append(eng.magnus_step(*st, args.ds, allow_unconverged=True, **step_kw)["E0"])
+    eng.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(pg)
+    eng.synchronize()
+    c0 = eng.magnus_step_counters()
+    t_wall0 = time.time()
+    eng.timer_begin()
+    for _ in range(K):
+        eng.magnus_step(*st, args.ds, wait=False, **step_kw)
+    ms = eng.timer_end()
+    t_wall1 = time.time()
+    eng.synchronize()
+    c1 = eng.magnus_step_counters()
+    barrier(pg)
+    clk = clocks.stop(t_wall0, t_wall1)
+    ms_max = allreduce_max(pg, ms)
+    n_comm = c1["commutators"] - c0["commutators"]
+    comm_all = allreduce_sum(pg, n_comm)
+    launches_all = int(allreduce_sum(pg, c1["kernels"] - c0["kernels"]))
+    value = comm_all / (ms_max * 1e-3)
+    timed = {"steps": K, "commutators": n_comm, "unconverged_bch_steps": c1["unconverged"] - c0["unconverged"],
+             "s_end": args.ds * (W + K)}
+    del st
+    # ---- plain FP64 GPU path: the same flow, same graph step; rate and |dE0|, ||dH(s)||
+    cmp = {}
+    fp64_rate = None
+    if args.fp64_steps > 0:
+        F = args.fp64_steps
+        eng64 = Engine(b, device=local, precision="fp64")
+        st64 = flow_state(eng64, H)
+        eng64.magnus_step(*st64, args.ds, allow_unconverged=True, **step_kw)
+        if F > 1:
+            k0 = eng64.magnus_step_counters()
+            eng64.timer_begin()
+            for _ in range(F - 1):
+                eng64.magnus_step(*st64, args.ds, wait=False, **step_kw)
+            ms64 = eng64.timer_end()
+            k1 = eng64.magnus_step_counters()
+            fp64_rate = (k1["commutators"] - k0["commutators"]) / (ms64 * 1e-3)
+        stm = flow_state(eng, H)
+        for _ in range(F):
+            eng.magnus_step(*stm, args.ds, allow_unconverged=True, **step_kw)
+        hs_m, hs_64 = stm[0].download(), st64[0].download()
+        cmp = {"flow_steps": F, "E0_mixed": float(hs_m[0]), "E0_fp64": float(hs_64[0]),
+               "dE0_keV": abs(float(hs_m[0] - hs_64[0])) * 1e3,
+               "dH_frob_rel": float(np.linalg.norm(hs_m - hs_64) / np.linalg.norm(hs_64))}
+        # one commutator [eta, H(s)] in both precisions on identical inputs
+        dR = eng.new_op(1)
+        dR64 = eng64.new_op(1)
+        eng.commutator(stm[2], stm[0], dR)
+        dE64, dHs64 = eng64.new_op(-1, stm[2].download()), eng64.new_op(1, hs_m)
+        eng64.commutator(dE64, dHs64, dR64)
+        r_m, r_64 = dR.download(), dR64.download()
+        cmp.update({"commutator_dE0_keV": abs(float(r_m[0] - r_64[0])) * 1e3,
+                    "commutator_max_rel_err": float(np.max(np.abs(r_m - r_64)) / np.max(np.abs(r_64)))})
+        del st64, dR64, dE64, dHs64, eng64
+        del stm
+
+    # ---- end to end through the C ABI: the flow kept in pinned host memory; every step
+    # uploads H, Omega, eta and downloads H(s), Omega, eta around imsrg_magnus_step
+    nbytes = 8 * eng.slab
+    st = flow_state(eng, H)
+    hb = []
+    for _ in range(4):
+        p = C.c_void_p()
+        eng._ck(eng.L.imsrg_pinned_alloc(nbytes, C.byref(p)))
+        hb.append(p)
+    for op, p in zip(st, hb):
+        eng._ck(eng.L.imsrg_op_download_slab(eng.h, op.h, p))
+    HS_, G_, DG_, H_ = st
+    e2e_comm = 0
+    for it in range(args.e2e_steps + 1):
+        if it == 1:
+            barrier(pg)
+            t0 = time.perf_counter()
+        for op, p in ((H_, hb[3]), (G_, hb[1]), (DG_, hb[2])):
+            eng._ck(eng.L.imsrg_op_upload_slab(eng.h, op.h, p))
+        info = eng.magnus_step(*st, args.ds, allow_unconverged=True, **step_kw)
+        for op, p in ((HS_, hb[0]), (G_, hb[1]), (DG_, hb[2])):
+            eng._ck(eng.L.imsrg_op_download_slab(eng.h, op.h, p))
+        if it >= 1:
+            e2e_comm += info["magnus_terms"] + info["bch_terms"]
+    e2e_s = allreduce_max(pg, time.perf_counter() - t0)
+    e2e_value = allreduce_sum(pg, e2e_comm) / e2e_s
+    for p in hb:
+        eng.L.imsrg_pinned_free(p)
+    del st, HS_, G_, DG_, H_
+
+    # ---- per-phase event timing of eager commutators for the roofline of the dominant kernel
     dH = eng.new_op(1, H)
     dE = eng.new_op(-1)
     dR = eng.new_op(1)
     eng.build_gs_white(dH, dE)
-
-    # ---- device-resident timing (the headline value)
-    for _ in range(max(args.warmup, 3)):
-        eng.commutator(dE, dH, dR)
-    eng.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier(pg)
-    eng.synchronize()
-    l0 = eng.launch_count()
-    eng.timer_begin()
-    for _ in range(args.steps):
-        eng.commutator(dE, dH, dR)
-    ms = eng.timer_end()
-    eng.synchronize()
-    launches = eng.launch_count() - l0
-    barrier(pg)
-    clk = clocks.stop()
-    ms_max = allreduce_max(pg, ms)
-    launches_all = int(allreduce_sum(pg, launches))
-    value = world * args.steps / (ms_max * 1e-3)
-
-    # ---- plain FP64 GPU path on the same inputs
-    eng64 = Engine(b, device=local, precision="fp64")
-    dH64 = eng64.new_op(1, H)
-    dE64 = eng64.new_op(-1)
-    dR64 = eng64.new_op(1)
-    eng64.build_gs_white(dH64, dE64)
-    eng64.commutator(dE64, dH64, dR64)
-    eng64.timer_begin()
-    for _ in range(args.fp64_steps):
-        eng64.commutator(dE64, dH64, dR64)
-    ms64 = eng64.timer_end() / args.fp64_steps
-    fp64_rate = 1e3 / ms64
-    R_mixed, R_64 = dR.download(), dR64.download()
-    comm_dE0 = abs(R_mixed[0] - R_64[0])
-    comm_rel = float(np.max(np.abs(R_mixed - R_64)) / np.max(np.abs(R_64)))
-    del dH64, dE64, dR64
-
-    # ---- end to end through the C ABI: pinned host operators in, result out, every step
-    nbytes = 8 * eng.slab
-    hbuf = []
-    for _ in range(3):
-        p = C.c_void_p()
-        eng._ck(eng.L.imsrg_pinned_alloc(nbytes, C.byref(p)))
-        hbuf.append(p)
-    hE = np.ctypeslib.as_array(C.cast(hbuf[0], C.POINTER(C.c_double)), shape=(eng.slab,))
-    hH = np.ctypeslib.as_array(C.cast(hbuf[1], C.POINTER(C.c_double)), shape=(eng.slab,))
-    hE[:] = dE.download()
-    hH[:] = H
-    e2e_steps = max(3, args.steps // 2)
-    for it in range(e2e_steps + 1):
-        if it == 1:
-            barrier(pg)
-            t0 = time.perf_counter()
-        eng._ck(eng.L.imsrg_op_upload_slab(eng.h, dE.h, hbuf[0]))
-        eng._ck(eng.L.imsrg_op_upload_slab(eng.h, dH.h, hbuf[1]))
-        eng.commutator(dE, dH, dR)
-        eng._ck(eng.L.imsrg_op_download_slab(eng.h, dR.h, hbuf[2]))
-    e2e_s = allreduce_max(pg, time.perf_counter() - t0)
-    e2e_value = world * e2e_steps / e2e_s
-    for p in hbuf:
-        eng.L.imsrg_pinned_free(p)
-
-    # ---- per-phase event timing (separate pass) for the roofline of the dominant kernel
+    eng.commutator(dE, dH, dR)
     eng.profile_phases(True)
     nprof = 3
     for _ in range(nprof):
@@ -330,19 +404,11 @@ def main():
         peak = peaks.get("hbm_gbs", 6800.0)
         achieved = (work or 0) / (dom_ms * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak}
-    roof.update({"traffic": traffic, "kernel_phase": dom, "kernel_ms": dom_ms,
-                 "algorithmic": work, "peak_source": "measured" if peaks else "fallback",
-                 "phases_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in phases.items() if v[1]}})
-
-    # ---- |dE0| of a short Magnus flow, mixed vs plain FP64
-    flow = {}
-    if args.flow_steps > 0:
-        r_mixed = magnus_decouple(eng, H, max_steps=args.flow_steps)
-        eng64b = Engine(b, device=local, precision="fp64")
-        r_64 = magnus_decouple(eng64b, H, max_steps=args.flow_steps)
-        flow = {"flow_steps": args.flow_steps, "E0_mixed": r_mixed.E0, "E0_fp64": r_64.E0,
-                "dE0_keV": abs(r_mixed.E0 - r_64.E0) * 1e3}
-        del eng64b
+    roof.update({"traffic": traffic, "kernel_phase": dom, "kernel_ms": dom_ms, "algorithmic": work,
+                 "peak_source": "measured" if peaks else "fallback",
+                 "phases_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in phases.items() if v[1]},
+                 "commutator_ms": round(sum(v[0] for v in phases.values()) / nprof, 4)})
+    del dH, dE, dR
 
     # ---- CPU restatement of the reference on the host cores (rank 0, N=1)
     cpu = None
@@ -354,19 +420,25 @@ def main():
 
     if rank == 0:
         out = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16", "data": "synthetic",
             "config": {
-                "workload": f"one [eta,H] IMSRG(2) commutator, eMax={args.emax} (132 orbits, 16O-like), "
-                            "seeded synthetic Hamiltonian + White generator",
-                "emax": args.emax, "precision": f"{args.mode}: split-BF16 tcgen05 channel GEMMs, FP32 accumulate, "
-                                                "FP32 gathers, FP64 operators and E0",
-                "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (0.27 GiB operators, 0.78 GiB Z)",
-                "fp64_commutators_per_s": fp64_rate * world, "speedup_vs_fp64": value / (fp64_rate * world),
-                "commutator_dE0_keV": comm_dE0 * 1e3, "commutator_max_rel_err": comm_rel, **flow,
+                "workload": f"Magnus flow steps at eMax={args.emax} ({b.norbits} orbits, 16O-like), seeded "
+                            "synthetic Hamiltonian, White generator; one step = MAGNUS_EXPAND + euler_step + "
+                            f"BCH_EXPAND (<= {args.bch_max_terms - 1} nested commutators or term norm < "
+                            f"{args.bch_conv:g}) + generator + MBPT2, one CUDA-graph replay",
+                "emax": args.emax, "ds": args.ds,
+                "precision": f"{args.mode}: split-BF16 tcgen05 channel GEMMs, FP32 accumulate, FP32 gathers, "
+                             "FP64 operators, E0 and norms",
+                "parallelism": f"replicas x{world}",
+                "l2": "inputs larger than L2 (0.27 GiB per operator, 0.78 GiB Z and Y each)",
+                "timed": timed, "warmup_E0": e0_steps,
+                "fp64_commutators_per_s": fp64_rate * world if fp64_rate else None,
+                "speedup_vs_fp64": value / (fp64_rate * world) if fp64_rate else None, **cmp,
             },
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * nbytes,
+                    "d2h_bytes_per_step": 3 * nbytes, "steps": args.e2e_steps, "commutators": e2e_comm},
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk,

@@ -212,6 +212,7 @@ Ctx::~Ctx() {
   if (ev_begin) cudaEventDestroy(ev_begin);
   if (ev_end) cudaEventDestroy(ev_end);
   tc_release();
+  graph_release();
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -365,7 +366,7 @@ imsrg_status Ctx::magnus_expand(double* DG, int hDG, const double* G, int hG, in
   CK(ensure_workspace());
   CK(ensure_flow_workspace());
   const double conv = (double)1e-6f;
-  static const double cof[7] = {1.0, -0.5, .0833333333, 0.0, -0.00138888888, 0.0, 3.306878e-5};
+  const double* cof = kMagnusCof;
   const size_t sb = sizeof(double) * (size_t)L.slab;
   double advals[8] = {0};
   CK(cuda(cudaMemcpyAsync(d_int2, DG, sb, cudaMemcpyDeviceToDevice, stream), "copy INT2"));
@@ -954,6 +955,30 @@ imsrg_status imsrg_bch_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, c
   imsrg_status s = c->bch_expand(HS->d, G->d, G->herm, H->d, H->herm, max_terms, conv, &t);
   if (terms_used) *terms_used = t;
   return s;
+}
+
+imsrg_status imsrg_magnus_step(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_op* DG, const imsrg_op* H, double ds,
+                               int32_t bch_max_terms, double bch_conv, int32_t use_graph, imsrg_step_info* info) {
+  CTX(ctx);
+  CK(check_op(c, HS, "imsrg_magnus_step"));
+  CK(check_op(c, G, "imsrg_magnus_step"));
+  CK(check_op(c, DG, "imsrg_magnus_step"));
+  CK(check_op(c, H, "imsrg_magnus_step"));
+  if (HS == G || HS == H || HS == DG || G == DG || G == H || DG == H)
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "HS, G, DG and H must be distinct operators");
+  if (bch_max_terms < 2) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "max_terms must be >= 2");
+  if (!use_graph && !info) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "the eager step needs info");
+  HS->herm = H->herm;
+  DG->herm = -1;
+  return c->magnus_step(HS->d, G->d, G->herm, DG->d, H->d, H->herm, ds, bch_max_terms, bch_conv, use_graph != 0,
+                        info);
+}
+
+imsrg_status imsrg_magnus_step_counters(imsrg_ctx* ctx, int64_t* commutators, int64_t* kernels, int64_t* steps,
+                                        int64_t* unconverged) {
+  CTX(ctx);
+  if (!commutators || !kernels || !steps || !unconverged) return IMSRG_ERR_INVALID_ARGUMENT;
+  return c->step_counters(commutators, kernels, steps, unconverged);
 }
 
 }  // extern "C"

@@ -14,6 +14,10 @@
 namespace imsrg {
 struct TcState;
 }
+struct StepGraph;
+
+// MAGNUS_EXPAND coefficients as the literals of src/IMSRG_MAGNUS.f90:646
+constexpr double kMagnusCof[7] = {1.0, -0.5, .0833333333, 0.0, -0.00138888888, 0.0, 3.306878e-5};
 
 // phases of one commutator for per-phase event timing (imsrg_profile_read)
 enum Phase : int {
@@ -60,6 +64,7 @@ struct Ctx {
   // Magnus / BCH intermediates
   double *d_int1 = nullptr, *d_int2 = nullptr, *d_ad = nullptr;
   imsrg::TcState* tc = nullptr;
+  StepGraph* sg = nullptr;  // captured Magnus step (graph.cu)
   // kernel launches issued (cumulative) and optional per-phase CUDA-event timing
   int64_t launches = 0;
   bool prof = false;
@@ -94,6 +99,16 @@ struct Ctx {
   imsrg_status magnus_expand(double* DG, int hDG, const double* G, int hG, int* used);
   imsrg_status bch_expand(double* HS, const double* G, int hG, const double* H, int hH, int max_terms, double conv,
                           int* terms);
+
+  // one Magnus step, eager or replayed from a CUDA graph (graph.cu)
+  imsrg_status magnus_step(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,
+                           int max_terms, double conv, bool use_graph, imsrg_step_info* info);
+  imsrg_status graph_capture(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,
+                             int max_terms, double conv);
+  template <class F>
+  imsrg_status capture_if(cudaGraphConditionalHandle h, F&& body);
+  imsrg_status step_counters(int64_t* commutators, int64_t* kernels, int64_t* steps, int64_t* unconverged);
+  imsrg_status graph_release();
 
   // tensor-core (split-BF16, tcgen05) path, gemm_tc.cu
   imsrg_status tc_prepare(int mode);

@@ -33,6 +33,11 @@ class Basis_t(C.Structure):
                 ("Aneut", C.c_int32)]
 
 
+class StepInfo_t(C.Structure):
+    _fields_ = [("E0", C.c_double), ("mbpt2", C.c_double), ("magnus_terms", C.c_int32), ("bch_terms", C.c_int32),
+                ("bch_converged", C.c_int32), ("graph_rebuilt", C.c_int32)]
+
+
 # (name, restype-is-status, argtypes)
 _vp, _i32, _i64, _d, _u64 = C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_uint64
 _pi32, _pi64, _pd, _pvp = C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_void_p)
@@ -80,6 +85,8 @@ SIGNATURES = {
     "imsrg_magnus_expand": [_vp, _vp, _vp, _pi32],
     "imsrg_euler_step": [_vp, _vp, _vp, _pd, _d],
     "imsrg_bch_expand": [_vp, _vp, _vp, _vp, _i32, _d, _pi32],
+    "imsrg_magnus_step": [_vp, _vp, _vp, _vp, _vp, _d, _i32, _d, _i32, C.POINTER(StepInfo_t)],
+    "imsrg_magnus_step_counters": [_vp, _pi64, _pi64, _pi64, _pi64],
     "imsrg_synthetic_hamiltonian": [_vp, _u64, _d, _vp],
     "imsrg_launch_count": [_vp, _pi64],
     "imsrg_timer_begin": [_vp],

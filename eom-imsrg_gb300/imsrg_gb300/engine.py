@@ -286,3 +286,28 @@ class Engine:
         n = C.c_int32()
         self._ck(self.L.imsrg_bch_expand(self.h, HS.h, G.h, H.h, int(max_terms), float(conv), C.byref(n)))
         return n.value
+
+    def magnus_step(self, HS: SqOp, G: SqOp, DG: SqOp, H: SqOp, ds: float, max_terms: int = 40, conv: float = CONV,
+                    graph: bool = True, wait: bool = True, allow_unconverged: bool = False):
+        """One step of magnus_decouple (MAGNUS_EXPAND, euler_step, BCH_EXPAND, White, MBPT2).
+
+        graph=True replays a CUDA graph of the step; wait=False only enqueues it (graph
+        mode) and returns None.  Returns a dict with E0, mbpt2 and the term counts."""
+        if not wait:
+            if not graph:
+                raise ValueError("the eager step always waits")
+            self._ck(self.L.imsrg_magnus_step(self.h, HS.h, G.h, DG.h, H.h, float(ds), int(max_terms), float(conv),
+                                              1, None))
+            return None
+        info = _lib.StepInfo_t()
+        st = self.L.imsrg_magnus_step(self.h, HS.h, G.h, DG.h, H.h, float(ds), int(max_terms), float(conv),
+                                      1 if graph else 0, C.byref(info))
+        if st != 0 and not (allow_unconverged and st == 4):
+            self._ck(st)
+        return {"E0": info.E0, "mbpt2": info.mbpt2, "magnus_terms": info.magnus_terms, "bch_terms": info.bch_terms,
+                "bch_converged": bool(info.bch_converged), "graph_rebuilt": bool(info.graph_rebuilt)}
+
+    def magnus_step_counters(self) -> dict:
+        v = [C.c_int64() for _ in range(4)]
+        self._ck(self.L.imsrg_magnus_step_counters(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("commutators", "kernels", "steps", "unconverged"), (x.value for x in v)))

@@ -26,8 +26,11 @@ class FlowResult:
 def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float | None = None,
                     max_steps: int | None = None, crit_stop: float = float(np.float32(1e-6)),
                     bch_max_terms: int = 40, bch_conv: float = CONV, generator: str = "white",
-                    ops: dict | None = None) -> FlowResult:
-    """Flow the Hamiltonian H0 (host slab, herm +1) to s_max / max_steps / |MBPT2| < crit."""
+                    ops: dict | None = None, graph: bool = False) -> FlowResult:
+    """Flow the Hamiltonian H0 (host slab, herm +1) to s_max / max_steps / |MBPT2| < crit.
+
+    graph=True runs each step as one replay of the CUDA graph of imsrg_magnus_step
+    (same operators as the eager step, bit for bit)."""
     if generator != "white":
         raise ValueError("only the White generator is implemented")
     HS = eng.new_op(1, H0)          # evolved Hamiltonian
@@ -47,13 +50,19 @@ def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float |
         if s_max is not None and s >= s_max - 1e-12:
             break
         steps += 1
-        nm = eng.magnus_expand(DG, G)
-        s = eng.euler_step(G, DG, s, ds)
-        nb = eng.bch_expand(HS, G, H, bch_max_terms, bch_conv)
-        eng.build_gs_white(HS, DG)
-        e2 = eng.mbpt2(HS)
+        if graph:
+            info = eng.magnus_step(HS, G, DG, H, ds, bch_max_terms, bch_conv, graph=True)
+            s += ds
+            e2, e0, nm, nb = info["mbpt2"], info["E0"], info["magnus_terms"], info["bch_terms"]
+        else:
+            nm = eng.magnus_expand(DG, G)
+            s = eng.euler_step(G, DG, s, ds)
+            nb = eng.bch_expand(HS, G, H, bch_max_terms, bch_conv)
+            eng.build_gs_white(HS, DG)
+            e2 = eng.mbpt2(HS)
+            e0 = HS.E0
         crit = abs(e2)
-        res.steps.append((steps, s, HS.E0, HS.E0 + e2, crit, nm, nb))
+        res.steps.append((steps, s, e0, e0 + e2, crit, nm, nb))
     if ops is not None:
         ops.update(HS=HS, G=G)
     return res

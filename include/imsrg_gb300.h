@@ -181,6 +181,29 @@ imsrg_status imsrg_euler_step(imsrg_ctx* ctx, imsrg_op* G, const imsrg_op* DG, d
 imsrg_status imsrg_bch_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H, int32_t max_terms,
                               double conv, int32_t* terms_used);
 
+/* One step of magnus_decouple (src/IMSRG_MAGNUS.f90:47-110): MAGNUS_EXPAND(DG, G),
+ * euler_step(G, DG, ds), BCH_EXPAND(HS, G, H, max_terms, conv), build_gs_white(HS, DG) and
+ * mbpt2(HS).  DG holds eta on entry and the new eta on exit.  With use_graph != 0 the step
+ * is captured once as a CUDA graph (both series' early exits are conditional graph nodes
+ * decided on the device) and replayed with one launch while the operators and parameters
+ * stay the same; the operators are bit-identical to the eager step (use_graph = 0).
+ * info != NULL: waits for the step and fills info; returns IMSRG_ERR_NOT_CONVERGED when
+ * BCH_EXPAND used all max_terms.  info == NULL (graph only): enqueues the step and returns. */
+typedef struct imsrg_step_info {
+  double E0;              /* E0 of HS after the step */
+  double mbpt2;           /* MBPT(2) energy of HS after the step */
+  int32_t magnus_terms;   /* nested commutators in MAGNUS_EXPAND */
+  int32_t bch_terms;      /* nested commutators in BCH_EXPAND */
+  int32_t bch_converged;  /* 1 when a BCH term fell below conv */
+  int32_t graph_rebuilt;  /* 1 when this call captured and instantiated the graph */
+} imsrg_step_info;
+imsrg_status imsrg_magnus_step(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_op* DG, const imsrg_op* H, double ds,
+                               int32_t bch_max_terms, double bch_conv, int32_t use_graph, imsrg_step_info* info);
+/* Totals over all graph-replayed steps of this context (no counterpart in the reference):
+ * nested commutators, kernels launched, steps, steps whose BCH series did not converge. */
+imsrg_status imsrg_magnus_step_counters(imsrg_ctx* ctx, int64_t* commutators, int64_t* kernels, int64_t* steps,
+                                        int64_t* unconverged);
+
 /* ---- input preparation (host, FP64): seeded synthetic Hamiltonian in the reference's
  * me2j -> pn J-scheme layout (read_me2j_interaction, src/interaction_IO.f90:282-557) plus the
  * harmonic-oscillator kinetic energy (calculate_h0_harm_osc, src/basic_IMSRG.f90:2093-2191),
