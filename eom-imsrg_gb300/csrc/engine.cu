@@ -213,6 +213,7 @@ Ctx::~Ctx() {
   if (ev_end) cudaEventDestroy(ev_end);
   tc_release();
   graph_release();
+  adjoint_release();
   if (stream) cudaStreamDestroy(stream);
 }
 

@@ -15,6 +15,7 @@ namespace imsrg {
 struct TcState;
 }
 struct StepGraph;
+struct AdjointState;
 
 // MAGNUS_EXPAND coefficients as the literals of src/IMSRG_MAGNUS.f90:646
 constexpr double kMagnusCof[7] = {1.0, -0.5, .0833333333, 0.0, -0.00138888888, 0.0, 3.306878e-5};
@@ -65,6 +66,7 @@ struct Ctx {
   double *d_int1 = nullptr, *d_int2 = nullptr, *d_ad = nullptr;
   imsrg::TcState* tc = nullptr;
   StepGraph* sg = nullptr;  // captured Magnus step (graph.cu)
+  AdjointState* adj = nullptr;  // reverse-mode workspaces (adjoint.cu)
   // kernel launches issued (cumulative) and optional per-phase CUDA-event timing
   int64_t launches = 0;
   bool prof = false;
@@ -109,6 +111,14 @@ struct Ctx {
   imsrg_status capture_if(cudaGraphConditionalHandle h, F&& body);
   imsrg_status step_counters(int64_t* commutators, int64_t* kernels, int64_t* steps, int64_t* unconverged);
   imsrg_status graph_release();
+
+  // reverse mode (FP64) of the commutator, the White generator and the slab inner product (adjoint.cu)
+  imsrg_status adjoint_prepare();
+  void adjoint_release();
+  imsrg_status commutator_vjp(const double* L, int hL, const double* R, int hR, int hRES, bool with_e0,
+                              const double* Cb, double* Lb, double* Rb);
+  imsrg_status white_vjp(const double* H, int hH, const double* ETAb, double* Hb);
+  imsrg_status dot(const double* A, const double* B, double* out);
 
   // tensor-core (split-BF16, tcgen05) path, gemm_tc.cu
   imsrg_status tc_prepare(int mode);

@@ -1,6 +1,6 @@
 // Grouped GEMM problem lists shared by the FP64 and the tensor-core paths.
 //
-// A problem is C = sum_t alpha_t * op(A_t) * op(B_t) with at most two terms, every
+// A problem is C (+)= sum_t alpha_t * op(A_t) * op(B_t) with at most kMaxTerms terms, every
 // matrix column-major and addressed as (operand id, element offset) so that one list,
 // built once per basis, serves any set of operator slabs.  alpha_t is +-1, +-herm(L)
 // or +-herm(R), resolved at launch time.
@@ -25,14 +25,16 @@ struct GemmTerm {
   int alpha;   // AlphaCode
 };
 
+constexpr int kMaxTerms = 6;
+
 struct GemmProb {
   int64_t c_off;
   int M, N;
   int ldc;
   int c_id;
   int nterm;
-  int pad;
-  GemmTerm t[2];
+  int accum;  // 0: C = sum, 1: C += sum
+  GemmTerm t[kMaxTerms];
 };
 
 struct GemmTile {
@@ -51,6 +53,13 @@ std::vector<GemmProb> build_pphh_problems(int nblocks, const std::vector<std::ar
                                           const std::vector<int64_t>& goff);
 std::vector<GemmProb> build_wcc_problems(int ncc, const std::vector<int>& rlen, const std::vector<int>& nph,
                                          const std::vector<int64_t>& cc_off, const std::vector<int64_t>& wcc_off);
+// transposes for the adjoint: with w1 / w2 holding the cotangents of the pphh products,
+// Lb and Rb (operands kOpL / kOpR of the output side) accumulate d<cotangent, W>/dL, dR
+std::vector<GemmProb> build_pphh_vjp_problems(int nblocks, const std::vector<std::array<int, 3>>& ncls,
+                                              const std::vector<int64_t>& goff);
+// LCCb = WCCb . RCC and RCCb = WCCb^T . LCC per cross-coupled channel (assigned)
+std::vector<GemmProb> build_wcc_vjp_problems(int ncc, const std::vector<int>& rlen, const std::vector<int>& nph,
+                                             const std::vector<int64_t>& cc_off, const std::vector<int64_t>& wcc_off);
 std::vector<GemmTile> build_tiles(const std::vector<GemmProb>& probs, int BM, int BN);
 
 }  // namespace imsrg

@@ -93,7 +93,10 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb* __restrict__ 
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int gm = tile.m0 + tx + 16 * i, gn = tile.n0 + ty + 16 * j;
-      if (gm < P.M && gn < P.N) C[gm + (int64_t)gn * P.ldc] = acc[i][j];
+      if (gm < P.M && gn < P.N) {
+        double* c = C + gm + (int64_t)gn * P.ldc;
+        *c = P.accum ? *c + acc[i][j] : acc[i][j];
+      }
     }
 }
 

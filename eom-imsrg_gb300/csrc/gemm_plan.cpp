@@ -25,6 +25,14 @@ GemmProb prob2(int c_id, int64_t c_off, int M, int N, int ldc, const GemmTerm& t
   return p;
 }
 
+GemmProb probn(int c_id, int64_t c_off, int M, int N, int ldc, const std::vector<GemmTerm>& ts, int accum) {
+  GemmProb p{};
+  p.c_id = c_id; p.c_off = c_off; p.M = M; p.N = N; p.ldc = ldc; p.accum = accum;
+  p.nterm = (int)ts.size();
+  for (size_t i = 0; i < ts.size(); ++i) p.t[i] = ts[i];
+  return p;
+}
+
 }  // namespace
 
 // Problems of commutator_222_pp_hh (src/commutators.f90:596-766) for one channel block
@@ -84,6 +92,100 @@ std::vector<GemmProb> build_wcc_problems(int ncc, const std::vector<int>& rlen, 
     const int r = rlen[q], nb = nph[q];
     if (r * nb == 0) continue;
     P.push_back(prob(kOpWCC, wcc_off[q], r, r, r, term(kOpLCC, cc_off[q], r, 0, kOpRCC, cc_off[q], r, 1, nb, kAlphaOne)));
+  }
+  return P;
+}
+
+// Reverse of build_pphh_problems: every product W = alpha op(X) op(Y) of the forward list
+// gives Xbar += alpha Wbar op(Y)^T-like terms; the terms of one output block are summed in
+// one problem (at most six, for the pphh blocks).
+std::vector<GemmProb> build_pphh_vjp_problems(int nblocks, const std::vector<std::array<int, 3>>& ncls,
+                                              const std::vector<int64_t>& goff) {
+  std::vector<GemmProb> P;
+  const int N = 0, T = 1;
+  const int one = kAlphaOne, hl = kAlphaHL, hr = kAlphaHR, neg = kAlphaNeg;
+  const int L = kOpL, R = kOpR, W1 = kOpW1, W2 = kOpW2;
+  for (int q = 0; q < nblocks; ++q) {
+    const int np = ncls[q][0], nb = ncls[q][1], nh = ncls[q][2];
+    auto o = [&](int g) { return goff[q * 6 + g]; };
+    std::vector<GemmTerm> t;
+    auto emit = [&](int c_id, int g, int M, int Nn, int ldc) {
+      if (M > 0 && Nn > 0 && !t.empty()) P.push_back(probn(c_id, o(g), M, Nn, ldc, t, 1));
+      t.clear();
+    };
+    // pppp (np x np)
+    if (np) t.push_back(term(W1, o(0), np, N, R, o(0), np, T, np, one));
+    if (np * nh) t.push_back(term(W1, o(2), np, N, R, o(2), np, T, nh, one));
+    if (np * nb) t.push_back(term(W1, o(1), np, N, R, o(1), np, T, nb, one));
+    emit(L, 0, np, np, np);
+    if (np) t.push_back(term(L, o(0), np, T, W1, o(0), np, N, np, one));
+    if (np * nh) t.push_back(term(W1, o(2), np, N, L, o(2), np, T, nh, neg | one));
+    if (np * nb) t.push_back(term(W1, o(1), np, N, L, o(1), np, T, nb, neg | one));
+    emit(R, 0, np, np, np);
+    // hhhh (nh x nh)
+    if (nh) t.push_back(term(W2, o(4), nh, N, R, o(4), nh, T, nh, one));
+    if (np * nh) t.push_back(term(R, o(2), np, T, W2, o(2), np, N, np, neg | one));
+    if (nb * nh) t.push_back(term(R, o(5), nb, T, W2, o(5), nb, N, nb, neg | one));
+    emit(L, 4, nh, nh, nh);
+    if (nh) t.push_back(term(L, o(4), nh, T, W2, o(4), nh, N, nh, one));
+    if (np * nh) t.push_back(term(L, o(2), np, T, W2, o(2), np, N, np, one));
+    if (nb * nh) t.push_back(term(L, o(5), nb, T, W2, o(5), nb, N, nb, one));
+    emit(R, 4, nh, nh, nh);
+    // pphh (np x nh)
+    if (np * nh) {
+      t.push_back(term(R, o(2), np, N, W1, o(4), nh, T, nh, hl));
+      t.push_back(term(W2, o(0), np, N, R, o(2), np, N, np, hr));
+      t.push_back(term(R, o(0), np, T, W1, o(2), np, N, np, neg | one));
+      t.push_back(term(W2, o(2), np, N, R, o(4), nh, T, nh, one));
+      if (nb) {
+        t.push_back(term(R, o(1), np, N, W1, o(5), nb, N, nb, neg | hr));
+        t.push_back(term(W2, o(1), np, N, R, o(5), nb, N, nb, hr));
+      }
+      emit(L, 2, np, nh, np);
+      t.push_back(term(L, o(2), np, N, W1, o(4), nh, N, nh, hl));
+      t.push_back(term(W2, o(0), np, T, L, o(2), np, N, np, hr));
+      t.push_back(term(L, o(0), np, T, W1, o(2), np, N, np, one));
+      t.push_back(term(W2, o(2), np, N, L, o(4), nh, T, nh, neg | one));
+      if (nb) {
+        t.push_back(term(L, o(1), np, N, W1, o(5), nb, N, nb, hl));
+        t.push_back(term(W2, o(1), np, N, L, o(5), nb, N, nb, neg | hl));
+      }
+      emit(R, 2, np, nh, np);
+    }
+    // phhh (nb x nh)
+    if (nb * nh) {
+      t.push_back(term(W2, o(3), nb, N, R, o(5), nb, N, nb, hr));
+      t.push_back(term(W2, o(5), nb, N, R, o(4), nh, T, nh, one));
+      if (np) t.push_back(term(W2, o(1), np, T, R, o(2), np, N, np, neg | hl));
+      emit(L, 5, nb, nh, nb);
+      t.push_back(term(W2, o(3), nb, T, L, o(5), nb, N, nb, hr));
+      t.push_back(term(W2, o(5), nb, N, L, o(4), nh, T, nh, neg | one));
+      if (np) t.push_back(term(W2, o(1), np, T, L, o(2), np, N, np, hr));
+      emit(R, 5, nb, nh, nb);
+    }
+    // ppph (np x nb)
+    if (np * nb) {
+      t.push_back(term(R, o(1), np, N, W1, o(3), nb, T, nb, hl));
+      t.push_back(term(R, o(0), np, T, W1, o(1), np, N, np, neg | one));
+      if (nh) t.push_back(term(R, o(2), np, N, W1, o(5), nb, T, nh, hl));
+      emit(L, 1, np, nb, np);
+      t.push_back(term(L, o(1), np, N, W1, o(3), nb, N, nb, hl));
+      t.push_back(term(L, o(0), np, T, W1, o(1), np, N, np, one));
+      if (nh) t.push_back(term(L, o(2), np, N, W1, o(5), nb, T, nh, neg | hr));
+      emit(R, 1, np, nb, np);
+    }
+  }
+  return P;
+}
+
+std::vector<GemmProb> build_wcc_vjp_problems(int ncc, const std::vector<int>& rlen, const std::vector<int>& nph,
+                                             const std::vector<int64_t>& cc_off, const std::vector<int64_t>& wcc_off) {
+  std::vector<GemmProb> P;
+  for (int q = 0; q < ncc; ++q) {
+    const int r = rlen[q], nb = nph[q];
+    if (r * nb == 0) continue;
+    P.push_back(prob(kOpLCC, cc_off[q], r, nb, r, term(kOpWCC, wcc_off[q], r, 0, kOpRCC, cc_off[q], r, 0, r, kAlphaOne)));
+    P.push_back(prob(kOpRCC, cc_off[q], r, nb, r, term(kOpWCC, wcc_off[q], r, 1, kOpLCC, cc_off[q], r, 0, r, kAlphaOne)));
   }
   return P;
 }

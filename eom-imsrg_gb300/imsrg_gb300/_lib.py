@@ -87,6 +87,9 @@ SIGNATURES = {
     "imsrg_bch_expand": [_vp, _vp, _vp, _vp, _i32, _d, _pi32],
     "imsrg_magnus_step": [_vp, _vp, _vp, _vp, _vp, _d, _i32, _d, _i32, C.POINTER(StepInfo_t)],
     "imsrg_magnus_step_counters": [_vp, _pi64, _pi64, _pi64, _pi64],
+    "imsrg_commutator_vjp": [_vp, _vp, _vp, _vp, _vp, _vp, _i32],
+    "imsrg_white_vjp": [_vp, _vp, _vp, _vp],
+    "imsrg_dot_sq_op": [_vp, _vp, _vp, _pd],
     "imsrg_synthetic_hamiltonian": [_vp, _u64, _d, _vp],
     "imsrg_launch_count": [_vp, _pi64],
     "imsrg_timer_begin": [_vp],

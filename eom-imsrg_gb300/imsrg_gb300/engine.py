@@ -307,6 +307,20 @@ class Engine:
         return {"E0": info.E0, "mbpt2": info.mbpt2, "magnus_terms": info.magnus_terms, "bch_terms": info.bch_terms,
                 "bch_converged": bool(info.bch_converged), "graph_rebuilt": bool(info.graph_rebuilt)}
 
+    # ---------------------------------------------------------------- reverse mode (FP64)
+    def commutator_vjp(self, L: SqOp, R: SqOp, RESb: SqOp, Lb: SqOp, Rb: SqOp, e0: bool = True):
+        """Lb += d<RESb,[L,R]>/dL, Rb += d<RESb,[L,R]>/dR (RESb.herm = herm of [L,R])."""
+        self._ck(self.L.imsrg_commutator_vjp(self.h, L.h, R.h, RESb.h, Lb.h, Rb.h, _lib.COMM_E0 if e0 else 0))
+
+    def white_vjp(self, H: SqOp, ETAb: SqOp, Hb: SqOp):
+        """Hb += d<ETAb, eta(H)>/dH for the White generator."""
+        self._ck(self.L.imsrg_white_vjp(self.h, H.h, ETAb.h, Hb.h))
+
+    def dot(self, A: SqOp, B: SqOp) -> float:
+        v = C.c_double()
+        self._ck(self.L.imsrg_dot_sq_op(self.h, A.h, B.h, C.byref(v)))
+        return v.value
+
     def magnus_step_counters(self) -> dict:
         v = [C.c_int64() for _ in range(4)]
         self._ck(self.L.imsrg_magnus_step_counters(self.h, *[C.byref(x) for x in v]))

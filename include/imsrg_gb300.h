@@ -204,6 +204,18 @@ imsrg_status imsrg_magnus_step(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_
 imsrg_status imsrg_magnus_step_counters(imsrg_ctx* ctx, int64_t* commutators, int64_t* kernels, int64_t* steps,
                                         int64_t* unconverged);
 
+/* ---- reverse mode (FP64) for adjoint derivatives of a flow (no counterpart in the
+ * reference, which has no derivative code).  Each call ACCUMULATES into its outputs:
+ * Lb += d<RESb, [L,R]>/dL and Rb += d<RESb, [L,R]>/dR for the FP64 commutator of
+ * imsrg_commutator (flags as there, RESb->herm = the herm of RES), the exact transpose of
+ * that routine in the plain slab inner product <A,B> = sum_k A[k] B[k]. */
+imsrg_status imsrg_commutator_vjp(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, const imsrg_op* RESb,
+                                  imsrg_op* Lb, imsrg_op* Rb, int32_t flags);
+/* Hb += d<ETAb, eta(H)>/dH for eta = build_gs_white(H) (numerators and denominators) */
+imsrg_status imsrg_white_vjp(imsrg_ctx* ctx, const imsrg_op* H, const imsrg_op* ETAb, imsrg_op* Hb);
+/* *out = sum_k A[k] B[k] over the slab (FP64) */
+imsrg_status imsrg_dot_sq_op(imsrg_ctx* ctx, const imsrg_op* A, const imsrg_op* B, double* out);
+
 /* ---- input preparation (host, FP64): seeded synthetic Hamiltonian in the reference's
  * me2j -> pn J-scheme layout (read_me2j_interaction, src/interaction_IO.f90:282-557) plus the
  * harmonic-oscillator kinetic energy (calculate_h0_harm_osc, src/basic_IMSRG.f90:2093-2191),

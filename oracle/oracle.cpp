@@ -1087,6 +1087,595 @@ double bf2(const Basis& B, const double* A, int hA, const double* Bo, int hB, in
 
 }  // namespace
 
+// ====================================================================== reverse mode
+// Exact transposes (vector-Jacobian products) of the forward routines above, used to
+// check the device adjoint of the Magnus flow (dE0/dtheta).  The reference has no
+// derivative code: each routine below is the reverse of this file's own restatement,
+// statement by statement, so <Cbar, F(L, R)> = <Lbar, L> = <Rbar, R> holds for the
+// bilinear pieces on ANY slabs (hermitian or not), which is what the tests check.
+
+struct Addr {
+  int64_t idx;  // slab index read by f_elem / v_elem (-1: the element is identically zero)
+  double c;     // value read = c * slab[idx]
+};
+
+inline Addr f_addr(const Basis& B, int herm, int a, int b) {
+  const int c1 = B.con[a], c2 = B.con[b];
+  switch (c1 + c2) {
+    case 0: return {B.off_fpp + B.loc[a] + (int64_t)B.loc[b] * B.P, 1.0};
+    case 1:
+      if (c1 > c2) return {B.off_fph + B.loc[b] + (int64_t)B.loc[a] * B.P, (double)herm};
+      return {B.off_fph + B.loc[a] + (int64_t)B.loc[b] * B.P, 1.0};
+    default: return {B.off_fhh + B.loc[a] + (int64_t)B.loc[b] * B.A, 1.0};
+  }
+}
+
+// the slab position v_elem reads, with its factor (same branches as v_elem)
+Addr v_addr(const Basis& B, int herm, int a, int b, int c, int d, int J) {
+  const int ja = B.jj[a], jb = B.jj[b], jc = B.jj[c], jd = B.jj[d];
+  if (!(tri(ja, jb, J) && tri(jc, jd, J))) return {-1, 0.0};
+  const int P = (B.ll[a] + B.ll[b]) % 2;
+  if ((B.ll[c] + B.ll[d]) % 2 != P) return {-1, 0.0};
+  const int T = (B.tz[a] + B.tz[b]) / 2;
+  if (B.tz[c] + B.tz[d] != 2 * T) return {-1, 0.0};
+  const int q = B.block(J, T, P);
+  const int C1 = B.con[a] + B.con[b], C2 = B.con[c] + B.con[d];
+  const int g = qx_of(std::min(C1, C2), std::max(C1, C2));
+  double pre = 1.0;
+  const int N = B.N, NJ = B.NJ;
+  int i1, i2;
+  if (a > b) {
+    i1 = B.pairpos[((size_t)b * N + a) * NJ + J / 2];
+    pre = sgn(1 + (ja + jb - J) / 2);
+  } else {
+    if (a == b) pre *= std::sqrt(2.0);
+    i1 = B.pairpos[((size_t)a * N + b) * NJ + J / 2];
+  }
+  if (c > d) {
+    i2 = B.pairpos[((size_t)d * N + c) * NJ + J / 2];
+    pre *= sgn(1 + (jc + jd - J) / 2);
+  } else {
+    if (c == d) pre *= std::sqrt(2.0);
+    i2 = B.pairpos[((size_t)c * N + d) * NJ + J / 2];
+  }
+  const int n1 = B.gn1[q][g];
+  if (C1 > C2) return {B.goff[q][g] + i2 + (int64_t)i1 * n1, herm * pre};
+  return {B.goff[q][g] + i1 + (int64_t)i2 * n1, pre};
+}
+
+inline void add_at(double* bar, const Addr& ad, double g) {
+  if (ad.idx >= 0) bar[ad.idx] += ad.c * g;
+}
+inline double val_at(const double* op, const Addr& ad) { return ad.idx >= 0 ? ad.c * op[ad.idx] : 0.0; }
+
+// Reverse of a square-array write "X(i,j) (+)= s; X(j,i) = X(i,j) * h" (i <= j) on the
+// running cotangent cb of X.  Returns the cotangent of s.  accumulate: the old X(i,j)
+// keeps a cotangent (it was added to); assign: the old values are overwritten.
+inline double fold_square(double* cb, int64_t ij, int64_t ji, bool diag, int h, bool accumulate) {
+  const double g = diag ? h * cb[ij] : cb[ij] + h * cb[ji];
+  cb[ij] = accumulate ? g : 0.0;
+  if (!diag) cb[ji] = 0.0;
+  return g;
+}
+
+// commutator_110 / commutator_220: d E0 / d(L, R) times ebar
+void comm110_vjp(const Basis& B, const double* L, int hL, const double* R, int hR, double ebar, double* Lb,
+                 double* Rb) {
+  for (int i = 0; i < B.A; ++i) {
+    const double w = ebar * (hL - hR) * (B.jj[B.holes[i]] + 1);
+    for (int a = 0; a < B.P; ++a) {
+      const int64_t k = B.off_fph + a + (int64_t)i * B.P;
+      Lb[k] += w * R[k];
+      Rb[k] += w * L[k];
+    }
+  }
+}
+
+void comm220_vjp(const Basis& B, const double* L, int hL, const double* R, int hR, double ebar, double* Lb,
+                 double* Rb) {
+  if (hR * hL != -1) return;
+  for (int q = 0; q < B.nblocks; ++q) {
+    const int64_t n = (int64_t)B.ncls[q][0] * B.ncls[q][2];
+    const double w = -2.0 * hR * (B.lamJ[q] + 1) * ebar;
+    const int64_t o = B.goff[q][2];
+    for (int64_t k = 0; k < n; ++k) {
+      Lb[o + k] += w * R[o + k];
+      Rb[o + k] += w * L[o + k];
+    }
+  }
+}
+
+// commutator_111: every one-body element of RES is assigned
+void comm111_vjp(const Basis& B, const double* L, int hL, const double* R, int hR, double* cb, double* Lb,
+                 double* Rb) {
+  const int A = B.A, P = B.P;
+  const double *Lhh = L + B.off_fhh, *Rhh = R + B.off_fhh, *Lph = L + B.off_fph, *Rph = R + B.off_fph;
+  const double *Lpp = L + B.off_fpp, *Rpp = R + B.off_fpp;
+  double *Lhhb = Lb + B.off_fhh, *Rhhb = Rb + B.off_fhh, *Lphb = Lb + B.off_fph, *Rphb = Rb + B.off_fph;
+  double *Lppb = Lb + B.off_fpp, *Rppb = Rb + B.off_fpp;
+  const double* Chh = cb + B.off_fhh;
+  const double* Cph = cb + B.off_fph;
+  const double* Cpp = cb + B.off_fpp;
+  std::vector<double> t1((size_t)std::max(A * A, P * P)), t2((size_t)std::max(A * A, P * P));
+  // fhh = th1 + hL th2 - hR (hL th1^T + th2^T), th1 = Lhh Rhh, th2 = Lph^T Rph
+  for (int j = 0; j < A; ++j)
+    for (int i = 0; i < A; ++i) {
+      t1[i + j * A] = Chh[i + j * A] - hL * hR * Chh[j + i * A];
+      t2[i + j * A] = hL * Chh[i + j * A] - hR * Chh[j + i * A];
+    }
+  if (A) {
+    dgemm('N', 'T', A, A, A, 1.0, t1.data(), A, Rhh, A, 1.0, Lhhb, A);
+    dgemm('T', 'N', A, A, A, 1.0, Lhh, A, t1.data(), A, 1.0, Rhhb, A);
+    if (P) {
+      dgemm('N', 'T', P, A, A, 1.0, Rph, P, t2.data(), A, 1.0, Lphb, P);
+      dgemm('N', 'N', P, A, A, 1.0, Lph, P, t2.data(), A, 1.0, Rphb, P);
+    }
+  }
+  // fph = Lph Rhh + Lpp Rph - Rph Lhh - Rpp Lph
+  if (P && A) {
+    dgemm('N', 'T', P, A, A, 1.0, Cph, P, Rhh, A, 1.0, Lphb, P);
+    dgemm('T', 'N', A, A, P, 1.0, Lph, P, Cph, P, 1.0, Rhhb, A);
+    dgemm('N', 'T', P, P, A, 1.0, Cph, P, Rph, P, 1.0, Lppb, P);
+    dgemm('T', 'N', P, A, P, 1.0, Lpp, P, Cph, P, 1.0, Rphb, P);
+    dgemm('N', 'T', P, A, A, -1.0, Cph, P, Lhh, A, 1.0, Rphb, P);
+    dgemm('T', 'N', A, A, P, -1.0, Rph, P, Cph, P, 1.0, Lhhb, A);
+    dgemm('N', 'T', P, P, A, -1.0, Cph, P, Lph, P, 1.0, Rppb, P);
+    dgemm('T', 'N', P, A, P, -1.0, Rpp, P, Cph, P, 1.0, Lphb, P);
+  }
+  // fpp = hR tp1 + tp2 - hL (tp1^T + hR tp2^T), tp1 = Lph Rph^T, tp2 = Lpp Rpp
+  for (int j = 0; j < P; ++j)
+    for (int i = 0; i < P; ++i) {
+      t1[i + (size_t)j * P] = hR * Cpp[i + (size_t)j * P] - hL * Cpp[j + (size_t)i * P];
+      t2[i + (size_t)j * P] = Cpp[i + (size_t)j * P] - hL * hR * Cpp[j + (size_t)i * P];
+    }
+  if (P) {
+    if (A) {
+      dgemm('N', 'N', P, A, P, 1.0, t1.data(), P, Rph, P, 1.0, Lphb, P);
+      dgemm('T', 'N', P, A, P, 1.0, t1.data(), P, Lph, P, 1.0, Rphb, P);
+    }
+    dgemm('N', 'T', P, P, P, 1.0, t2.data(), P, Rpp, P, 1.0, Lppb, P);
+    dgemm('T', 'N', P, P, P, 1.0, Lpp, P, t2.data(), P, 1.0, Rppb, P);
+  }
+  std::fill(cb + B.off_fhh, cb + B.off_fph + (int64_t)P * A, 0.0);
+}
+
+// commutator_121: one-body outputs accumulate (hh / pp squares then mirrored)
+void comm121_vjp(const Basis& B, const double* L, int hL, const double* R, int hR, int hRES, double* cb,
+                 double* Lb, double* Rb) {
+  auto inner_vjp = [&](int pk, int qk, double sbar) {
+    const int jq = B.jj[qk];
+    for (int a = 0; a < B.P; ++a) {
+      const int ak = B.parts[a];
+      for (int i = 0; i < B.A; ++i) {
+        const int ik = B.holes[i];
+        if (B.jj[ik] != B.jj[ak] || B.ll[ik] != B.ll[ak] || B.tz[ik] != B.tz[ak]) continue;
+        const int ji = B.jj[ik];
+        const int64_t ph = B.off_fph + a + (int64_t)i * B.P;
+        const double lai = L[ph], rai = R[ph];
+        double smx = 0, smy = 0, smx2 = 0, smy2 = 0;
+        for (int JT = std::abs(ji - jq); JT <= ji + jq; JT += 2) {
+          const Addr rx = v_addr(B, hR, ak, pk, ik, qk, JT), ry = v_addr(B, hR, ik, pk, ak, qk, JT);
+          const Addr lx = v_addr(B, hL, ak, pk, ik, qk, JT), ly = v_addr(B, hL, ik, pk, ak, qk, JT);
+          smx += val_at(R, rx) * (JT + 1);
+          smy += val_at(R, ry) * (JT + 1);
+          smx2 += val_at(L, lx) * (JT + 1);
+          smy2 += val_at(L, ly) * (JT + 1);
+          add_at(Rb, rx, sbar * lai * hL * (JT + 1));
+          add_at(Rb, ry, -sbar * lai * (JT + 1));
+          add_at(Lb, lx, -sbar * rai * hR * (JT + 1));
+          add_at(Lb, ly, sbar * rai * (JT + 1));
+        }
+        Lb[ph] += sbar * (hL * smx - smy);
+        Rb[ph] -= sbar * (hR * smx2 - smy2);
+      }
+    }
+  };
+  auto same = [&](int x, int y) { return B.jj[x] == B.jj[y] && B.ll[x] == B.ll[y] && B.tz[x] == B.tz[y]; };
+  for (int p = 0; p < B.A; ++p)
+    for (int q = p; q < B.A; ++q) {
+      const int pk = B.holes[p], qk = B.holes[q];
+      if (!same(pk, qk)) continue;
+      const double g = fold_square(cb, B.off_fhh + p + (int64_t)q * B.A, B.off_fhh + q + (int64_t)p * B.A, p == q,
+                                   hRES, true);
+      inner_vjp(pk, qk, g / (B.jj[pk] + 1.0));
+    }
+  for (int p = 0; p < B.P; ++p)
+    for (int q = p; q < B.P; ++q) {
+      const int pk = B.parts[p], qk = B.parts[q];
+      if (!same(pk, qk)) continue;
+      const double g = fold_square(cb, B.off_fpp + p + (int64_t)q * B.P, B.off_fpp + q + (int64_t)p * B.P, p == q,
+                                   hRES, true);
+      inner_vjp(pk, qk, g / (B.jj[pk] + 1.0));
+    }
+  for (int p = 0; p < B.P; ++p)
+    for (int q = 0; q < B.A; ++q) {
+      const int pk = B.parts[p], qk = B.holes[q];
+      if (!same(pk, qk)) continue;
+      inner_vjp(pk, qk, cb[B.off_fph + p + (int64_t)q * B.P] / (B.jj[pk] + 1.0));
+    }
+}
+
+// commutator_122: every two-body element is assigned
+void comm122_vjp(const Basis& B, const double* L, int hL, const double* R, int hR, int hRES, double* cb,
+                 double* Lb, double* Rb) {
+  for (int q = 0; q < B.nblocks; ++q) {
+    const int JT = B.lamJ[q];
+    for (int g = 0; g < 6; ++g) {
+      const int n1 = B.gn1[q][g], n2 = B.gn2[q][g];
+      if (n1 * n2 == 0) continue;
+      const int c1 = SEA1[g], c2 = SEA2[g];
+      const int64_t o = B.goff[q][g];
+      for (int IX = 0; IX < n1; ++IX) {
+        const int a = B.qa[q][c1][IX], b = B.qb[q][c1][IX];
+        for (int JX = SQS[g] ? IX : 0; JX < n2; ++JX) {
+          const int c = B.qa[q][c2][JX], d = B.qb[q][c2][JX];
+          const int64_t ij = o + IX + (int64_t)JX * n1, ji = o + JX + (int64_t)IX * n1;
+          double s;
+          if (SQS[g]) {
+            s = fold_square(cb, ij, ji, IX == JX, hRES, false);
+          } else {
+            s = cb[ij];
+            cb[ij] = 0.0;
+          }
+          s = s / std::sqrt(1.0 + kd(a, b)) / std::sqrt(1.0 + kd(c, d));
+          if (s == 0.0) continue;
+          // each term sm += X * Y contributes Xbar += s * Y, Ybar += s * X
+          auto term = [&](const Addr& fL, const Addr& vR, const Addr& fR, const Addr& vL, double sign) {
+            add_at(Lb, fL, sign * s * val_at(R, vR));
+            add_at(Rb, vR, sign * s * val_at(L, fL));
+            add_at(Rb, fR, -sign * s * val_at(L, vL));
+            add_at(Lb, vL, -sign * s * val_at(R, fR));
+          };
+          for (int i : B.same[a])
+            term(f_addr(B, hL, a, i), v_addr(B, hR, i, b, c, d, JT), f_addr(B, hR, a, i),
+                 v_addr(B, hL, i, b, c, d, JT), 1.0);
+          for (int i : B.same[b])
+            term(f_addr(B, hL, b, i), v_addr(B, hR, a, i, c, d, JT), f_addr(B, hR, b, i),
+                 v_addr(B, hL, a, i, c, d, JT), 1.0);
+          for (int i : B.same[c])
+            term(f_addr(B, hL, i, c), v_addr(B, hR, a, b, i, d, JT), f_addr(B, hR, i, c),
+                 v_addr(B, hL, a, b, i, d, JT), -1.0);
+          for (int i : B.same[d])
+            term(f_addr(B, hL, i, d), v_addr(B, hR, a, b, c, i, JT), f_addr(B, hR, i, d),
+                 v_addr(B, hL, a, b, c, i, JT), -1.0);
+        }
+      }
+    }
+  }
+}
+
+// commutator_222_pp_hh: RES accumulates W1 - W2 combinations (cb passes through); w1b, w2b
+// carry the cotangents of the w1 / w2 workspaces from commutator_221
+void comm222pphh_vjp(const Basis& B, const double* L, int hL, const double* R, int hR, const double* cb,
+                     const double* w1b, const double* w2b, double* Lb, double* Rb) {
+  const double pm = hR * hL;
+  for (int q = 0; q < B.nblocks; ++q) {
+    const int np = B.ncls[q][0], nb = B.ncls[q][1], nh = B.ncls[q][2];
+    auto blk = [&](const double* op, int g) { return B.X(op, q, g); };
+    auto blkw = [&](double* op, int g) { return B.X(op, q, g); };
+    const double *L1 = blk(L, 0), *L2 = blk(L, 1), *L3 = blk(L, 2), *L5 = blk(L, 4), *L6 = blk(L, 5);
+    const double *R1 = blk(R, 0), *R2 = blk(R, 1), *R3 = blk(R, 2), *R5 = blk(R, 4), *R6 = blk(R, 5);
+    double *L1b = blkw(Lb, 0), *L2b = blkw(Lb, 1), *L3b = blkw(Lb, 2), *L5b = blkw(Lb, 4), *L6b = blkw(Lb, 5);
+    double *R1b = blkw(Rb, 0), *R2b = blkw(Rb, 1), *R3b = blkw(Rb, 2), *R5b = blkw(Rb, 4), *R6b = blkw(Rb, 5);
+    // cotangents of the twelve W blocks
+    std::vector<double> W1[6], W2[6];
+    for (int g = 0; g < 6; ++g) {
+      const int64_t n = (int64_t)B.gn1[q][g] * B.gn2[q][g];
+      W1[g].assign(blk(w1b, g), blk(w1b, g) + n);
+      W2[g].assign(blk(w2b, g), blk(w2b, g) + n);
+    }
+    auto antisym = [&](int g, int n) {
+      const double* C = blk(cb, g);
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const double v = C[i + (int64_t)j * n] - pm * C[j + (int64_t)i * n];
+          W1[g][i + (int64_t)j * n] += v;
+          W2[g][i + (int64_t)j * n] -= v;
+        }
+    };
+    auto plain = [&](int g) {
+      const double* C = blk(cb, g);
+      const int64_t n = (int64_t)B.gn1[q][g] * B.gn2[q][g];
+      for (int64_t k = 0; k < n; ++k) {
+        W1[g][k] += C[k];
+        W2[g][k] -= C[k];
+      }
+    };
+    antisym(0, np);
+    antisym(4, nh);
+    antisym(3, nb);
+    plain(2);
+    plain(5);
+    plain(1);
+    const double *W11 = W1[0].data(), *W12 = W1[1].data(), *W13 = W1[2].data(), *W14 = W1[3].data(),
+                 *W15 = W1[4].data(), *W16 = W1[5].data();
+    const double *W21 = W2[0].data(), *W22 = W2[1].data(), *W23 = W2[2].data(), *W24 = W2[3].data(),
+                 *W25 = W2[4].data(), *W26 = W2[5].data();
+    if (np != 0) {  // W11 = L1 R1
+      dgemm('N', 'T', np, np, np, 1.0, W11, np, R1, np, 1.0, L1b, np);
+      dgemm('T', 'N', np, np, np, 1.0, L1, np, W11, np, 1.0, R1b, np);
+    }
+    if (nh != 0) {  // W25 = L5 R5
+      dgemm('N', 'T', nh, nh, nh, 1.0, W25, nh, R5, nh, 1.0, L5b, nh);
+      dgemm('T', 'N', nh, nh, nh, 1.0, L5, nh, W25, nh, 1.0, R5b, nh);
+    }
+    if (np * nh != 0) {
+      // W15 = hL L3^T R3
+      dgemm('N', 'T', np, nh, nh, 1.0 * hL, R3, np, W15, nh, 1.0, L3b, np);
+      dgemm('N', 'N', np, nh, nh, 1.0 * hL, L3, np, W15, nh, 1.0, R3b, np);
+      // W21 = hR L3 R3^T
+      dgemm('N', 'N', np, nh, np, 1.0 * hR, W21, np, R3, np, 1.0, L3b, np);
+      dgemm('T', 'N', np, nh, np, 1.0 * hR, W21, np, L3, np, 1.0, R3b, np);
+      // W13 = L1 R3 - R1 L3
+      dgemm('N', 'T', np, np, nh, 1.0, W13, np, R3, np, 1.0, L1b, np);
+      dgemm('T', 'N', np, nh, np, 1.0, L1, np, W13, np, 1.0, R3b, np);
+      dgemm('N', 'T', np, np, nh, -1.0, W13, np, L3, np, 1.0, R1b, np);
+      dgemm('T', 'N', np, nh, np, -1.0, R1, np, W13, np, 1.0, L3b, np);
+      // W23 = L3 R5 - R3 L5
+      dgemm('N', 'T', np, nh, nh, 1.0, W23, np, R5, nh, 1.0, L3b, np);
+      dgemm('T', 'N', nh, nh, np, 1.0, L3, np, W23, np, 1.0, R5b, nh);
+      dgemm('N', 'T', np, nh, nh, -1.0, W23, np, L5, nh, 1.0, R3b, np);
+      dgemm('T', 'N', nh, nh, np, -1.0, R3, np, W23, np, 1.0, L5b, nh);
+    }
+    if (nb * nh != 0) {  // W24 = hR L6 R6^T
+      dgemm('N', 'N', nb, nh, nb, 1.0 * hR, W24, nb, R6, nb, 1.0, L6b, nb);
+      dgemm('T', 'N', nb, nh, nb, 1.0 * hR, W24, nb, L6, nb, 1.0, R6b, nb);
+    }
+    if (nb * np != 0) {  // W14 = hL L2^T R2
+      dgemm('N', 'T', np, nb, nb, 1.0 * hL, R2, np, W14, nb, 1.0, L2b, np);
+      dgemm('N', 'N', np, nb, nb, 1.0 * hL, L2, np, W14, nb, 1.0, R2b, np);
+    }
+    if (nb * nh != 0) {  // W26 = L6 R5 - R6 L5
+      dgemm('N', 'T', nb, nh, nh, 1.0, W26, nb, R5, nh, 1.0, L6b, nb);
+      dgemm('T', 'N', nh, nh, nb, 1.0, L6, nb, W26, nb, 1.0, R5b, nh);
+      dgemm('N', 'T', nb, nh, nh, -1.0, W26, nb, L5, nh, 1.0, R6b, nb);
+      dgemm('T', 'N', nh, nh, nb, -1.0, R6, nb, W26, nb, 1.0, L5b, nh);
+    }
+    if (nb * np != 0) {  // W12 = L1 R2 - R1 L2
+      dgemm('N', 'T', np, np, nb, 1.0, W12, np, R2, np, 1.0, L1b, np);
+      dgemm('T', 'N', np, nb, np, 1.0, L1, np, W12, np, 1.0, R2b, np);
+      dgemm('N', 'T', np, np, nb, -1.0, W12, np, L2, np, 1.0, R1b, np);
+      dgemm('T', 'N', np, nb, np, -1.0, R1, np, W12, np, 1.0, L2b, np);
+    }
+    if (nb * np * nh != 0) {
+      // W16 = hL L2^T R3 - hR R2^T L3
+      dgemm('N', 'T', np, nb, nh, 1.0 * hL, R3, np, W16, nb, 1.0, L2b, np);
+      dgemm('N', 'N', np, nh, nb, 1.0 * hL, L2, np, W16, nb, 1.0, R3b, np);
+      dgemm('N', 'T', np, nb, nh, -1.0 * hR, L3, np, W16, nb, 1.0, R2b, np);
+      dgemm('N', 'N', np, nh, nb, -1.0 * hR, R2, np, W16, nb, 1.0, L3b, np);
+      // W22 = hR L3 R6^T - hL R3 L6^T
+      dgemm('N', 'N', np, nh, nb, 1.0 * hR, W22, np, R6, nb, 1.0, L3b, np);
+      dgemm('T', 'N', nb, nh, np, 1.0 * hR, W22, np, L3, np, 1.0, R6b, nb);
+      dgemm('N', 'N', np, nh, nb, -1.0 * hL, W22, np, L6, nb, 1.0, R3b, np);
+      dgemm('T', 'N', nb, nh, np, -1.0 * hL, W22, np, R3, np, 1.0, L6b, nb);
+    }
+  }
+}
+
+// commutator_221: one-body outputs accumulate traces of w1 (hole c) and w2 (particle c)
+void comm221_vjp(const Basis& B, int hL, int hR, int hRES, double* cb, double* w1b, double* w2b) {
+  const int pm = hR * hL;
+  auto same = [&](int x, int y) { return B.jj[x] == B.jj[y] && B.ll[x] == B.ll[y] && B.tz[x] == B.tz[y]; };
+  auto trace_vjp = [&](int ik, int jk, bool antisym, double tb) {
+    const int ji = B.jj[ik];
+    for (int side = 0; side < 2; ++side) {
+      const std::vector<int>& cs = side == 0 ? B.holes : B.parts;
+      double* wb = side == 0 ? w1b : w2b;
+      for (int ck : cs) {
+        const int jc = B.jj[ck];
+        for (int JT = std::abs(jc - ji); JT <= jc + ji; JT += 2) {
+          add_at(wb, v_addr(B, 1, ck, ik, ck, jk, JT), tb * (JT + 1));
+          if (antisym) add_at(wb, v_addr(B, 1, ck, jk, ck, ik, JT), -pm * tb * (JT + 1));
+        }
+      }
+    }
+  };
+  for (int i = 0; i < B.A; ++i)
+    for (int j = i; j < B.A; ++j) {
+      const int ik = B.holes[i], jk = B.holes[j];
+      if (!same(ik, jk)) continue;
+      const double g = fold_square(cb, B.off_fhh + i + (int64_t)j * B.A, B.off_fhh + j + (int64_t)i * B.A, i == j,
+                                   hRES, true);
+      trace_vjp(ik, jk, true, g / (B.jj[ik] + 1.0));
+    }
+  for (int i = 0; i < B.P; ++i)
+    for (int j = i; j < B.P; ++j) {
+      const int ik = B.parts[i], jk = B.parts[j];
+      if (!same(ik, jk)) continue;
+      const double g = fold_square(cb, B.off_fpp + i + (int64_t)j * B.P, B.off_fpp + j + (int64_t)i * B.P, i == j,
+                                   hRES, true);
+      trace_vjp(ik, jk, true, g / (B.jj[ik] + 1.0));
+    }
+  for (int i = 0; i < B.P; ++i)
+    for (int j = 0; j < B.A; ++j) {
+      const int ik = B.parts[i], jk = B.holes[j];
+      if (!same(ik, jk)) continue;
+      trace_vjp(ik, jk, false, cb[B.off_fph + i + (int64_t)j * B.P] / (B.jj[ik] + 1.0));
+    }
+}
+
+// calculate_cross_coupled: every CC element is assigned from v_elem values of op
+void cross_coupled_vjp(const Basis& B, int herm, const double* ccb, double* opb) {
+  for (int q1 = 0; q1 < B.ncc; ++q1) {
+    const int JC = B.cc_J[q1];
+    const int rlen = B.cc_rlen[q1];
+    const double* CC = ccb + B.cc_off[q1];
+    for (int nbx = 0; nbx < B.cc_nph[q1]; ++nbx) {
+      const int p = B.cc_php[q1][nbx], h = B.cc_phh[q1][nbx];
+      const int jp = B.jj[p], jh = B.jj[h], lp = B.ll[p], lh = B.ll[h], tp = B.tz[p], th = B.tz[h];
+      for (int r = 0; r < rlen; ++r) {
+        const int a = B.cc_pa[q1][r], b = B.cc_pb[q1][r];
+        const int ja = B.jj[a], jb = B.jj[b], la = B.ll[a], lb = B.ll[b], ta = B.tz[a], tb = B.tz[b];
+        if (!(((la + lh) % 2 == (lb + lp) % 2) && (ta + th == tb + tp))) continue;
+        const double g = CC[r + (int64_t)nbx * rlen] * sgn((jh + jb + JC) / 2) * std::sqrt(JC + 1.0);
+        if (g == 0.0) continue;
+        const int Jmin = std::max(std::abs(jp - jb), std::abs(ja - jh));
+        const int Jmax = std::min(jp + jb, ja + jh);
+        for (int JT = Jmin; JT <= Jmax; JT += 2)
+          add_at(opb, v_addr(B, herm, h, a, p, b, JT), g * sgn(JT / 2) * (JT + 1) * sixj(jp, jh, JC, ja, jb, JT));
+      }
+    }
+  }
+}
+
+// commutator_222_ph: WCC = LCC RCC^T, then the recoupled WCC accumulates into RES
+void comm222ph_vjp(const Basis& B, const double* LCC, int hL, const double* RCC, int hR, int hRES, double* cb,
+                   double* LCCb, double* RCCb) {
+  std::vector<double> Wb(std::max<int64_t>(B.wcc_size, 1), 0.0);
+  const int N = B.N, NJ = B.NJ;
+  auto rv = [&](int a, int b, int JP) { return B.ccr[((size_t)a * N + b) * NJ + JP / 2]; };
+  for (int q = 0; q < B.nblocks; ++q) {
+    const int Jtot = B.lamJ[q];
+    for (int g = 0; g < 6; ++g) {
+      const int n1 = B.gn1[q][g], n2 = B.gn2[q][g];
+      if (n1 * n2 == 0) continue;
+      const int c1 = SEA1[g], c2 = SEA2[g];
+      const int64_t o = B.goff[q][g];
+      for (int IX = 0; IX < n1; ++IX) {
+        const int i = B.qa[q][c1][IX], j = B.qb[q][c1][IX];
+        const double pre = (i == j) ? .70710678118 : 1.0;
+        const int ji = B.jj[i], jj_ = B.jj[j], li = B.ll[i], lj = B.ll[j], ti = B.tz[i], tj = B.tz[j];
+        for (int JX = SQS[g] ? IX : 0; JX < n2; ++JX) {
+          const int k = B.qa[q][c2][JX], l = B.qb[q][c2][JX];
+          const double pre2 = (k == l) ? .70710678118 : 1.0;
+          const int jk = B.jj[k], jl = B.jj[l], lk = B.ll[k], ll = B.ll[l], tk = B.tz[k], tl = B.tz[l];
+          // the forward skips the element (no update, no mirror) unless both checks pass
+          const int Tz1 = std::abs(ti - tk) / 2, PAR1 = (li + lk) % 2;
+          if (std::abs(tl - tj) != Tz1 * 2 || (ll + lj) % 2 != PAR1) continue;
+          const int Tz2 = std::abs(ti - tl) / 2, PAR2 = (li + ll) % 2;
+          if (std::abs(tk - tj) != Tz2 * 2 || (lk + lj) % 2 != PAR2) continue;
+          const int64_t ij = o + IX + (int64_t)JX * n1, ji_ = o + JX + (int64_t)IX * n1;
+          const double s = (SQS[g] ? fold_square(cb, ij, ji_, IX == JX, hRES, true) : cb[ij]) * pre * pre2;
+          if (s == 0.0) continue;
+          const double phase = sgn((ji + jj_ + jk + jl) / 2);
+          int jmin = std::max(std::abs(jj_ - jl), std::abs(ji - jk));
+          int jmax = std::min(jj_ + jl, ji + jk);
+          for (int JP = jmin; JP <= jmax; JP += 2) {
+            const int qx = B.ccq(JP, Tz1, PAR1);
+            double* W = Wb.data() + B.wcc_off[qx];
+            const int64_t rl = B.cc_rlen[qx];
+            const int rjl = rv(j, l, JP), rik = rv(i, k, JP), gjl = rv(l, j, JP), gik = rv(k, i, JP);
+            const double c = -sgn((jl + jk + Jtot) / 2) * sixj(ji, jj_, Jtot, jl, jk, JP) * s;
+            W[gik + rjl * rl] += c * hL;
+            W[gjl + rik * rl] += c * phase * hL;
+            W[rik + gjl * rl] -= c * phase * hR;
+            W[rjl + gik * rl] -= c * hR;
+          }
+          jmin = std::max(std::abs(ji - jl), std::abs(jj_ - jk));
+          jmax = std::min(ji + jl, jj_ + jk);
+          for (int JP = jmin; JP <= jmax; JP += 2) {
+            const int qx = B.ccq(JP, Tz2, PAR2);
+            double* W = Wb.data() + B.wcc_off[qx];
+            const int64_t rl = B.cc_rlen[qx];
+            const int ril = rv(i, l, JP), rjk = rv(j, k, JP), gil = rv(l, i, JP), gjk = rv(k, j, JP);
+            const double c = sixj(ji, jj_, Jtot, jk, jl, JP) * s;
+            W[gil + rjk * rl] += c * hL;
+            W[gjk + ril * rl] += c * phase * hL;
+            W[ril + gjk * rl] -= c * phase * hR;
+            W[rjk + gil * rl] -= c * hR;
+          }
+        }
+      }
+    }
+  }
+  for (int q = 0; q < B.ncc; ++q) {
+    const int nb = B.cc_nph[q], r = B.cc_rlen[q];
+    if (nb * r == 0) continue;
+    const double* W = Wb.data() + B.wcc_off[q];
+    dgemm('N', 'N', r, nb, r, 1.0, W, r, RCC + B.cc_off[q], r, 1.0, LCCb + B.cc_off[q], r);
+    dgemm('T', 'N', r, nb, r, 1.0, W, r, LCC + B.cc_off[q], r, 1.0, RCCb + B.cc_off[q], r);
+  }
+}
+
+// Reverse of full_commutator: Lb += d<Cb, [L,R]>/dL, Rb += d<Cb, [L,R]>/dR.  RES enters the
+// forward only through E0 when with_e0 is false; that carried value has no cotangent here.
+void full_commutator_vjp(const Basis& B, const double* L, int hL, const double* R, int hR, int hRES,
+                         bool with_e0, const double* Cb, double* Lb, double* Rb) {
+  std::vector<double> cb(Cb, Cb + B.slab), w1b(B.slab, 0.0), w2b(B.slab, 0.0);
+  std::vector<double> lcc(std::max<int64_t>(B.cc_size, 1)), rcc(std::max<int64_t>(B.cc_size, 1));
+  std::vector<double> lccb(std::max<int64_t>(B.cc_size, 1), 0.0), rccb(std::max<int64_t>(B.cc_size, 1), 0.0);
+  cross_coupled(B, L, hL, lcc.data());
+  cross_coupled(B, R, hR, rcc.data());
+  comm222ph_vjp(B, lcc.data(), hL, rcc.data(), hR, hRES, cb.data(), lccb.data(), rccb.data());
+  comm221_vjp(B, hL, hR, hRES, cb.data(), w1b.data(), w2b.data());
+  comm222pphh_vjp(B, L, hL, R, hR, cb.data(), w1b.data(), w2b.data(), Lb, Rb);
+  comm122_vjp(B, L, hL, R, hR, hRES, cb.data(), Lb, Rb);
+  comm121_vjp(B, L, hL, R, hR, hRES, cb.data(), Lb, Rb);
+  comm111_vjp(B, L, hL, R, hR, cb.data(), Lb, Rb);
+  if (with_e0) {
+    comm110_vjp(B, L, hL, R, hR, cb[0], Lb, Rb);
+    comm220_vjp(B, L, hL, R, hR, cb[0], Lb, Rb);
+  }
+  cross_coupled_vjp(B, hL, lccb.data(), Lb);
+  cross_coupled_vjp(B, hR, rccb.data(), Rb);
+}
+
+// build_gs_white: Hb += d<ETAb, eta(H)>/dH (eta = H_ai / D_ai and V_abij / D_abij with the
+// denominators' one-body diagonals and monopoles differentiated too)
+void white_vjp(const Basis& B, const double* H, int hH, const double* ETAb, double* Hb) {
+  for (int a = 0; a < B.P; ++a) {
+    const int ak = B.parts[a];
+    for (int i = 0; i < B.A; ++i) {
+      const int ik = B.holes[i];
+      if (B.jj[ik] != B.jj[ak] || B.ll[ik] != B.ll[ak] || B.tz[ik] != B.tz[ak]) continue;
+      const int ji = B.jj[ik];
+      const int64_t ph = B.off_fph + a + (int64_t)i * B.P;
+      const double eb = ETAb[ph];
+      if (eb == 0.0) continue;
+      double Eden = 0.0;
+      for (int JT = 0; JT <= 2 * ji; JT += 2) Eden -= (JT + 1) * v_elem(B, H, hH, ak, ik, ak, ik, JT);
+      Eden = Eden / (ji + 1.0) / (ji + 1.0);
+      Eden = Eden + cfpp(B, H, a, a) - cfhh(B, H, i, i);
+      Hb[ph] += eb / Eden;
+      const double db = -eb * H[ph] / (Eden * Eden);
+      Hb[B.off_fpp + a + (int64_t)a * B.P] += db;
+      Hb[B.off_fhh + i + (int64_t)i * B.A] -= db;
+      for (int JT = 0; JT <= 2 * ji; JT += 2)
+        add_at(Hb, v_addr(B, hH, ak, ik, ak, ik, JT), -db * (JT + 1) / (ji + 1.0) / (ji + 1.0));
+    }
+  }
+  auto mono_vjp = [&](int a, int b, double g) {
+    const int ja = B.jj[a], jb = B.jj[b];
+    for (int JT = std::abs(ja - jb); JT <= ja + jb; JT += 2)
+      add_at(Hb, v_addr(B, hH, a, b, a, b, JT), g * (JT + 1) / (ja + 1.0) / (jb + 1.0));
+  };
+  for (int q = 0; q < B.nblocks; ++q) {
+    const int np = B.ncls[q][0], nh = B.ncls[q][2];
+    const double* HX = B.X(H, q, 2);
+    const double* EB = B.X(ETAb, q, 2);
+    const int64_t o = B.goff[q][2];
+    for (int IX = 0; IX < np; ++IX) {
+      const int a = B.qa[q][0][IX], b = B.qb[q][0][IX];
+      for (int JX = 0; JX < nh; ++JX) {
+        const double eb = EB[IX + (int64_t)JX * np];
+        if (eb == 0.0) continue;
+        const int i = B.qa[q][2][JX], j = B.qb[q][2][JX];
+        double Eden = 0.0;
+        Eden += monopole(B, H, hH, a, b);
+        Eden += monopole(B, H, hH, i, j);
+        Eden -= monopole(B, H, hH, a, i);
+        Eden -= monopole(B, H, hH, a, j);
+        Eden -= monopole(B, H, hH, i, b);
+        Eden -= monopole(B, H, hH, j, b);
+        Eden += f_elem(B, H, hH, a, a) + f_elem(B, H, hH, b, b) - f_elem(B, H, hH, i, i) - f_elem(B, H, hH, j, j);
+        const double hx = HX[IX + (int64_t)JX * np];
+        Hb[o + IX + (int64_t)JX * np] += eb / Eden;
+        const double db = -eb * hx / (Eden * Eden);
+        mono_vjp(a, b, db);
+        mono_vjp(i, j, db);
+        mono_vjp(a, i, -db);
+        mono_vjp(a, j, -db);
+        mono_vjp(i, b, -db);
+        mono_vjp(j, b, -db);
+        add_at(Hb, f_addr(B, hH, a, a), db);
+        add_at(Hb, f_addr(B, hH, b, b), db);
+        add_at(Hb, f_addr(B, hH, i, i), -db);
+        add_at(Hb, f_addr(B, hH, j, j), -db);
+      }
+    }
+  }
+}
+
 // ====================================================================== C interface
 extern "C" {
 
@@ -1182,6 +1771,19 @@ void orc_full_commutator(void* b, const double* L, int hL, const double* R, int 
   full_commutator(B, L, hL, R, hR, RES, hRES, w, true);
 }
 void orc_build_gs_white(void* b, const double* H, int hH, double* ETA) { white(*(Basis*)b, H, hH, ETA); }
+void orc_commutator_e0(void* b, const double* L, int hL, const double* R, int hR, double* RES, int hRES,
+                       int with_e0) {
+  Basis& B = *(Basis*)b;
+  Work w(B);
+  full_commutator(B, L, hL, R, hR, RES, hRES, w, with_e0 != 0);
+}
+void orc_commutator_vjp(void* b, const double* L, int hL, const double* R, int hR, int hRES, int with_e0,
+                        const double* Cb, double* Lb, double* Rb) {
+  full_commutator_vjp(*(Basis*)b, L, hL, R, hR, hRES, with_e0 != 0, Cb, Lb, Rb);
+}
+void orc_white_vjp(void* b, const double* H, int hH, const double* ETAb, double* Hb) {
+  white_vjp(*(Basis*)b, H, hH, ETAb, Hb);
+}
 double orc_mat_frob_norm(void* b, const double* op) { return frob(*(Basis*)b, op); }
 double orc_mbpt2(void* b, const double* H, int hH) { return mbpt2(*(Basis*)b, H, hH); }
 void orc_add_sq_op(void* b, const double* A, double ax, const double* Bop, double bx, double* C) {

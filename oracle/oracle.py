@@ -65,6 +65,9 @@ def lib():
         "orc_commutator_222_ph": (None, [vp, _dp, i, _dp, i, _dp, i, _dp]),
         "orc_full_commutator": (None, [vp, _dp, i, _dp, i, _dp, i]),
         "orc_build_gs_white": (None, [vp, _dp, i, _dp]),
+        "orc_commutator_e0": (None, [vp, _dp, i, _dp, i, _dp, i, i]),
+        "orc_commutator_vjp": (None, [vp, _dp, i, _dp, i, i, i, _dp, _dp, _dp]),
+        "orc_white_vjp": (None, [vp, _dp, i, _dp, _dp]),
         "orc_mat_frob_norm": (d, [vp, _dp]),
         "orc_mbpt2": (d, [vp, _dp, i]),
         "orc_add_sq_op": (None, [vp, _dp, d, _dp, d, _dp]),
@@ -191,6 +194,22 @@ class Oracle:
         RES = self.new()
         self.L.orc_full_commutator(self.h, L, hL, R, hR, RES, hRES)
         return RES
+
+    def commutator_e0(self, L, hL, R, hR, hRES, with_e0):
+        RES = self.new()
+        self.L.orc_commutator_e0(self.h, L, hL, R, hR, RES, hRES, 1 if with_e0 else 0)
+        return RES
+
+    def commutator_vjp(self, L, hL, R, hR, hRES, with_e0, Cb):
+        """(Lb, Rb): gradients of <Cb, [L, R]> (exact transpose of the forward routine)."""
+        Lb, Rb = self.new(), self.new()
+        self.L.orc_commutator_vjp(self.h, L, hL, R, hR, hRES, 1 if with_e0 else 0, Cb, Lb, Rb)
+        return Lb, Rb
+
+    def white_vjp(self, H, hH, ETAb):
+        Hb = self.new()
+        self.L.orc_white_vjp(self.h, H, hH, ETAb, Hb)
+        return Hb
 
     def white(self, H, hH=1):
         ETA = self.new()
