@@ -92,6 +92,18 @@ class ClockSampler:
         except Exception:
             self.proc = None
 
+    def wait_running(self, timeout: float = 15.0):
+        """Block until nvidia-smi has written two samples (it is past its start-up)."""
+        t = time.time()
+        while self.proc is not None and time.time() - t < timeout:
+            try:
+                with open(self.path) as f:
+                    if sum(1 for _ in f) >= 2:
+                        return
+            except OSError:
+                pass
+            time.sleep(0.1)
+
     @staticmethod
     def _stamp(s: str) -> float:
         import datetime
@@ -242,13 +254,72 @@ def reference_arm(args):
     }), flush=True)
 
 
+def adjoint_workload(args, local: int):
+    """dE0/dtheta through a FP64 Magnus flow by the device adjoint, checked against central
+    finite differences of the same flow: H(theta) = H0 + sum_k theta_k V_k with K seeded
+    channel-structured V_k ~ N(0, 0.1 MeV), theta = 0, eMax=6, ds=0.5 to s=30."""
+    import numpy as np
+    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300.adjoint import EngineBackend, MagnusFlowAdjoint, channel_perturbations
+    emax = args.emax if args.emax is not None else 6
+    K, h = args.adjoint_k, 1e-4
+    steps = int(round(args.s_end / args.ds))
+    b = make_basis(emax)
+    eng = Engine(b, device=local, precision="fp64")
+    H0 = eng.synthetic_hamiltonian(seed=1)
+    V = channel_perturbations(eng, K, sigma=0.1, seed=2)
+    fl = MagnusFlowAdjoint(EngineBackend(eng), H0, V, ds=args.ds, steps=steps)
+    theta = np.zeros(K)
+    t = time.perf_counter()
+    plan = fl.plan(theta)
+    eng.synchronize()
+    t_plan = time.perf_counter() - t
+    t = time.perf_counter()
+    e0 = fl.forward(theta, plan)
+    eng.synchronize()
+    t_fwd = time.perf_counter() - t
+    l0 = eng.launch_count()
+    t = time.perf_counter()
+    grad = fl.gradient()
+    eng.synchronize()
+    t_adj = time.perf_counter() - t
+    launches = eng.launch_count() - l0
+    nfd = K if args.fd_components is None else min(K, args.fd_components)
+    fd = np.zeros(nfd)
+    t = time.perf_counter()
+    for k in range(nfd):
+        tp, tm = theta.copy(), theta.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd[k] = (fl.forward(tp, plan) - fl.forward(tm, plan)) / (2 * h)
+    t_fd = time.perf_counter() - t
+    err = float(np.max(np.abs(grad[:nfd] - fd)) / np.max(np.abs(fd)))
+    print(json.dumps({
+        "metric": f"adjoint dE0/dtheta wall time, K={K}, eMax={emax} Magnus flow to s={args.s_end:g}",
+        "value": t_adj, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * t_adj,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"differentiable Magnus flow, eMax={emax} ({b.norbits} orbits), K={K} channel "
+                               f"perturbations N(0,0.1 MeV), theta=0, ds={args.ds}, {steps} steps, White generator",
+                   "plan_commutators": plan.commutators, "magnus_terms": plan.magnus, "bch_terms": plan.bch,
+                   "E0": e0, "forward_s": t_fwd, "plan_s": t_plan, "adjoint_s": t_adj,
+                   "adjoint_over_forward": t_adj / t_fwd, "fd_s": t_fd, "fd_h": h, "fd_components": nfd,
+                   "grad": grad.tolist(), "fd": fd.tolist(), "max_rel_err_vs_fd": err,
+                   "l2": "operators fit in L2 at this size (6.5 MiB per slab)"},
+        "gpu_launches": launches,
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20, help="timed Magnus steps")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--emax", type=int, default=10)
+    ap.add_argument("--emax", type=int, default=None, help="default 10 (flow), 6 (adjoint)")
+    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint"])
+    ap.add_argument("--adjoint-k", type=int, default=16)
+    ap.add_argument("--s-end", type=float, default=30.0, help="adjoint workload: flow length")
+    ap.add_argument("--fd-components", type=int, default=None)
     ap.add_argument("--mode", default="bf16x6", choices=["bf16x3", "bf16x6"])
     ap.add_argument("--ds", type=float, default=0.5)
     ap.add_argument("--bch-max-terms", type=int, default=11, help="BCH_EXPAND max_terms (10 nested commutators)")
@@ -258,11 +329,20 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    args.e2e_steps = max(1, args.e2e_steps)
     world, rank, local, pg = dist_setup()
 
+    if args.emax is None and args.workload == "flow":
+        args.emax = 10
     if args.impl == "reference":
         if rank == 0:
+            if args.emax is None:
+                args.emax = 6
             reference_arm(args)
+        return
+    if args.workload == "adjoint":
+        if rank == 0:
+            adjoint_workload(args, local)
         return
 
     from imsrg_gb300 import Engine, make_basis
@@ -276,14 +356,16 @@ def main():
     H = eng.synthetic_hamiltonian(seed=1)
 
     # ---- timed: K Magnus steps of the flow, each one CUDA-graph replay (after W warm-up steps)
+    # the clock sampler starts before the warm-up: nvidia-smi's own start-up can stall the
+    # device for seconds, which must not fall into the timed region
+    clocks = ClockSampler(local)
+    clocks.start()
     st = flow_state(eng, H)
     e0_steps = []
     for _ in range(W):
         e0_steps.append(eng.magnus_step(*st, args.ds, allow_unconverged=True, **step_kw)["E0"])
     eng.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
+    clocks.wait_running()
     barrier(pg)
     eng.synchronize()
     c0 = eng.magnus_step_counters()

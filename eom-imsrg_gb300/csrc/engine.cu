@@ -211,6 +211,8 @@ Ctx::~Ctx() {
   for (auto e : prof_pool) cudaEventDestroy(e);
   if (ev_begin) cudaEventDestroy(ev_begin);
   if (ev_end) cudaEventDestroy(ev_end);
+  if (stream) cudaStreamSynchronize(stream);
+  for (double* p : op_pool) cudaFree(p);
   tc_release();
   graph_release();
   adjoint_release();
@@ -402,17 +404,17 @@ imsrg_status Ctx::bch_expand(double* HS, const double* G, int hG, const double* 
   CK(ensure_flow_workspace());
   const size_t sb = sizeof(double) * (size_t)L.slab;
   CK(cuda(cudaMemcpyAsync(HS, H, sb, cudaMemcpyDeviceToDevice, stream), "copy HS"));
-  CK(cuda(cudaMemcpyAsync(d_int2, H, sb, cudaMemcpyDeviceToDevice, stream), "copy INT2"));
+  // ad^(n-1)(H) and ad^n(H) alternate between two buffers; the commutator assigns every
+  // element of its output (E0 included), so neither a copy nor a clear is needed
   double coef = 1.0;
   int iw;
   for (iw = 2; iw <= max_terms; ++iw) {
     coef = coef / (iw - 1.0);
-    CK(cuda(cudaMemcpyAsync(d_int1, HS, sb, cudaMemcpyDeviceToDevice, stream), "copy INT1"));
-    CK(cuda(cudaMemcpyAsync(d_ad, d_int2, sb, cudaMemcpyDeviceToDevice, stream), "copy AD"));
-    CK(cuda(cudaMemsetAsync(d_int2, 0, sb, stream), "clear INT2"));
-    CK(commutator(G, hG, d_ad, hH, d_int2, hH, true));
-    CK(axpby(d_int1, 1.0, d_int2, coef, HS));
-    CK(frob_async(d_int2, coef, 0));
+    const double* ad = (iw == 2) ? H : ((iw & 1) ? d_int2 : d_ad);
+    double* out = (iw & 1) ? d_ad : d_int2;
+    CK(commutator(G, hG, ad, hH, out, hH, true));
+    CK(axpby(HS, 1.0, out, coef, HS));
+    CK(frob_async(out, coef, 0));
     CK(read_scalars(1));
     if (h_scalars[0] < conv) break;
   }
@@ -612,7 +614,13 @@ imsrg_status imsrg_op_create(imsrg_ctx* ctx, int32_t herm, imsrg_op** out) {
   imsrg_op* op = new (std::nothrow) imsrg_op();
   if (!op) return IMSRG_ERR_OUT_OF_MEMORY;
   const size_t sb = sizeof(double) * (size_t)c->L.slab;
-  imsrg_status s = c->cuda(cudaMalloc(&op->d, sb), "cudaMalloc(operator)");
+  imsrg_status s = IMSRG_OK;
+  if (!c->op_pool.empty()) {  // recycled slab: stream order makes the reuse safe
+    op->d = c->op_pool.back();
+    c->op_pool.pop_back();
+  } else {
+    s = c->cuda(cudaMalloc(&op->d, sb), "cudaMalloc(operator)");
+  }
   if (s == IMSRG_OK) s = c->cuda(cudaMemsetAsync(op->d, 0, sb, c->stream), "memset(operator)");
   if (s != IMSRG_OK) {
     if (op->d) cudaFree(op->d);
@@ -629,8 +637,15 @@ imsrg_status imsrg_op_destroy(imsrg_ctx* ctx, imsrg_op* op) {
   CTX(ctx);
   if (!op) return IMSRG_OK;
   CK(check_op(c, op, "imsrg_op_destroy"));
-  cudaStreamSynchronize(c->stream);
-  cudaFree(op->d);
+  // keep up to 16 GiB of operator slabs for reuse (work still queued on the context's
+  // stream finishes before a later op_create's memset on the same stream touches them)
+  const size_t sb = sizeof(double) * (size_t)c->L.slab;
+  if ((c->op_pool.size() + 1) * sb <= (size_t(16) << 30)) {
+    c->op_pool.push_back(op->d);
+  } else {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(op->d);
+  }
   delete op;
   return IMSRG_OK;
 }

@@ -67,6 +67,7 @@ struct Ctx {
   imsrg::TcState* tc = nullptr;
   StepGraph* sg = nullptr;  // captured Magnus step (graph.cu)
   AdjointState* adj = nullptr;  // reverse-mode workspaces (adjoint.cu)
+  std::vector<double*> op_pool;  // slabs of destroyed operators, reused by imsrg_op_create
   // kernel launches issued (cumulative) and optional per-phase CUDA-event timing
   int64_t launches = 0;
   bool prof = false;

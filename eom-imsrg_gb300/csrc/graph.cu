@@ -210,20 +210,19 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
     CK_TC(axpby(G, 1.0, DG, ds, G));
     // ---- BCH_EXPAND
     CK_TC(cuda(cudaMemcpyAsync(HS, H, sb, cudaMemcpyDeviceToDevice, stream), "copy HS"));
-    CK_TC(cuda(cudaMemcpyAsync(d_int2, H, sb, cudaMemcpyDeviceToDevice, stream), "copy INT2"));
     fixed += launches - l0;
     double coef = 1.0;
     for (int iw = 2; iw <= max_terms; ++iw) {
       coef = coef / (iw - 1.0);
       const double c = coef;
+      // the same alternating buffers as Ctx::bch_expand
+      const double* ad = (iw == 2) ? H : ((iw & 1) ? d_int2 : d_ad);
+      double* out = (iw & 1) ? d_ad : d_int2;
       CK_TC(capture_if(hb[iw - 2], [&]() -> imsrg_status {
         const int64_t b0 = launches;
-        CK_TC(cuda(cudaMemcpyAsync(d_int1, HS, sb, cudaMemcpyDeviceToDevice, stream), "copy INT1"));
-        CK_TC(cuda(cudaMemcpyAsync(d_ad, d_int2, sb, cudaMemcpyDeviceToDevice, stream), "copy AD"));
-        CK_TC(cuda(cudaMemsetAsync(d_int2, 0, sb, stream), "clear INT2"));
-        CK_TC(commutator(G, hG, d_ad, hH, d_int2, hH, true));
-        CK_TC(axpby(d_int1, 1.0, d_int2, c, HS));
-        CK_TC(frob_async(d_int2, c, 0));
+        CK_TC(commutator(G, hG, ad, hH, out, hH, true));
+        CK_TC(axpby(HS, 1.0, out, c, HS));
+        CK_TC(frob_async(out, c, 0));
         const int body = (int)(launches - b0) + 1;
         const bool has_next = iw < max_terms;
         k_bch_next<<<1, 1, 0, stream>>>(iw, d_scalars, sg->d_state, has_next ? hb[iw - 1] : hb[0], has_next ? 1 : 0,
