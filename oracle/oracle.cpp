@@ -1676,6 +1676,10 @@ void white_vjp(const Basis& B, const double* H, int hH, const double* ETAb, doub
   }
 }
 
+namespace {
+#include "oracle_tensor.inc"
+}  // namespace
+
 // ====================================================================== C interface
 extern "C" {
 
@@ -1805,6 +1809,39 @@ double orc_bf_1body(void* b, const double* A, int hA, const double* Bo, int hB, 
 }
 double orc_bf_2body(void* b, const double* A, int hA, const double* Bo, int hB, int a, int bb, int c, int d, int J) {
   return bf2(*(Basis*)b, A, hA, Bo, hB, a, bb, c, d, J);
+}
+
+// ---- tensor operators (oracle_tensor.inc)
+void* orc_tbasis_create(void* b, int rank, int dpar) { return build_tbasis((Basis*)b, rank, dpar); }
+void orc_tbasis_destroy(void* t) { delete (TBasis*)t; }
+int64_t orc_tslab_size(void* t) { return ((TBasis*)t)->slab; }
+int orc_tnblocks(void* t) { return ((TBasis*)t)->nblocks; }
+void orc_tblock_info(void* t, int* J1, int* J2, int* Tz, int* P1, int* q1, int* q2) {
+  const TBasis& T = *(TBasis*)t;
+  for (int q = 0; q < T.nblocks; ++q) {
+    J1[q] = T.J1[q]; J2[q] = T.J2[q]; Tz[q] = T.T[q]; P1[q] = T.P1[q]; q1[q] = T.q1[q]; q2[q] = T.q2[q];
+  }
+}
+void orc_random_tensor(void* t, uint64_t seed, int herm, double* op) { random_tensor_op(*(TBasis*)t, seed, herm, op); }
+void orc_tensor_commutator(void* t, const double* L, int hL, const double* R, int hR, double* RES, int mask) {
+  tensor_commutator(*(TBasis*)t, L, hL, R, hR, RES, mask);
+}
+double orc_tensor_elem(void* t, const double* op, int herm, int a, int b, int c, int d, int J1, int J2) {
+  return tensor_elem(*(TBasis*)t, op, herm, a, b, c, d, J1, J2);
+}
+double orc_f_tensor_elem(void* t, const double* op, int herm, int a, int b) {
+  return f_tensor_elem(*(TBasis*)t, op, herm, a, b);
+}
+double orc_tensor_frob(void* t, const double* op) { return tensor_frob(*(TBasis*)t, op); }
+int orc_bch_tensor(void* t, const double* G, double* HS, int max_terms, double conv) {
+  return bch_tensor(*(TBasis*)t, G, HS, max_terms, conv);
+}
+double orc_tensor_bf1(void* t, const double* A, int hA, const double* Bo, int hB, int a, int b) {
+  return tensor_bf1(*(TBasis*)t, A, hA, Bo, hB, a, b);
+}
+double orc_tensor_bf2(void* t, const double* A, int hA, const double* Bo, int hB, int a, int b, int c, int d, int J1,
+                      int J2) {
+  return tensor_bf2(*(TBasis*)t, A, hA, Bo, hB, a, b, c, d, J1, J2);
 }
 
 }  // extern "C"

@@ -68,6 +68,19 @@ def lib():
         "orc_commutator_e0": (None, [vp, _dp, i, _dp, i, _dp, i, i]),
         "orc_commutator_vjp": (None, [vp, _dp, i, _dp, i, i, i, _dp, _dp, _dp]),
         "orc_white_vjp": (None, [vp, _dp, i, _dp, _dp]),
+        "orc_tbasis_create": (vp, [vp, i, i]),
+        "orc_tbasis_destroy": (None, [vp]),
+        "orc_tslab_size": (i64, [vp]),
+        "orc_tnblocks": (i, [vp]),
+        "orc_tblock_info": (None, [vp, _ip, _ip, _ip, _ip, _ip, _ip]),
+        "orc_random_tensor": (None, [vp, u64, i, _dp]),
+        "orc_tensor_commutator": (None, [vp, _dp, i, _dp, i, _dp, i]),
+        "orc_tensor_elem": (d, [vp, _dp, i, i, i, i, i, i, i]),
+        "orc_f_tensor_elem": (d, [vp, _dp, i, i, i]),
+        "orc_tensor_frob": (d, [vp, _dp]),
+        "orc_bch_tensor": (i, [vp, _dp, _dp, i, d]),
+        "orc_tensor_bf1": (d, [vp, _dp, i, _dp, i, i, i]),
+        "orc_tensor_bf2": (d, [vp, _dp, i, _dp, i, i, i, i, i, i, i]),
         "orc_mat_frob_norm": (d, [vp, _dp]),
         "orc_mbpt2": (d, [vp, _dp, i]),
         "orc_add_sq_op": (None, [vp, _dp, d, _dp, d, _dp]),
@@ -240,3 +253,59 @@ class Oracle:
 
     def bf_2body(self, A, hA, B, hB, a, b, c, d, J):
         return self.L.orc_bf_2body(self.h, A, hA, B, hB, a, b, c, d, J)
+
+
+class TensorOracle:
+    """Rank-lambda tensor operators of the oracle on a scalar Oracle's basis (test-only)."""
+
+    def __init__(self, o: "Oracle", rank: int, dpar: int = 0):
+        self.o, self.L, self.rank, self.dpar = o, o.L, rank, dpar
+        self.h = self.L.orc_tbasis_create(o.h, rank, dpar)
+        self.slab = int(self.L.orc_tslab_size(self.h))
+        self.nblocks = int(self.L.orc_tnblocks(self.h))
+
+    def __del__(self):
+        try:
+            self.L.orc_tbasis_destroy(self.h)
+        except Exception:
+            pass
+
+    def new(self):
+        return np.zeros(self.slab)
+
+    def block_info(self):
+        arrs = [np.zeros(self.nblocks, np.int32) for _ in range(6)]
+        self.L.orc_tblock_info(self.h, *arrs)
+        return dict(zip(("J1", "J2", "Tz", "P1", "q1", "q2"), arrs))
+
+    def random(self, seed: int, herm: int):
+        op = self.new()
+        self.L.orc_random_tensor(self.h, seed, herm, op)
+        return op
+
+    def commutator(self, L, hL, R, hR, mask=127):
+        """[L (scalar), R (tensor)]; RES herm = -hL*hR."""
+        RES = self.new()
+        self.L.orc_tensor_commutator(self.h, L, hL, R, hR, RES, mask)
+        return RES
+
+    def elem(self, op, herm, a, b, c, d, J1, J2):
+        return self.L.orc_tensor_elem(self.h, op, herm, a, b, c, d, J1, J2)
+
+    def f_elem(self, op, herm, a, b):
+        return self.L.orc_f_tensor_elem(self.h, op, herm, a, b)
+
+    def frob(self, op):
+        return self.L.orc_tensor_frob(self.h, op)
+
+    def bch(self, G, HS, max_terms=30, conv=float(np.float32(1e-6))):
+        out = np.array(HS, dtype=np.float64)
+        n = self.L.orc_bch_tensor(self.h, G, out, max_terms, conv)
+        return out, n
+
+    def bf1(self, A, hA, B, hB, a, b):
+        return self.L.orc_tensor_bf1(self.h, A, hA, B, hB, a, b)
+
+    def bf2(self, A, hA, B, hB, a, b, c, d, J1, J2):
+        return self.L.orc_tensor_bf2(self.h, A, hA, B, hB, a, b, c, d, J1, J2)
+
