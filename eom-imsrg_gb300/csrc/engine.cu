@@ -168,7 +168,8 @@ imsrg_status Ctx::upload_tables() {
   d_pphh_probs = pp_p; d_pphh_tiles = pp_t; d_wcc_probs = wc_p; d_wcc_tiles = wc_t;
   d_seg_start = seg_s; d_seg_len = seg_l; d_seg_w = seg_w;
   d_upd_tiles = ut;
-  CK(cuda(cudaMalloc(&d_partial, sizeof(double) * (std::max(nseg, l.nblocks) + 64)), "cudaMalloc(partials)"));
+  partial_capacity = std::max(nseg, l.nblocks) + 64;
+  CK(cuda(cudaMalloc(&d_partial, sizeof(double) * partial_capacity), "cudaMalloc(partials)"));
   CK(cuda(cudaMalloc(&d_scalars, sizeof(double) * 64), "cudaMalloc(scalars)"));
   CK(cuda(cudaMallocHost(&h_scalars, sizeof(double) * 64), "cudaMallocHost(scalars)"));
   CK(cuda(cudaMalloc(&d_mono, sizeof(double) * (size_t)l.N * l.N), "cudaMalloc(monopole)"));
@@ -216,6 +217,7 @@ Ctx::~Ctx() {
   tc_release();
   graph_release();
   adjoint_release();
+  tensor_release();
   if (stream) cudaStreamDestroy(stream);
 }
 

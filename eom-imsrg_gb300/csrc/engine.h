@@ -16,6 +16,7 @@ struct TcState;
 }
 struct StepGraph;
 struct AdjointState;
+struct TensorState;
 
 // MAGNUS_EXPAND coefficients as the literals of src/IMSRG_MAGNUS.f90:646
 constexpr double kMagnusCof[7] = {1.0, -0.5, .0833333333, 0.0, -0.00138888888, 0.0, 3.306878e-5};
@@ -55,6 +56,7 @@ struct Ctx {
   const int8_t* d_seg_w = nullptr;
   int nseg = 0;
   double* d_partial = nullptr;
+  int64_t partial_capacity = 0;  // entries of d_partial
   double* d_scalars = nullptr;
   double* h_scalars = nullptr;
   double* d_mono = nullptr;
@@ -120,6 +122,14 @@ struct Ctx {
                               const double* Cb, double* Lb, double* Rb);
   imsrg_status white_vjp(const double* H, int hH, const double* ETAb, double* Hb);
   imsrg_status dot(const double* A, const double* B, double* out);
+
+  // rank-lambda tensor operators (tensor.cu)
+  imsrg_status tensor_state(int rank, int dpar, TensorState** out);
+  void tensor_release();
+  imsrg_status tensor_commutator(TensorState& S, const double* L, int hL, const double* R, int hR, double* RES,
+                                 int pieces);
+  imsrg_status tensor_frob(TensorState& S, const double* op, double scale, int slot);
+  imsrg_status bch_tensor(TensorState& S, const double* G, int hG, double* HS, int max_terms, double conv, int* terms);
 
   // tensor-core (split-BF16, tcgen05) path, gemm_tc.cu
   imsrg_status tc_prepare(int mode);

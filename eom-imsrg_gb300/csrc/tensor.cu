@@ -1,0 +1,444 @@
+// Rank-lambda tensor operators on the device: layout tables, the scalar-tensor commutator
+// [L, R] of src/TS_commutators.f90 in the call order of BCH_TENSOR (src/IMSRG_MAGNUS.f90:418-455),
+// BCH_TENSOR itself, norms, and their C ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+
+#include "../../include/imsrg_gb300.h"
+#include "engine.h"
+#include "kernels.h"
+#include "tensor.h"
+
+using namespace imsrg;
+
+namespace imsrg {
+__global__ void k_ts111(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_ts121(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES,
+                        int hRES);
+__global__ void k_ts211(DevLayout D, DevTLayout T, const double* LCC, int hL, const double* R, int hR, double* RES,
+                        int hRES);
+__global__ void k_ts221(DevLayout D, DevTLayout T, const double* w1, const double* w2, int pm, double* RES, int hRES);
+__global__ void k_ts122(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_ts212(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_ts_pphh_update(int64_t n, int64_t off, double* RES, const double* w1, const double* w2);
+__global__ void k_tpandya(DevLayout D, DevTLayout T, const double* R, int hR, int J3, int J4, int qa, int qb, int term,
+                          double scale, double* out);
+__global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* Wx, const double* Wy, int J3, int J4,
+                                  int qa, int qb, int hL, int hR, double* RES);
+}  // namespace imsrg
+
+// device state of one (rank, dpar) layout
+struct TensorState {
+  TLayout T;
+  DevTLayout DT{};
+  void* tables = nullptr;
+  const GemmProb* pphh_p = nullptr;
+  const GemmTile* pphh_t = nullptr;
+  int n_pphh_t = 0;
+  // per cross-coupled block: GEMM problems (Wx, Wy) and their tile range
+  const GemmProb* cb_p = nullptr;
+  const GemmTile* cb_t = nullptr;
+  std::vector<int> cb_tile_start, cb_tile_n;
+  const int64_t* seg_start = nullptr;
+  const int* seg_len = nullptr;
+  const int8_t* seg_w = nullptr;
+  int nseg = 0;
+  double *w1 = nullptr, *w2 = nullptr;           // tensor-shaped ladder intermediates
+  double *ccx = nullptr, *ccr = nullptr;         // cross-coupled tensor blocks
+  double *wx = nullptr, *wy = nullptr;           // recoupling products
+  double *bch_a = nullptr, *bch_b = nullptr;     // BCH_TENSOR terms
+};
+
+struct imsrg_tensor {
+  double* d = nullptr;
+  int herm = 1;
+  TensorState* ts = nullptr;
+  Ctx* owner = nullptr;
+};
+
+namespace {
+
+int grid_n(int64_t n, int threads = 256, int cap = 152 * 16) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, cap));
+}
+
+std::map<std::pair<Ctx*, int>, std::unique_ptr<TensorState>>& registry() {
+  static std::map<std::pair<Ctx*, int>, std::unique_ptr<TensorState>> r;
+  return r;
+}
+
+struct Pack {
+  std::vector<char> buf;
+  std::vector<std::pair<size_t, const void**>> fix;
+  template <class V>
+  void add(const std::vector<V>& v, const V** dst) {
+    const size_t o = (buf.size() + 255) & ~size_t(255);
+    buf.resize(o + std::max<size_t>(v.size() * sizeof(V), 1));
+    if (!v.empty()) std::memcpy(buf.data() + o, v.data(), v.size() * sizeof(V));
+    fix.push_back({o, reinterpret_cast<const void**>(dst)});
+  }
+};
+
+}  // namespace
+
+#define CKT(expr)                 \
+  do {                            \
+    imsrg_status _s = (expr);     \
+    if (_s != IMSRG_OK) return _s; \
+  } while (0)
+
+// layout, device tables and workspaces of a (rank, dpar) pair, built on first use
+imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
+  auto& reg = registry();
+  const auto key = std::make_pair(this, rank * 4 + dpar);
+  auto it = reg.find(key);
+  if (it != reg.end()) {
+    *out = it->second.get();
+    return IMSRG_OK;
+  }
+  auto st = std::make_unique<TensorState>();
+  TLayout& T = st->T;
+  const std::string e = build_tlayout(T, L, rank, dpar);
+  if (!e.empty()) return fail(IMSRG_ERR_INVALID_ARGUMENT, e);
+  if (device < 0) {  // host-only context: layout queries only
+    *out = st.get();
+    reg[key] = std::move(st);
+    return IMSRG_OK;
+  }
+  CKT(ensure_workspace());
+  const auto pphh = build_tensor_pphh_problems(T, L);
+  const auto pphh_tiles = build_tiles(pphh, 64, 64);
+  // per cross-coupled block: Wx = hL LCC(qa) CCR and Wy = CCX LCC(qb)^T
+  std::vector<GemmProb> cbp;
+  std::vector<GemmTile> cbt;
+  for (size_t b = 0; b < T.cb_J3.size(); ++b) {
+    const int qa = T.cb_qa[b], qb = T.cb_qb[b];
+    const int r1 = L.cc_rlen[qa], r2 = L.cc_rlen[qb], nb1 = L.cc_nph[qa], nb2 = L.cc_nph[qb];
+    std::vector<GemmProb> ps;
+    if (nb1) {
+      GemmProb p{};
+      p.c_id = kOpW1; p.M = r1; p.N = r2; p.ldc = r1; p.nterm = 1;
+      GemmTerm& t = p.t[0];
+      t.a_id = kOpLCC; t.a_off = L.cc_off[qa]; t.lda = r1; t.ta = 0;
+      t.b_id = kOpRCC; t.b_off = 0; t.ldb = nb1; t.tb = 0;
+      t.K = nb1; t.alpha = kAlphaHL;
+      ps.push_back(p);
+    }
+    if (nb2 && T.cb_J3[b] != T.cb_J4[b]) {
+      GemmProb p{};
+      p.c_id = kOpW2; p.M = r1; p.N = r2; p.ldc = r1; p.nterm = 1;
+      GemmTerm& t = p.t[0];
+      t.a_id = kOpWCC; t.a_off = 0; t.lda = r1; t.ta = 0;
+      t.b_id = kOpLCC; t.b_off = L.cc_off[qb]; t.ldb = r2; t.tb = 1;
+      t.K = nb2; t.alpha = kAlphaOne;
+      ps.push_back(p);
+    }
+    const int base = (int)cbp.size();
+    auto tiles = build_tiles(ps, 64, 64);
+    st->cb_tile_start.push_back((int)cbt.size());
+    st->cb_tile_n.push_back((int)tiles.size());
+    for (auto& t : tiles) {
+      t.prob += base;
+      cbt.push_back(t);
+    }
+    for (auto& p : ps) cbp.push_back(p);
+  }
+  Pack pk;
+  DevTLayout& d = st->DT;
+  d.rank = T.rank; d.dpar = T.dpar; d.nblocks = T.nblocks; d.n_ob = (int)T.ob_kind.size();
+  d.six_nJ = T.six_nJ; d.six_nh = T.six_nh; d.six_nhx = T.six_nhx;
+  d.off_fhh = T.off_fhh; d.off_fpp = T.off_fpp; d.off_fph = T.off_fph; d.slab = T.slab; d.n2b = T.n2b;
+  pk.add(T.J1, &d.J1); pk.add(T.J2, &d.J2); pk.add(T.q1, &d.q1); pk.add(T.q2, &d.q2); pk.add(T.lut, &d.lut);
+  pk.add(T.goff, &d.goff); pk.add(T.n1, &d.n1); pk.add(T.n2, &d.n2);
+  pk.add(T.ob_kind, &d.ob_kind); pk.add(T.ob_p, &d.ob_p); pk.add(T.ob_q, &d.ob_q); pk.add(T.ob_pk, &d.ob_pk);
+  pk.add(T.ob_qk, &d.ob_qk);
+  pk.add(T.six, &d.six); pk.add(T.six_m, &d.six_m); pk.add(T.ccnb, &d.ccnb);
+  pk.add(pphh, &st->pphh_p); pk.add(pphh_tiles, &st->pphh_t);
+  pk.add(cbp, &st->cb_p); pk.add(cbt, &st->cb_t);
+  pk.add(T.seg_start, &st->seg_start); pk.add(T.seg_len, &st->seg_len); pk.add(T.seg_w, &st->seg_w);
+  CKT(cuda(cudaMalloc(&st->tables, pk.buf.size()), "cudaMalloc(tensor tables)"));
+  CKT(cuda(cudaMemcpy(st->tables, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tensor tables)"));
+  for (auto& f : pk.fix) *f.second = static_cast<const char*>(st->tables) + f.first;
+  st->n_pphh_t = (int)pphh_tiles.size();
+  st->nseg = (int)T.seg_start.size();
+  const size_t tb = sizeof(double) * (size_t)T.slab;
+  for (double** p : {&st->w1, &st->w2, &st->bch_a, &st->bch_b}) {
+    CKT(cuda(cudaMalloc(p, tb), "cudaMalloc(tensor workspace)"));
+    CKT(cuda(cudaMemsetAsync(*p, 0, tb, stream), "memset(tensor workspace)"));
+  }
+  const size_t xb = sizeof(double) * (size_t)std::max<int64_t>(T.cb_max_x, 1);
+  const size_t wb = sizeof(double) * (size_t)std::max<int64_t>(T.cb_max_w, 1);
+  CKT(cuda(cudaMalloc(&st->ccx, xb), "cudaMalloc(CCX tensor)"));
+  CKT(cuda(cudaMalloc(&st->ccr, xb), "cudaMalloc(CCR tensor)"));
+  CKT(cuda(cudaMalloc(&st->wx, wb), "cudaMalloc(Wx)"));
+  CKT(cuda(cudaMalloc(&st->wy, wb), "cudaMalloc(Wy)"));
+  *out = st.get();
+  reg[key] = std::move(st);
+  return IMSRG_OK;
+}
+
+void Ctx::tensor_release() {
+  auto& reg = registry();
+  for (auto it = reg.begin(); it != reg.end();) {
+    if (it->first.first != this) {
+      ++it;
+      continue;
+    }
+    TensorState* s = it->second.get();
+    for (void* p : {(void*)s->w1, (void*)s->w2, (void*)s->ccx, (void*)s->ccr, (void*)s->wx, (void*)s->wy,
+                    (void*)s->bch_a, (void*)s->bch_b, s->tables})
+      if (p) cudaFree(p);
+    it = reg.erase(it);
+  }
+}
+
+// [L (scalar, hL), R (tensor, hR)] -> RES (tensor, herm -hL hR); pieces as imsrg_tensor_commutator
+imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, const double* R, int hR, double* RES,
+                                    int pieces) {
+  CKT(ensure_workspace());
+  const DevTLayout& T = S.DT;
+  const int hRES = -hL * hR;
+  if (L.cc_size) CKT(pandya(Lp, hL, d_lcc));
+  const int nob = T.n_ob;
+  if (pieces & 1) {
+    const int64_t n1 = (int64_t)L.A * L.A + (int64_t)L.P * L.A + (int64_t)L.P * L.P;
+    k_ts111<<<grid_n(n1 * 32), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+    CKT(launched("k_ts111"));
+  }
+  if ((pieces & 2) && nob) {
+    k_ts121<<<(nob * 32 + 255) / 256, 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES, hRES);
+    CKT(launched("k_ts121"));
+  }
+  if ((pieces & 4) && nob) {
+    k_ts211<<<(nob * 32 + 255) / 256, 256, 0, stream>>>(D, T, d_lcc, hL, R, hR, RES, hRES);
+    CKT(launched("k_ts211"));
+  }
+  if ((pieces & 8) && T.n2b) {
+    k_ts122<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+    CKT(launched("k_ts122"));
+  }
+  if ((pieces & 16) && T.n2b) {
+    k_ts212<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+    CKT(launched("k_ts212"));
+  }
+  if (pieces & 32) {
+    const size_t tb = sizeof(double) * (size_t)T.slab;
+    CKT(cuda(cudaMemsetAsync(S.w1, 0, tb, stream), "memset(tensor w1)"));
+    CKT(cuda(cudaMemsetAsync(S.w2, 0, tb, stream), "memset(tensor w2)"));
+    if (S.n_pphh_t) {
+      GemmOperands ops{};
+      ops.in[kOpL] = Lp; ops.in[kOpR] = R;
+      ops.out[kOpW1] = S.w1; ops.out[kOpW2] = S.w2;
+      ops.hL = hL; ops.hR = hR;
+      k_gemm_fp64<<<S.n_pphh_t, 256, 0, stream>>>(S.pphh_p, S.pphh_t, ops);
+      CKT(launched("k_gemm_fp64(tensor pphh)"));
+    }
+    if (T.n2b) {
+      k_ts_pphh_update<<<grid_n(T.n2b), 256, 0, stream>>>(T.n2b, S.T.goff.empty() ? 0 : S.T.goff[0], RES, S.w1, S.w2);
+      CKT(launched("k_ts_pphh_update"));
+    }
+    if (nob) {
+      k_ts221<<<(nob * 32 + 255) / 256, 256, 0, stream>>>(D, T, S.w1, S.w2, hL * hR, RES, hRES);
+      CKT(launched("k_ts221"));
+    }
+  }
+  if (pieces & 64) {
+    const TLayout& H = S.T;
+    for (size_t b = 0; b < H.cb_J3.size(); ++b) {
+      const int J3 = H.cb_J3[b], J4 = H.cb_J4[b], qa = H.cb_qa[b], qb = H.cb_qb[b];
+      const int r1 = L.cc_rlen[qa], r2 = L.cc_rlen[qb], nb1 = L.cc_nph[qa], nb2 = L.cc_nph[qb];
+      const bool dox = nb1 > 0, doy = nb2 > 0 && J3 != J4;
+      if (!dox && !doy) continue;
+      if (dox) {
+        k_tpandya<<<grid_n((int64_t)nb1 * r2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 2,
+                                                                 1.0 / std::sqrt(J3 + 1.0), S.ccr);
+        CKT(launched("k_tpandya"));
+      } else {
+        CKT(cuda(cudaMemsetAsync(S.wx, 0, sizeof(double) * (size_t)r1 * r2, stream), "memset(Wx)"));
+      }
+      if (doy) {
+        k_tpandya<<<grid_n((int64_t)r1 * nb2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 1,
+                                                                 1.0 / std::sqrt(J4 + 1.0), S.ccx);
+        CKT(launched("k_tpandya"));
+      }
+      if (S.cb_tile_n[b]) {
+        GemmOperands ops{};
+        ops.in[kOpLCC] = d_lcc; ops.in[kOpRCC] = S.ccr; ops.in[kOpWCC] = S.ccx;
+        ops.out[kOpW1] = S.wx; ops.out[kOpW2] = S.wy;
+        ops.hL = hL; ops.hR = hR;
+        k_gemm_fp64<<<S.cb_tile_n[b], 256, 0, stream>>>(S.cb_p, S.cb_t + S.cb_tile_start[b], ops);
+        CKT(launched("k_gemm_fp64(tensor ph)"));
+      }
+      k_ts222ph_scatter<<<grid_n((int64_t)r1 * r2), 256, 0, stream>>>(D, T, S.wx, doy ? S.wy : nullptr, J3, J4, qa,
+                                                                      qb, hL, hR, RES);
+      CKT(launched("k_ts222ph_scatter"));
+    }
+  }
+  return IMSRG_OK;
+}
+
+imsrg_status Ctx::tensor_frob(TensorState& S, const double* op, double scale, int slot) {
+  if (S.nseg == 0) return cuda(cudaMemsetAsync(d_scalars + slot, 0, sizeof(double), stream), "memset(norm)");
+  if ((int64_t)S.nseg > partial_capacity) {  // one partial per segment: grow the buffer
+    double* p = nullptr;
+    CKT(cuda(cudaMalloc(&p, sizeof(double) * (size_t)S.nseg), "cudaMalloc(partials)"));
+    CKT(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize"));
+    cudaFree(d_partial);
+    d_partial = p;
+    partial_capacity = S.nseg;
+  }
+  k_frob_partial<<<S.nseg, 256, 0, stream>>>(op, S.seg_start, S.seg_len, S.seg_w, d_partial);
+  CKT(launched("k_frob_partial"));
+  k_sum_sqrt<<<1, 1024, 0, stream>>>(d_partial, S.nseg, scale, d_scalars + slot);
+  return launched("k_sum_sqrt");
+}
+
+// BCH_TENSOR (src/IMSRG_MAGNUS.f90:389-464): HS <- e^G HS e^-G, HS a hermitian tensor, G an
+// anti-hermitian scalar; stops when coef * ||ad^n(HS)|| < conv (the reference uses 1e-6, up to 30 terms)
+imsrg_status Ctx::bch_tensor(TensorState& S, const double* G, int hG, double* HS, int max_terms, double conv,
+                             int* terms) {
+  const size_t tb = sizeof(double) * (size_t)S.T.slab;
+  double coef = 1.0;
+  int iw;
+  for (iw = 2; iw <= max_terms; ++iw) {
+    coef = coef / (iw - 1.0);
+    const double* ad = (iw == 2) ? HS : ((iw & 1) ? S.bch_a : S.bch_b);
+    double* out = (iw & 1) ? S.bch_b : S.bch_a;
+    CKT(cuda(cudaMemsetAsync(out, 0, tb, stream), "memset(BCH term)"));
+    CKT(tensor_commutator(S, G, hG, ad, 1, out, 127));
+    k_axpby<<<grid_n(S.T.slab), 256, 0, stream>>>(S.T.slab, HS, 1.0, out, coef, HS);
+    CKT(launched("k_axpby"));
+    CKT(tensor_frob(S, out, coef, 0));
+    CKT(read_scalars(1));
+    if (h_scalars[0] < conv) break;
+  }
+  *terms = (iw > max_terms) ? max_terms - 1 : iw - 1;
+  if (iw > max_terms) return fail(IMSRG_ERR_NOT_CONVERGED, "tensor BCH series did not converge within max_terms");
+  return IMSRG_OK;
+}
+
+// ====================================================================== C ABI
+#define TCTX(ptr)                                                                        \
+  if (!(ptr)) return IMSRG_ERR_INVALID_ARGUMENT;                                         \
+  Ctx* c = reinterpret_cast<Ctx*>(ptr);                                                  \
+  if (c->device < 0) return c->fail(IMSRG_ERR_UNSUPPORTED, "host-only context (device < 0)"); \
+  {                                                                                      \
+    cudaError_t _e = cudaSetDevice(c->device);                                           \
+    if (_e != cudaSuccess) return c->cuda(_e, "cudaSetDevice");                          \
+  }
+
+extern "C" {
+
+imsrg_status imsrg_tensor_sizes(imsrg_ctx* ctx, int32_t rank2, int32_t dpar2, int64_t* slab, int32_t* nblocks) {
+  if (!ctx) return IMSRG_ERR_INVALID_ARGUMENT;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  TensorState* s = nullptr;
+  CKT(c->tensor_state(rank2, dpar2, &s));
+  if (slab) *slab = s->T.slab;
+  if (nblocks) *nblocks = s->T.nblocks;
+  return IMSRG_OK;
+}
+
+imsrg_status imsrg_tensor_block_info(imsrg_ctx* ctx, int32_t rank2, int32_t dpar2, int32_t* J1, int32_t* J2,
+                                     int32_t* Tz, int32_t* P1) {
+  if (!ctx) return IMSRG_ERR_INVALID_ARGUMENT;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  TensorState* s = nullptr;
+  CKT(c->tensor_state(rank2, dpar2, &s));
+  for (int q = 0; q < s->T.nblocks; ++q) {
+    if (J1) J1[q] = s->T.J1[q];
+    if (J2) J2[q] = s->T.J2[q];
+    if (Tz) Tz[q] = s->T.T[q];
+    if (P1) P1[q] = s->T.P1[q];
+  }
+  return IMSRG_OK;
+}
+
+imsrg_status imsrg_tensor_create(imsrg_ctx* ctx, int32_t rank2, int32_t dpar2, int32_t herm, imsrg_tensor** out) {
+  TCTX(ctx);
+  if (!out || (herm != 1 && herm != -1)) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "herm must be +1 or -1");
+  *out = nullptr;
+  TensorState* s = nullptr;
+  CKT(c->tensor_state(rank2, dpar2, &s));
+  imsrg_tensor* t = new (std::nothrow) imsrg_tensor();
+  if (!t) return IMSRG_ERR_OUT_OF_MEMORY;
+  const size_t tb = sizeof(double) * (size_t)s->T.slab;
+  imsrg_status st = c->cuda(cudaMalloc(&t->d, tb), "cudaMalloc(tensor operator)");
+  if (st == IMSRG_OK) st = c->cuda(cudaMemsetAsync(t->d, 0, tb, c->stream), "memset(tensor operator)");
+  if (st != IMSRG_OK) {
+    if (t->d) cudaFree(t->d);
+    delete t;
+    return st;
+  }
+  t->herm = herm;
+  t->ts = s;
+  t->owner = c;
+  *out = t;
+  return IMSRG_OK;
+}
+
+imsrg_status imsrg_tensor_destroy(imsrg_ctx* ctx, imsrg_tensor* t) {
+  TCTX(ctx);
+  if (!t) return IMSRG_OK;
+  if (t->owner != c) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "tensor of another context");
+  cudaStreamSynchronize(c->stream);
+  cudaFree(t->d);
+  delete t;
+  return IMSRG_OK;
+}
+
+imsrg_status imsrg_tensor_upload_slab(imsrg_ctx* ctx, imsrg_tensor* t, const double* host) {
+  TCTX(ctx);
+  if (!t || t->owner != c || !host) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_tensor_upload_slab");
+  CKT(c->cuda(cudaMemcpyAsync(t->d, host, sizeof(double) * (size_t)t->ts->T.slab, cudaMemcpyHostToDevice, c->stream),
+              "H2D tensor"));
+  return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+}
+
+imsrg_status imsrg_tensor_download_slab(imsrg_ctx* ctx, const imsrg_tensor* t, double* host) {
+  TCTX(ctx);
+  if (!t || t->owner != c || !host) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_tensor_download_slab");
+  CKT(c->cuda(cudaMemcpyAsync(host, t->d, sizeof(double) * (size_t)t->ts->T.slab, cudaMemcpyDeviceToHost, c->stream),
+              "D2H tensor"));
+  return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+}
+
+imsrg_status imsrg_tensor_commutator(imsrg_ctx* ctx, const imsrg_op* Lop, const imsrg_tensor* R, imsrg_tensor* RES,
+                                     int32_t pieces) {
+  TCTX(ctx);
+  if (!Lop || Lop->owner != c || !R || R->owner != c || !RES || RES->owner != c)
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_tensor_commutator: operand of another context or NULL");
+  if (R->ts != RES->ts) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "R and RES must have the same rank and parity");
+  if (R == RES) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "RES must not alias R");
+  RES->herm = -Lop->herm * R->herm;
+  return c->tensor_commutator(*R->ts, Lop->d, Lop->herm, R->d, R->herm, RES->d, pieces);
+}
+
+imsrg_status imsrg_bch_tensor(imsrg_ctx* ctx, const imsrg_op* G, imsrg_tensor* HS, int32_t max_terms, double conv,
+                              int32_t* terms_used) {
+  TCTX(ctx);
+  if (!G || G->owner != c || !HS || HS->owner != c)
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_bch_tensor: operand of another context or NULL");
+  if (max_terms < 2) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "max_terms must be >= 2");
+  int t = 0;
+  imsrg_status s = c->bch_tensor(*HS->ts, G->d, G->herm, HS->d, max_terms, conv, &t);
+  if (terms_used) *terms_used = t;
+  return s;
+}
+
+imsrg_status imsrg_tensor_frob_norm(imsrg_ctx* ctx, const imsrg_tensor* t, double* out) {
+  TCTX(ctx);
+  if (!t || t->owner != c || !out) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_tensor_frob_norm");
+  CKT(c->tensor_frob(*t->ts, t->d, 1.0, 0));
+  CKT(c->read_scalars(1));
+  *out = c->h_scalars[0];
+  return IMSRG_OK;
+}
+
+}  // extern "C"

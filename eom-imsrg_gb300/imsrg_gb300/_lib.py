@@ -87,6 +87,15 @@ SIGNATURES = {
     "imsrg_bch_expand": [_vp, _vp, _vp, _vp, _i32, _d, _pi32],
     "imsrg_magnus_step": [_vp, _vp, _vp, _vp, _vp, _d, _i32, _d, _i32, C.POINTER(StepInfo_t)],
     "imsrg_magnus_step_counters": [_vp, _pi64, _pi64, _pi64, _pi64],
+    "imsrg_tensor_sizes": [_vp, _i32, _i32, _pi64, _pi32],
+    "imsrg_tensor_block_info": [_vp, _i32, _i32, _pi32, _pi32, _pi32, _pi32],
+    "imsrg_tensor_create": [_vp, _i32, _i32, _i32, _pvp],
+    "imsrg_tensor_destroy": [_vp, _vp],
+    "imsrg_tensor_upload_slab": [_vp, _vp, _vp],
+    "imsrg_tensor_download_slab": [_vp, _vp, _vp],
+    "imsrg_tensor_commutator": [_vp, _vp, _vp, _vp, _i32],
+    "imsrg_bch_tensor": [_vp, _vp, _vp, _i32, _d, _pi32],
+    "imsrg_tensor_frob_norm": [_vp, _vp, _pd],
     "imsrg_commutator_vjp": [_vp, _vp, _vp, _vp, _vp, _vp, _i32],
     "imsrg_white_vjp": [_vp, _vp, _vp, _vp],
     "imsrg_dot_sq_op": [_vp, _vp, _vp, _pd],

@@ -73,6 +73,44 @@ class SqOp:
         return v.value
 
 
+class TensorOp:
+    """A rank-lambda tensor operator on the device (imsrg_tensor); rank2 / dpar2 doubled."""
+
+    def __init__(self, eng: "Engine", rank2: int, dpar2: int = 0, herm: int = 1):
+        self.eng, self.rank2, self.dpar2 = eng, int(rank2), int(dpar2)
+        self.slab = eng.tensor_sizes(rank2, dpar2)[0]
+        h = C.c_void_p()
+        eng._ck(eng.L.imsrg_tensor_create(eng.h, self.rank2, self.dpar2, int(herm), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.eng.L.imsrg_tensor_destroy(self.eng.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, slab: np.ndarray):
+        slab = np.ascontiguousarray(slab, dtype=np.float64)
+        if slab.size != self.slab:
+            raise ValueError(f"tensor slab has {self.slab} elements, got {slab.size}")
+        self.eng._ck(self.eng.L.imsrg_tensor_upload_slab(self.eng.h, self.h, slab.ctypes.data))
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.slab)
+        self.eng._ck(self.eng.L.imsrg_tensor_download_slab(self.eng.h, self.h, out.ctypes.data))
+        return out
+
+    def frob(self) -> float:
+        v = C.c_double()
+        self.eng._ck(self.eng.L.imsrg_tensor_frob_norm(self.eng.h, self.h, C.byref(v)))
+        return v.value
+
+
 class CCMat:
     """A device-resident type(cc_mat): kind 0 = CCX storage, kind 1 = WCC workspace."""
 
@@ -320,6 +358,33 @@ class Engine:
         v = C.c_double()
         self._ck(self.L.imsrg_dot_sq_op(self.h, A.h, B.h, C.byref(v)))
         return v.value
+
+    # ---------------------------------------------------------------- tensor operators
+    def tensor_sizes(self, rank2: int, dpar2: int = 0):
+        slab, nb = C.c_int64(), C.c_int32()
+        self._ck(self.L.imsrg_tensor_sizes(self.h, int(rank2), int(dpar2), C.byref(slab), C.byref(nb)))
+        return slab.value, nb.value
+
+    def tensor_block_info(self, rank2: int, dpar2: int = 0) -> dict:
+        nb = self.tensor_sizes(rank2, dpar2)[1]
+        arrs = [np.zeros(nb, np.int32) for _ in range(4)]
+        P = C.POINTER(C.c_int32)
+        self._ck(self.L.imsrg_tensor_block_info(self.h, int(rank2), int(dpar2), *[a.ctypes.data_as(P) for a in arrs]))
+        return dict(zip(("J1", "J2", "Tz", "P1"), arrs))
+
+    def new_tensor(self, rank2: int, dpar2: int = 0, herm: int = 1, slab: np.ndarray | None = None) -> "TensorOp":
+        t = TensorOp(self, rank2, dpar2, herm)
+        if slab is not None:
+            t.upload(slab)
+        return t
+
+    def tensor_commutator(self, L: SqOp, R: "TensorOp", RES: "TensorOp", pieces: int = 127):
+        self._ck(self.L.imsrg_tensor_commutator(self.h, L.h, R.h, RES.h, int(pieces)))
+
+    def bch_tensor(self, G: SqOp, HS: "TensorOp", max_terms: int = 30, conv: float = CONV) -> int:
+        n = C.c_int32()
+        self._ck(self.L.imsrg_bch_tensor(self.h, G.h, HS.h, int(max_terms), float(conv), C.byref(n)))
+        return n.value
 
     def magnus_step_counters(self) -> dict:
         v = [C.c_int64() for _ in range(4)]

@@ -204,6 +204,30 @@ imsrg_status imsrg_magnus_step(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_
 imsrg_status imsrg_magnus_step_counters(imsrg_ctx* ctx, int64_t* commutators, int64_t* kernels, int64_t* steps,
                                         int64_t* unconverged);
 
+/* ---- rank-lambda tensor operators (BCH_TENSOR, src/IMSRG_MAGNUS.f90:389-464; allocate_tensor,
+ * src/basic_IMSRG.f90:688-951).  rank2 and dpar2 are doubled (rank 2 -> 4, even parity -> 0).
+ * Slab: [E0][fhh A*A][fpp P*P][fph P*A][block q = (J1 <= J2, Tz, bra parity): tgam(1..9)],
+ * tgam = (pp,pp) (pp,ph) (pp,hh) (ph,ph) (hh,hh) (ph,hh) (hh,pp) (ph,pp) (hh,ph), column-major. */
+typedef struct imsrg_tensor imsrg_tensor;
+imsrg_status imsrg_tensor_sizes(imsrg_ctx* ctx, int32_t rank2, int32_t dpar2, int64_t* slab, int32_t* nblocks);
+imsrg_status imsrg_tensor_block_info(imsrg_ctx* ctx, int32_t rank2, int32_t dpar2, int32_t* J1, int32_t* J2,
+                                     int32_t* Tz, int32_t* P1);
+imsrg_status imsrg_tensor_create(imsrg_ctx* ctx, int32_t rank2, int32_t dpar2, int32_t herm, imsrg_tensor** out);
+imsrg_status imsrg_tensor_destroy(imsrg_ctx* ctx, imsrg_tensor* t);
+imsrg_status imsrg_tensor_upload_slab(imsrg_ctx* ctx, imsrg_tensor* t, const double* host);
+imsrg_status imsrg_tensor_download_slab(imsrg_ctx* ctx, const imsrg_tensor* t, double* host);
+/* [L (scalar), R (tensor)] -> RES (RES->herm = -L->herm * R->herm), FP64.  pieces: 1 TS_111,
+ * 2 TS_121, 4 TS_211, 8 TS_122, 16 TS_212, 32 TS_222_pp_hh + TS_221, 64 TS_222_ph
+ * (src/TS_commutators.f90); 127 = the full commutator.  111 and 122 assign, the rest accumulate. */
+imsrg_status imsrg_tensor_commutator(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_tensor* R, imsrg_tensor* RES,
+                                     int32_t pieces);
+/* BCH_TENSOR: HS <- e^G HS e^-G for a hermitian tensor HS and an anti-hermitian scalar G; stops when
+ * a term's norm times its coefficient falls below conv (the reference: 1e-6, 30 terms). */
+imsrg_status imsrg_bch_tensor(imsrg_ctx* ctx, const imsrg_op* G, imsrg_tensor* HS, int32_t max_terms, double conv,
+                              int32_t* terms_used);
+/* mat_frob_norm of a tensor operator (src/basic_IMSRG.f90:4056-4087) */
+imsrg_status imsrg_tensor_frob_norm(imsrg_ctx* ctx, const imsrg_tensor* t, double* out);
+
 /* ---- reverse mode (FP64) for adjoint derivatives of a flow (no counterpart in the
  * reference, which has no derivative code).  Each call ACCUMULATES into its outputs:
  * Lb += d<RESb, [L,R]>/dL and Rb += d<RESb, [L,R]>/dR for the FP64 commutator of

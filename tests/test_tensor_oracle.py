@@ -73,3 +73,18 @@ def test_bch_tensor_first_order(oracles):
     lin = Q + t.commutator(G, -1, Q, 1)
     assert np.abs(out - lin).max() < 1e-5 * np.abs(Q).max()
     assert np.abs(out - Q).max() > 1e-6
+
+
+@pytest.mark.parametrize("emax,rank", [(2, 4), (4, 2), (4, 4), (10, 4)])
+def test_device_tensor_layout_matches_oracle(built_lib, oracles, emax, rank):
+    from imsrg_gb300 import Engine, make_basis
+    eng = Engine(make_basis(emax), device=-1)
+    slab, nb = eng.tensor_sizes(rank, 0)
+    if emax > 4:  # the oracle is not run at this size: the layout only has to build
+        assert slab > eng.slab and nb > 0
+        return
+    o, t = _tensor(oracles, emax, rank)
+    assert (slab, nb) == (t.slab, t.nblocks)
+    info, ref = eng.tensor_block_info(rank, 0), t.block_info()
+    for k in ("J1", "J2", "Tz", "P1"):
+        assert np.array_equal(info[k], ref[k])
