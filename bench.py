@@ -309,6 +309,155 @@ def adjoint_workload(args, local: int):
     }), flush=True)
 
 
+def precision_workload(args, local: int):
+    """eMax=8: one [eta,H] commutator and a 20-step Magnus flow in plain FP64 and in the split-BF16
+    modes (6 and 3 slice products, FP32 accumulation); |dE0| and ||dH_2b||_F against FP64."""
+    import numpy as np
+    from imsrg_gb300 import CONV, Engine, make_basis
+    emax = args.emax if args.emax is not None else 8
+    b = make_basis(emax)
+    A_ = b.nholes
+    P_ = b.norbits - A_
+    n1 = 1 + A_ * A_ + P_ * P_ + P_ * A_
+    H = None
+    out = {}
+    ref = {}
+    for mode in ("fp64", "bf16x6", "bf16x3"):
+        eng = Engine(b, device=local, precision=mode)
+        if H is None:
+            H = eng.synthetic_hamiltonian(seed=1)
+        dH, dE, dR = eng.new_op(1, H), eng.new_op(-1), eng.new_op(1)
+        eng.build_gs_white(dH, dE)
+        eng.commutator(dE, dH, dR)
+        eng.timer_begin()
+        for _ in range(5):
+            eng.commutator(dE, dH, dR)
+        ms = eng.timer_end() / 5
+        comm = dR.download()
+        st = flow_state(eng, H)
+        t = time.perf_counter()
+        e0 = [eng.magnus_step(*st, args.ds, 40, CONV, graph=True, allow_unconverged=True)["E0"]
+              for _ in range(args.precision_flow_steps)]
+        eng.synchronize()
+        t_flow = time.perf_counter() - t
+        hs = st[0].download()
+        if mode == "fp64":
+            ref = {"comm": comm, "hs": hs}
+        entry = {"commutator_ms": ms, "flow_s": t_flow, "E0_flow": e0[-1]}
+        if mode != "fp64":
+            entry.update({
+                "commutator_dE0_keV": abs(float(comm[0] - ref["comm"][0])) * 1e3,
+                "commutator_dH2b_frob_rel": float(np.linalg.norm(comm[n1:] - ref["comm"][n1:]) /
+                                                  np.linalg.norm(ref["comm"][n1:])),
+                "flow_dE0_keV": abs(float(hs[0] - ref["hs"][0])) * 1e3,
+                "flow_dH2b_frob_rel": float(np.linalg.norm(hs[n1:] - ref["hs"][n1:]) / np.linalg.norm(ref["hs"][n1:])),
+                "speedup_commutator": out["fp64"]["commutator_ms"] / ms})
+        out[mode] = entry
+        del st, dH, dE, dR, eng
+    print(json.dumps({
+        "metric": f"split-BF16 vs FP64 at eMax={emax}: commutator and {args.precision_flow_steps}-step flow",
+        "value": out["bf16x6"]["flow_dE0_keV"], "unit": "keV |dE0| (bf16x6 flow)", "n_gpus": 1,
+        "steps": args.precision_flow_steps, "warmup": 1, "ms_per_step": 1e3 * out["bf16x6"]["flow_s"] /
+        args.precision_flow_steps, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": f"[eta,H] and a Magnus flow (ds={args.ds}) at eMax={emax} ({b.norbits} orbits)",
+                   "modes": out, "not_built": "FP8 and TF32-compensated products (only split-BF16 is implemented)"},
+    }), flush=True)
+
+
+def observables_workload(args, local: int):
+    """Mixed-precision Magnus flow at eMax=12 to s=50, then BCH transformations of a scalar r^2
+    one-body operator and of a rank-2 one-body tensor (synthetic HO radial matrix elements)
+    through the scalar and the tensor commutators; peak HBM, |dE0| and d<r^2> against FP64."""
+    import numpy as np
+    import torch
+    from imsrg_gb300 import CONV, Engine, make_basis
+    from imsrg_gb300.operators import q2_operator, r2_operator
+
+    def used_gib():
+        free, total = torch.cuda.mem_get_info(local)
+        return (total - free) / 2**30
+
+    emax = args.emax if args.emax is not None else 12
+    steps = int(round(args.s_end / args.ds))
+    b = make_basis(emax)
+    A = b.Aprot + b.Aneut
+    base = used_gib()
+    peak = 0.0
+    eng = Engine(b, device=local, precision=args.mode)
+    H = eng.synthetic_hamiltonian(seed=1)
+    st = flow_state(eng, H)
+    kw = dict(max_terms=args.obs_bch_max_terms, conv=CONV, graph=True, allow_unconverged=True)
+    e0s, crit = [], []
+    t = time.perf_counter()
+    for k in range(steps):
+        info = eng.magnus_step(*st, args.ds, **kw)
+        e0s.append(info["E0"])
+        crit.append(abs(info["mbpt2"]))
+        peak = max(peak, used_gib())
+    eng.synchronize()
+    t_flow = time.perf_counter() - t
+    counters = eng.magnus_step_counters()
+    HS, G = st[0], st[1]
+    G_host = G.download()
+    # r^2 through BCH_EXPAND with the final Omega, mixed and FP64
+    R2 = r2_operator(eng)
+    dR2, dR2s = eng.new_op(1, R2), eng.new_op(1)
+    t = time.perf_counter()
+    n_r2 = eng.bch_expand(dR2s, G, dR2, 40, CONV)
+    eng.synchronize()
+    t_r2 = time.perf_counter() - t
+    r2_mixed = dR2s.E0 / A
+    peak = max(peak, used_gib())
+    # FP64: the first F steps of the same flow (|dE0|, ||dH||) and the r^2 transformation
+    cmp = {}
+    eng64 = Engine(b, device=local, precision="fp64")
+    st64 = flow_state(eng64, H)
+    F = min(args.fp64_steps, steps)
+    for _ in range(F):
+        eng64.magnus_step(*st64, args.ds, **kw)
+    peak = max(peak, used_gib())
+    if F:
+        stm = flow_state(eng, H)
+        for _ in range(F):
+            eng.magnus_step(*stm, args.ds, **kw)
+        hm, h64 = stm[0].download(), st64[0].download()
+        cmp = {"fp64_steps": F, "dE0_keV": abs(float(hm[0] - h64[0])) * 1e3,
+               "dH_frob_rel": float(np.linalg.norm(hm - h64) / np.linalg.norm(h64))}
+        del stm
+    del st64
+    G64, R64, R64s = eng64.new_op(-1, G_host), eng64.new_op(1, R2), eng64.new_op(1)
+    eng64.bch_expand(R64s, G64, R64, 40, CONV)
+    r2_fp64 = R64s.E0 / A
+    peak = max(peak, used_gib())
+    del G64, R64, R64s, eng64
+    # rank-2 tensor through BCH_TENSOR (FP64 tensor commutators) with the final Omega
+    Q = q2_operator(eng, 4)
+    dQ = eng.new_tensor(4, 0, 1, Q)
+    q0 = dQ.frob()
+    t = time.perf_counter()
+    n_q = eng.bch_tensor(G, dQ, 30, CONV)
+    eng.synchronize()
+    t_q = time.perf_counter() - t
+    q1 = dQ.frob()
+    peak = max(peak, used_gib())
+    print(json.dumps({
+        "metric": f"observables after a mixed-precision Magnus flow, eMax={emax}", "value": r2_mixed,
+        "unit": "fm^2 (<r^2> per nucleon)", "n_gpus": 1, "steps": steps, "warmup": 0,
+        "ms_per_step": 1e3 * t_flow / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": f"Magnus flow at eMax={emax} ({b.norbits} orbits) to s={args.ds * steps:g} with "
+                               f"{args.mode} commutators (graph steps, BCH up to {args.obs_bch_max_terms - 1} terms), "
+                               "then BCH of r^2 (scalar) and r^2 Y2 (rank 2, FP64 tensor commutators)",
+                   "E0_final": e0s[-1], "E0_first_steps": e0s[:5], "mbpt2_final": crit[-1],
+                   "flow_s": t_flow, "flow_commutators": counters["commutators"],
+                   "r2_mixed_fm2": r2_mixed, "r2_fp64_fm2": r2_fp64, "d_r2_fm2": abs(r2_mixed - r2_fp64),
+                   "r2_bare_fm2": R2[0] / A, "r2_bch_terms": n_r2, "r2_bch_s": t_r2,
+                   "q2_norm_bare": q0, "q2_norm_evolved": q1, "q2_bch_terms": n_q, "q2_bch_s": t_q,
+                   "tensor_slab_doubles": dQ.slab, "peak_hbm_gib": round(peak - base, 2), **cmp},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -316,7 +465,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--emax", type=int, default=None, help="default 10 (flow), 6 (adjoint)")
-    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision"])
+    ap.add_argument("--precision-flow-steps", type=int, default=20)
+    ap.add_argument("--obs-bch-max-terms", type=int, default=40)
     ap.add_argument("--adjoint-k", type=int, default=16)
     ap.add_argument("--s-end", type=float, default=30.0, help="adjoint workload: flow length")
     ap.add_argument("--fd-components", type=int, default=None)
@@ -343,6 +494,16 @@ def main():
     if args.workload == "adjoint":
         if rank == 0:
             adjoint_workload(args, local)
+        return
+    if args.workload == "precision":
+        if rank == 0:
+            precision_workload(args, local)
+        return
+    if args.workload == "observables":
+        if rank == 0:
+            if args.s_end == 30.0:
+                args.s_end = 50.0
+            observables_workload(args, local)
         return
 
     from imsrg_gb300 import Engine, make_basis
