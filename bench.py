@@ -192,6 +192,41 @@ def cpu_commutators(emax: int, n_warm: int, n_steps: int, seed: int = 1):
     return dt, cores, blas_name, keep
 
 
+def prepared_hamiltonian(eng, reference: str, seed: int = 1, time_transform: bool = False):
+    """The flow's starting Hamiltonian: the bare synthetic Hamiltonian (kinetic energy + V)
+    after calc_HF on the device (mean-field tensor and two-body basis change on the GPU, the
+    small self-consistency loop on the host) or after calc_HO (HO reference).  Returns the
+    host slab, D(HO orbit, HF orbit) and a record of the step."""
+    bare = eng.synthetic_bare_hamiltonian(seed=seed)
+    op = eng.new_op(1, bare)
+    eng.synchronize()
+    t = time.perf_counter()
+    D, info = eng.calc_hf(op) if reference == "hf" else eng.calc_ho(op)
+    eng.synchronize()
+    rec = {"reference": reference, "E0": info["e_hf"], "iterations": info["iterations"],
+           "wall_ms": 1e3 * (time.perf_counter() - t)}
+    H = op.download()
+    if time_transform and reference == "hf":
+        # the two-body basis change alone, CUDA events on the engine's stream (bare V, slab in place)
+        A = eng.basis.nholes
+        P = eng.basis.norbits - A
+        n2b = eng.slab - (1 + A * A + P * P + P * A)
+        op.upload(bare)
+        eng.transform_2b_to_hf(op, D)  # warm-up (tables, allocation)
+        reps = []
+        for _ in range(3):
+            op.upload(bare)
+            eng.synchronize()
+            eng.timer_begin()
+            eng.transform_2b_to_hf(op, D)
+            reps.append(eng.timer_end())
+        ms = min(reps)
+        rec.update({"transform_2b_ms": ms, "transform_2b_gbs": 2 * 8 * n2b / (ms * 1e-3) / 1e9,
+                    "transform_2b_bytes": 2 * 8 * n2b})
+    op.close()
+    return H, D, rec
+
+
 # ---------------------------------------------------------------- roofline bookkeeping
 def algorithmic_work(eng, mode: str, phase: str):
     """Algorithmic bytes (or FLOPs) of one launch of a phase at this basis.
@@ -266,8 +301,14 @@ def adjoint_workload(args, local: int):
     steps = int(round(args.s_end / args.ds))
     b = make_basis(emax)
     eng = Engine(b, device=local, precision="fp64")
-    H0 = eng.synthetic_hamiltonian(seed=1)
+    # HF frozen: H0 in the HF basis, each V_k moved to the same basis and normal ordered
+    H0, Dhf, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
     V = channel_perturbations(eng, K, sigma=0.1, seed=2)
+    for k, v in enumerate(V):
+        op = eng.new_op(1, v)
+        eng.sqop_to_hf(op, Dhf)
+        V[k] = op.download()
+        op.close()
     fl = MagnusFlowAdjoint(EngineBackend(eng), H0, V, ds=args.ds, steps=steps)
     theta = np.zeros(K)
     t = time.perf_counter()
@@ -300,6 +341,7 @@ def adjoint_workload(args, local: int):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"differentiable Magnus flow, eMax={emax} ({b.norbits} orbits), K={K} channel "
                                f"perturbations N(0,0.1 MeV), theta=0, ds={args.ds}, {steps} steps, White generator",
+                   "reference_state": hf_rec,
                    "plan_commutators": plan.commutators, "magnus_terms": plan.magnus, "bch_terms": plan.bch,
                    "E0": e0, "forward_s": t_fwd, "plan_s": t_plan, "adjoint_s": t_adj,
                    "adjoint_over_forward": t_adj / t_fwd, "fd_s": t_fd, "fd_h": h, "fd_components": nfd,
@@ -325,7 +367,7 @@ def precision_workload(args, local: int):
     for mode in ("fp64", "bf16x6", "bf16x3"):
         eng = Engine(b, device=local, precision=mode)
         if H is None:
-            H = eng.synthetic_hamiltonian(seed=1)
+            H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
         dH, dE, dR = eng.new_op(1, H), eng.new_op(-1), eng.new_op(1)
         eng.build_gs_white(dH, dE)
         eng.commutator(dE, dH, dR)
@@ -361,7 +403,8 @@ def precision_workload(args, local: int):
         args.precision_flow_steps, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16", "data": "synthetic",
         "config": {"workload": f"[eta,H] and a Magnus flow (ds={args.ds}) at eMax={emax} ({b.norbits} orbits)",
-                   "modes": out, "not_built": "FP8 and TF32-compensated products (only split-BF16 is implemented)"},
+                   "reference_state": hf_rec, "modes": out,
+                   "not_built": "FP8 and TF32-compensated products (only split-BF16 is implemented)"},
     }), flush=True)
 
 
@@ -385,7 +428,7 @@ def observables_workload(args, local: int):
     base = used_gib()
     peak = 0.0
     eng = Engine(b, device=local, precision=args.mode)
-    H = eng.synthetic_hamiltonian(seed=1)
+    H, Dhf, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
     st = flow_state(eng, H)
     kw = dict(max_terms=args.obs_bch_max_terms, conv=CONV, graph=True, allow_unconverged=True)
     e0s, crit = [], []
@@ -401,7 +444,7 @@ def observables_workload(args, local: int):
     HS, G = st[0], st[1]
     G_host = G.download()
     # r^2 through BCH_EXPAND with the final Omega, mixed and FP64
-    R2 = r2_operator(eng)
+    R2 = r2_operator(eng, coefs=Dhf)
     dR2, dR2s = eng.new_op(1, R2), eng.new_op(1)
     t = time.perf_counter()
     n_r2 = eng.bch_expand(dR2s, G, dR2, 40, CONV)
@@ -432,7 +475,7 @@ def observables_workload(args, local: int):
     peak = max(peak, used_gib())
     del G64, R64, R64s, eng64
     # rank-2 tensor through BCH_TENSOR (FP64 tensor commutators) with the final Omega
-    Q = q2_operator(eng, 4)
+    Q = q2_operator(eng, 4, coefs=Dhf)
     dQ = eng.new_tensor(4, 0, 1, Q)
     q0 = dQ.frob()
     t = time.perf_counter()
@@ -449,6 +492,7 @@ def observables_workload(args, local: int):
         "config": {"workload": f"Magnus flow at eMax={emax} ({b.norbits} orbits) to s={args.ds * steps:g} with "
                                f"{args.mode} commutators (graph steps, BCH up to {args.obs_bch_max_terms - 1} terms), "
                                "then BCH of r^2 (scalar) and r^2 Y2 (rank 2, FP64 tensor commutators)",
+                   "reference_state": hf_rec,
                    "E0_final": e0s[-1], "E0_first_steps": e0s[:5], "mbpt2_final": crit[-1],
                    "flow_s": t_flow, "flow_commutators": counters["commutators"],
                    "r2_mixed_fm2": r2_mixed, "r2_fp64_fm2": r2_fp64, "d_r2_fm2": abs(r2_mixed - r2_fp64),
@@ -479,6 +523,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--reference", default="hf", choices=["hf", "ho"],
+                    help="reference state of the flow: calc_HF (default) or calc_HO")
     args = ap.parse_args()
     args.e2e_steps = max(1, args.e2e_steps)
     world, rank, local, pg = dist_setup()
@@ -514,7 +560,7 @@ def main():
     step_kw = dict(max_terms=args.bch_max_terms, conv=args.bch_conv, graph=True)
     b = make_basis(args.emax)
     eng = Engine(b, device=local, precision=args.mode)
-    H = eng.synthetic_hamiltonian(seed=1)
+    H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1, time_transform=True)
 
     # ---- timed: K Magnus steps of the flow, each one CUDA-graph replay (after W warm-up steps)
     # the clock sampler starts before the warm-up: nvidia-smi's own start-up can stall the
@@ -676,6 +722,7 @@ def main():
                              "FP64 operators, E0 and norms",
                 "parallelism": f"replicas x{world}",
                 "l2": "inputs larger than L2 (0.27 GiB per operator, 0.78 GiB Z and Y each)",
+                "reference_state": hf_rec,
                 "timed": timed, "warmup_E0": e0_steps,
                 "fp64_commutators_per_s": fp64_rate * world if fp64_rate else None,
                 "speedup_vs_fp64": value / (fp64_rate * world) if fp64_rate else None, **cmp,

@@ -218,6 +218,7 @@ Ctx::~Ctx() {
   graph_release();
   adjoint_release();
   tensor_release();
+  hf_release();
   if (stream) cudaStreamDestroy(stream);
 }
 

@@ -17,6 +17,7 @@ struct TcState;
 struct StepGraph;
 struct AdjointState;
 struct TensorState;
+struct HFState;
 
 // MAGNUS_EXPAND coefficients as the literals of src/IMSRG_MAGNUS.f90:646
 constexpr double kMagnusCof[7] = {1.0, -0.5, .0833333333, 0.0, -0.00138888888, 0.0, 3.306878e-5};
@@ -69,6 +70,7 @@ struct Ctx {
   imsrg::TcState* tc = nullptr;
   StepGraph* sg = nullptr;  // captured Magnus step (graph.cu)
   AdjointState* adj = nullptr;  // reverse-mode workspaces (adjoint.cu)
+  HFState* hf = nullptr;        // Hartree-Fock tables (hf.cu)
   std::vector<double*> op_pool;  // slabs of destroyed operators, reused by imsrg_op_create
   // kernel launches issued (cumulative) and optional per-phase CUDA-event timing
   int64_t launches = 0;
@@ -130,6 +132,14 @@ struct Ctx {
                                  int pieces);
   imsrg_status tensor_frob(TensorState& S, const double* op, double scale, int slot);
   imsrg_status bch_tensor(TensorState& S, const double* G, int hG, double* HS, int max_terms, double conv, int* terms);
+
+  // Hartree-Fock and normal ordering (hf.cu)
+  imsrg_status hf_prepare();
+  void hf_release();
+  imsrg_status hf_mean_field(const double* op, int herm, std::vector<double>& M);
+  imsrg_status hf_transform_2b(double* op, int herm, const double* coefs);
+  imsrg_status hf_run(double* op, int herm, int mode, int max_iter, const double* coefs_in, double* coefs_out,
+                      imsrg_hf_info* info);
 
   // tensor-core (split-BF16, tcgen05) path, gemm_tc.cu
   imsrg_status tc_prepare(int mode);

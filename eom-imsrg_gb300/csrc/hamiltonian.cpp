@@ -48,7 +48,9 @@ inline double sgn(int n) { return (n & 1) ? -1.0 : 1.0; }
 
 }  // namespace
 
-extern "C" imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* out) {
+namespace {
+
+imsrg_status synthetic(imsrg_ctx* ctx, uint64_t seed, double v_scale, bool bare, double* out) {
   if (!ctx || !out) return IMSRG_ERR_INVALID_ARGUMENT;
   Ctx* c = reinterpret_cast<Ctx*>(ctx);
   const imsrg::Layout& L = c->L;
@@ -145,6 +147,16 @@ extern "C" imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t see
       t1[(size_t)i * N + j] = T;
       t1[(size_t)j * N + i] = T;
     }
+  if (bare) {  // the Hamiltonian as calc_HF receives it: T in the one-body arrays, E0 = 0
+    for (int a = 0; a < L.A; ++a)
+      for (int b = 0; b < L.A; ++b) H[L.off_fhh + a + (int64_t)b * L.A] = t1[(size_t)L.holes[a] * N + L.holes[b]];
+    for (int a = 0; a < L.P; ++a)
+      for (int b = 0; b < L.P; ++b) H[L.off_fpp + a + (int64_t)b * L.P] = t1[(size_t)L.parts[a] * N + L.parts[b]];
+    for (int a = 0; a < L.P; ++a)
+      for (int b = 0; b < L.A; ++b) H[L.off_fph + a + (int64_t)b * L.P] = t1[(size_t)L.parts[a] * N + L.holes[b]];
+    std::memcpy(out, H.data(), sizeof(double) * H.size());
+    return IMSRG_OK;
+  }
   // normal ordering (src/basic_IMSRG.f90:2419-2550)
   double sm = 0.0;
   for (int i = 0; i < N; ++i) sm += t1[(size_t)i * N + i] * L.con[i] * (L.jj[i] + 1);
@@ -188,4 +200,15 @@ extern "C" imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t see
     }
   std::memcpy(out, H.data(), sizeof(double) * H.size());
   return IMSRG_OK;
+}
+
+}  // namespace
+
+extern "C" imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* out) {
+  return synthetic(ctx, seed, v_scale, false, out);
+}
+
+extern "C" imsrg_status imsrg_synthetic_bare_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale,
+                                                          double* out) {
+  return synthetic(ctx, seed, v_scale, true, out);
 }

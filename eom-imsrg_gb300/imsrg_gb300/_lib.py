@@ -33,6 +33,10 @@ class Basis_t(C.Structure):
                 ("Aneut", C.c_int32)]
 
 
+class HFInfo_t(C.Structure):
+    _fields_ = [("e_hf", C.c_double), ("crit", C.c_double), ("iterations", C.c_int32)]
+
+
 class StepInfo_t(C.Structure):
     _fields_ = [("E0", C.c_double), ("mbpt2", C.c_double), ("magnus_terms", C.c_int32), ("bch_terms", C.c_int32),
                 ("bch_converged", C.c_int32), ("graph_rebuilt", C.c_int32)]
@@ -100,6 +104,12 @@ SIGNATURES = {
     "imsrg_white_vjp": [_vp, _vp, _vp, _vp],
     "imsrg_dot_sq_op": [_vp, _vp, _vp, _pd],
     "imsrg_synthetic_hamiltonian": [_vp, _u64, _d, _vp],
+    "imsrg_synthetic_bare_hamiltonian": [_vp, _u64, _d, _vp],
+    "imsrg_calc_hf": [_vp, _vp, _i32, _vp, C.POINTER(HFInfo_t)],
+    "imsrg_calc_ho": [_vp, _vp, _vp, C.POINTER(HFInfo_t)],
+    "imsrg_sqop_to_hf": [_vp, _vp, _vp],
+    "imsrg_transform_2b_to_hf": [_vp, _vp, _vp],
+    "imsrg_normal_order": [_vp, _vp],
     "imsrg_launch_count": [_vp, _pi64],
     "imsrg_timer_begin": [_vp],
     "imsrg_timer_end": [_vp, C.POINTER(C.c_float)],

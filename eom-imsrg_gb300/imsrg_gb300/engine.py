@@ -248,6 +248,45 @@ class Engine:
         self._ck(self.L.imsrg_synthetic_hamiltonian(self.h, C.c_uint64(seed), float(v_scale), out.ctypes.data))
         return out
 
+    def synthetic_bare_hamiltonian(self, seed: int = 1, v_scale: float = 1.0) -> np.ndarray:
+        """The synthetic Hamiltonian before normal ordering (kinetic energy in f, E0 = 0)."""
+        out = np.zeros(self.slab, np.float64)
+        self._ck(self.L.imsrg_synthetic_bare_hamiltonian(self.h, C.c_uint64(seed), float(v_scale),
+                                                          out.ctypes.data))
+        return out
+
+    # ---------------------------------------------------------------- Hartree-Fock
+    def calc_hf(self, H: SqOp, max_iter: int = 1000):
+        """calc_HF (src/HF_mod.f90:14-105): H (bare) becomes the normal-ordered HF-basis
+        Hamiltonian.  Returns (D, info) with D(HO orbit, HF orbit) as an N x N array."""
+        N = self.basis.norbits
+        D = np.zeros(N * N)
+        info = _lib.HFInfo_t()
+        self._ck(self.L.imsrg_calc_hf(self.h, H.h, int(max_iter), D.ctypes.data, C.byref(info)))
+        return D.reshape(N, N, order="F"), {"e_hf": info.e_hf, "crit": info.crit, "iterations": info.iterations}
+
+    def calc_ho(self, H: SqOp):
+        """calc_HO (src/HF_mod.f90:107-179): normal ordering w.r.t. the HO reference."""
+        N = self.basis.norbits
+        D = np.zeros(N * N)
+        info = _lib.HFInfo_t()
+        self._ck(self.L.imsrg_calc_ho(self.h, H.h, D.ctypes.data, C.byref(info)))
+        return D.reshape(N, N, order="F"), {"e_hf": info.e_hf, "crit": info.crit, "iterations": info.iterations}
+
+    def sqop_to_hf(self, op: SqOp, D: np.ndarray):
+        """sqop_to_HF (src/HF_mod.f90:181-209) of a bare scalar operator, in place."""
+        Df = np.ascontiguousarray(np.asarray(D, np.float64).ravel(order="F"))
+        self._ck(self.L.imsrg_sqop_to_hf(self.h, op.h, Df.ctypes.data))
+
+    def transform_2b_to_hf(self, op: SqOp, D: np.ndarray):
+        """transform_2b_to_HF (src/HF_mod.f90:567-692), in place."""
+        Df = np.ascontiguousarray(np.asarray(D, np.float64).ravel(order="F"))
+        self._ck(self.L.imsrg_transform_2b_to_hf(self.h, op.h, Df.ctypes.data))
+
+    def normal_order(self, op: SqOp):
+        """normal_order (src/basic_IMSRG.f90:2419-2550), in place."""
+        self._ck(self.L.imsrg_normal_order(self.h, op.h))
+
     # ---------------------------------------------------------------- algebra
     def copy_sq_op(self, H: SqOp, op: SqOp):
         self._ck(self.L.imsrg_copy_sq_op(self.h, H.h, op.h))

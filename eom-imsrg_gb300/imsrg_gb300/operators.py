@@ -9,7 +9,9 @@ q2_operator:  a rank-2, even-parity one-body tensor  <a||r^2 Y_2||b>: the same H
               the reference's tensor hermiticity f(b,a) = (-1)^((ja-jb)/2) f(a,b)
               (construct_random_rankX, src/brute_force_testing.f90:123-265).
 Both are synthetic stand-ins (the reference builds its observables from the same HO pieces);
-neither carries a two-body part.
+neither carries a two-body part.  With coefs = D(HO orbit, HF orbit) the one-body matrix is
+moved to the Hartree-Fock basis first, F' = D^T F D, as transform_1b_to_HF and
+transform_1b_to_HF_tensor do (src/HF_mod.f90:481-564, 695-758).
 """
 from __future__ import annotations
 
@@ -63,9 +65,16 @@ def y2_reduced(la: int, ja: int, lb: int, jb: int, k: int = 2) -> float:
             threej(ja, 2 * k, jb, -1, 0, 1))
 
 
-def _onebody_slab(eng, size: int, f) -> np.ndarray:
-    """A slab of `size` elements whose fhh / fpp / fph are f(orbit a, orbit b)."""
+def _onebody_slab(eng, size: int, f, coefs=None) -> np.ndarray:
+    """A slab of `size` elements whose fhh / fpp / fph are f(orbit a, orbit b), or the
+    elements of D^T F D when coefs D is given."""
     b = eng.basis
+    if coefs is not None:
+        N = b.norbits
+        F = np.array([[f(a, c) for c in range(N)] for a in range(N)])
+        D = np.asarray(coefs, dtype=np.float64)
+        Fp = D.T @ F @ D
+        f = lambda a, c: Fp[a, c]  # noqa: E731
     con = np.array(b.con)
     holes = [i for i in range(b.norbits) if con[i]]
     parts = [i for i in range(b.norbits) if not con[i]]
@@ -85,8 +94,9 @@ def _onebody_slab(eng, size: int, f) -> np.ndarray:
     return s
 
 
-def r2_operator(eng) -> np.ndarray:
-    """Scalar slab of the intrinsic r^2 operator (fm^2), normal ordered w.r.t. the reference."""
+def r2_operator(eng, coefs=None) -> np.ndarray:
+    """Scalar slab of the intrinsic r^2 operator (fm^2), normal ordered w.r.t. the reference
+    (in the basis of coefs when given)."""
     b = eng.basis
     A = b.Aprot + b.Aneut
     b2 = HBARC * HBARC / (M_NUC * b.hw)
@@ -97,13 +107,16 @@ def r2_operator(eng) -> np.ndarray:
             return 0.0
         return b2 * (1.0 - 1.0 / A) * ho_r2(int(nn[a]), int(nn[c]), int(ll[a]))
 
-    s = _onebody_slab(eng, eng.slab, f)
-    s[0] = sum((jj[h] + 1) * f(h, h) for h in range(b.norbits) if con[h])
+    s = _onebody_slab(eng, eng.slab, f, coefs)
+    A_, P_ = b.nholes, b.norbits - b.nholes
+    holes = [i for i in range(b.norbits) if con[i]]
+    s[0] = sum((jj[h] + 1) * s[1 + k + k * A_] for k, h in enumerate(holes))
     return s
 
 
-def q2_operator(eng, rank2: int = 4) -> np.ndarray:
-    """Tensor slab (rank2 doubled, even parity) of <a||r^2 Y_2||b> (fm^2), l-diagonal radial part."""
+def q2_operator(eng, rank2: int = 4, coefs=None) -> np.ndarray:
+    """Tensor slab (rank2 doubled, even parity) of <a||r^2 Y_2||b> (fm^2), l-diagonal radial part
+    (in the basis of coefs when given)."""
     b = eng.basis
     b2 = HBARC * HBARC / (M_NUC * b.hw)
     nn, ll, jj, tz = (np.array(x) for x in (b.nn, b.ll, b.jj, b.itzp))
@@ -120,4 +133,4 @@ def q2_operator(eng, rank2: int = 4) -> np.ndarray:
             return g(a, c)
         return (-1) ** ((int(jj[c]) - int(jj[a])) // 2) * g(c, a)
 
-    return _onebody_slab(eng, eng.tensor_sizes(rank2, 0)[0], f)
+    return _onebody_slab(eng, eng.tensor_sizes(rank2, 0)[0], f, coefs)

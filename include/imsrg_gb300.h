@@ -246,6 +246,36 @@ imsrg_status imsrg_dot_sq_op(imsrg_ctx* ctx, const imsrg_op* A, const imsrg_op* 
  * normal ordered w.r.t. the reference state (normal_order, src/basic_IMSRG.f90:2419-2550).
  * Writes one host slab (herm = +1). */
 imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* host_slab);
+/* The same Hamiltonian before normal ordering, as calc_HF receives it after read_me2j_interaction
+ * and calculate_h0_harm_osc (src/main_IMSRG.f90:125-157): the kinetic energy in fhh/fpp/fph, V in
+ * the two-body arrays, E0 = 0. */
+imsrg_status imsrg_synthetic_bare_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* host_slab);
+
+/* ---- Hartree-Fock and normal ordering (FP64).  The self-consistency loop runs on the host
+ * (blocks of orbits sharing (l, j, tz), at most eMax/2+1 orbits each, cyclic Jacobi in place of
+ * LAPACK dsyev); the mean-field contraction of V and the two-body basis change run on the device.
+ * coefs is the reference's full_sp_block_mat D as one host N x N column-major matrix
+ * D(HO orbit, HF orbit); entries between different (l, j, tz) blocks are zero (and ignored). */
+typedef struct {
+  double e_hf;        /* E0 of the result (e_HF, src/HF_mod.f90:449-478) */
+  double crit;        /* last convergence measure: sum over blocks of |eps_new - eps_old|_2 */
+  int32_t iterations; /* self-consistency iterations (0 for calc_HO) */
+} imsrg_hf_info;
+/* calc_HF (src/HF_mod.f90:14-105), without a three-body force: H (herm +1) holds the bare
+ * Hamiltonian and is replaced by the normal-ordered Hamiltonian in the HF basis; coefs and info
+ * may be NULL.  Iterates while crit > 1e-6 (the reference's literal); IMSRG_ERR_NOT_CONVERGED
+ * after max_iter iterations, H unchanged. */
+imsrg_status imsrg_calc_hf(imsrg_ctx* ctx, imsrg_op* H, int32_t max_iter, double* coefs, imsrg_hf_info* info);
+/* calc_HO (src/HF_mod.f90:107-179): normal ordering w.r.t. the HO reference, coefs = 1 */
+imsrg_status imsrg_calc_ho(imsrg_ctx* ctx, imsrg_op* H, double* coefs, imsrg_hf_info* info);
+/* sqop_to_HF (src/HF_mod.f90:181-209) of a bare scalar operator: f and V to the basis of coefs,
+ * then normal ordering */
+imsrg_status imsrg_sqop_to_hf(imsrg_ctx* ctx, imsrg_op* op, const double* coefs);
+/* transform_2b_to_HF (src/HF_mod.f90:567-692): the two-body part alone, in place */
+imsrg_status imsrg_transform_2b_to_hf(imsrg_ctx* ctx, imsrg_op* op, const double* coefs);
+/* normal_order (src/basic_IMSRG.f90:2419-2550): E0 and the one-body elements between orbits
+ * sharing (l, j, tz) from the operator's f and V w.r.t. the reference state; V unchanged */
+imsrg_status imsrg_normal_order(imsrg_ctx* ctx, imsrg_op* op);
 
 #ifdef __cplusplus
 }

@@ -1678,6 +1678,7 @@ void white_vjp(const Basis& B, const double* H, int hH, const double* ETAb, doub
 
 namespace {
 #include "oracle_tensor.inc"
+#include "oracle_hf.inc"
 }  // namespace
 
 // ====================================================================== C interface
@@ -1843,5 +1844,13 @@ double orc_tensor_bf2(void* t, const double* A, int hA, const double* Bo, int hB
                       int J2) {
   return tensor_bf2(*(TBasis*)t, A, hA, Bo, hB, a, b, c, d, J1, J2);
 }
+
+
+// ---- Hartree-Fock input preparation (oracle_hf.inc)
+void orc_gamma_matrix(void* b, const double* op, int herm, const double* rho, double* gam) {
+  gamma_matrix(*(Basis*)b, op, herm, rho, gam);
+}
+void orc_transform_2b_to_hf(void* b, double* op, const double* D) { transform_2b_to_hf(*(Basis*)b, op, D); }
+void orc_normal_order(void* b, const double* in, int herm, double* out) { normal_order(*(Basis*)b, in, herm, out); }
 
 }  // extern "C"

@@ -89,6 +89,9 @@ def lib():
         "orc_bf_0body": (d, [vp, _dp, i, _dp, i]),
         "orc_bf_1body": (d, [vp, _dp, i, _dp, i, i, i]),
         "orc_bf_2body": (d, [vp, _dp, i, _dp, i, i, i, i, i, i]),
+        "orc_gamma_matrix": (None, [vp, _dp, i, _dp, _dp]),
+        "orc_transform_2b_to_hf": (None, [vp, _dp, _dp]),
+        "orc_normal_order": (None, [vp, _dp, i, _dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -108,6 +111,9 @@ def use_blas_dgemm(addr: int, ilp64: bool) -> None:
 
 # reference default-real literal 1e-6 (src/IMSRG_MAGNUS.f90:152)
 BCH_CONV = float(np.float32(1e-6))
+# calc_HF's convergence test `crit > 1e-6` compares with the same default-real literal
+# (src/HF_mod.f90:49)
+HF_CONV = float(np.float32(1e-6))
 
 
 class Oracle:
@@ -253,6 +259,142 @@ class Oracle:
 
     def bf_2body(self, A, hA, B, hB, a, b, c, d, J):
         return self.L.orc_bf_2body(self.h, A, hA, B, hB, a, b, c, d, J)
+
+    # ---- Hartree-Fock input preparation (src/HF_mod.f90)
+    def sp_blocks(self) -> list:
+        """Orbits sharing (l, j, tz), ascending: the blocks of a full_sp_block_mat."""
+        b = self.basis
+        groups: dict = {}
+        for i in range(b.norbits):
+            groups.setdefault((int(b.ll[i]), int(b.jj[i]), int(b.itzp[i])), []).append(i)
+        return [np.array(v) for v in groups.values()]
+
+    def gamma_matrix(self, H, hH, rho) -> np.ndarray:
+        """gamma_matrix (src/HF_mod.f90:242-305) of a density scaled by (2j+1)."""
+        N = self.basis.norbits
+        out = np.zeros(N * N)
+        self.L.orc_gamma_matrix(self.h, H, hH, np.ascontiguousarray(rho.ravel(order="F")), out)
+        return out.reshape(N, N, order="F")
+
+    def normal_order(self, op, herm=1) -> np.ndarray:
+        """normal_order (src/basic_IMSRG.f90:2419-2550)."""
+        out = np.zeros(self.slab)
+        self.L.orc_normal_order(self.h, op, herm, out)
+        return out
+
+    def transform_2b_to_hf(self, op, D) -> np.ndarray:
+        """transform_2b_to_HF (src/HF_mod.f90:567-692); D(HO orbit, HF orbit), N x N."""
+        out = np.array(op, dtype=np.float64, copy=True)
+        self.L.orc_transform_2b_to_hf(self.h, out, np.ascontiguousarray(D.ravel(order="F")))
+        return out
+
+    def _kin_matrix(self, op, herm=1) -> np.ndarray:
+        """write_kin_matrix (src/HF_mod.f90:211-240): f_elem on each block's upper triangle."""
+        N = self.basis.norbits
+        T = np.zeros((N, N))
+        for st in self.sp_blocks():
+            for x in range(len(st)):
+                for y in range(x, len(st)):
+                    T[st[x], st[y]] = T[st[y], st[x]] = self.f_elem(op, herm, int(st[x]), int(st[y]))
+        return T
+
+    def _write_f(self, out, st, Fp) -> None:
+        """The remap of transform_1b_to_HF (src/HF_mod.f90:530-560) for one block."""
+        b = self.basis
+        con = np.array(b.con)
+        A, P = b.nholes, b.norbits - b.nholes
+        loc = np.zeros(b.norbits, dtype=int)
+        loc[con == 1] = np.arange(A)
+        loc[con == 0] = np.arange(P)
+        o_hh, o_pp = 1, 1 + A * A
+        o_ph = o_pp + P * P
+        for x in range(len(st)):
+            for y in range(x, len(st)):
+                i, j = int(st[x]), int(st[y])
+                c1, c2 = con[i], con[j]
+                if c1 + c2 == 0:
+                    out[o_pp + loc[i] + loc[j] * P] = out[o_pp + loc[j] + loc[i] * P] = Fp[x, y]
+                elif c1 + c2 == 1:
+                    if c2 > c1:
+                        out[o_ph + loc[i] + loc[j] * P] = Fp[x, y]
+                    else:
+                        out[o_ph + loc[j] + loc[i] * P] = Fp[y, x]
+                else:
+                    out[o_hh + loc[i] + loc[j] * A] = out[o_hh + loc[j] + loc[i] * A] = Fp[x, y]
+
+    def _hf(self, H, max_iter, iterate):
+        b = self.basis
+        N = b.norbits
+        jj, con = np.array(b.jj), np.array(b.con)
+        blocks = self.sp_blocks()
+        T = self._kin_matrix(H)
+        D = [np.eye(len(st)) for st in blocks]
+        eig = [np.zeros(len(st)) for st in blocks]
+
+        def density():  # density_matrix (src/HF_mod.f90:419-446)
+            rho = np.zeros((N, N))
+            for k, st in enumerate(blocks):
+                Dx = D[k] * con[st][None, :]
+                rho[np.ix_(st, st)] = (Dx @ Dx.T) * (jj[st[0]] + 1)
+            return rho
+
+        r = 0
+        if iterate:  # calc_HF main loop (src/HF_mod.f90:56-81)
+            crit = 10.0
+            while crit > HF_CONV:
+                if r >= max_iter:
+                    raise RuntimeError("Hartree-Fock did not converge")
+                Vgam = self.gamma_matrix(H, 1, density())
+                crit = 0.0
+                for k, st in enumerate(blocks):
+                    ix = np.ix_(st, st)
+                    w, v = np.linalg.eigh(T[ix] + Vgam[ix], UPLO="U")  # dsyev('V','U')
+                    crit += float(np.sqrt(np.sum((eig[k] - w) ** 2)))
+                    D[k], eig[k] = v, w
+                r += 1
+        else:  # calc_HO (src/HF_mod.f90:107-179)
+            Vgam = self.gamma_matrix(H, 1, density())
+        out = np.array(H, dtype=np.float64, copy=True)
+        Dfull = np.zeros((N, N))
+        E = 0.0
+        for k, st in enumerate(blocks):
+            Dk = D[k]
+            for i in range(len(st)):
+                if Dk[i, i] < 0.0:
+                    Dk[:, i] = -Dk[:, i]
+            ix = np.ix_(st, st)
+            F = T[ix] + Vgam[ix]
+            Fp = Dk.T @ (F @ Dk)
+            Tp = Dk.T @ (T[ix] @ Dk)
+            Vp = Dk.T @ (Vgam[ix] @ Dk)
+            self._write_f(out, st, Fp)
+            # e_HF (src/HF_mod.f90:449-478)
+            E += float(np.sum((np.diag(Tp) + 0.5 * np.diag(Vp)) * con[st] * (jj[st[0]] + 1.0)))
+            Dfull[ix] = Dk
+        out[0] = E
+        out = self.transform_2b_to_hf(out, Dfull)
+        return out, Dfull, E, r
+
+    def calc_hf(self, H, max_iter: int = 10000):
+        """calc_HF (src/HF_mod.f90:14-105) of a bare Hamiltonian slab (kinetic energy in the
+        one-body arrays, V in the two-body arrays, E0 unused).  Returns the normal-ordered
+        Hamiltonian in the HF basis, D(HO orbit, HF orbit), E_HF and the iteration count."""
+        return self._hf(H, max_iter, True)
+
+    def calc_ho(self, H):
+        """calc_HO (src/HF_mod.f90:107-179): the same steps with D = 1 and no iteration."""
+        return self._hf(H, 0, False)
+
+    def sqop_to_hf(self, op, D) -> np.ndarray:
+        """sqop_to_HF (src/HF_mod.f90:181-209) of a bare hermitian scalar operator."""
+        out = np.array(op, dtype=np.float64, copy=True)
+        T = self._kin_matrix(op)
+        for st in self.sp_blocks():
+            ix = np.ix_(st, st)
+            Dk = D[ix]
+            self._write_f(out, st, Dk.T @ (T[ix] @ Dk))
+        out = self.transform_2b_to_hf(out, D)
+        return self.normal_order(out, 1)
 
 
 class TensorOracle:

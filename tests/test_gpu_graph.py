@@ -48,11 +48,19 @@ def test_graph_step_equals_eager(built_lib, precision):
     assert c1["kernels"] > c0["kernels"]
 
 
-def test_graph_flow_matches_oracle(built_lib, oracles):
+@pytest.mark.parametrize("reference", ["ho", "hf"])
+def test_graph_flow_matches_oracle(built_lib, oracles, reference):
     from imsrg_gb300 import Engine, make_basis
     o = oracles(4)
     eng = Engine(make_basis(4), device=0, precision="fp64")
-    H = eng.synthetic_hamiltonian(seed=4)
+    if reference == "hf":  # calc_HF first, as the reference's driver does with hartree_fock set
+        bare = eng.synthetic_bare_hamiltonian(seed=4)
+        Hop = eng.new_op(1, bare)
+        eng.calc_hf(Hop)
+        H = Hop.download()
+        assert rel_err(H, o.calc_hf(bare)[0]) < 1e-10
+    else:
+        H = eng.synthetic_hamiltonian(seed=4)
     HS, G, DG, dH = _state(eng, H)
     oG = o.new()
     oDG = o.white(H, 1)
