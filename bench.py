@@ -408,6 +408,63 @@ def precision_workload(args, local: int):
     }), flush=True)
 
 
+def hf_flow_workload(args, local: int):
+    """The small end-to-end case: calc_HF, then the FP64 Magnus flow (White generator, ds=0.5,
+    BCH to 40 terms or term norm < 1e-6) to s=50 at eMax=4, once on the GPU (one CUDA-graph
+    replay per step) and once on the CPU restatement of the reference's algorithm (the oracle,
+    all host cores): wall time of each and the agreement of E0 and H(s)."""
+    import numpy as np
+    from imsrg_gb300 import CONV, Engine, make_basis
+    from oracle import oracle as orc
+    emax = args.emax if args.emax is not None else 4
+    steps = int(round(args.s_end / args.ds))
+    b = make_basis(emax)
+    eng = Engine(b, device=local, precision="fp64")
+    H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
+    st = flow_state(eng, H)
+    kw = dict(max_terms=40, conv=CONV, graph=True)
+    eng.synchronize()
+    c0 = eng.magnus_step_counters()
+    t = time.perf_counter()
+    for _ in range(steps):
+        eng.magnus_step(*st, args.ds, wait=False, **kw)
+    eng.synchronize()
+    t_gpu = time.perf_counter() - t
+    c1 = eng.magnus_step_counters()
+    HS_gpu = st[0].download()
+    o = orc.Oracle(b)
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    t = time.perf_counter()
+    G = o.new()
+    DG = o.white(H, 1)
+    n_cpu = 0
+    for _ in range(steps):
+        used = o.magnus_expand(DG, G)
+        G += args.ds * DG
+        HS, n = o.bch_expand(G, H, 40, orc.BCH_CONV)
+        DG = o.white(HS, 1)
+        n_cpu += used + n
+    t_cpu = time.perf_counter() - t
+    n_gpu = c1["commutators"] - c0["commutators"]
+    print(json.dumps({
+        "metric": f"HF + FP64 Magnus flow to s={args.ds * steps:g} at eMax={emax}, wall time",
+        "value": t_gpu, "unit": "s", "n_gpus": 1, "steps": steps, "warmup": 0, "ms_per_step": 1e3 * t_gpu / steps,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"calc_HF, then {steps} Magnus steps (ds={args.ds}) at eMax={emax} ({b.norbits} orbits), "
+                               "White generator, BCH <= 40 terms / 1e-6; GPU graph steps vs the CPU restatement",
+                   "reference_state": hf_rec, "gpu_s": t_gpu, "cpu_s": t_cpu, "cpu_cores": cores,
+                   "cpu_over_gpu": t_cpu / t_gpu, "commutators_gpu": n_gpu, "commutators_cpu": n_cpu,
+                   "unconverged_bch_steps_gpu": c1["unconverged"] - c0["unconverged"],
+                   "E0_gpu": float(HS_gpu[0]), "E0_cpu": float(HS[0]), "dE0_keV": 1e3 * abs(HS_gpu[0] - HS[0]),
+                   "H_max_rel_err": float(np.max(np.abs(HS_gpu - HS)) / np.max(np.abs(HS))),
+                   "mbpt2_final": o.mbpt2(HS, 1)},
+        "cpu_baseline": {"value": t_cpu, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"the same {steps}-step flow with the oracle (FP64, OpenMP x{cores})"},
+        "gpu_launches": c1["kernels"] - c0["kernels"],
+    }), flush=True)
+
+
 def observables_workload(args, local: int):
     """Mixed-precision Magnus flow at eMax=12 to s=50, then BCH transformations of a scalar r^2
     one-body operator and of a rank-2 one-body tensor (synthetic HO radial matrix elements)
@@ -509,7 +566,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--emax", type=int, default=None, help="default 10 (flow), 6 (adjoint)")
-    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision", "hf-flow"])
     ap.add_argument("--precision-flow-steps", type=int, default=20)
     ap.add_argument("--obs-bch-max-terms", type=int, default=40)
     ap.add_argument("--adjoint-k", type=int, default=16)
@@ -540,6 +597,12 @@ def main():
     if args.workload == "adjoint":
         if rank == 0:
             adjoint_workload(args, local)
+        return
+    if args.workload == "hf-flow":
+        if rank == 0:
+            if args.s_end == 30.0:
+                args.s_end = 50.0
+            hf_flow_workload(args, local)
         return
     if args.workload == "precision":
         if rank == 0:
