@@ -337,30 +337,32 @@ __global__ void k_ts122(DevLayout D, DevTLayout T, const double* __restrict__ L,
 
 __global__ void k_ts212(DevLayout D, DevTLayout T, const double* __restrict__ L, int hL, const double* __restrict__ R,
                         int hR, double* __restrict__ RES) {
-  const int rank = T.rank, dp = T.dpar >> 1;
+  const int rank = T.rank;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T.n2b; e += (int64_t)gridDim.x * blockDim.x) {
     int q, g, a, b, c, d;
     d_tdecode(D, T, e, q, g, a, b, c, d);
     const int J1 = T.J1[q], J2 = T.J2[q];
     const int ja = D.jj[a], jb = D.jj[b], jc = D.jj[c], jd = D.jj[d];
-    double sm = 0.0;
-    for (int i = 0; i < D.N; ++i) {
-      const int ji = D.jj[i], ti = D.tz[i], mli = (D.ll[i] + dp) & 1;
-      double s1 = 0, s2 = 0, s3 = 0, s4 = 0;
-      if (ti == D.tz[a] && mli == (D.ll[a] & 1) && d_tri(ji, ja, rank))
-        s1 = -d_six_t(T, J1, J2, ji, ja, jb) * d_ftelem(D, T, R, hR, a, i) * d_v_elem(D, L, hL, i, b, c, d, J2);
-      s1 *= d_sgn((ja + jb - J2) >> 1);
-      if (ti == D.tz[b] && mli == (D.ll[b] & 1) && d_tri(ji, jb, rank))
-        s2 = d_six_t(T, J1, J2, ji, jb, ja) * d_ftelem(D, T, R, hR, b, i) * d_v_elem(D, L, hL, i, a, c, d, J2);
-      s2 *= d_sgn((J1 + J2) >> 1);
-      if (ti == D.tz[d] && mli == (D.ll[d] & 1) && d_tri(ji, jd, rank))
-        s3 = d_six_t(T, J1, J2, jd, ji, jc) * d_ftelem(D, T, R, hR, i, d) * d_v_elem(D, L, hL, a, b, c, i, J1);
-      s3 *= d_sgn((jc + jd - J1) >> 1);
-      if (ti == D.tz[c] && mli == (D.ll[c] & 1) && d_tri(ji, jc, rank))
-        s4 = -d_six_t(T, J1, J2, jc, ji, jd) * d_ftelem(D, T, R, hR, i, c) * d_v_elem(D, L, hL, a, b, d, i, J1);
-      s4 *= d_sgn((J2 + J1) >> 1);
-      sm += s1 + s2 + s3 + s4;
+    // each sum runs over the orbits the tensor one-body element can couple (tz, parity, rank)
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0;
+    for (int t = 0, s0 = T.tnb_start[a], n = T.tnb_count[a]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s1 -= d_six_t(T, J1, J2, D.jj[i], ja, jb) * d_ftelem(D, T, R, hR, a, i) * d_v_elem(D, L, hL, i, b, c, d, J2);
     }
+    for (int t = 0, s0 = T.tnb_start[b], n = T.tnb_count[b]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s2 += d_six_t(T, J1, J2, D.jj[i], jb, ja) * d_ftelem(D, T, R, hR, b, i) * d_v_elem(D, L, hL, i, a, c, d, J2);
+    }
+    for (int t = 0, s0 = T.tnb_start[d], n = T.tnb_count[d]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s3 += d_six_t(T, J1, J2, jd, D.jj[i], jc) * d_ftelem(D, T, R, hR, i, d) * d_v_elem(D, L, hL, a, b, c, i, J1);
+    }
+    for (int t = 0, s0 = T.tnb_start[c], n = T.tnb_count[c]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s4 -= d_six_t(T, J1, J2, jc, D.jj[i], jd) * d_ftelem(D, T, R, hR, i, c) * d_v_elem(D, L, hL, a, b, d, i, J1);
+    }
+    const double sm = s1 * d_sgn((ja + jb - J2) >> 1) + s2 * d_sgn((J1 + J2) >> 1) + s3 * d_sgn((jc + jd - J1) >> 1) +
+                      s4 * d_sgn((J2 + J1) >> 1);
     RES[T.goff[0] + e] += sm * sqrt((J1 + 1.0) * (J2 + 1.0) / (1.0 + (a == b ? 1.0 : 0.0)) /
                                     (1.0 + (c == d ? 1.0 : 0.0))) * d_sgn(rank >> 1);
   }

@@ -159,6 +159,7 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
   pk.add(T.ob_kind, &d.ob_kind); pk.add(T.ob_p, &d.ob_p); pk.add(T.ob_q, &d.ob_q); pk.add(T.ob_pk, &d.ob_pk);
   pk.add(T.ob_qk, &d.ob_qk);
   pk.add(T.six, &d.six); pk.add(T.six_m, &d.six_m); pk.add(T.ccnb, &d.ccnb);
+  pk.add(T.tnb_start, &d.tnb_start); pk.add(T.tnb_count, &d.tnb_count); pk.add(T.tnb_list, &d.tnb_list);
   pk.add(pphh, &st->pphh_p); pk.add(pphh_tiles, &st->pphh_t);
   pk.add(cbp, &st->cb_p); pk.add(cbt, &st->cb_t);
   pk.add(T.seg_start, &st->seg_start); pk.add(T.seg_len, &st->seg_len); pk.add(T.seg_w, &st->seg_w);

@@ -35,6 +35,8 @@ struct TLayout {
   // six_m[((((c-1)/2*nh + (d-1)/2)*nh + (b-1)/2)*nhx + (x-1)/2)*nJ*nJ + (J2/2)*nJ + J4/2]
   std::vector<double> six_m;
   std::vector<int> ccnb;  // [(p*N+h)*NJ + JC/2] -> ph column of (p,h) in its cross-coupled channel, -1
+  // orbits i a tensor one-body element f(a,i) can couple: same tz, parity l_i + dpar/2 = l_a, |j_i - j_a| <= rank
+  std::vector<int> tnb_start, tnb_count, tnb_list;
   // cross-coupled tensor blocks of TS_commutator_222_ph: (J3, J4 >= J3, Tz 0/1, PAR) and their
   // scalar cross-coupled channels qa (J3, Tz, PAR), qb (J4, Tz, PAR xor dpar/2)
   std::vector<int> cb_J3, cb_J4, cb_Tz, cb_PAR, cb_qa, cb_qb;
@@ -77,6 +79,9 @@ struct DevTLayout {
   const double* six;
   const double* six_m;
   const int* ccnb;
+  const int* tnb_start;
+  const int* tnb_count;
+  const int* tnb_list;
 };
 
 }  // namespace imsrg

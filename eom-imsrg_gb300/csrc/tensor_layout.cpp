@@ -113,6 +113,18 @@ std::string build_tlayout(TLayout& T, const Layout& L, int rank, int dpar) {
       T.ccnb[((size_t)p * L.N + h) * NJ + L.cc_J[c] / 2] = k;
     }
 
+  // orbits a tensor one-body element f(a, i) can couple to (TS_commutator_212's sums)
+  T.tnb_start.assign(L.N, 0);
+  T.tnb_count.assign(L.N, 0);
+  T.tnb_list.clear();
+  for (int a = 0; a < L.N; ++a) {
+    T.tnb_start[a] = (int)T.tnb_list.size();
+    for (int i = 0; i < L.N; ++i)
+      if (L.tz[i] == L.tz[a] && ((L.ll[i] + dpar / 2) & 1) == (L.ll[a] & 1) && tri(L.jj[i], L.jj[a], rank))
+        T.tnb_list.push_back(i);
+    T.tnb_count[a] = (int)T.tnb_list.size() - T.tnb_start[a];
+  }
+
   // cross-coupled tensor blocks of the particle-hole term
   for (int j3 = 0; j3 <= 2 * L.JM; j3 += 2)
     for (int j4 = std::max(std::abs(j3 - rank), j3); j4 <= j3 + rank; j4 += 2)
