@@ -22,6 +22,7 @@
 #include "dev.cuh"
 #include "engine.h"
 #include "kernels.h"
+#include "pair_groups.h"
 #include "tc.h"
 
 namespace imsrg {
@@ -490,15 +491,13 @@ struct TcState {
   const uint64_t* d_quads = nullptr;
   std::vector<SplitChunk> chunks;
   const SplitChunk* d_chunks = nullptr;
-  // commutator_122 neighbour lists, indexed by the global pair-list index
-  std::vector<int> nb_start;
-  std::vector<NbEntry> nb;
-  const int* d_nb_start = nullptr;
-  const NbEntry* d_nb = nullptr;
-  float* d_ft = nullptr;
-  float4* d_coef = nullptr;
-  std::vector<int4> u_chunks;  // 122 work: (array, first unique element, count, 0)
-  const int4* d_u_chunks = nullptr;
+  // commutator_122 by pair groups: sub-blocks of at most g122_small elements go one per warp,
+  // the larger ones one per CTA (tasks in channel order, so a channel's L and R stay in L2)
+  std::vector<int4> g122_warp, g122_cta;
+  PairGroupsDev g122_w{}, g122_c{};
+  int g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
+  std::vector<int> g_start, g_n, g_orb, g_b1, g_b2, g_blk_off;
+  float* g122_fb = nullptr;  // f(x, y) of L and R on every (l, j, tz) block
   int num_sms = 148;
 };
 
@@ -544,8 +543,7 @@ void Ctx::tc_release() {
   if (tc->zbuf) cudaFree(tc->zbuf);
   if (tc->ybuf) cudaFree(tc->ybuf);
   if (tc->d_err) cudaFree(tc->d_err);
-  if (tc->d_ft) cudaFree(tc->d_ft);
-  if (tc->d_coef) cudaFree(tc->d_coef);
+  if (tc->g122_fb) cudaFree(tc->g122_fb);
   delete tc;
   tc = nullptr;
 }
@@ -672,45 +670,22 @@ imsrg_status Ctx::tc_prepare(int mode) {
   tc->z_tiles = make_tiles(tc->z_probs);
   tc->total_tiles = tiles;
   if (l.JM + 1 > 26) return fail(IMSRG_ERR_UNSUPPORTED, "mixed recoupling supports 2j <= 25 (eMax <= 12)");
-  // ---- commutator_122 neighbour lists (one list per channel pair, a-side then b-side)
+  // ---- commutator_122 tasks: the group pairs G1 <= G2 of each channel
   {
-    const int N = l.N, NJ = l.NJ;
-    const int npairs = l.pair_off[l.nblocks * 3];
-    tc->nb_start.assign(npairs + 1, 0);
-    for (int q = 0; q < l.nblocks; ++q) {
-      const int J = l.lamJ[q];
-      for (int c = 0; c < 3; ++c)
-        for (int p = 0; p < l.ncls[q][c]; ++p) {
-          const int o = l.pair_off[q * 3 + c] + p;
-          const int a = l.pair_a[o], b = l.pair_b[o];
-          tc->nb_start[o] = (int)tc->nb.size();
-          for (int side = 0; side < 2; ++side) {
-            const int x = side == 0 ? a : b, other = side == 0 ? b : a;
-            for (int t = 0; t < l.same_count[x]; ++t) {
-              const int i = l.same_list[l.same_start[x] + t];
-              // replaced pair: side 0 -> (i, b), side 1 -> (a, i)
-              const int first = side == 0 ? i : other, second = side == 0 ? other : i;
-              const int u = std::min(first, second), v = std::max(first, second);
-              NbEntry e{};
-              e.pos = (int16_t)l.pairpos[((size_t)u * N + v) * NJ + J / 2];
-              e.cls = (int8_t)(l.con[u] + l.con[v]);
-              int flags = side;
-              if (first > second && ((1 + (l.jj[first] + l.jj[second] - J) / 2) & 1)) flags |= 2;
-              if (first == second) flags |= 4;
-              e.flags = (int8_t)flags;
-              e.fkey = (int16_t)(l.same_start[x] + t);
-              if (e.pos < 0) return fail(IMSRG_ERR_MISMATCH, "122 neighbour outside its channel");
-              tc->nb.push_back(e);
-            }
-          }
+    PairGroups pg;
+    build_pair_groups(pg, l);
+    tc->g_start = pg.spb_start; tc->g_n = pg.spb_n; tc->g_orb = pg.spb_orb;
+    tc->g_b1 = pg.grp_b1; tc->g_b2 = pg.grp_b2; tc->g_blk_off = pg.blk_off;
+    tc->g122_nspb = pg.nspb;
+    tc->g122_nblk2 = pg.nblk2;
+    tc->g122_nmax2 = pg.nmax * pg.nmax;
+    tc->g122_nmax4 = tc->g122_nmax2 * tc->g122_nmax2;
+    for (int q = 0; q < l.nblocks; ++q)
+      for (int G2 = pg.grp_first[q]; G2 < pg.grp_first[q + 1]; ++G2)
+        for (int G1 = pg.grp_first[q]; G1 <= G2; ++G1) {
+          const int4 t = make_int4(q, G1, G2, 0);
+          if (pg.elems(G1, G2) <= tc->g122_small) tc->g122_warp.push_back(t); else tc->g122_cta.push_back(t);
         }
-    }
-    tc->nb_start[npairs] = (int)tc->nb.size();
-    for (int k = 0; k < l.nblocks * 6; ++k) {
-      const int64_t n = l.uoff[k + 1] - l.uoff[k];
-      for (int64_t e0 = 0; e0 < n; e0 += 2048)
-        tc->u_chunks.push_back(make_int4(k, (int)e0, (int)std::min<int64_t>(2048, n - e0), 0));
-    }
   }
   // ---- recoupling quadruples: bra (i<=j) of class c1, ket (k<=l) of class c2, with
   //      c1 < c2, or c1 == c2 and (i,j) <= (k,l) (the unique stored elements), matching
@@ -750,8 +725,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   CK_TC(cuda(cudaMalloc(&tc->ybuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(Y)"));
   CK_TC(cuda(cudaMemset(tc->ybuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(Y)"));
   CK_TC(cuda(cudaMalloc(&tc->d_err, sizeof(int)), "cudaMalloc(err)"));
-  CK_TC(cuda(cudaMalloc(&tc->d_ft, sizeof(float) * 4 * std::max<size_t>(l.same_list.size(), 1)), "cudaMalloc(ft)"));
-  CK_TC(cuda(cudaMalloc(&tc->d_coef, sizeof(float4) * std::max<size_t>(tc->nb.size(), 1)), "cudaMalloc(coef)"));
+  CK_TC(cuda(cudaMalloc(&tc->g122_fb, sizeof(float) * 2 * std::max(tc->g122_nblk2, 1)), "cudaMalloc(122 blocks)"));
   CK_TC(cuda(cudaMemset(tc->d_err, 0, sizeof(int)), "memset(err)"));
   DevPacker pk;
   pk.add(tc->split_ops, &tc->d_split_ops);
@@ -770,12 +744,22 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->swap_row, &tc->d_swap_row);
   pk.add(tc->quads, &tc->d_quads);
   pk.add(tc->chunks, &tc->d_chunks);
-  pk.add(tc->nb_start, &tc->d_nb_start);
-  pk.add(tc->nb, &tc->d_nb);
-  pk.add(tc->u_chunks, &tc->d_u_chunks);
+  pk.add(tc->g_start, &tc->g122_w.spb_start);
+  pk.add(tc->g_n, &tc->g122_w.spb_n);
+  pk.add(tc->g_orb, &tc->g122_w.spb_orb);
+  pk.add(tc->g_b1, &tc->g122_w.grp_b1);
+  pk.add(tc->g_b2, &tc->g122_w.grp_b2);
+  pk.add(tc->g_blk_off, &tc->g122_w.blk_off);
+  pk.add(tc->g122_warp, &tc->g122_w.tasks);
+  pk.add(tc->g122_cta, &tc->g122_c.tasks);
   CK_TC(cuda(cudaMalloc(&tc->d_mem, pk.buf.size()), "cudaMalloc(tc tables)"));
   CK_TC(cuda(cudaMemcpy(tc->d_mem, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tc tables)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(tc->d_mem) + f.first;
+  {
+    const int4* ct = tc->g122_c.tasks;
+    tc->g122_c = tc->g122_w;
+    tc->g122_c.tasks = ct;
+  }
 
   // tensor map over the whole operand buffer: rows of 64 bf16 (128 bytes), box 64 x 128
   void* fn = nullptr;
@@ -875,14 +859,24 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   CK_TC(c121(Lp, hL, Rp, hR, RES, hRES));
   mark(kPhaseOneBody);
   if (L.n_unique) {
-    k_ft122<<<(L.N + 127) / 128, 128, 0, stream>>>(D, Lp, hL, Rp, hR, tc->d_ft);
-    CK_TC(launched("k_ft122"));
-    const int nnb = (int)tc->nb.size();
-    k_coef122<<<(nnb + 255) / 256, 256, 0, stream>>>(tc->d_nb, nnb, tc->d_ft, tc->d_coef);
-    CK_TC(launched("k_coef122"));
-    k_comm122_chunks<<<(int)tc->u_chunks.size(), 256, 0, stream>>>(D, tc->d_u_chunks, tc->d_nb_start, tc->d_nb,
-                                                                   tc->d_coef, Lp, hL, Rp, hR, RES);
-    CK_TC(launched("k_comm122_chunks"));
+    k_comm122_fblocks<<<tc->g122_nspb, 64, 0, stream>>>(D, tc->g122_w, tc->g122_nspb, tc->g122_nblk2, Lp, hL, Rp, hR,
+                                                         tc->g122_fb);
+    CK_TC(launched("k_comm122_fblocks"));
+    if (!tc->g122_warp.empty()) {
+      const int nt = (int)tc->g122_warp.size();
+      const int grid = std::min((nt + 7) / 8, tc->num_sms * 8);
+      const size_t smem = sizeof(float) * 8 * (size_t)(2 * tc->g122_small + 12 * tc->g122_nmax2);
+      k_comm122_groups_warp<<<grid, 256, smem, stream>>>(D, tc->g122_w, nt, tc->g122_small, tc->g122_nmax2, Lp, hL,
+                                                         Rp, hR, RES, hRES, tc->g122_fb, tc->g122_nblk2);
+      CK_TC(launched("k_comm122_groups_warp"));
+    }
+    if (!tc->g122_cta.empty()) {
+      const size_t smem = sizeof(float) * (size_t)(2 * tc->g122_nmax4 + 12 * tc->g122_nmax2);
+      k_comm122_groups_cta<<<(int)tc->g122_cta.size(), 256, smem, stream>>>(D, tc->g122_c, tc->g122_nmax4,
+                                                                             tc->g122_nmax2, Lp, hL, Rp, hR, RES, hRES,
+                                                                             tc->g122_fb, tc->g122_nblk2);
+      CK_TC(launched("k_comm122_groups_cta"));
+    }
   }
   mark(kPhase122);
   CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2, true));

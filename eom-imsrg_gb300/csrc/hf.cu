@@ -27,6 +27,7 @@
 
 #include "../../include/imsrg_gb300.h"
 #include "engine.h"
+#include "pair_groups.h"
 
 using namespace imsrg;
 
@@ -263,27 +264,19 @@ imsrg_status Ctx::hf_prepare() {
   HFState* S = new (std::nothrow) HFState();
   if (!S) return IMSRG_ERR_OUT_OF_MEMORY;
   hf = S;
-  const int N = L.N;
-  // blocks of orbits sharing (l, j, tz) in order of their first orbit
-  S->orb_spb.assign(N, -1);
-  S->orb_pos.assign(N, 0);
-  for (int i = 0; i < N; ++i) {
-    if (S->orb_spb[i] >= 0) continue;
-    const int B = S->nspb++;
-    S->spb_start.push_back((int)S->spb_orb.size());
-    S->spb_j.push_back(L.jj[i]);
-    int n = 0, holes = 0;
-    for (int k = i; k < N; ++k)
-      if (L.ll[k] == L.ll[i] && L.jj[k] == L.jj[i] && L.tz[k] == L.tz[i]) {
-        S->orb_spb[k] = B;
-        S->orb_pos[k] = n++;
-        S->spb_orb.push_back(k);
-        holes += L.con[k];
-      }
-    S->spb_n.push_back(n);
-    S->spb_hole.push_back(holes > 0);
-    S->nmax = std::max(S->nmax, n);
-  }
+  PairGroups PG;
+  build_pair_groups(PG, L);
+  S->nspb = PG.nspb;
+  S->nmax = PG.nmax;
+  S->spb_start = PG.spb_start;
+  S->spb_n = PG.spb_n;
+  S->spb_orb = PG.spb_orb;
+  S->spb_j = PG.spb_j;
+  S->spb_hole = PG.spb_hole;
+  S->orb_spb = PG.orb_spb;
+  S->orb_pos = PG.orb_pos;
+  S->grp_b1 = PG.grp_b1;
+  S->grp_b2 = PG.grp_b2;
   std::vector<int> mri, mrj, mcg, mch;
   for (int B = 0; B < S->nspb; ++B) {
     const int n = S->spb_n[B], s0 = S->spb_start[B];
@@ -308,24 +301,10 @@ imsrg_status Ctx::hf_prepare() {
       S->col_off.push_back(-1);
     }
   }
-  // pair groups of each channel: blocks (B1 <= B2) whose j's couple to J with the
-  // channel's parity and Tz; tasks are the group pairs G1 <= G2 of one channel
-  std::vector<int> grp_first(L.nblocks + 1, 0);
-  for (int q = 0; q < L.nblocks; ++q) {
-    grp_first[q] = (int)S->grp_b1.size();
-    const int J = L.lamJ[q], P = L.lamP[q], T = L.lamT[q];
-    for (int B1 = 0; B1 < S->nspb; ++B1)
-      for (int B2 = B1; B2 < S->nspb; ++B2) {
-        const int a = S->spb_orb[S->spb_start[B1]], b = S->spb_orb[S->spb_start[B2]];
-        if ((L.ll[a] + L.ll[b]) % 2 != P || L.tz[a] + L.tz[b] != 2 * T) continue;
-        if (J > L.jj[a] + L.jj[b] || J < std::abs(L.jj[a] - L.jj[b])) continue;
-        S->grp_b1.push_back(B1);
-        S->grp_b2.push_back(B2);
-      }
-    const int g0 = grp_first[q], g1 = (int)S->grp_b1.size();
-    for (int G2 = g0; G2 < g1; ++G2)
-      for (int G1 = g0; G1 <= G2; ++G1) S->tasks.push_back(make_int4(q, G1, G2, 0));
-  }
+  // tasks: the group pairs G1 <= G2 of each channel
+  for (int q = 0; q < L.nblocks; ++q)
+    for (int G2 = PG.grp_first[q]; G2 < PG.grp_first[q + 1]; ++G2)
+      for (int G1 = PG.grp_first[q]; G1 <= G2; ++G1) S->tasks.push_back(make_int4(q, G1, G2, 0));
   S->prefix = L.off_fph + (int64_t)L.P * L.A;
   // one device allocation for the integer tables
   std::vector<char> buf;

@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include "dev.cuh"
+#include "pair_groups.h"
 #include "gemm.h"
 #include "tc.h"
 
@@ -40,12 +41,13 @@ void launch_pandya_tc(int S, int grid, cudaStream_t stream, const DevLayout& D, 
                       __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s,
                       const int* nkb, const int* swap_row);
 __global__ void k_comm122f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
-__global__ void k_ft122(DevLayout D, const double* L, int hL, const double* R, int hR, float* ft);
-__global__ void k_comm122_nb(DevLayout D, const int* nb_start, const NbEntry* nb, const float* ft, const double* L,
-                             int hL, const double* R, int hR, double* RES, int hRES, int mirror);
-__global__ void k_coef122(const NbEntry* nb, int n, const float* ft, float4* coef);
-__global__ void k_comm122_chunks(DevLayout D, const int4* chunks, const int* nb_start, const NbEntry* nb,
-                                 const float4* coef, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_comm122_fblocks(DevLayout D, PairGroupsDev G, int nspb, int nblk2, const double* L, int hL,
+                                  const double* R, int hR, float* FB);
+__global__ void k_comm122_groups_warp(DevLayout D, PairGroupsDev G, int ntasks, int small, int nmax2, const double* L,
+                                      int hL, const double* R, int hR, double* RES, int hRES, const float* FB,
+                                      int nblk2);
+__global__ void k_comm122_groups_cta(DevLayout D, PairGroupsDev G, int nmax4, int nmax2, const double* L, int hL,
+                                     const double* R, int hR, double* RES, int hRES, const float* FB, int nblk2);
 __global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
                                 float pm);
 __global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);

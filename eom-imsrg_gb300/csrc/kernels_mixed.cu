@@ -5,6 +5,7 @@
 
 #include "dev.cuh"
 #include "kernels.h"
+#include "pair_groups.h"
 
 namespace imsrg {
 
@@ -153,186 +154,6 @@ __global__ void k_comm221f(DevLayout D, int pm, double* __restrict__ RES, int hR
       double* g = (kind == 0) ? RES + D.off_fhh + q + (int64_t)p * D.A : RES + D.off_fpp + q + (int64_t)p * D.P;
       *g = v * hRES;
     }
-  }
-}
-
-// One-body coefficients of commutator_122 for every (x, i) with i of the same (l,j,tz):
-// ft[4*key + 0..3] = fL(x,i), fR(x,i), fL(i,x), fR(i,x)
-__global__ void k_ft122(DevLayout D, const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
-                        float* __restrict__ ft) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= D.N) return;
-  const int s0 = D.same_start[x], n = D.same_count[x];
-  for (int t = 0; t < n; ++t) {
-    const int i = D.same_list[s0 + t];
-    float* o = ft + 4 * (s0 + t);
-    o[0] = d_f_elem_f(D, L, hL, x, i);
-    o[1] = d_f_elem_f(D, R, hR, x, i);
-    o[2] = d_f_elem_f(D, L, hL, i, x);
-    o[3] = d_f_elem_f(D, R, hR, i, x);
-  }
-}
-
-// Per-call coefficients of the 122 neighbour entries: the one-body element times the
-// entry's swap phase / sqrt(2): (bra fL, bra fR, ket fL, ket fR)
-__global__ void k_coef122(const NbEntry* __restrict__ nb, int n, const float* __restrict__ ft,
-                          float4* __restrict__ coef) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  const NbEntry x = nb[e];
-  float s = (x.flags & 4) ? 1.41421356f : 1.0f;
-  if (x.flags & 2) s = -s;
-  const float4 f = *reinterpret_cast<const float4*>(ft + 4 * x.fkey);
-  coef[e] = make_float4(f.x * s, f.y * s, -f.z * s, -f.w * s);
-}
-
-// commutator_122 over a chunk list (one block = a run of unique elements of one array,
-// no search), with premultiplied neighbour coefficients.  FP32, ASSIGNS, upper triangle.
-__global__ void __launch_bounds__(256) k_comm122_chunks(DevLayout D, const int4* __restrict__ chunks,
-                                                        const int* __restrict__ nb_start,
-                                                        const NbEntry* __restrict__ nb, const float4* __restrict__ coef,
-                                                        const double* __restrict__ L, int hL,
-                                                        const double* __restrict__ R, int hR,
-                                                        double* __restrict__ RES) {
-  const int4 ch = chunks[blockIdx.x];  // (array k, first local element, count, 0)
-  const int k = ch.x;
-  const int q = k / 6, g = k - q * 6;
-  const bool square = (g == 0 || g == 3 || g == 4);
-  const int c1 = (g < 3) ? 0 : (g == 4 ? 2 : 1);
-  const int c2 = (g == 0) ? 0 : ((g == 1 || g == 3) ? 1 : 2);
-  const int n1 = D.gn1[k];
-  const int64_t* go = D.goff + q * 6;
-  const int* gn = D.gn1 + q * 6;
-  const int po1 = D.pair_off[q * 3 + c1], po2 = D.pair_off[q * 3 + c2];
-  const bool hLn = hL < 0, hRn = hR < 0;
-  for (int t = threadIdx.x; t < ch.z; t += blockDim.x) {
-    const int64_t e = (int64_t)ch.y + t;
-    int IX, JX;
-    if (square) {
-      int j = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
-      while ((int64_t)(j + 1) * (j + 2) / 2 <= e) ++j;
-      while ((int64_t)j * (j + 1) / 2 > e) --j;
-      JX = j;
-      IX = (int)(e - (int64_t)j * (j + 1) / 2);
-    } else {
-      JX = (int)(e / n1);
-      IX = (int)(e - (int64_t)JX * n1);
-    }
-    const int o1 = po1 + IX, o2 = po2 + JX;
-    float bra = 0.0f, ket = 0.0f;
-    for (int x = nb_start[o1], xe = nb_start[o1 + 1]; x < xe; ++x) {
-      const NbEntry n = nb[x];
-      const float4 cf = coef[x];
-      const int ct = n.cls;
-      int64_t idx;
-      bool tr;
-      if (ct <= c2) {
-        const int gg = (ct == 0) ? c2 : (ct == 1 ? (c2 == 1 ? 3 : 5) : 4);
-        idx = go[gg] + n.pos + (int64_t)JX * gn[gg];
-        tr = false;
-      } else {
-        const int gg = (c2 == 0) ? ct : (c2 == 1 ? (ct == 1 ? 3 : 5) : 4);
-        idx = go[gg] + JX + (int64_t)n.pos * gn[gg];
-        tr = true;
-      }
-      float vR = f64_to_f32(R[idx]), vL = f64_to_f32(L[idx]);
-      if (tr && hRn) vR = -vR;
-      if (tr && hLn) vL = -vL;
-      bra += cf.x * vR - cf.y * vL;
-    }
-    for (int x = nb_start[o2], xe = nb_start[o2 + 1]; x < xe; ++x) {
-      const NbEntry n = nb[x];
-      const float4 cf = coef[x];
-      const int ct = n.cls;
-      int64_t idx;
-      bool tr;
-      if (c1 <= ct) {
-        const int gg = (c1 == 0) ? ct : (c1 == 1 ? (ct == 1 ? 3 : 5) : 4);
-        idx = go[gg] + IX + (int64_t)n.pos * gn[gg];
-        tr = false;
-      } else {
-        const int gg = (ct == 0) ? c1 : (ct == 1 ? (c1 == 1 ? 3 : 5) : 4);
-        idx = go[gg] + n.pos + (int64_t)IX * gn[gg];
-        tr = true;
-      }
-      float vR = f64_to_f32(R[idx]), vL = f64_to_f32(L[idx]);
-      if (tr && hRn) vR = -vR;
-      if (tr && hLn) vL = -vL;
-      ket += cf.z * vR - cf.w * vL;
-    }
-    const int a = D.pair_a[o1], b = D.pair_b[o1], c = D.pair_a[o2], d = D.pair_b[o2];
-    const float sm = bra * ((a == b) ? 0.70710678f : 1.0f) + ket * ((c == d) ? 0.70710678f : 1.0f);
-    RES[D.goff[k] + IX + (int64_t)JX * n1] = f32_to_f64(sm);
-  }
-}
-
-// commutator_122 (src/commutators.f90:283-396) with precomputed neighbour lists:
-// bra neighbours of pair IX give the a- and b-replaced terms, ket neighbours of pair JX
-// the c- and d-replaced terms.  FP32 arithmetic, ASSIGNS every 2b element.
-__global__ void k_comm122_nb(DevLayout D, const int* __restrict__ nb_start, const NbEntry* __restrict__ nb,
-                             const float* __restrict__ ft, const double* __restrict__ L, int hL,
-                             const double* __restrict__ R, int hR, double* __restrict__ RES, int hRES, int mirror) {
-  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < D.n_unique; u += (int64_t)gridDim.x * blockDim.x) {
-    int q, g, IX, JX;
-    d_unique_decode(D, u, q, g, IX, JX);
-    const int c1 = (g < 3) ? 0 : (g == 4 ? 2 : 1);
-    const int c2 = (g == 0) ? 0 : ((g == 1 || g == 3) ? 1 : 2);
-    const int o1 = D.pair_off[q * 3 + c1] + IX, o2 = D.pair_off[q * 3 + c2] + JX;
-    const int a = D.pair_a[o1], b = D.pair_b[o1], c = D.pair_a[o2], d = D.pair_b[o2];
-    const int64_t* go = D.goff + q * 6;
-    const int* gn = D.gn1 + q * 6;
-    float bra = 0.0f, ket = 0.0f;
-    // bra side: sum_i f(x,i) V(target, cd)
-    for (int e = nb_start[o1]; e < nb_start[o1 + 1]; ++e) {
-      const NbEntry n = nb[e];
-      const int ct = n.cls;
-      int64_t idx;
-      bool tr;
-      if (ct <= c2) {
-        const int gg = (ct == 0) ? c2 : (ct == 1 ? (c2 == 1 ? 3 : 5) : 4);
-        idx = go[gg] + n.pos + (int64_t)JX * gn[gg];
-        tr = false;
-      } else {
-        const int gg = (c2 == 0) ? ct : (c2 == 1 ? (ct == 1 ? 3 : 5) : 4);
-        idx = go[gg] + JX + (int64_t)n.pos * gn[gg];
-        tr = true;
-      }
-      float s = (n.flags & 4) ? 1.41421356f : 1.0f;
-      if (n.flags & 2) s = -s;
-      const float vR = f64_to_f32(R[idx]) * ((tr && hR < 0) ? -s : s);
-      const float vL = f64_to_f32(L[idx]) * ((tr && hL < 0) ? -s : s);
-      const float4 f = *reinterpret_cast<const float4*>(ft + 4 * n.fkey);
-      bra += f.x * vR - f.y * vL;
-    }
-    // ket side: sum_i -f(i,x) V(ab, target)
-    for (int e = nb_start[o2]; e < nb_start[o2 + 1]; ++e) {
-      const NbEntry n = nb[e];
-      const int ct = n.cls;
-      int64_t idx;
-      bool tr;
-      if (c1 <= ct) {
-        const int gg = (c1 == 0) ? ct : (c1 == 1 ? (ct == 1 ? 3 : 5) : 4);
-        idx = go[gg] + IX + (int64_t)n.pos * gn[gg];
-        tr = false;
-      } else {
-        const int gg = (ct == 0) ? c1 : (ct == 1 ? (c1 == 1 ? 3 : 5) : 4);
-        idx = go[gg] + n.pos + (int64_t)IX * gn[gg];
-        tr = true;
-      }
-      float s = (n.flags & 4) ? 1.41421356f : 1.0f;
-      if (n.flags & 2) s = -s;
-      const float vR = f64_to_f32(R[idx]) * ((tr && hR < 0) ? -s : s);
-      const float vL = f64_to_f32(L[idx]) * ((tr && hL < 0) ? -s : s);
-      const float4 f = *reinterpret_cast<const float4*>(ft + 4 * n.fkey);
-      ket += -f.z * vR + f.w * vL;
-    }
-    // v_elem carries sqrt(2) for the untouched identical pair; 122 divides by both
-    const float sm = bra * ((a == b) ? 0.70710678f : 1.0f) + ket * ((c == d) ? 0.70710678f : 1.0f);
-    const int k = q * 6 + g;
-    double* X = RES + D.goff[k];
-    const int n1 = D.gn1[k];
-    X[IX + (int64_t)JX * n1] = f32_to_f64(sm);
-    if (mirror && (g == 0 || g == 3 || g == 4)) X[JX + (int64_t)IX * n1] = f32_to_f64(hRES < 0 ? -sm : sm);
   }
 }
 
@@ -638,6 +459,199 @@ __global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t*
       *X = f32_to_f64(f64_to_f32(*X) + sm);
     }
   }
+}
+
+
+// ---------------------------------------------------------------- commutator_122 by pair groups
+// commutator_122 (src/commutators.f90:283-396) of one group-pair sub-block (G1 <= G2) of
+// channel q, FP32.  In the ordered-pair form X_A(ab,cd) (what v_elem returns) the one-body
+// factors act on one index at a time:
+//   OUT[a,b,c,d] = sum_a' fL(a,a') R_A[a',b,c,d] - fR(a,a') L_A[a',b,c,d]   (and b)
+//                - sum_c' fL(c',c) R_A[a,b,c',d] - fR(c',c) L_A[a,b,c',d]   (and d)
+// with a' etc. running over the orbits of the same (l, j, tz) block.  Each element of L and
+// R is gathered once per sub-block (the neighbour-list form gathers every neighbour of
+// every output), the result is written to the stored pairs with the exchange phase and
+// 1/sqrt(2) for identical orbits, and for G1 != G2 also mirrored with hRES.  ASSIGNS.
+namespace {
+template <bool kWarp>
+__device__ __forceinline__ void g122_sync() {
+  if (kWarp) __syncwarp(); else __syncthreads();
+}
+
+// floor(e / n) for 0 <= e, e (n - 1) < 2^32, with m = ceil(2^32 / n)
+__device__ __forceinline__ int g122_div(int e, unsigned long long m) {
+  return (int)(((unsigned long long)e * m) >> 32);
+}
+__device__ __forceinline__ unsigned long long g122_magic(int n) {
+  return ((1ull << 32) + (unsigned long long)n - 1) / (unsigned long long)n;
+}
+
+// Shared-memory slice of one task: XL / XR, the ordered four-index sub-blocks of L and R
+// (element x0 + n0 (x1 + n1 (x2 + n2 x3))); M, the signed one-body factors
+// M[(op*4 + axis)*nmax2 + i*n + a] (op 0: f of L, 1: f of R), copied from FB (the f(x, y)
+// matrices of every block, FB[blk_off[B] + x*n + y] for L and FB[nblk2 + ...] for R);
+// PB / PK, the stored position of every bra pair (x0, x1) and ket pair (x2, x3):
+// (index in its class list << 2 | class) and the factor pre with V_A = pre x stored
+// (sqrt 2 for identical orbits, the exchange phase when the stored order is swapped).
+struct G122Smem {
+  float *XL, *XR, *M;
+  int *PB, *PK;
+  float *FBp, *FKp;
+};
+
+template <bool kWarp>
+__device__ __forceinline__ void g122_task(const DevLayout& D, const PairGroupsDev& G, int4 t,
+                                          const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
+                                          double* __restrict__ RES, int hRES, const float* __restrict__ FB,
+                                          int nblk2, const G122Smem& S, int nmax2, int tid, int nth) {
+  const int q = t.x, G1 = t.y, G2 = t.z;
+  const int b0 = G.grp_b1[G1], b1 = G.grp_b2[G1], b2 = G.grp_b1[G2], b3 = G.grp_b2[G2];
+  const int n0 = G.spb_n[b0], n1 = G.spb_n[b1], n2 = G.spb_n[b2], n3 = G.spb_n[b3];
+  const int* o0 = G.spb_orb + G.spb_start[b0];
+  const int* o1 = G.spb_orb + G.spb_start[b1];
+  const int* o2 = G.spb_orb + G.spb_start[b2];
+  const int* o3 = G.spb_orb + G.spb_start[b3];
+  const int J = D.lamJ[q];
+  const int nb = n0 * n1, nk = n2 * n3, ntot = nb * nk;
+  const unsigned long long m0 = g122_magic(n0), m2 = g122_magic(n2), mb = g122_magic(nb);
+  float* M = S.M;
+  for (int x = tid; x < 4 * nmax2; x += nth) {  // signed block matrices from FB
+    const int ax = x / nmax2, r = x - ax * nmax2;
+    const int n = ax == 0 ? n0 : (ax == 1 ? n1 : (ax == 2 ? n2 : n3));
+    if (r >= n * n) continue;
+    const int blk = ax == 0 ? b0 : (ax == 1 ? b1 : (ax == 2 ? b2 : b3));
+    const int i = r / n, a = r - (r / n) * n;
+    const int src = G.blk_off[blk] + (ax < 2 ? i * n + a : a * n + i);
+    M[ax * nmax2 + r] = ax < 2 ? FB[src] : -FB[src];
+    M[(4 + ax) * nmax2 + r] = ax < 2 ? FB[nblk2 + src] : -FB[nblk2 + src];
+  }
+  const int NJ = D.NJ, N = D.N, Jh = J >> 1;
+  for (int x = tid; x < nb + nk; x += nth) {  // stored positions of the bra and ket pairs
+    const bool bra = x < nb;
+    const int y = bra ? x : x - nb;
+    const int na = bra ? n0 : n2;
+    const int xa = y % na, xb = y / na;
+    const int oa = bra ? o0[xa] : o2[xa], ob = bra ? o1[xb] : o3[xb];
+    const int lo = min(oa, ob), hi = max(oa, ob);
+    float pre = 1.0f;
+    if (oa == ob) pre = 1.41421356f;
+    else if (oa > ob && ((1 + ((D.jj[oa] + D.jj[ob] - J) >> 1)) & 1)) pre = -1.0f;
+    const int code = (D.pairpos[(lo * N + hi) * NJ + Jh] << 2) | (D.con[lo] + D.con[hi]);
+    if (bra) { S.PB[y] = code; S.FBp[y] = pre; } else { S.PK[y] = code; S.FKp[y] = pre; }
+  }
+  g122_sync<kWarp>();
+  const int64_t* go = D.goff + q * 6;
+  const int* gn = D.gn1 + q * 6;
+  for (int e = tid; e < ntot; e += nth) {  // gather V_A of L and R
+    const int ek = g122_div(e, mb), eb = e - ek * nb;
+    const int cb = S.PB[eb], ck = S.PK[ek];
+    const int C1 = cb & 3, C2 = ck & 3;
+    const int lo = min(C1, C2), hi = max(C1, C2);
+    const int g = (lo == 0) ? hi : (lo == 1 ? (hi == 1 ? 3 : 5) : 4);
+    const int64_t idx = C1 <= C2 ? go[g] + (cb >> 2) + (int64_t)(ck >> 2) * gn[g]
+                                 : go[g] + (ck >> 2) + (int64_t)(cb >> 2) * gn[g];
+    const float pre = S.FBp[eb] * S.FKp[ek];
+    const float sl = (C1 > C2 && hL < 0) ? -pre : pre, sr = (C1 > C2 && hR < 0) ? -pre : pre;
+    S.XL[e] = f64_to_f32(L[idx]) * sl;
+    S.XR[e] = f64_to_f32(R[idx]) * sr;
+  }
+  g122_sync<kWarp>();
+  const int s1 = n0, s2 = nb, s3 = nb * n2;
+  const float* XL = S.XL;
+  const float* XR = S.XR;
+  for (int e = tid; e < ntot; e += nth) {
+    const int ek = g122_div(e, mb), eb = e - ek * nb;
+    const int x1 = g122_div(eb, m0), x0 = eb - x1 * n0;
+    const int x3 = g122_div(ek, m2), x2 = ek - x3 * n2;
+    if ((b0 == b1 && x0 > x1) || (b2 == b3 && x2 > x3)) continue;  // the other order is stored
+    float out = 0.0f;
+    {
+      const float* mL = M + x0 * n0;
+      const float* mR = M + 4 * nmax2 + x0 * n0;
+      const int base = e - x0;
+      for (int a = 0; a < n0; ++a) out += mL[a] * XR[base + a] - mR[a] * XL[base + a];
+    }
+    {
+      const float* mL = M + nmax2 + x1 * n1;
+      const float* mR = M + 5 * nmax2 + x1 * n1;
+      const int base = e - x1 * s1;
+      for (int a = 0; a < n1; ++a) out += mL[a] * XR[base + a * s1] - mR[a] * XL[base + a * s1];
+    }
+    {
+      const float* mL = M + 2 * nmax2 + x2 * n2;
+      const float* mR = M + 6 * nmax2 + x2 * n2;
+      const int base = e - x2 * s2;
+      for (int a = 0; a < n2; ++a) out += mL[a] * XR[base + a * s2] - mR[a] * XL[base + a * s2];
+    }
+    {
+      const float* mL = M + 3 * nmax2 + x3 * n3;
+      const float* mR = M + 7 * nmax2 + x3 * n3;
+      const int base = e - x3 * s3;
+      for (int a = 0; a < n3; ++a) out += mL[a] * XR[base + a * s3] - mR[a] * XL[base + a * s3];
+    }
+    const int cb = S.PB[eb], ck = S.PK[ek];
+    const int C1 = cb & 3, C2 = ck & 3;
+    const float w = out / (S.FBp[eb] * S.FKp[ek]);  // stored = V_A / pre
+    const int lo = min(C1, C2), hi = max(C1, C2);
+    const int g = (lo == 0) ? hi : (lo == 1 ? (hi == 1 ? 3 : 5) : 4);
+    if (C1 <= C2) RES[go[g] + (cb >> 2) + (int64_t)(ck >> 2) * gn[g]] = f32_to_f64(w);
+    if (G1 != G2 && C2 <= C1) RES[go[g] + (ck >> 2) + (int64_t)(cb >> 2) * gn[g]] = f32_to_f64(hRES < 0 ? -w : w);
+  }
+  g122_sync<kWarp>();
+}
+}  // namespace
+
+// FB: f(x, y) of L (first nblk2 entries) and of R for the orbits x, y of every block
+__global__ void k_comm122_fblocks(DevLayout D, PairGroupsDev G, int nspb, int nblk2, const double* __restrict__ L,
+                                  int hL, const double* __restrict__ R, int hR, float* __restrict__ FB) {
+  const int B = blockIdx.x;
+  if (B >= nspb) return;
+  const int n = G.spb_n[B];
+  const int* o = G.spb_orb + G.spb_start[B];
+  for (int r = threadIdx.x; r < n * n; r += blockDim.x) {
+    const int x = r / n, y = r - (r / n) * n;
+    FB[G.blk_off[B] + r] = d_f_elem_f(D, L, hL, o[x], o[y]);
+    FB[nblk2 + G.blk_off[B] + r] = d_f_elem_f(D, R, hR, o[x], o[y]);
+  }
+}
+
+// one warp per task (sub-blocks of at most `small` elements); 8 warps per CTA, each with
+// its own shared-memory slice [XL small | XR small | M 8 nmax2 | PB, PK, FBp, FKp nmax2 each]
+__global__ void __launch_bounds__(256) k_comm122_groups_warp(DevLayout D, PairGroupsDev G, int ntasks, int small,
+                                                             int nmax2, const double* __restrict__ L, int hL,
+                                                             const double* __restrict__ R, int hR,
+                                                             double* __restrict__ RES, int hRES,
+                                                             const float* __restrict__ FB, int nblk2) {
+  extern __shared__ float g122_sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  G122Smem S;
+  S.XL = g122_sm + (size_t)warp * (2 * small + 12 * nmax2);
+  S.XR = S.XL + small;
+  S.M = S.XR + small;
+  S.PB = reinterpret_cast<int*>(S.M + 8 * nmax2);
+  S.PK = S.PB + nmax2;
+  S.FBp = reinterpret_cast<float*>(S.PK + nmax2);
+  S.FKp = S.FBp + nmax2;
+  for (int t = blockIdx.x * 8 + warp; t < ntasks; t += gridDim.x * 8)
+    g122_task<true>(D, G, G.tasks[t], L, hL, R, hR, RES, hRES, FB, nblk2, S, nmax2, lane, 32);
+}
+
+// one CTA per task (the larger sub-blocks): [XL nmax4 | XR nmax4 | M 8 nmax2 | PB, PK, FBp, FKp]
+__global__ void __launch_bounds__(256) k_comm122_groups_cta(DevLayout D, PairGroupsDev G, int nmax4, int nmax2,
+                                                            const double* __restrict__ L, int hL,
+                                                            const double* __restrict__ R, int hR,
+                                                            double* __restrict__ RES, int hRES,
+                                                            const float* __restrict__ FB, int nblk2) {
+  extern __shared__ float g122_sm[];
+  G122Smem S;
+  S.XL = g122_sm;
+  S.XR = S.XL + nmax4;
+  S.M = S.XR + nmax4;
+  S.PB = reinterpret_cast<int*>(S.M + 8 * nmax2);
+  S.PK = S.PB + nmax2;
+  S.FBp = reinterpret_cast<float*>(S.PK + nmax2);
+  S.FKp = S.FBp + nmax2;
+  g122_task<false>(D, G, G.tasks[blockIdx.x], L, hL, R, hR, RES, hRES, FB, nblk2, S, nmax2, threadIdx.x, blockDim.x);
 }
 
 }  // namespace imsrg

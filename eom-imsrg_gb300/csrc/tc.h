@@ -32,16 +32,6 @@ struct TcTile {
   int prob, m0, n0, pad;
 };
 
-// one neighbour of a stored pair (a<=b) in its channel: the pair with a (side 0) or b
-// (side 1) replaced by an orbit i of the same (l, j, tz), for commutator_122
-struct NbEntry {
-  int16_t pos;    // position of the stored pair (min, max) in its class list
-  int8_t cls;     // its class: 0 pp, 1 ph, 2 hh
-  int8_t flags;   // bit 0 side, bit 1 negative phase, bit 2 identical orbits (sqrt 2)
-  int16_t fkey;   // same_start[x] + index of i in same(x): x = a (side 0) or b (side 1)
-  int16_t pad;
-};
-
 // split chunk: a contiguous run of rows of one split operand
 struct SplitChunk {
   int op;
