@@ -493,9 +493,10 @@ struct TcState {
   const SplitChunk* d_chunks = nullptr;
   // commutator_122 by pair groups: sub-blocks of at most g122_small elements go one per warp,
   // the larger ones one per CTA (tasks in channel order, so a channel's L and R stay in L2)
-  std::vector<int4> g122_warp, g122_cta;
-  PairGroupsDev g122_w{}, g122_c{};
-  int g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
+  // (tiny sub-blocks, up to g122_tiny elements, go to 8-lane groups, four per warp)
+  std::vector<int4> g122_tiny, g122_warp, g122_cta;
+  PairGroupsDev g122_t{}, g122_w{}, g122_c{};
+  int g122_tiny_cap = 64, g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
   std::vector<int> g_start, g_n, g_orb, g_b1, g_b2, g_blk_off;
   float* g122_fb = nullptr;  // f(x, y) of L and R on every (l, j, tz) block
   int num_sms = 148;
@@ -684,7 +685,10 @@ imsrg_status Ctx::tc_prepare(int mode) {
       for (int G2 = pg.grp_first[q]; G2 < pg.grp_first[q + 1]; ++G2)
         for (int G1 = pg.grp_first[q]; G1 <= G2; ++G1) {
           const int4 t = make_int4(q, G1, G2, 0);
-          if (pg.elems(G1, G2) <= tc->g122_small) tc->g122_warp.push_back(t); else tc->g122_cta.push_back(t);
+          const int64_t ne = pg.elems(G1, G2);
+          if (ne <= tc->g122_tiny_cap) tc->g122_tiny.push_back(t);
+          else if (ne <= tc->g122_small) tc->g122_warp.push_back(t);
+          else tc->g122_cta.push_back(t);
         }
   }
   // ---- recoupling quadruples: bra (i<=j) of class c1, ket (k<=l) of class c2, with
@@ -750,6 +754,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->g_b1, &tc->g122_w.grp_b1);
   pk.add(tc->g_b2, &tc->g122_w.grp_b2);
   pk.add(tc->g_blk_off, &tc->g122_w.blk_off);
+  pk.add(tc->g122_tiny, &tc->g122_t.tasks);
   pk.add(tc->g122_warp, &tc->g122_w.tasks);
   pk.add(tc->g122_cta, &tc->g122_c.tasks);
   CK_TC(cuda(cudaMalloc(&tc->d_mem, pk.buf.size()), "cudaMalloc(tc tables)"));
@@ -757,8 +762,11 @@ imsrg_status Ctx::tc_prepare(int mode) {
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(tc->d_mem) + f.first;
   {
     const int4* ct = tc->g122_c.tasks;
+    const int4* tt = tc->g122_t.tasks;
     tc->g122_c = tc->g122_w;
     tc->g122_c.tasks = ct;
+    tc->g122_t = tc->g122_w;
+    tc->g122_t.tasks = tt;
   }
 
   // tensor map over the whole operand buffer: rows of 64 bf16 (128 bytes), box 64 x 128
@@ -862,16 +870,24 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     k_comm122_fblocks<<<tc->g122_nspb, 64, 0, stream>>>(D, tc->g122_w, tc->g122_nspb, tc->g122_nblk2, Lp, hL, Rp, hR,
                                                          tc->g122_fb);
     CK_TC(launched("k_comm122_fblocks"));
-    if (!tc->g122_warp.empty()) {
+    if (!tc->g122_tiny.empty()) {  // 8 lanes per task, 32 tasks per CTA
+      const int nt = (int)tc->g122_tiny.size();
+      const int grid = std::min((nt + 31) / 32, tc->num_sms * 8);
+      const size_t smem = sizeof(float) * 32 * (size_t)(2 * tc->g122_tiny_cap + 4 * tc->g122_nmax2);
+      launch_comm122_lanes(8, grid, smem, stream, D, tc->g122_t, nt, tc->g122_tiny_cap, tc->g122_nmax2, Lp, hL, Rp, hR,
+                           RES, hRES, tc->g122_fb, tc->g122_nblk2);
+      CK_TC(launched("k_comm122_groups_lanes<8>"));
+    }
+    if (!tc->g122_warp.empty()) {  // a warp per task, 8 tasks per CTA
       const int nt = (int)tc->g122_warp.size();
       const int grid = std::min((nt + 7) / 8, tc->num_sms * 8);
-      const size_t smem = sizeof(float) * 8 * (size_t)(2 * tc->g122_small + 12 * tc->g122_nmax2);
-      k_comm122_groups_warp<<<grid, 256, smem, stream>>>(D, tc->g122_w, nt, tc->g122_small, tc->g122_nmax2, Lp, hL,
-                                                         Rp, hR, RES, hRES, tc->g122_fb, tc->g122_nblk2);
-      CK_TC(launched("k_comm122_groups_warp"));
+      const size_t smem = sizeof(float) * 8 * (size_t)(2 * tc->g122_small + 4 * tc->g122_nmax2);
+      launch_comm122_lanes(32, grid, smem, stream, D, tc->g122_w, nt, tc->g122_small, tc->g122_nmax2, Lp, hL, Rp, hR,
+                           RES, hRES, tc->g122_fb, tc->g122_nblk2);
+      CK_TC(launched("k_comm122_groups_lanes<32>"));
     }
     if (!tc->g122_cta.empty()) {
-      const size_t smem = sizeof(float) * (size_t)(2 * tc->g122_nmax4 + 12 * tc->g122_nmax2);
+      const size_t smem = sizeof(float) * (size_t)(2 * tc->g122_nmax4 + 4 * tc->g122_nmax2);
       k_comm122_groups_cta<<<(int)tc->g122_cta.size(), 256, smem, stream>>>(D, tc->g122_c, tc->g122_nmax4,
                                                                              tc->g122_nmax2, Lp, hL, Rp, hR, RES, hRES,
                                                                              tc->g122_fb, tc->g122_nblk2);

@@ -473,11 +473,6 @@ __global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t*
 // every output), the result is written to the stored pairs with the exchange phase and
 // 1/sqrt(2) for identical orbits, and for G1 != G2 also mirrored with hRES.  ASSIGNS.
 namespace {
-template <bool kWarp>
-__device__ __forceinline__ void g122_sync() {
-  if (kWarp) __syncwarp(); else __syncthreads();
-}
-
 // floor(e / n) for 0 <= e, e (n - 1) < 2^32, with m = ceil(2^32 / n)
 __device__ __forceinline__ int g122_div(int e, unsigned long long m) {
   return (int)(((unsigned long long)e * m) >> 32);
@@ -487,23 +482,24 @@ __device__ __forceinline__ unsigned long long g122_magic(int n) {
 }
 
 // Shared-memory slice of one task: XL / XR, the ordered four-index sub-blocks of L and R
-// (element x0 + n0 (x1 + n1 (x2 + n2 x3))); M, the signed one-body factors
-// M[(op*4 + axis)*nmax2 + i*n + a] (op 0: f of L, 1: f of R), copied from FB (the f(x, y)
-// matrices of every block, FB[blk_off[B] + x*n + y] for L and FB[nblk2 + ...] for R);
-// PB / PK, the stored position of every bra pair (x0, x1) and ket pair (x2, x3):
-// (index in its class list << 2 | class) and the factor pre with V_A = pre x stored
-// (sqrt 2 for identical orbits, the exchange phase when the stored order is swapped).
+// (element x0 + n0 (x1 + n1 (x2 + n2 x3))); PB / PK, the stored position of every bra pair
+// (x0, x1) and ket pair (x2, x3): (index in its class list << 2 | class), with FBp / FKp the
+// factor pre of V_A = pre x stored (sqrt 2 for identical orbits, the exchange phase when the
+// stored order is swapped).
 struct G122Smem {
-  float *XL, *XR, *M;
+  float *XL, *XR;
   int *PB, *PK;
   float *FBp, *FKp;
 };
 
-template <bool kWarp>
+// kLanes lanes of a warp per task (mask: those lanes), or the whole CTA (kLanes == 0).
+// FB: f(x, y) of L (first nblk2 entries) and of R for the orbits x, y of every block,
+// FB[blk_off[B] + x*n + y].
+template <int kLanes>
 __device__ __forceinline__ void g122_task(const DevLayout& D, const PairGroupsDev& G, int4 t,
                                           const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
-                                          double* __restrict__ RES, int hRES, const float* __restrict__ FB,
-                                          int nblk2, const G122Smem& S, int nmax2, int tid, int nth) {
+                                          double* __restrict__ RES, int hRES, const float* __restrict__ FB, int nblk2,
+                                          const G122Smem& S, int tid, int nth, unsigned mask) {
   const int q = t.x, G1 = t.y, G2 = t.z;
   const int b0 = G.grp_b1[G1], b1 = G.grp_b2[G1], b2 = G.grp_b1[G2], b3 = G.grp_b2[G2];
   const int n0 = G.spb_n[b0], n1 = G.spb_n[b1], n2 = G.spb_n[b2], n3 = G.spb_n[b3];
@@ -514,17 +510,6 @@ __device__ __forceinline__ void g122_task(const DevLayout& D, const PairGroupsDe
   const int J = D.lamJ[q];
   const int nb = n0 * n1, nk = n2 * n3, ntot = nb * nk;
   const unsigned long long m0 = g122_magic(n0), m2 = g122_magic(n2), mb = g122_magic(nb);
-  float* M = S.M;
-  for (int x = tid; x < 4 * nmax2; x += nth) {  // signed block matrices from FB
-    const int ax = x / nmax2, r = x - ax * nmax2;
-    const int n = ax == 0 ? n0 : (ax == 1 ? n1 : (ax == 2 ? n2 : n3));
-    if (r >= n * n) continue;
-    const int blk = ax == 0 ? b0 : (ax == 1 ? b1 : (ax == 2 ? b2 : b3));
-    const int i = r / n, a = r - (r / n) * n;
-    const int src = G.blk_off[blk] + (ax < 2 ? i * n + a : a * n + i);
-    M[ax * nmax2 + r] = ax < 2 ? FB[src] : -FB[src];
-    M[(4 + ax) * nmax2 + r] = ax < 2 ? FB[nblk2 + src] : -FB[nblk2 + src];
-  }
   const int NJ = D.NJ, N = D.N, Jh = J >> 1;
   for (int x = tid; x < nb + nk; x += nth) {  // stored positions of the bra and ket pairs
     const bool bra = x < nb;
@@ -539,7 +524,7 @@ __device__ __forceinline__ void g122_task(const DevLayout& D, const PairGroupsDe
     const int code = (D.pairpos[(lo * N + hi) * NJ + Jh] << 2) | (D.con[lo] + D.con[hi]);
     if (bra) { S.PB[y] = code; S.FBp[y] = pre; } else { S.PK[y] = code; S.FKp[y] = pre; }
   }
-  g122_sync<kWarp>();
+  if (kLanes) __syncwarp(mask); else __syncthreads();
   const int64_t* go = D.goff + q * 6;
   const int* gn = D.gn1 + q * 6;
   for (int e = tid; e < ntot; e += nth) {  // gather V_A of L and R
@@ -555,39 +540,42 @@ __device__ __forceinline__ void g122_task(const DevLayout& D, const PairGroupsDe
     S.XL[e] = f64_to_f32(L[idx]) * sl;
     S.XR[e] = f64_to_f32(R[idx]) * sr;
   }
-  g122_sync<kWarp>();
+  if (kLanes) __syncwarp(mask); else __syncthreads();
   const int s1 = n0, s2 = nb, s3 = nb * n2;
   const float* XL = S.XL;
   const float* XR = S.XR;
+  const float* FL0 = FB + G.blk_off[b0];
+  const float* FL1 = FB + G.blk_off[b1];
+  const float* FL2 = FB + G.blk_off[b2];
+  const float* FL3 = FB + G.blk_off[b3];
   for (int e = tid; e < ntot; e += nth) {
     const int ek = g122_div(e, mb), eb = e - ek * nb;
     const int x1 = g122_div(eb, m0), x0 = eb - x1 * n0;
     const int x3 = g122_div(ek, m2), x2 = ek - x3 * n2;
     if ((b0 == b1 && x0 > x1) || (b2 == b3 && x2 > x3)) continue;  // the other order is stored
     float out = 0.0f;
-    {
-      const float* mL = M + x0 * n0;
-      const float* mR = M + 4 * nmax2 + x0 * n0;
+    {  // sum_a' f(a, a') X[a', ...]
+      const float* fL = FL0 + x0 * n0;
       const int base = e - x0;
-      for (int a = 0; a < n0; ++a) out += mL[a] * XR[base + a] - mR[a] * XL[base + a];
+      for (int a = 0; a < n0; ++a) out += __ldg(fL + a) * XR[base + a] - __ldg(fL + nblk2 + a) * XL[base + a];
     }
     {
-      const float* mL = M + nmax2 + x1 * n1;
-      const float* mR = M + 5 * nmax2 + x1 * n1;
+      const float* fL = FL1 + x1 * n1;
       const int base = e - x1 * s1;
-      for (int a = 0; a < n1; ++a) out += mL[a] * XR[base + a * s1] - mR[a] * XL[base + a * s1];
+      for (int a = 0; a < n1; ++a)
+        out += __ldg(fL + a) * XR[base + a * s1] - __ldg(fL + nblk2 + a) * XL[base + a * s1];
     }
-    {
-      const float* mL = M + 2 * nmax2 + x2 * n2;
-      const float* mR = M + 6 * nmax2 + x2 * n2;
+    {  // - sum_c' f(c', c) X[..., c', ...]
+      const float* fL = FL2 + x2;
       const int base = e - x2 * s2;
-      for (int a = 0; a < n2; ++a) out += mL[a] * XR[base + a * s2] - mR[a] * XL[base + a * s2];
+      for (int a = 0; a < n2; ++a)
+        out -= __ldg(fL + a * n2) * XR[base + a * s2] - __ldg(fL + nblk2 + a * n2) * XL[base + a * s2];
     }
     {
-      const float* mL = M + 3 * nmax2 + x3 * n3;
-      const float* mR = M + 7 * nmax2 + x3 * n3;
+      const float* fL = FL3 + x3;
       const int base = e - x3 * s3;
-      for (int a = 0; a < n3; ++a) out += mL[a] * XR[base + a * s3] - mR[a] * XL[base + a * s3];
+      for (int a = 0; a < n3; ++a)
+        out -= __ldg(fL + a * n3) * XR[base + a * s3] - __ldg(fL + nblk2 + a * n3) * XL[base + a * s3];
     }
     const int cb = S.PB[eb], ck = S.PK[ek];
     const int C1 = cb & 3, C2 = ck & 3;
@@ -597,7 +585,16 @@ __device__ __forceinline__ void g122_task(const DevLayout& D, const PairGroupsDe
     if (C1 <= C2) RES[go[g] + (cb >> 2) + (int64_t)(ck >> 2) * gn[g]] = f32_to_f64(w);
     if (G1 != G2 && C2 <= C1) RES[go[g] + (ck >> 2) + (int64_t)(cb >> 2) * gn[g]] = f32_to_f64(hRES < 0 ? -w : w);
   }
-  g122_sync<kWarp>();
+  if (kLanes) __syncwarp(mask); else __syncthreads();
+}
+
+__device__ __forceinline__ void g122_slice(float* base, int cap, int nmax2, G122Smem& S) {
+  S.XL = base;
+  S.XR = base + cap;
+  S.PB = reinterpret_cast<int*>(base + 2 * cap);
+  S.PK = S.PB + nmax2;
+  S.FBp = reinterpret_cast<float*>(S.PK + nmax2);
+  S.FKp = S.FBp + nmax2;
 }
 }  // namespace
 
@@ -615,28 +612,35 @@ __global__ void k_comm122_fblocks(DevLayout D, PairGroupsDev G, int nspb, int nb
   }
 }
 
-// one warp per task (sub-blocks of at most `small` elements); 8 warps per CTA, each with
-// its own shared-memory slice [XL small | XR small | M 8 nmax2 | PB, PK, FBp, FKp nmax2 each]
-__global__ void __launch_bounds__(256) k_comm122_groups_warp(DevLayout D, PairGroupsDev G, int ntasks, int small,
-                                                             int nmax2, const double* __restrict__ L, int hL,
-                                                             const double* __restrict__ R, int hR,
-                                                             double* __restrict__ RES, int hRES,
-                                                             const float* __restrict__ FB, int nblk2) {
+// kLanes-lane groups inside the warps of a 256-thread CTA, each group with its own
+// shared-memory slice [XL cap | XR cap | PB, PK, FBp, FKp nmax2 each]; tasks of at most cap
+// elements (the host split guarantees it)
+template <int kLanes>
+__global__ void __launch_bounds__(256) k_comm122_groups_lanes(DevLayout D, PairGroupsDev G, int ntasks, int cap,
+                                                              int nmax2, const double* __restrict__ L, int hL,
+                                                              const double* __restrict__ R, int hR,
+                                                              double* __restrict__ RES, int hRES,
+                                                              const float* __restrict__ FB, int nblk2) {
   extern __shared__ float g122_sm[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kGroups = 256 / kLanes;
+  const int grp = threadIdx.x / kLanes, lane = threadIdx.x % kLanes;
+  const unsigned mask =
+      (kLanes == 32) ? 0xffffffffu : (((1u << kLanes) - 1u) << (((threadIdx.x & 31) / kLanes) * kLanes));
   G122Smem S;
-  S.XL = g122_sm + (size_t)warp * (2 * small + 12 * nmax2);
-  S.XR = S.XL + small;
-  S.M = S.XR + small;
-  S.PB = reinterpret_cast<int*>(S.M + 8 * nmax2);
-  S.PK = S.PB + nmax2;
-  S.FBp = reinterpret_cast<float*>(S.PK + nmax2);
-  S.FKp = S.FBp + nmax2;
-  for (int t = blockIdx.x * 8 + warp; t < ntasks; t += gridDim.x * 8)
-    g122_task<true>(D, G, G.tasks[t], L, hL, R, hR, RES, hRES, FB, nblk2, S, nmax2, lane, 32);
+  g122_slice(g122_sm + (size_t)grp * (2 * cap + 4 * nmax2), cap, nmax2, S);
+  for (int t = blockIdx.x * kGroups + grp; t < ntasks; t += gridDim.x * kGroups)
+    g122_task<kLanes>(D, G, G.tasks[t], L, hL, R, hR, RES, hRES, FB, nblk2, S, lane, kLanes, mask);
+}
+void launch_comm122_lanes(int lanes, int grid, size_t smem, cudaStream_t st, const DevLayout& D,
+                          const PairGroupsDev& G, int ntasks, int cap, int nmax2, const double* L, int hL,
+                          const double* R, int hR, double* RES, int hRES, const float* FB, int nblk2) {
+  if (lanes == 8)
+    k_comm122_groups_lanes<8><<<grid, 256, smem, st>>>(D, G, ntasks, cap, nmax2, L, hL, R, hR, RES, hRES, FB, nblk2);
+  else
+    k_comm122_groups_lanes<32><<<grid, 256, smem, st>>>(D, G, ntasks, cap, nmax2, L, hL, R, hR, RES, hRES, FB, nblk2);
 }
 
-// one CTA per task (the larger sub-blocks): [XL nmax4 | XR nmax4 | M 8 nmax2 | PB, PK, FBp, FKp]
+// one CTA per task (the larger sub-blocks): [XL nmax4 | XR nmax4 | PB, PK, FBp, FKp]
 __global__ void __launch_bounds__(256) k_comm122_groups_cta(DevLayout D, PairGroupsDev G, int nmax4, int nmax2,
                                                             const double* __restrict__ L, int hL,
                                                             const double* __restrict__ R, int hR,
@@ -644,14 +648,8 @@ __global__ void __launch_bounds__(256) k_comm122_groups_cta(DevLayout D, PairGro
                                                             const float* __restrict__ FB, int nblk2) {
   extern __shared__ float g122_sm[];
   G122Smem S;
-  S.XL = g122_sm;
-  S.XR = S.XL + nmax4;
-  S.M = S.XR + nmax4;
-  S.PB = reinterpret_cast<int*>(S.M + 8 * nmax2);
-  S.PK = S.PB + nmax2;
-  S.FBp = reinterpret_cast<float*>(S.PK + nmax2);
-  S.FKp = S.FBp + nmax2;
-  g122_task<false>(D, G, G.tasks[blockIdx.x], L, hL, R, hR, RES, hRES, FB, nblk2, S, nmax2, threadIdx.x, blockDim.x);
+  g122_slice(g122_sm, nmax4, nmax2, S);
+  g122_task<0>(D, G, G.tasks[blockIdx.x], L, hL, R, hR, RES, hRES, FB, nblk2, S, threadIdx.x, blockDim.x, 0u);
 }
 
 }  // namespace imsrg
