@@ -150,6 +150,9 @@ struct Ctx {
   imsrg_status tc_error();
   imsrg_status tc_commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
   void tc_release();
+  imsrg_status tc_g122_partition(int tiny_cap, int small_cap);
+  imsrg_status tc_set_gemm_order(int order);
+  imsrg_status tc_autotune(const double* L, int hL, const double* R, int hR, double* RES, imsrg_tune_info* info);
 };
 
 #define CK_TC(expr)              \

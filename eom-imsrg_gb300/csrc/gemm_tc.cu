@@ -494,9 +494,18 @@ struct TcState {
   // commutator_122 by pair groups: sub-blocks of at most g122_small elements go one per warp,
   // the larger ones one per CTA (tasks in channel order, so a channel's L and R stay in L2)
   // (tiny sub-blocks, up to g122_tiny elements, go to 8-lane groups, four per warp)
-  std::vector<int4> g122_tiny, g122_warp, g122_cta;
+  // All tasks in channel order with their sizes; the device list holds them partitioned into
+  // [tiny | warp | cta] runs by the current caps (tc_g122_partition).
+  std::vector<int4> g122_all;
+  std::vector<int64_t> g122_elems;
+  int4* d_g122_tasks = nullptr;
+  int g122_ntiny = 0, g122_nwarp = 0, g122_ncta = 0;
   PairGroupsDev g122_t{}, g122_w{}, g122_c{};
   int g122_tiny_cap = 64, g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
+  // tuned launch parameters (imsrg_autotune): CTAs of the recoupling kernel, GEMM tile order
+  int recouple_ctas = 152 * 16;
+  int gemm_order = 0;  // 0: longest K first, 1: problem order
+  std::vector<TcTile> pphh_tiles_lpt, z_tiles_lpt;
   std::vector<int> g_start, g_n, g_orb, g_b1, g_b2, g_blk_off;
   float* g122_fb = nullptr;  // f(x, y) of L and R on every (l, j, tz) block
   int num_sms = 148;
@@ -545,6 +554,7 @@ void Ctx::tc_release() {
   if (tc->ybuf) cudaFree(tc->ybuf);
   if (tc->d_err) cudaFree(tc->d_err);
   if (tc->g122_fb) cudaFree(tc->g122_fb);
+  if (tc->d_g122_tasks) cudaFree(tc->d_g122_tasks);
   delete tc;
   tc = nullptr;
 }
@@ -685,10 +695,8 @@ imsrg_status Ctx::tc_prepare(int mode) {
       for (int G2 = pg.grp_first[q]; G2 < pg.grp_first[q + 1]; ++G2)
         for (int G1 = pg.grp_first[q]; G1 <= G2; ++G1) {
           const int4 t = make_int4(q, G1, G2, 0);
-          const int64_t ne = pg.elems(G1, G2);
-          if (ne <= tc->g122_tiny_cap) tc->g122_tiny.push_back(t);
-          else if (ne <= tc->g122_small) tc->g122_warp.push_back(t);
-          else tc->g122_cta.push_back(t);
+          tc->g122_all.push_back(t);
+          tc->g122_elems.push_back(pg.elems(G1, G2));
         }
   }
   // ---- recoupling quadruples: bra (i<=j) of class c1, ket (k<=l) of class c2, with
@@ -754,20 +762,17 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->g_b1, &tc->g122_w.grp_b1);
   pk.add(tc->g_b2, &tc->g122_w.grp_b2);
   pk.add(tc->g_blk_off, &tc->g122_w.blk_off);
-  pk.add(tc->g122_tiny, &tc->g122_t.tasks);
-  pk.add(tc->g122_warp, &tc->g122_w.tasks);
-  pk.add(tc->g122_cta, &tc->g122_c.tasks);
+
   CK_TC(cuda(cudaMalloc(&tc->d_mem, pk.buf.size()), "cudaMalloc(tc tables)"));
   CK_TC(cuda(cudaMemcpy(tc->d_mem, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tc tables)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(tc->d_mem) + f.first;
-  {
-    const int4* ct = tc->g122_c.tasks;
-    const int4* tt = tc->g122_t.tasks;
-    tc->g122_c = tc->g122_w;
-    tc->g122_c.tasks = ct;
-    tc->g122_t = tc->g122_w;
-    tc->g122_t.tasks = tt;
-  }
+  CK_TC(cuda(cudaMalloc(&tc->d_g122_tasks, sizeof(int4) * std::max<size_t>(tc->g122_all.size(), 1)),
+             "cudaMalloc(122 tasks)"));
+  tc->g122_t = tc->g122_c = tc->g122_w;
+  CK_TC(tc_g122_partition(tc->g122_tiny_cap, tc->g122_small));
+  tc->recouple_ctas = tc->num_sms * 16;
+  tc->pphh_tiles_lpt = tc->pphh_tiles;
+  tc->z_tiles_lpt = tc->z_tiles;
 
   // tensor map over the whole operand buffer: rows of 64 bf16 (128 bytes), box 64 x 128
   void* fn = nullptr;
@@ -870,25 +875,25 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     k_comm122_fblocks<<<tc->g122_nspb, 64, 0, stream>>>(D, tc->g122_w, tc->g122_nspb, tc->g122_nblk2, Lp, hL, Rp, hR,
                                                          tc->g122_fb);
     CK_TC(launched("k_comm122_fblocks"));
-    if (!tc->g122_tiny.empty()) {  // 8 lanes per task, 32 tasks per CTA
-      const int nt = (int)tc->g122_tiny.size();
+    if (tc->g122_ntiny) {  // 8 lanes per task, 32 tasks per CTA
+      const int nt = tc->g122_ntiny;
       const int grid = std::min((nt + 31) / 32, tc->num_sms * 8);
       const size_t smem = sizeof(float) * 32 * (size_t)(2 * tc->g122_tiny_cap + 4 * tc->g122_nmax2);
       launch_comm122_lanes(8, grid, smem, stream, D, tc->g122_t, nt, tc->g122_tiny_cap, tc->g122_nmax2, Lp, hL, Rp, hR,
                            RES, hRES, tc->g122_fb, tc->g122_nblk2);
       CK_TC(launched("k_comm122_groups_lanes<8>"));
     }
-    if (!tc->g122_warp.empty()) {  // a warp per task, 8 tasks per CTA
-      const int nt = (int)tc->g122_warp.size();
+    if (tc->g122_nwarp) {  // a warp per task, 8 tasks per CTA
+      const int nt = tc->g122_nwarp;
       const int grid = std::min((nt + 7) / 8, tc->num_sms * 8);
       const size_t smem = sizeof(float) * 8 * (size_t)(2 * tc->g122_small + 4 * tc->g122_nmax2);
       launch_comm122_lanes(32, grid, smem, stream, D, tc->g122_w, nt, tc->g122_small, tc->g122_nmax2, Lp, hL, Rp, hR,
                            RES, hRES, tc->g122_fb, tc->g122_nblk2);
       CK_TC(launched("k_comm122_groups_lanes<32>"));
     }
-    if (!tc->g122_cta.empty()) {
+    if (tc->g122_ncta) {
       const size_t smem = sizeof(float) * (size_t)(2 * tc->g122_nmax4 + 4 * tc->g122_nmax2);
-      k_comm122_groups_cta<<<(int)tc->g122_cta.size(), 256, smem, stream>>>(D, tc->g122_c, tc->g122_nmax4,
+      k_comm122_groups_cta<<<tc->g122_ncta, 256, smem, stream>>>(D, tc->g122_c, tc->g122_nmax4,
                                                                              tc->g122_nmax2, Lp, hL, Rp, hR, RES, hRES,
                                                                              tc->g122_fb, tc->g122_nblk2);
       CK_TC(launched("k_comm122_groups_cta"));
@@ -905,7 +910,7 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   mark(kPhasePhGemm);
   if (!tc->quads.empty()) {
     const int64_t nq = (int64_t)tc->quads.size();
-    const int grid = (int)std::min<int64_t>((nq + 255) / 256, 152 * 16);
+    const int grid = (int)std::min<int64_t>((nq + 255) / 256, tc->recouple_ctas);
     k_recouple_y<<<grid, 256, 0, stream>>>(D, tc->d_quads, nq, tc->zbuf, tc->ybuf, RES, hL * hR);
     CK_TC(launched("k_recouple_y"));
   }
@@ -915,4 +920,150 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   }
   mark(kPhaseRecouple);
   return IMSRG_OK;
+}
+
+// ---------------------------------------------------------------- autotuner
+// Splits the 122 tasks into [tiny | warp | cta] runs by size, keeping channel order inside
+// each run, and uploads the list.  The caps must keep the per-CTA shared memory of the
+// 8-lane and warp kernels within the 48 KiB default.
+imsrg_status Ctx::tc_g122_partition(int tiny_cap, int small_cap) {
+  const size_t lim = 48 * 1024;
+  if (tiny_cap < 1 || small_cap < tiny_cap ||
+      sizeof(float) * 32 * (size_t)(2 * tiny_cap + 4 * tc->g122_nmax2) > lim ||
+      sizeof(float) * 8 * (size_t)(2 * small_cap + 4 * tc->g122_nmax2) > lim)
+    return fail(IMSRG_ERR_INVALID_ARGUMENT, "122 task caps out of range");
+  const size_t n = tc->g122_all.size();
+  std::vector<int4> v;
+  v.reserve(n);
+  int nt = 0, nw = 0;
+  for (size_t i = 0; i < n; ++i)
+    if (tc->g122_elems[i] <= tiny_cap) { v.push_back(tc->g122_all[i]); ++nt; }
+  for (size_t i = 0; i < n; ++i)
+    if (tc->g122_elems[i] > tiny_cap && tc->g122_elems[i] <= small_cap) { v.push_back(tc->g122_all[i]); ++nw; }
+  for (size_t i = 0; i < n; ++i)
+    if (tc->g122_elems[i] > small_cap) v.push_back(tc->g122_all[i]);
+  if (n) {
+    CK_TC(cuda(cudaMemcpyAsync(tc->d_g122_tasks, v.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, stream),
+               "cudaMemcpyAsync(122 tasks)"));
+    CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize(122 tasks)"));
+  }
+  tc->g122_ntiny = nt;
+  tc->g122_nwarp = nw;
+  tc->g122_ncta = (int)n - nt - nw;
+  tc->g122_t.tasks = tc->d_g122_tasks;
+  tc->g122_w.tasks = tc->d_g122_tasks + nt;
+  tc->g122_c.tasks = tc->d_g122_tasks + nt + nw;
+  tc->g122_tiny_cap = tiny_cap;
+  tc->g122_small = small_cap;
+  return IMSRG_OK;
+}
+
+// Order of the persistent GEMM tile lists: 0 = longest K first, 1 = problem order.
+imsrg_status Ctx::tc_set_gemm_order(int order) {
+  auto sorted = [&](const std::vector<TcTile>& lpt) {
+    std::vector<TcTile> t = lpt;
+    if (order == 1)
+      std::stable_sort(t.begin(), t.end(), [](const TcTile& a, const TcTile& b) {
+        return a.prob != b.prob ? a.prob < b.prob : (a.m0 != b.m0 ? a.m0 < b.m0 : a.n0 < b.n0);
+      });
+    return t;
+  };
+  tc->pphh_tiles = sorted(tc->pphh_tiles_lpt);
+  tc->z_tiles = sorted(tc->z_tiles_lpt);
+  if (!tc->pphh_tiles.empty())
+    CK_TC(cuda(cudaMemcpyAsync(const_cast<TcTile*>(tc->d_pphh_tiles), tc->pphh_tiles.data(),
+                               sizeof(TcTile) * tc->pphh_tiles.size(), cudaMemcpyHostToDevice, stream),
+               "cudaMemcpyAsync(GEMM tiles)"));
+  if (!tc->z_tiles.empty())
+    CK_TC(cuda(cudaMemcpyAsync(const_cast<TcTile*>(tc->d_z_tiles), tc->z_tiles.data(),
+                               sizeof(TcTile) * tc->z_tiles.size(), cudaMemcpyHostToDevice, stream),
+               "cudaMemcpyAsync(GEMM tiles)"));
+  CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize(GEMM tiles)"));
+  tc->gemm_order = order;
+  return IMSRG_OK;
+}
+
+// Times one mixed commutator [L, R] per candidate launch configuration on this basis and keeps
+// the fastest, one knob at a time (122 task caps, recoupling CTAs, GEMM tile order).  Every
+// candidate computes the same result: no output element depends on the partition, the grid or
+// the tile order.  A captured Magnus-step graph is dropped, so the next step re-captures it.
+imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR, double* RES, imsrg_tune_info* info) {
+  if (!tc) return fail(IMSRG_ERR_UNSUPPORTED, "autotune needs a mixed-precision context");
+  const int hRES = -hL * hR;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK_TC(cuda(cudaEventCreate(&e0), "cudaEventCreate"));
+  CK_TC(cuda(cudaEventCreate(&e1), "cudaEventCreate"));
+  auto time_one = [&](float* ms) -> imsrg_status {
+    CK_TC(commutator(Lp, hL, Rp, hR, RES, hRES, true));  // warm-up
+    CK_TC(cuda(cudaEventRecord(e0, stream), "cudaEventRecord"));
+    for (int r = 0; r < 3; ++r) CK_TC(commutator(Lp, hL, Rp, hR, RES, hRES, true));
+    CK_TC(cuda(cudaEventRecord(e1, stream), "cudaEventRecord"));
+    CK_TC(cuda(cudaEventSynchronize(e1), "cudaEventSynchronize"));
+    CK_TC(cuda(cudaEventElapsedTime(ms, e0, e1), "cudaEventElapsedTime"));
+    *ms /= 3.0f;
+    return IMSRG_OK;
+  };
+  imsrg_status st = IMSRG_OK;
+  float base = 0.0f, best = 0.0f;
+  do {
+    if ((st = time_one(&base)) != IMSRG_OK) break;
+    best = base;
+    // 122 caps
+    static const int caps[][2] = {{16, 256}, {32, 128}, {32, 256}, {64, 256}, {64, 512}};
+    int bt = tc->g122_tiny_cap, bs = tc->g122_small;
+    for (const auto& c : caps) {
+      if ((st = tc_g122_partition(c[0], c[1])) != IMSRG_OK) break;
+      float ms;
+      if ((st = time_one(&ms)) != IMSRG_OK) break;
+      if (ms < best) { best = ms; bt = c[0]; bs = c[1]; }
+    }
+    if (st != IMSRG_OK || (st = tc_g122_partition(bt, bs)) != IMSRG_OK) break;
+    // recoupling CTAs
+    int br = tc->recouple_ctas;
+    for (int mult : {4, 8, 16, 32}) {
+      tc->recouple_ctas = tc->num_sms * mult;
+      float ms;
+      if ((st = time_one(&ms)) != IMSRG_OK) break;
+      if (ms < best) { best = ms; br = tc->recouple_ctas; }
+    }
+    tc->recouple_ctas = br;
+    if (st != IMSRG_OK) break;
+    // GEMM tile order
+    int bo = tc->gemm_order;
+    for (int order : {0, 1}) {
+      if ((st = tc_set_gemm_order(order)) != IMSRG_OK) break;
+      float ms;
+      if ((st = time_one(&ms)) != IMSRG_OK) break;
+      if (ms < best) { best = ms; bo = order; }
+    }
+    if (st != IMSRG_OK || (st = tc_set_gemm_order(bo)) != IMSRG_OK) break;
+    float after = 0.0f;
+    if ((st = time_one(&after)) != IMSRG_OK) break;
+    if (info) {
+      info->tiny_cap = tc->g122_tiny_cap;
+      info->small_cap = tc->g122_small;
+      info->recouple_ctas = tc->recouple_ctas;
+      info->gemm_order = tc->gemm_order;
+      info->ms_before = base;
+      info->ms_after = after;
+    }
+  } while (false);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st == IMSRG_OK) graph_release();
+  return st;
+}
+
+extern "C" imsrg_status imsrg_autotune(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES,
+                                       imsrg_tune_info* info) {
+  if (!ctx) return IMSRG_ERR_INVALID_ARGUMENT;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  if (c->device < 0) return c->fail(IMSRG_ERR_UNSUPPORTED, "host-only context (device < 0)");
+  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(IMSRG_ERR_CUDA, "cudaSetDevice");
+  if (!L || !R || !RES || L->owner != c || R->owner != c || RES->owner != c || RES == L || RES == R)
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_autotune: operators of this context, RES distinct");
+  if (c->precision == IMSRG_PREC_FP64) return c->fail(IMSRG_ERR_UNSUPPORTED, "autotune applies to the mixed modes");
+  CK_TC(c->ensure_workspace());
+  CK_TC(c->tc_prepare(c->precision));
+  return c->tc_autotune(L->d, L->herm, R->d, R->herm, RES->d, info);
 }

@@ -37,6 +37,11 @@ class HFInfo_t(C.Structure):
     _fields_ = [("e_hf", C.c_double), ("crit", C.c_double), ("iterations", C.c_int32)]
 
 
+class TuneInfo_t(C.Structure):
+    _fields_ = [("tiny_cap", C.c_int32), ("small_cap", C.c_int32), ("recouple_ctas", C.c_int32),
+                ("gemm_order", C.c_int32), ("ms_before", C.c_double), ("ms_after", C.c_double)]
+
+
 class StepInfo_t(C.Structure):
     _fields_ = [("E0", C.c_double), ("mbpt2", C.c_double), ("magnus_terms", C.c_int32), ("bch_terms", C.c_int32),
                 ("bch_converged", C.c_int32), ("graph_rebuilt", C.c_int32)]
@@ -53,6 +58,7 @@ SIGNATURES = {
     "imsrg_block_pairs": [_vp, _i32, _i32, _pi32],
     "imsrg_cc_info": [_vp, _pi32, _pi32, _pi32],
     "imsrg_set_precision": [_vp, _i32],
+    "imsrg_autotune": [_vp, _vp, _vp, _vp, C.POINTER(TuneInfo_t)],
     "imsrg_synchronize": [_vp],
     "imsrg_op_create": [_vp, _i32, _pvp],
     "imsrg_op_destroy": [_vp, _vp],

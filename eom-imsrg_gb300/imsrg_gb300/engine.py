@@ -205,6 +205,13 @@ class Engine:
         self._ck(self.L.imsrg_set_precision(self.h, _lib.PREC[mode]))
         self.precision = mode
 
+    def autotune(self, L: SqOp, R: SqOp, RES: SqOp) -> dict:
+        """Pick the launch configuration of the mixed commutator on this basis (imsrg_autotune);
+        RES is overwritten with [L, R]."""
+        info = _lib.TuneInfo_t()
+        self._ck(self.L.imsrg_autotune(self.h, L.h, R.h, RES.h, C.byref(info)))
+        return {k: getattr(info, k) for k, _ in _lib.TuneInfo_t._fields_}
+
     def synchronize(self):
         self._ck(self.L.imsrg_synchronize(self.h))
 
