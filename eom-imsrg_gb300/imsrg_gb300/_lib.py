@@ -111,6 +111,11 @@ SIGNATURES = {
     "imsrg_dot_sq_op": [_vp, _vp, _vp, _pd],
     "imsrg_synthetic_hamiltonian": [_vp, _u64, _d, _vp],
     "imsrg_synthetic_bare_hamiltonian": [_vp, _u64, _d, _vp],
+    "imsrg_neq": [_vp, _pi64],
+    "imsrg_vectorize_slab": [_vp, _vp, _vp],
+    "imsrg_repackage_slab": [_vp, _vp, _i32, _vp],
+    "imsrg_write_omega_checkpoint": [_vp, _vp, C.c_char_p],
+    "imsrg_read_omega_checkpoint": [_vp, _vp, C.c_char_p],
     "imsrg_calc_hf": [_vp, _vp, _i32, _vp, C.POINTER(HFInfo_t)],
     "imsrg_calc_ho": [_vp, _vp, _vp, C.POINTER(HFInfo_t)],
     "imsrg_sqop_to_hf": [_vp, _vp, _vp],

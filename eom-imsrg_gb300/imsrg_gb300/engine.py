@@ -262,6 +262,35 @@ class Engine:
                                                           out.ctypes.data))
         return out
 
+    # ---------------------------------------------------------------- flat vectors, checkpoints
+    @property
+    def neq(self) -> int:
+        v = C.c_int64()
+        self._ck(self.L.imsrg_neq(self.h, C.byref(v)))
+        return v.value
+
+    def vectorize(self, slab: np.ndarray) -> np.ndarray:
+        """vectorize (src/basic_IMSRG.f90:3929-3985) of a host slab."""
+        slab = np.ascontiguousarray(slab, dtype=np.float64)
+        out = np.empty(self.neq)
+        self._ck(self.L.imsrg_vectorize_slab(self.h, slab.ctypes.data, out.ctypes.data))
+        return out
+
+    def repackage(self, vec: np.ndarray, herm: int = 1) -> np.ndarray:
+        """repackage (src/basic_IMSRG.f90:3988-4053) into a host slab."""
+        vec = np.ascontiguousarray(vec, dtype=np.float64)
+        if vec.size != self.neq:
+            raise ValueError(f"vector has {vec.size} values, this basis needs {self.neq}")
+        out = np.zeros(self.slab)
+        self._ck(self.L.imsrg_repackage_slab(self.h, vec.ctypes.data, int(herm), out.ctypes.data))
+        return out
+
+    def write_omega_checkpoint(self, G: SqOp, path: str):
+        self._ck(self.L.imsrg_write_omega_checkpoint(self.h, G.h, str(path).encode()))
+
+    def read_omega_checkpoint(self, G: SqOp, path: str):
+        self._ck(self.L.imsrg_read_omega_checkpoint(self.h, G.h, str(path).encode()))
+
     # ---------------------------------------------------------------- Hartree-Fock
     def calc_hf(self, H: SqOp, max_iter: int = 1000):
         """calc_HF (src/HF_mod.f90:14-105): H (bare) becomes the normal-ordered HF-basis

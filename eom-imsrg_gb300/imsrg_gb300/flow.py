@@ -7,11 +7,43 @@ scalars (norms, E0, MBPT2) come back to the host.
 """
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
 
 from .engine import CONV, Engine
+
+
+def omega_checkpoint_name(prefix: str, s: float) -> str:
+    """File name of the Omega checkpoint at flow parameter s, as write_omega_checkpoint builds it
+    (src/basic_IMSRG.f90:3215-3251): the prefix cut after 'hwHO0' and two more characters (or
+    after 'hw' and two more), then '_s' and s in six characters with three decimals."""
+    k = prefix.find("hwHO0")
+    cut = k + 7 if k >= 0 else prefix.find("hw") + 4
+    if cut < 4:
+        raise ValueError("the prefix names no hw value")
+    txt = f"{s:6.3f}".strip()
+    if s < 10.0:
+        txt += "0"
+    return f"{prefix[:cut]}_s{txt}.bin"
+
+
+def latest_omega_checkpoint(directory: str, prefix: str, ds: float = 0.5, s_top: float = 95.5):
+    """(path, s) of the newest checkpoint, searched from s = 95.5 down in steps of ds as
+    read_omega_checkpoint does (src/basic_IMSRG.f90:3300-3330), or None."""
+    s = s_top
+    while s > 1.0:
+        path = os.path.join(directory, omega_checkpoint_name(prefix, s))
+        if os.path.exists(path):
+            return path, s
+        s -= ds
+    return None
+
+
+def checkpoint_interval(emax: int) -> int:
+    """Steps between checkpoints (src/IMSRG_MAGNUS.f90:55-61)."""
+    return 12 if emax == 14 else (4 if emax > 14 else 24)
 
 
 @dataclass
@@ -26,11 +58,18 @@ class FlowResult:
 def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float | None = None,
                     max_steps: int | None = None, crit_stop: float = float(np.float32(1e-6)),
                     bch_max_terms: int = 40, bch_conv: float = CONV, generator: str = "white",
-                    ops: dict | None = None, graph: bool = False) -> FlowResult:
+                    ops: dict | None = None, graph: bool = False, checkpoint: tuple | None = None,
+                    checkpoint_every: int | None = None) -> FlowResult:
     """Flow the Hamiltonian H0 (host slab, herm +1) to s_max / max_steps / |MBPT2| < crit.
 
     graph=True runs each step as one replay of the CUDA graph of imsrg_magnus_step
-    (same operators as the eager step, bit for bit)."""
+    (same operators as the eager step, bit for bit).
+
+    checkpoint=(directory, prefix) follows the reference's checkpointing: on entry the newest
+    Omega checkpoint is read, H(s) rebuilt by BCH_EXPAND and the flow resumes there; every
+    checkpoint_every steps (default: the reference's interval for eMax) Omega is written at
+    the start of the step, the first one after a restart skipped, and the file written
+    checkpoint_every steps earlier removed."""
     if generator != "white":
         raise ValueError("only the White generator is implemented")
     HS = eng.new_op(1, H0)          # evolved Hamiltonian
@@ -41,15 +80,34 @@ def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float |
     eng.build_gs_white(HS, DG)
     res = FlowResult()
     s, steps = 0.0, 0
+    chk = checkpoint_every or checkpoint_interval(eng.basis.eMax)
+    first = False
+    found = latest_omega_checkpoint(checkpoint[0], checkpoint[1], ds) if checkpoint else None
+    if found:  # checkpoint restart (src/IMSRG_MAGNUS.f90:73-84)
+        eng.read_omega_checkpoint(G, found[0])
+        eng.bch_expand(HS, G, H, bch_max_terms, bch_conv)
+        eng.build_gs_white(HS, DG)
+        s = found[1]
+        steps = int(round(s / ds))
+        first = True
     e2 = eng.mbpt2(HS)
     crit = abs(e2)
-    res.steps.append((0, s, HS.E0, HS.E0 + e2, crit, 0, 0))
+    res.steps.append((steps, s, HS.E0, HS.E0 + e2, crit, 0, 0))
     while crit > crit_stop:
         if max_steps is not None and steps >= max_steps:
             break
         if s_max is not None and s >= s_max - 1e-12:
             break
         steps += 1
+        if checkpoint and steps % chk == 0:
+            if first:
+                first = False
+            else:
+                eng.write_omega_checkpoint(G, os.path.join(checkpoint[0], omega_checkpoint_name(checkpoint[1], s)))
+                old = os.path.join(checkpoint[0], omega_checkpoint_name(checkpoint[1], s - chk * ds)) \
+                    if s - chk * ds > 0 else None
+                if old and os.path.exists(old):
+                    os.remove(old)
         if graph:
             info = eng.magnus_step(HS, G, DG, H, ds, bch_max_terms, bch_conv, graph=True)
             s += ds

@@ -255,6 +255,20 @@ imsrg_status imsrg_white_vjp(imsrg_ctx* ctx, const imsrg_op* H, const imsrg_op* 
 /* *out = sum_k A[k] B[k] over the slab (FP64) */
 imsrg_status imsrg_dot_sq_op(imsrg_ctx* ctx, const imsrg_op* A, const imsrg_op* B, double* out);
 
+/* ---- flat operator vectors and Omega checkpoints.  vectorize / repackage
+ * (src/basic_IMSRG.f90:3929-4053): E0, fhh, fpp, fph in full, then per block and array the
+ * on-and-below-diagonal rows of each column of the square arrays and every row of the others;
+ * repackage fills the upper triangles with herm x the lower.  The *_slab forms work on host
+ * slabs and need no GPU (host-only contexts too).  write/read_omega_checkpoint
+ * (src/basic_IMSRG.f90:3215-3407) store the vector of a device operator as a raw stream of
+ * neq native-endian FP64 values, the reference's access='stream' file; the caller names the
+ * file.  Reading a file whose size is not neq values returns IMSRG_ERR_MISMATCH. */
+imsrg_status imsrg_neq(const imsrg_ctx* ctx, int64_t* neq);
+imsrg_status imsrg_vectorize_slab(const imsrg_ctx* ctx, const double* host_slab, double* host_vec);
+imsrg_status imsrg_repackage_slab(const imsrg_ctx* ctx, const double* host_vec, int32_t herm, double* host_slab);
+imsrg_status imsrg_write_omega_checkpoint(imsrg_ctx* ctx, const imsrg_op* G, const char* path);
+imsrg_status imsrg_read_omega_checkpoint(imsrg_ctx* ctx, imsrg_op* G, const char* path);
+
 /* ---- input preparation (host, FP64): seeded synthetic Hamiltonian in the reference's
  * me2j -> pn J-scheme layout (read_me2j_interaction, src/interaction_IO.f90:282-557) plus the
  * harmonic-oscillator kinetic energy (calculate_h0_harm_osc, src/basic_IMSRG.f90:2093-2191),

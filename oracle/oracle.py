@@ -92,6 +92,7 @@ def lib():
         "orc_gamma_matrix": (None, [vp, _dp, i, _dp, _dp]),
         "orc_transform_2b_to_hf": (None, [vp, _dp, _dp]),
         "orc_normal_order": (None, [vp, _dp, i, _dp]),
+        "orc_vectorize": (i64, [vp, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -281,6 +282,12 @@ class Oracle:
         out = np.zeros(self.slab)
         self.L.orc_normal_order(self.h, op, herm, out)
         return out
+
+    def vectorize(self, op) -> np.ndarray:
+        """vectorize (src/basic_IMSRG.f90:3929-3985)."""
+        out = np.zeros(self.slab)  # the vector is never longer than the slab
+        n = self.L.orc_vectorize(self.h, op, out)
+        return out[:n].copy()
 
     def transform_2b_to_hf(self, op, D) -> np.ndarray:
         """transform_2b_to_HF (src/HF_mod.f90:567-692); D(HO orbit, HF orbit), N x N."""
