@@ -1,5 +1,7 @@
 // Engine state behind the opaque C-ABI handles.
 #pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -127,6 +129,7 @@ struct Ctx {
 
   // rank-lambda tensor operators (tensor.cu)
   imsrg_status tensor_state(int rank, int dpar, TensorState** out);
+  imsrg_status tensor_tc_prepare(TensorState& S);
   void tensor_release();
   imsrg_status tensor_commutator(TensorState& S, const double* L, int hL, const double* R, int hR, double* RES,
                                  int pieces);
@@ -150,6 +153,12 @@ struct Ctx {
   imsrg_status tc_error();
   imsrg_status tc_commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
   void tc_release();
+  imsrg_status tc_gemm_on(const CUtensorMap& map, int64_t slice_rows, const imsrg::TcProb* probs,
+                          const imsrg::TcTile* tiles, int ntiles, imsrg::TcOut out, int hL, int hR);
+  imsrg_status tc_encode_map(CUtensorMap* map, void* buf, int64_t total_rows);
+  imsrg_status tc_split_on(const imsrg::TcSplitOp* ops, const imsrg::SplitChunk* chunks, int nchunks, const double* L,
+                           const double* R, __nv_bfloat16* buf, int64_t slice_elems);
+  int tc_slices() const;  // bf16 slices of the tensor-core path (0 before tc_prepare)
   imsrg_status tc_g122_partition(int tiny_cap, int small_cap);
   imsrg_status tc_set_gemm_order(int order);
   imsrg_status tc_autotune(const double* L, int hL, const double* R, int hR, double* RES, imsrg_tune_info* info);

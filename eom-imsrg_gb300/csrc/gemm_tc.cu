@@ -362,13 +362,18 @@ __global__ void __launch_bounds__(256) k_split_chunks(const TcSplitOp* __restric
   const TcSplitOp o = ops[ch.op];
   const double* src = (o.src == 0 ? L : R) + o.src_off;
   const int nvec = (o.K + 7) >> 3;
-  const int total = (ch.r1 - ch.r0) * nvec;
+  const int nr = ch.r1 - ch.r0;
+  const int total = nr * nvec;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    const int r = ch.r0 + t / nvec;
-    const int k0 = (t - (r - ch.r0) * nvec) << 3;
+    // rows fastest for transposed sources (coalesced reads down a column), K fastest otherwise
+    const int r = o.trans ? ch.r0 + t % nr : ch.r0 + t / nvec;
+    const int k0 = (o.trans ? t / nr : t - (r - ch.r0) * nvec) << 3;
     float x[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) x[u] = (k0 + u < o.K) ? f64_to_f32(src[k0 + u + (int64_t)r * o.K]) : 0.0f;
+    for (int u = 0; u < 8; ++u)
+      x[u] = (k0 + u < o.K)
+                 ? f64_to_f32(o.trans ? src[r + (int64_t)(k0 + u) * o.ld] : src[k0 + u + (int64_t)r * o.K])
+                 : 0.0f;
     const int64_t dst = ((int64_t)(o.tile_base + (r / BM) * o.nkb + k0 / BK) * BM + (r % BM)) * BK + (k0 % BK);
 #pragma unroll
     for (int sl = 0; sl < S; ++sl) {
@@ -775,20 +780,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   tc->z_tiles_lpt = tc->z_tiles;
 
   // tensor map over the whole operand buffer: rows of 64 bf16 (128 bytes), box 64 x 128
-  void* fn = nullptr;
-  cudaDriverEntryPointQueryResult q;
-  CK_TC(cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
-             "cudaGetDriverEntryPointByVersion"));
-  if (!fn || q != cudaDriverEntryPointSuccess) return fail(IMSRG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  const cuuint64_t gdim[2] = {(cuuint64_t)BK, (cuuint64_t)std::max<int64_t>((int64_t)S * tc->slice_rows, BM)};
-  const cuuint64_t gstride[1] = {(cuuint64_t)(BK * sizeof(__nv_bfloat16))};
-  const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
-  const cuuint32_t estride[2] = {1, 1};
-  CUresult r = reinterpret_cast<EncodeTiledFn>(fn)(&tc->tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, tc->buf, gdim,
-                                                    gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return fail(IMSRG_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  CK_TC(tc_encode_map(&tc->tmap, tc->buf, (int64_t)S * tc->slice_rows));
   const size_t sm = S == 2 ? smem_bytes<2>() : smem_bytes<3>();
   if (S == 2)
     CK_TC(cuda(cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem attr"));
@@ -798,15 +790,53 @@ imsrg_status Ctx::tc_prepare(int mode) {
 }
 
 imsrg_status Ctx::tc_gemm(const TcProb* probs, const TcTile* tiles, int ntiles, TcOut out, int hL, int hR) {
+  return tc_gemm_on(tc->tmap, tc->slice_rows, probs, tiles, ntiles, out, hL, hR);
+}
+
+int Ctx::tc_slices() const { return tc ? tc->S : 0; }
+
+// the persistent split-BF16 GEMM over any operand buffer of this context's slice count
+imsrg_status Ctx::tc_gemm_on(const CUtensorMap& map, int64_t slice_rows, const TcProb* probs, const TcTile* tiles,
+                             int ntiles, TcOut out, int hL, int hR) {
   if (ntiles == 0) return IMSRG_OK;
   const int grid = std::min(ntiles, tc->num_sms);
   if (tc->S == 2)
-    k_tc_gemm<2><<<grid, NUM_THREADS, smem_bytes<2>(), stream>>>(tc->tmap, tc->slice_rows, probs, tiles, ntiles, out, hL,
-                                                                  hR, tc->d_err);
+    k_tc_gemm<2><<<grid, NUM_THREADS, smem_bytes<2>(), stream>>>(map, slice_rows, probs, tiles, ntiles, out, hL, hR,
+                                                                  tc->d_err);
   else
-    k_tc_gemm<3><<<grid, NUM_THREADS, smem_bytes<3>(), stream>>>(tc->tmap, tc->slice_rows, probs, tiles, ntiles, out, hL,
-                                                                  hR, tc->d_err);
+    k_tc_gemm<3><<<grid, NUM_THREADS, smem_bytes<3>(), stream>>>(map, slice_rows, probs, tiles, ntiles, out, hL, hR,
+                                                                  tc->d_err);
   return launched("k_tc_gemm");
+}
+
+// rows of 64 bf16 (128 bytes) over total_rows rows, box 64 x 128, 128-byte swizzle
+imsrg_status Ctx::tc_encode_map(CUtensorMap* map, void* buf, int64_t total_rows) {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  CK_TC(cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
+             "cudaGetDriverEntryPointByVersion"));
+  if (!fn || q != cudaDriverEntryPointSuccess) return fail(IMSRG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const cuuint64_t gdim[2] = {(cuuint64_t)BK, (cuuint64_t)std::max<int64_t>(total_rows, BM)};
+  const cuuint64_t gstride[1] = {(cuuint64_t)(BK * sizeof(__nv_bfloat16))};
+  const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
+  const cuuint32_t estride[2] = {1, 1};
+  CUresult r = reinterpret_cast<EncodeTiledFn>(fn)(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, buf, gdim, gstride, box,
+                                                    estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(IMSRG_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return IMSRG_OK;
+}
+
+// operand split of any op / chunk list into a buffer of this context's slice count
+imsrg_status Ctx::tc_split_on(const TcSplitOp* ops, const SplitChunk* chunks, int nchunks, const double* Lp,
+                              const double* Rp, __nv_bfloat16* buf, int64_t slice_elems) {
+  if (nchunks == 0) return IMSRG_OK;
+  if (tc->S == 2)
+    k_split_chunks<2><<<nchunks, 256, 0, stream>>>(ops, chunks, Lp, Rp, buf, slice_elems);
+  else
+    k_split_chunks<3><<<nchunks, 256, 0, stream>>>(ops, chunks, Lp, Rp, buf, slice_elems);
+  return launched("k_split_chunks");
 }
 
 imsrg_status Ctx::tc_pphh(const double* Lp, int hL, const double* Rp, int hR, double* w1, double* w2) {

@@ -4,6 +4,9 @@
 
 namespace imsrg {
 
+// tile shape of the split operand buffers: 128 rows of 64 K-contiguous bf16 per tile
+constexpr int kTcTileRows = 128, kTcTileK = 64;
+
 // term sign: bit 0 times herm(L), bit 1 times herm(R), bit 2 negative
 enum TcSign : int { kSignHL = 1, kSignHR = 2, kSignNeg = 4 };
 
@@ -14,6 +17,8 @@ struct TcSplitOp {
   int rows, K;   // rows = columns of the stored array, K = its leading dimension
   int nkb;       // K blocks of 64
   int tile_base;
+  int trans;     // 1: rows are the stored array's rows, element (r, k) at src[r + k*ld]
+  int ld;        // leading dimension of the stored array when trans
 };
 
 struct TcTermDesc {

@@ -9,6 +9,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 
 #include "../../include/imsrg_gb300.h"
 #include "engine.h"
@@ -33,6 +34,9 @@ __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* Wx, c
                                   int qa, int qb, int hL, int hR, double* RES);
 }  // namespace imsrg
 
+// output slot of the second product of a tensor ladder problem (TcOut::f64 index)
+constexpr int kTensorOpW3 = 7;
+
 // device state of one (rank, dpar) layout
 struct TensorState {
   TLayout T;
@@ -53,6 +57,22 @@ struct TensorState {
   double *ccx = nullptr, *ccr = nullptr;         // cross-coupled tensor blocks
   double *wx = nullptr, *wy = nullptr;           // recoupling products
   double *bch_a = nullptr, *bch_b = nullptr;     // BCH_TENSOR terms
+  // split-BF16 tensor-core form of the ladder's products through pp pairs (mixed modes):
+  // one single-term problem per product, the first product of a (block, class pair) into
+  // w1, the second into w3; the products through hh pairs (K = nhh) stay FP64 into w2
+  int tc_S = 0;
+  __nv_bfloat16* tc_buf = nullptr;
+  int64_t tc_slice_rows = 0, tc_slice_elems = 0;
+  CUtensorMap tc_map;
+  void* tc_tables = nullptr;
+  const TcSplitOp* tc_ops = nullptr;
+  const SplitChunk* tc_chunks = nullptr;
+  const TcProb* tc_probs = nullptr;
+  const TcTile* tc_tiles = nullptr;
+  const GemmProb* hh_p = nullptr;
+  const GemmTile* hh_t = nullptr;
+  int tc_nchunks = 0, tc_ntiles = 0, n_hh_t = 0;
+  double* w3 = nullptr;
 };
 
 struct imsrg_tensor {
@@ -193,13 +213,93 @@ void Ctx::tensor_release() {
     }
     TensorState* s = it->second.get();
     for (void* p : {(void*)s->w1, (void*)s->w2, (void*)s->ccx, (void*)s->ccr, (void*)s->wx, (void*)s->wy,
-                    (void*)s->bch_a, (void*)s->bch_b, s->tables})
+                    (void*)s->bch_a, (void*)s->bch_b, s->tables, (void*)s->tc_buf, s->tc_tables, (void*)s->w3})
       if (p) cudaFree(p);
     it = reg.erase(it);
   }
 }
 
 // [L (scalar, hL), R (tensor, hR)] -> RES (tensor, herm -hL hR); pieces as imsrg_tensor_commutator
+// Split-BF16 plan of the tensor ladder for the context's slice count: every product through
+// pp pairs of the FP64 problem list becomes a single-term tensor-core problem over K-major
+// operand tiles (columns of a stored array, or its rows through the transposed split); the
+// products through hh pairs keep their FP64 problems.
+imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
+  if (!tc_slices()) return fail(IMSRG_ERR_UNSUPPORTED, "tensor-core ladder needs a mixed-precision context");
+  if (S.tc_S == tc_slices()) return IMSRG_OK;
+  for (void* p : {(void*)S.tc_buf, S.tc_tables, (void*)S.w3})
+    if (p) cudaFree(p);
+  S.tc_buf = nullptr; S.tc_tables = nullptr; S.w3 = nullptr; S.tc_S = 0;
+  const int BMr = kTcTileRows, BKk = kTcTileK;
+  const auto P = build_tensor_pphh_problems(S.T, L);
+  std::vector<TcSplitOp> ops;
+  std::map<std::tuple<int, int64_t, int, int, int, int>, int> seen;  // operand -> tile base
+  int tiles = 0;
+  auto split = [&](int src, int64_t off, int rows, int K, int trans, int ld) {
+    const auto key = std::make_tuple(src, off, rows, K, trans, ld);
+    auto it = seen.find(key);
+    if (it != seen.end()) return it->second;
+    TcSplitOp o{};
+    o.src = src; o.src_off = off; o.rows = rows; o.K = K; o.nkb = (K + BKk - 1) / BKk;
+    o.tile_base = tiles; o.trans = trans; o.ld = ld;
+    tiles += ((rows + BMr - 1) / BMr) * o.nkb;
+    ops.push_back(o);
+    seen[key] = o.tile_base;
+    return o.tile_base;
+  };
+  std::vector<TcProb> probs;
+  std::vector<GemmProb> hh;
+  for (const GemmProb& p : P) {
+    if (p.c_id == kOpW2) { hh.push_back(p); continue; }
+    for (int ti = 0; ti < p.nterm; ++ti) {
+      const GemmTerm& t = p.t[ti];
+      if ((t.ta == 1 && t.lda != t.K) || (t.tb == 0 && t.ldb != t.K))
+        return fail(IMSRG_ERR_MISMATCH, "tensor ladder operand with padded leading dimension");
+      const int sa = t.a_id == kOpL ? 0 : 1, sb = t.b_id == kOpL ? 0 : 1;
+      const int a_tile = t.ta == 1 ? split(sa, t.a_off, p.M, t.K, 0, 0) : split(sa, t.a_off, p.M, t.K, 1, t.lda);
+      const int b_tile = t.tb == 0 ? split(sb, t.b_off, p.N, t.K, 0, 0) : split(sb, t.b_off, p.N, t.K, 1, t.ldb);
+      TcProb q{};
+      q.M = p.M; q.N = p.N; q.nkb = (t.K + BKk - 1) / BKk; q.nterm = 1;
+      q.t[0] = TcTermDesc{a_tile, b_tile, t.alpha};  // the alpha bits are the TcSign bits
+      q.out_f32 = 0; q.c_id = ti == 0 ? kOpW1 : kTensorOpW3; q.c_off = p.c_off; q.ldc = p.ldc;
+      probs.push_back(q);
+    }
+  }
+  std::vector<TcTile> tl;
+  for (int i = 0; i < (int)probs.size(); ++i)
+    for (int m0 = 0; m0 < probs[i].M; m0 += BMr)
+      for (int n0 = 0; n0 < probs[i].N; n0 += BMr) tl.push_back(TcTile{i, m0, n0, 0});
+  std::stable_sort(tl.begin(), tl.end(), [&](const TcTile& a, const TcTile& b) { return probs[a.prob].nkb > probs[b.prob].nkb; });
+  std::vector<SplitChunk> chunks;
+  for (int op = 0; op < (int)ops.size(); ++op) {
+    const int rows_per = std::max(1, 4096 / std::max(ops[op].K, 1));
+    for (int r0 = 0; r0 < ops[op].rows; r0 += rows_per)
+      chunks.push_back(SplitChunk{op, r0, std::min(ops[op].rows, r0 + rows_per)});
+  }
+  const auto hh_tiles = build_tiles(hh, 64, 64);
+  const int Sl = tc_slices();
+  S.tc_slice_rows = (int64_t)tiles * BMr;
+  S.tc_slice_elems = S.tc_slice_rows * BKk;
+  if ((int64_t)Sl * S.tc_slice_rows >= (int64_t)1 << 31)
+    return fail(IMSRG_ERR_UNSUPPORTED, "tensor ladder operands too large for 32-bit TMA rows");
+  const size_t bytes = sizeof(__nv_bfloat16) * (size_t)Sl * (size_t)S.tc_slice_elems;
+  CKT(cuda(cudaMalloc(&S.tc_buf, std::max<size_t>(bytes, 256)), "cudaMalloc(tensor ladder operands)"));
+  CKT(cuda(cudaMemset(S.tc_buf, 0, std::max<size_t>(bytes, 256)), "memset(tensor ladder operands)"));
+  CKT(tc_encode_map(&S.tc_map, S.tc_buf, (int64_t)Sl * S.tc_slice_rows));
+  Pack pk;
+  pk.add(ops, &S.tc_ops); pk.add(chunks, &S.tc_chunks); pk.add(probs, &S.tc_probs); pk.add(tl, &S.tc_tiles);
+  pk.add(hh, &S.hh_p); pk.add(hh_tiles, &S.hh_t);
+  CKT(cuda(cudaMalloc(&S.tc_tables, pk.buf.size()), "cudaMalloc(tensor ladder tables)"));
+  CKT(cuda(cudaMemcpy(S.tc_tables, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tensor ladder)"));
+  for (auto& f : pk.fix) *f.second = static_cast<const char*>(S.tc_tables) + f.first;
+  S.tc_nchunks = (int)chunks.size();
+  S.tc_ntiles = (int)tl.size();
+  S.n_hh_t = (int)hh_tiles.size();
+  CKT(cuda(cudaMalloc(&S.w3, sizeof(double) * (size_t)S.T.slab), "cudaMalloc(tensor w3)"));
+  S.tc_S = Sl;
+  return IMSRG_OK;
+}
+
 imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, const double* R, int hR, double* RES,
                                     int pieces) {
   CKT(ensure_workspace());
@@ -228,7 +328,36 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
     k_ts212<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
     CKT(launched("k_ts212"));
   }
-  if (pieces & 32) {
+  if ((pieces & 32) && precision != IMSRG_PREC_FP64) {  // split-BF16 products through pp pairs
+    CKT(tensor_tc_prepare(S));
+    const size_t tb = sizeof(double) * (size_t)T.slab;
+    CKT(cuda(cudaMemsetAsync(S.w1, 0, tb, stream), "memset(tensor w1)"));
+    CKT(cuda(cudaMemsetAsync(S.w2, 0, tb, stream), "memset(tensor w2)"));
+    CKT(cuda(cudaMemsetAsync(S.w3, 0, tb, stream), "memset(tensor w3)"));
+    CKT(tc_split_on(S.tc_ops, S.tc_chunks, S.tc_nchunks, Lp, R, S.tc_buf, S.tc_slice_elems));
+    TcOut out{};
+    out.f64[kOpW1] = S.w1;
+    out.f64[kTensorOpW3] = S.w3;
+    CKT(tc_gemm_on(S.tc_map, S.tc_slice_rows, S.tc_probs, S.tc_tiles, S.tc_ntiles, out, hL, hR));
+    if (S.n_hh_t) {
+      GemmOperands ops{};
+      ops.in[kOpL] = Lp; ops.in[kOpR] = R;
+      ops.out[kOpW1] = S.w1; ops.out[kOpW2] = S.w2;
+      ops.hL = hL; ops.hR = hR;
+      k_gemm_fp64<<<S.n_hh_t, 256, 0, stream>>>(S.hh_p, S.hh_t, ops);
+      CKT(launched("k_gemm_fp64(tensor hh ladder)"));
+    }
+    k_axpby<<<grid_n(T.slab), 256, 0, stream>>>(T.slab, S.w1, 1.0, S.w3, 1.0, S.w1);
+    CKT(launched("k_axpby"));
+    if (T.n2b) {
+      k_ts_pphh_update<<<grid_n(T.n2b), 256, 0, stream>>>(T.n2b, S.T.goff.empty() ? 0 : S.T.goff[0], RES, S.w1, S.w2);
+      CKT(launched("k_ts_pphh_update"));
+    }
+    if (nob) {
+      k_ts221<<<(nob * 32 + 255) / 256, 256, 0, stream>>>(D, T, S.w1, S.w2, hL * hR, RES, hRES);
+      CKT(launched("k_ts221"));
+    }
+  } else if (pieces & 32) {
     const size_t tb = sizeof(double) * (size_t)T.slab;
     CKT(cuda(cudaMemsetAsync(S.w1, 0, tb, stream), "memset(tensor w1)"));
     CKT(cuda(cudaMemsetAsync(S.w2, 0, tb, stream), "memset(tensor w2)"));

@@ -41,3 +41,25 @@ def test_bch_tensor_matches_oracle(oracles, engines):
     assert eng.bch_tensor(dG, dQ, 30, 1e-8) == n
     assert rel_err(dQ.download(), ref) < TOL
     assert abs(dQ.frob() - t.frob(ref)) <= 1e-12 * t.frob(ref)
+
+
+@pytest.mark.parametrize("mode,tol", [("bf16x6", 2e-6), ("bf16x3", 2e-5)])
+@pytest.mark.parametrize("emax,rank", [(4, 4), (4, 2)])
+def test_tensor_ladder_on_tensor_cores(oracles, emax, rank, mode, tol):
+    """In a mixed mode the ladder's products through pp pairs run as split-BF16 tcgen05 GEMMs
+    (FP32 accumulate); the rest of the tensor commutator stays FP64."""
+    from imsrg_gb300 import Engine, make_basis
+    from oracle.oracle import TensorOracle
+    o = oracles(emax)
+    t = TensorOracle(o, rank, 0)
+    eng = Engine(make_basis(emax), device=0, precision=mode)
+    A, B = o.random(23, -1), t.random(24, 1)
+    dA = eng.new_op(-1, A)
+    dB = eng.new_tensor(rank, 0, 1, B)
+    for pieces in (32, 127):
+        ref = t.commutator(A, -1, B, 1, pieces)
+        dR = eng.new_tensor(rank, 0, 1)
+        eng.tensor_commutator(dA, dB, dR, pieces)
+        err = rel_err(dR.download(), ref)
+        assert err < tol, (pieces, err)
+        assert err > 0.0  # the products did run in reduced precision
