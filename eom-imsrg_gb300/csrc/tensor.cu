@@ -73,6 +73,12 @@ struct TensorState {
   const GemmTile* hh_t = nullptr;
   int tc_nchunks = 0, tc_ntiles = 0, n_hh_t = 0;
   double* w3 = nullptr;
+  // particle-hole products on the same tensor cores: the cross-coupled L of every channel is
+  // split once per commutator (LCC rows, K = nph); per cross-coupled tensor block, CCR and CCX
+  // are split into shared regions of the buffer and Wx = hL LCC(qa) CCR, Wy = CCX LCC(qb)^T run
+  // as single-term problems
+  int ph_lcc_nchunks = 0;
+  std::vector<int> ph_chunk_start, ph_chunk_n, ph_tile_start, ph_tile_n;  // per block
 };
 
 struct imsrg_tensor {
@@ -271,11 +277,73 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
       for (int n0 = 0; n0 < probs[i].N; n0 += BMr) tl.push_back(TcTile{i, m0, n0, 0});
   std::stable_sort(tl.begin(), tl.end(), [&](const TcTile& a, const TcTile& b) { return probs[a.prob].nkb > probs[b.prob].nkb; });
   std::vector<SplitChunk> chunks;
-  for (int op = 0; op < (int)ops.size(); ++op) {
+  auto add_chunks = [&](int op) {
     const int rows_per = std::max(1, 4096 / std::max(ops[op].K, 1));
     for (int r0 = 0; r0 < ops[op].rows; r0 += rows_per)
       chunks.push_back(SplitChunk{op, r0, std::min(ops[op].rows, r0 + rows_per)});
+  };
+  for (int op = 0; op < (int)ops.size(); ++op) add_chunks(op);
+  const int ladder_nchunks = (int)chunks.size();
+  // ---- particle-hole: LCC rows of every channel (src 0 = d_lcc), split once per commutator
+  std::vector<int> lcc_tile(L.ncc, -1);
+  const size_t lcc_op0 = ops.size();
+  for (int q = 0; q < L.ncc; ++q) {
+    const int r = L.cc_rlen[q], nb = L.cc_nph[q];
+    if (r == 0 || nb == 0) continue;
+    lcc_tile[q] = split(0, L.cc_off[q], r, nb, 1, r);
   }
+  for (size_t op = lcc_op0; op < ops.size(); ++op) add_chunks((int)op);
+  S.ph_lcc_nchunks = (int)chunks.size() - ladder_nchunks;
+  // per block: CCR (src 0, its columns, K = nb1) and CCX (src 1, its rows, K = nb2) into two
+  // regions shared by all blocks, then Wx = hL LCC(qa) CCR and Wy = CCX LCC(qb)^T
+  const TLayout& TT = S.T;
+  int ccr_tiles_max = 0, ccx_tiles_max = 0;
+  for (size_t b = 0; b < TT.cb_J3.size(); ++b) {
+    const int qa = TT.cb_qa[b], qb = TT.cb_qb[b];
+    const int r1 = L.cc_rlen[qa], r2 = L.cc_rlen[qb], nb1 = L.cc_nph[qa], nb2 = L.cc_nph[qb];
+    ccr_tiles_max = std::max(ccr_tiles_max, ((r2 + BMr - 1) / BMr) * ((nb1 + BKk - 1) / BKk));
+    ccx_tiles_max = std::max(ccx_tiles_max, ((r1 + BMr - 1) / BMr) * ((nb2 + BKk - 1) / BKk));
+  }
+  const int ccr_base = tiles, ccx_base = tiles + ccr_tiles_max;
+  tiles += ccr_tiles_max + ccx_tiles_max;
+  std::vector<TcTile> tph;
+  S.ph_chunk_start.clear(); S.ph_chunk_n.clear(); S.ph_tile_start.clear(); S.ph_tile_n.clear();
+  for (size_t b = 0; b < TT.cb_J3.size(); ++b) {
+    const int qa = TT.cb_qa[b], qb = TT.cb_qb[b];
+    const int r1 = L.cc_rlen[qa], r2 = L.cc_rlen[qb], nb1 = L.cc_nph[qa], nb2 = L.cc_nph[qb];
+    const bool dox = nb1 > 0, doy = nb2 > 0 && TT.cb_J3[b] != TT.cb_J4[b];
+    S.ph_chunk_start.push_back((int)chunks.size());
+    S.ph_tile_start.push_back((int)(tl.size() + tph.size()));
+    auto add_prob = [&](int K, TcTermDesc t, int c_id) {
+      TcProb q{};
+      q.M = r1; q.N = r2; q.nkb = (K + BKk - 1) / BKk; q.nterm = 1; q.t[0] = t;
+      q.out_f32 = 0; q.c_id = c_id; q.c_off = 0; q.ldc = r1;
+      probs.push_back(q);
+      const int pi = (int)probs.size() - 1;
+      for (int m0 = 0; m0 < r1; m0 += BMr)
+        for (int n0 = 0; n0 < r2; n0 += BMr) tph.push_back(TcTile{pi, m0, n0, 0});
+    };
+    if (dox && r1 && r2) {
+      TcSplitOp o{};
+      o.src = 0; o.src_off = 0; o.rows = r2; o.K = nb1; o.nkb = (nb1 + BKk - 1) / BKk; o.tile_base = ccr_base;
+      ops.push_back(o);
+      add_chunks((int)ops.size() - 1);
+      add_prob(nb1, TcTermDesc{lcc_tile[qa], ccr_base, kSignHL}, kOpW1);
+    }
+    if (doy && r1 && r2) {
+      TcSplitOp o{};
+      o.src = 1; o.src_off = 0; o.rows = r1; o.K = nb2; o.nkb = (nb2 + BKk - 1) / BKk; o.tile_base = ccx_base;
+      o.trans = 1; o.ld = r1;
+      ops.push_back(o);
+      add_chunks((int)ops.size() - 1);
+      add_prob(nb2, TcTermDesc{ccx_base, lcc_tile[qb], 0}, kOpW2);
+    }
+    S.ph_chunk_n.push_back((int)chunks.size() - S.ph_chunk_start.back());
+    S.ph_tile_n.push_back((int)(tl.size() + tph.size()) - S.ph_tile_start.back());
+  }
+  tl.insert(tl.end(), tph.begin(), tph.end());
+  S.tc_ntiles = 0;  // set below: the ladder's tiles come first
+  const int ladder_ntiles = (int)(tl.size() - tph.size());
   const auto hh_tiles = build_tiles(hh, 64, 64);
   const int Sl = tc_slices();
   S.tc_slice_rows = (int64_t)tiles * BMr;
@@ -292,8 +360,8 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
   CKT(cuda(cudaMalloc(&S.tc_tables, pk.buf.size()), "cudaMalloc(tensor ladder tables)"));
   CKT(cuda(cudaMemcpy(S.tc_tables, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tensor ladder)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(S.tc_tables) + f.first;
-  S.tc_nchunks = (int)chunks.size();
-  S.tc_ntiles = (int)tl.size();
+  S.tc_nchunks = ladder_nchunks;
+  S.tc_ntiles = ladder_ntiles;
   S.n_hh_t = (int)hh_tiles.size();
   CKT(cuda(cudaMalloc(&S.w3, sizeof(double) * (size_t)S.T.slab), "cudaMalloc(tensor w3)"));
   S.tc_S = Sl;
@@ -378,7 +446,40 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       CKT(launched("k_ts221"));
     }
   }
-  if (pieces & 64) {
+  if ((pieces & 64) && precision != IMSRG_PREC_FP64) {  // split-BF16 cross-coupled products
+    CKT(tensor_tc_prepare(S));
+    const TLayout& H = S.T;
+    CKT(tc_split_on(S.tc_ops, S.tc_chunks + S.tc_nchunks, S.ph_lcc_nchunks, d_lcc, nullptr, S.tc_buf,
+                    S.tc_slice_elems));
+    for (size_t b = 0; b < H.cb_J3.size(); ++b) {
+      const int J3 = H.cb_J3[b], J4 = H.cb_J4[b], qa = H.cb_qa[b], qb = H.cb_qb[b];
+      const int r1 = L.cc_rlen[qa], r2 = L.cc_rlen[qb], nb1 = L.cc_nph[qa], nb2 = L.cc_nph[qb];
+      const bool dox = nb1 > 0, doy = nb2 > 0 && J3 != J4;
+      if (!dox && !doy) continue;
+      if (dox) {
+        k_tpandya<<<grid_n((int64_t)nb1 * r2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 2,
+                                                                 1.0 / std::sqrt(J3 + 1.0), S.ccr);
+        CKT(launched("k_tpandya"));
+      } else {
+        CKT(cuda(cudaMemsetAsync(S.wx, 0, sizeof(double) * (size_t)r1 * r2, stream), "memset(Wx)"));
+      }
+      if (doy) {
+        k_tpandya<<<grid_n((int64_t)r1 * nb2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 1,
+                                                                 1.0 / std::sqrt(J4 + 1.0), S.ccx);
+        CKT(launched("k_tpandya"));
+      }
+      CKT(tc_split_on(S.tc_ops, S.tc_chunks + S.ph_chunk_start[b], S.ph_chunk_n[b], S.ccr, S.ccx, S.tc_buf,
+                      S.tc_slice_elems));
+      TcOut out{};
+      out.f64[kOpW1] = S.wx;
+      out.f64[kOpW2] = S.wy;
+      CKT(tc_gemm_on(S.tc_map, S.tc_slice_rows, S.tc_probs, S.tc_tiles + S.ph_tile_start[b], S.ph_tile_n[b], out, hL,
+                     hR));
+      k_ts222ph_scatter<<<grid_n((int64_t)r1 * r2), 256, 0, stream>>>(D, T, S.wx, doy ? S.wy : nullptr, J3, J4, qa,
+                                                                      qb, hL, hR, RES);
+      CKT(launched("k_ts222ph_scatter"));
+    }
+  } else if (pieces & 64) {
     const TLayout& H = S.T;
     for (size_t b = 0; b < H.cb_J3.size(); ++b) {
       const int J3 = H.cb_J3[b], J4 = H.cb_J4[b], qa = H.cb_qa[b], qb = H.cb_qb[b];

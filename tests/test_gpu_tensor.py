@@ -46,8 +46,9 @@ def test_bch_tensor_matches_oracle(oracles, engines):
 @pytest.mark.parametrize("mode,tol", [("bf16x6", 2e-6), ("bf16x3", 2e-5)])
 @pytest.mark.parametrize("emax,rank", [(4, 4), (4, 2)])
 def test_tensor_ladder_on_tensor_cores(oracles, emax, rank, mode, tol):
-    """In a mixed mode the ladder's products through pp pairs run as split-BF16 tcgen05 GEMMs
-    (FP32 accumulate); the rest of the tensor commutator stays FP64."""
+    """In a mixed mode the ladder's products through pp pairs and the cross-coupled products of
+    the particle-hole term run as split-BF16 tcgen05 GEMMs (FP32 accumulate); the rest of the
+    tensor commutator stays FP64."""
     from imsrg_gb300 import Engine, make_basis
     from oracle.oracle import TensorOracle
     o = oracles(emax)
@@ -56,7 +57,7 @@ def test_tensor_ladder_on_tensor_cores(oracles, emax, rank, mode, tol):
     A, B = o.random(23, -1), t.random(24, 1)
     dA = eng.new_op(-1, A)
     dB = eng.new_tensor(rank, 0, 1, B)
-    for pieces in (32, 127):
+    for pieces in (32, 64, 127):
         ref = t.commutator(A, -1, B, 1, pieces)
         dR = eng.new_tensor(rank, 0, 1)
         eng.tensor_commutator(dA, dB, dR, pieces)
