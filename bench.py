@@ -531,7 +531,8 @@ def observables_workload(args, local: int):
     r2_fp64 = R64s.E0 / A
     peak = max(peak, used_gib())
     del G64, R64, R64s, eng64
-    # rank-2 tensor through BCH_TENSOR (FP64 tensor commutators) with the final Omega
+    # rank-2 tensor through BCH_TENSOR with the final Omega: in the flow's mixed mode (ladder and
+    # cross-coupled products on the tensor cores, the other pieces in FP32), then in FP64
     Q = q2_operator(eng, 4, coefs=Dhf)
     dQ = eng.new_tensor(4, 0, 1, Q)
     q0 = dQ.frob()
@@ -540,7 +541,20 @@ def observables_workload(args, local: int):
     eng.synchronize()
     t_q = time.perf_counter() - t
     q1 = dQ.frob()
+    q_mixed = dQ.download()
+    tslab = dQ.slab
     peak = max(peak, used_gib())
+    del dQ
+    e64q = Engine(b, device=local, precision="fp64")
+    G64q, dQ64 = e64q.new_op(-1, G_host), e64q.new_tensor(4, 0, 1, Q)
+    t = time.perf_counter()
+    n_q64 = e64q.bch_tensor(G64q, dQ64, 30, CONV)
+    e64q.synchronize()
+    t_q64 = time.perf_counter() - t
+    q_fp64 = dQ64.download()
+    peak = max(peak, used_gib())
+    del G64q, dQ64, e64q
+    dq_rel = float(np.linalg.norm(q_mixed - q_fp64) / np.linalg.norm(q_fp64))
     print(json.dumps({
         "metric": f"observables after a mixed-precision Magnus flow, eMax={emax}", "value": r2_mixed,
         "unit": "fm^2 (<r^2> per nucleon)", "n_gpus": 1, "steps": steps, "warmup": 0,
@@ -548,14 +562,15 @@ def observables_workload(args, local: int):
         "dtype": "bf16", "data": "synthetic",
         "config": {"workload": f"Magnus flow at eMax={emax} ({b.norbits} orbits) to s={args.ds * steps:g} with "
                                f"{args.mode} commutators (graph steps, BCH up to {args.obs_bch_max_terms - 1} terms), "
-                               "then BCH of r^2 (scalar) and r^2 Y2 (rank 2, FP64 tensor commutators)",
+                               "then BCH of r^2 (scalar) and r^2 Y2 (rank 2, tensor commutators in the same mode and in FP64)",
                    "reference_state": hf_rec,
                    "E0_final": e0s[-1], "E0_first_steps": e0s[:5], "mbpt2_final": crit[-1],
                    "flow_s": t_flow, "flow_commutators": counters["commutators"],
                    "r2_mixed_fm2": r2_mixed, "r2_fp64_fm2": r2_fp64, "d_r2_fm2": abs(r2_mixed - r2_fp64),
                    "r2_bare_fm2": R2[0] / A, "r2_bch_terms": n_r2, "r2_bch_s": t_r2,
                    "q2_norm_bare": q0, "q2_norm_evolved": q1, "q2_bch_terms": n_q, "q2_bch_s": t_q,
-                   "tensor_slab_doubles": dQ.slab, "peak_hbm_gib": round(peak - base, 2), **cmp},
+                   "q2_bch_terms_fp64": n_q64, "q2_bch_s_fp64": t_q64, "q2_mixed_vs_fp64_frob_rel": dq_rel,
+                   "tensor_slab_doubles": tslab, "peak_hbm_gib": round(peak - base, 2), **cmp},
     }), flush=True)
 
 

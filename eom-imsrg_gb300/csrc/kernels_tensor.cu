@@ -531,4 +531,116 @@ __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __res
   }
 }
 
+
+// ---------------------------------------------------------------- FP32 forms for the mixed modes
+// The same sums as k_ts122 / k_ts212 in FP32 (FP64 elements converted with integer
+// instructions, products and sums in FP32, the result added to the FP64 slab).
+namespace {
+__device__ __forceinline__ float d_six_tf(const DevTLayout& T, int J1, int J2, int j4, int j5, int j6) {
+  const int a = J1 >> 1, b = J2 >> 1, x = (j4 - 1) >> 1, y = (j5 - 1) >> 1, z = (j6 - 1) >> 1;
+  if (a < 0 || b < 0 || a >= T.six_nJ || b >= T.six_nJ || x < 0 || x >= T.six_nhx || y < 0 || y >= T.six_nh ||
+      z < 0 || z >= T.six_nh)
+    return 0.0f;
+  const int nh = T.six_nh;
+  return __ldg(T.six_f + (((size_t)a * T.six_nJ + b) * T.six_nhx + x) * nh * nh + (size_t)y * nh + z);
+}
+
+__device__ __forceinline__ float d_ftelem_f(const DevLayout& D, const DevTLayout& T, const double* op, int herm, int a,
+                                            int b) {
+  const int c1 = D.con[a], c2 = D.con[b];
+  if (c1 + c2 == 0) return f64_to_f32(op[T.off_fpp + D.loc[a] + (int64_t)D.loc[b] * D.P]);
+  if (c1 + c2 == 2) return f64_to_f32(op[T.off_fhh + D.loc[a] + (int64_t)D.loc[b] * D.A]);
+  if (c1 > c2) {
+    const float v = f64_to_f32(op[T.off_fph + D.loc[b] + (int64_t)D.loc[a] * D.P]);
+    const bool neg = (herm < 0) != ((((D.jj[a] - D.jj[b]) >> 1) & 1) != 0);
+    return neg ? -v : v;
+  }
+  return f64_to_f32(op[T.off_fph + D.loc[a] + (int64_t)D.loc[b] * D.P]);
+}
+
+__device__ __forceinline__ float d_velem_f(const DevLayout& D, const double* op, int herm, int a, int b, int c, int d,
+                                           int J) {
+  VRefF r;
+  return d_vref_f(D, a, b, c, d, J, r) ? f64_to_f32(op[r.idx]) * r.scale(herm) : 0.0f;
+}
+
+// tensor_elem in FP32: the position from d_tref, its factor (+-1, +-sqrt 2, +-2) in FP32
+__device__ __forceinline__ float d_telem_f(const DevLayout& D, const DevTLayout& T, const double* op, int herm, int a,
+                                           int b, int c, int d, int J1, int J2) {
+  TRef r;
+  if (!d_tref(D, T, herm, a, b, c, d, J1, J2, r)) return 0.0f;
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(r.f);
+  const bool neg = (bits >> 63) != 0;
+  // |f| is 1, sqrt 2 or 2 (sqrt 2 squared, possibly an ulp above 2)
+  const int e = (int)((bits >> 52) & 0x7FF) - 1023;
+  const float m = e >= 1 ? 2.0f : ((bits & 0xFFFFFFFFFFFFFull) ? 1.41421356f : 1.0f);
+  const float v = f64_to_f32(op[r.idx]) * m;
+  return neg ? -v : v;
+}
+}  // namespace
+
+__global__ void k_ts122f(DevLayout D, DevTLayout T, const double* __restrict__ L, int hL, const double* __restrict__ R,
+                         int hR, double* __restrict__ RES) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T.n2b; e += (int64_t)gridDim.x * blockDim.x) {
+    int q, g, a, b, c, d;
+    d_tdecode(D, T, e, q, g, a, b, c, d);
+    const int J1 = T.J1[q], J2 = T.J2[q];
+    float sm = 0.0f;
+    for (int t = 0, s0 = D.same_start[a], n = D.same_count[a]; t < n; ++t) {
+      const int i = D.same_list[s0 + t];
+      sm += d_f_elem_f(D, L, hL, a, i) * d_telem_f(D, T, R, hR, i, b, c, d, J1, J2);
+    }
+    for (int t = 0, s0 = D.same_start[b], n = D.same_count[b]; t < n; ++t) {
+      const int i = D.same_list[s0 + t];
+      sm += d_f_elem_f(D, L, hL, b, i) * d_telem_f(D, T, R, hR, a, i, c, d, J1, J2);
+    }
+    for (int t = 0, s0 = D.same_start[c], n = D.same_count[c]; t < n; ++t) {
+      const int i = D.same_list[s0 + t];
+      sm -= d_f_elem_f(D, L, hL, i, c) * d_telem_f(D, T, R, hR, a, b, i, d, J1, J2);
+    }
+    for (int t = 0, s0 = D.same_start[d], n = D.same_count[d]; t < n; ++t) {
+      const int i = D.same_list[s0 + t];
+      sm -= d_f_elem_f(D, L, hL, i, d) * d_telem_f(D, T, R, hR, a, b, c, i, J1, J2);
+    }
+    const float nrm = ((a == b) ? 0.70710678f : 1.0f) * ((c == d) ? 0.70710678f : 1.0f);
+    RES[T.goff[0] + e] = f32_to_f64(sm * nrm);
+  }
+}
+
+__global__ void k_ts212f(DevLayout D, DevTLayout T, const double* __restrict__ L, int hL, const double* __restrict__ R,
+                         int hR, double* __restrict__ RES) {
+  const int rank = T.rank;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T.n2b; e += (int64_t)gridDim.x * blockDim.x) {
+    int q, g, a, b, c, d;
+    d_tdecode(D, T, e, q, g, a, b, c, d);
+    const int J1 = T.J1[q], J2 = T.J2[q];
+    const int ja = D.jj[a], jb = D.jj[b], jc = D.jj[c], jd = D.jj[d];
+    float s1 = 0.0f, s2 = 0.0f, s3 = 0.0f, s4 = 0.0f;
+    for (int t = 0, s0 = T.tnb_start[a], n = T.tnb_count[a]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s1 -= d_six_tf(T, J1, J2, D.jj[i], ja, jb) * d_ftelem_f(D, T, R, hR, a, i) * d_velem_f(D, L, hL, i, b, c, d, J2);
+    }
+    for (int t = 0, s0 = T.tnb_start[b], n = T.tnb_count[b]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s2 += d_six_tf(T, J1, J2, D.jj[i], jb, ja) * d_ftelem_f(D, T, R, hR, b, i) * d_velem_f(D, L, hL, i, a, c, d, J2);
+    }
+    for (int t = 0, s0 = T.tnb_start[d], n = T.tnb_count[d]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s3 += d_six_tf(T, J1, J2, jd, D.jj[i], jc) * d_ftelem_f(D, T, R, hR, i, d) * d_velem_f(D, L, hL, a, b, c, i, J1);
+    }
+    for (int t = 0, s0 = T.tnb_start[c], n = T.tnb_count[c]; t < n; ++t) {
+      const int i = T.tnb_list[s0 + t];
+      s4 -= d_six_tf(T, J1, J2, jc, D.jj[i], jd) * d_ftelem_f(D, T, R, hR, i, c) * d_velem_f(D, L, hL, a, b, d, i, J1);
+    }
+    auto sg = [](int n) { return (n & 1) ? -1.0f : 1.0f; };
+    const float sm = s1 * sg((ja + jb - J2) >> 1) + s2 * sg((J1 + J2) >> 1) + s3 * sg((jc + jd - J1) >> 1) +
+                     s4 * sg((J2 + J1) >> 1);
+    // sqrt((J1+1)(J2+1)) / sqrt((1+d_ab)(1+d_cd)) (-1)^(rank/2), in FP32
+    const float f = sqrtf((float)((J1 + 1) * (J2 + 1))) * ((a == b) ? 0.70710678f : 1.0f) *
+                    ((c == d) ? 0.70710678f : 1.0f) * sg(rank >> 1);
+    double* X = RES + T.goff[0] + e;
+    *X = f32_to_f64(f64_to_f32(*X) + sm * f);
+  }
+}
+
 }  // namespace imsrg

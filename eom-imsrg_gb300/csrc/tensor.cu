@@ -27,6 +27,8 @@ __global__ void k_ts211(DevLayout D, DevTLayout T, const double* LCC, int hL, co
 __global__ void k_ts221(DevLayout D, DevTLayout T, const double* w1, const double* w2, int pm, double* RES, int hRES);
 __global__ void k_ts122(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
 __global__ void k_ts212(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_ts122f(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_ts212f(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
 __global__ void k_ts_pphh_update(int64_t n, int64_t off, double* RES, const double* w1, const double* w2);
 __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* R, int hR, int J3, int J4, int qa, int qb, int term,
                           double scale, double* out);
@@ -185,6 +187,8 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
   pk.add(T.ob_kind, &d.ob_kind); pk.add(T.ob_p, &d.ob_p); pk.add(T.ob_q, &d.ob_q); pk.add(T.ob_pk, &d.ob_pk);
   pk.add(T.ob_qk, &d.ob_qk);
   pk.add(T.six, &d.six); pk.add(T.six_m, &d.six_m); pk.add(T.ccnb, &d.ccnb);
+  const std::vector<float> six_f(T.six.begin(), T.six.end());
+  pk.add(six_f, &d.six_f);
   pk.add(T.tnb_start, &d.tnb_start); pk.add(T.tnb_count, &d.tnb_count); pk.add(T.tnb_list, &d.tnb_list);
   pk.add(pphh, &st->pphh_p); pk.add(pphh_tiles, &st->pphh_t);
   pk.add(cbp, &st->cb_p); pk.add(cbt, &st->cb_t);
@@ -389,11 +393,17 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
     CKT(launched("k_ts211"));
   }
   if ((pieces & 8) && T.n2b) {
-    k_ts122<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+    if (precision != IMSRG_PREC_FP64)
+      k_ts122f<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+    else
+      k_ts122<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
     CKT(launched("k_ts122"));
   }
   if ((pieces & 16) && T.n2b) {
-    k_ts212<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+    if (precision != IMSRG_PREC_FP64)
+      k_ts212f<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+    else
+      k_ts212<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
     CKT(launched("k_ts212"));
   }
   if ((pieces & 32) && precision != IMSRG_PREC_FP64) {  // split-BF16 products through pp pairs

@@ -78,6 +78,7 @@ struct DevTLayout {
   const int* ob_qk;
   const double* six;
   const double* six_m;
+  const float* six_f;  // six in FP32
   const int* ccnb;
   const int* tnb_start;
   const int* tnb_count;
