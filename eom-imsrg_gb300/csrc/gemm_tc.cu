@@ -509,6 +509,7 @@ struct TcState {
   int g122_tiny_cap = 64, g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
   // tuned launch parameters (imsrg_autotune): CTAs of the recoupling kernel, GEMM tile order
   int recouple_ctas = 152 * 16;
+  int recouple_minb = 4;  // launch-bounds variant of k_recouple_y
   int gemm_order = 0;  // 0: longest K first, 1: problem order
   std::vector<TcTile> pphh_tiles_lpt, z_tiles_lpt;
   std::vector<int> g_start, g_n, g_orb, g_b1, g_b2, g_blk_off;
@@ -941,7 +942,7 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   if (!tc->quads.empty()) {
     const int64_t nq = (int64_t)tc->quads.size();
     const int grid = (int)std::min<int64_t>((nq + 255) / 256, tc->recouple_ctas);
-    k_recouple_y<<<grid, 256, 0, stream>>>(D, tc->d_quads, nq, tc->zbuf, tc->ybuf, RES, hL * hR);
+    launch_recouple_y(tc->recouple_minb, grid, stream, D, tc->d_quads, nq, tc->zbuf, tc->ybuf, RES, hL * hR);
     CK_TC(launched("k_recouple_y"));
   }
   if (!upd_tiles.empty()) {
@@ -1048,7 +1049,16 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
       if (ms < best) { best = ms; bt = c[0]; bs = c[1]; }
     }
     if (st != IMSRG_OK || (st = tc_g122_partition(bt, bs)) != IMSRG_OK) break;
-    // recoupling CTAs
+    // recoupling: launch-bounds variant, then CTAs
+    int bm = tc->recouple_minb;
+    for (int minb : {4, 5, 6, 8}) {
+      tc->recouple_minb = minb;
+      float ms;
+      if ((st = time_one(&ms)) != IMSRG_OK) break;
+      if (ms < best) { best = ms; bm = minb; }
+    }
+    tc->recouple_minb = bm;
+    if (st != IMSRG_OK) break;
     int br = tc->recouple_ctas;
     for (int mult : {4, 8, 16, 32}) {
       tc->recouple_ctas = tc->num_sms * mult;
@@ -1073,6 +1083,7 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
       info->tiny_cap = tc->g122_tiny_cap;
       info->small_cap = tc->g122_small;
       info->recouple_ctas = tc->recouple_ctas;
+      info->recouple_min_blocks = tc->recouple_minb;
       info->gemm_order = tc->gemm_order;
       info->ms_before = base;
       info->ms_after = after;

@@ -52,8 +52,9 @@ __global__ void k_comm122_groups_cta(DevLayout D, PairGroupsDev G, int nmax4, in
 __global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
                                 float pm);
 __global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);
-__global__ void k_recouple_y(DevLayout D, const uint64_t* quads, int64_t nquads, const float* Z, const float* Y,
-                             double* RES, int pm);
+// k_recouple_y with launch bounds (256, min_blocks), min_blocks 4, 5, 6 or 8
+void launch_recouple_y(int min_blocks, int grid, cudaStream_t st, const DevLayout& D, const uint64_t* quads,
+                       int64_t nquads, const float* Z, const float* Y, double* RES, int pm);
 __global__ void k_comm222ph_z(DevLayout D, const float* Z, double* RES, int hRES);
 __global__ void k_recouple_quad(DevLayout D, const uint64_t* quads, int64_t nquads, const float* Z, double* RES, int hRES);
 

@@ -379,7 +379,10 @@ __global__ void k_recouple_quad(DevLayout D, const uint64_t* __restrict__ quads,
 // whose rows advance with j; quadruples are ordered j fastest and the J' and J loops are
 // warp-uniform, so each warp reads consecutive rows of one channel matrix and writes
 // consecutive rows of one RES column.  Upper triangles only (mirror pass afterwards).
-__global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t* __restrict__ quads, int64_t nquads,
+// kMinBlocks: the resident-CTA hint of the launch bounds (registers traded for occupancy),
+// one of the choices of the autotuner
+template <int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_recouple_y(DevLayout D, const uint64_t* __restrict__ quads, int64_t nquads,
                                                     const float* __restrict__ Z, const float* __restrict__ Y,
                                                     double* __restrict__ RES, int pm) {
   const int lane = threadIdx.x & 31;
@@ -461,6 +464,16 @@ __global__ void __launch_bounds__(256) k_recouple_y(DevLayout D, const uint64_t*
   }
 }
 
+
+void launch_recouple_y(int min_blocks, int grid, cudaStream_t st, const DevLayout& D, const uint64_t* quads,
+                       int64_t nquads, const float* Z, const float* Y, double* RES, int pm) {
+  switch (min_blocks) {
+    case 5: k_recouple_y<5><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
+    case 6: k_recouple_y<6><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
+    case 8: k_recouple_y<8><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
+    default: k_recouple_y<4><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
+  }
+}
 
 // ---------------------------------------------------------------- commutator_122 by pair groups
 // commutator_122 (src/commutators.f90:283-396) of one group-pair sub-block (G1 <= G2) of

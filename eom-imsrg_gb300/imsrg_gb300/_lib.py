@@ -39,7 +39,8 @@ class HFInfo_t(C.Structure):
 
 class TuneInfo_t(C.Structure):
     _fields_ = [("tiny_cap", C.c_int32), ("small_cap", C.c_int32), ("recouple_ctas", C.c_int32),
-                ("gemm_order", C.c_int32), ("ms_before", C.c_double), ("ms_after", C.c_double)]
+                ("gemm_order", C.c_int32), ("recouple_min_blocks", C.c_int32), ("ms_before", C.c_double),
+                ("ms_after", C.c_double)]
 
 
 class StepInfo_t(C.Structure):

@@ -86,13 +86,15 @@ imsrg_status imsrg_synchronize(imsrg_ctx* ctx);
  * no GPU path).  In a mixed mode it times one commutator [L, R] into RES per candidate on
  * this basis and keeps the fastest, one knob at a time: the size caps that send the
  * commutator_122 sub-blocks to 8-lane groups, warps or CTAs; the CTA count of the
- * particle-hole recoupling; the tile order of the persistent tcgen05 GEMMs.  The result of a
+ * particle-hole recoupling and its register / occupancy variant; the tile order of the
+ * persistent tcgen05 GEMMs.  The result of a
  * commutator does not depend on these choices.  A captured Magnus-step graph is dropped and
  * re-captured by the next step.  IMSRG_ERR_UNSUPPORTED in FP64 mode. */
 typedef struct {
   int32_t tiny_cap, small_cap; /* sub-blocks up to tiny_cap elements: 8 lanes; up to small_cap: a warp */
   int32_t recouple_ctas;       /* CTAs of the recoupling kernel */
   int32_t gemm_order;          /* 0: tiles with the longest K first, 1: problem order */
+  int32_t recouple_min_blocks; /* launch-bounds variant of the recoupling kernel: 4, 5, 6 or 8 CTAs per SM */
   double ms_before, ms_after;  /* one commutator before and after tuning */
 } imsrg_tune_info;
 imsrg_status imsrg_autotune(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES,

@@ -22,7 +22,7 @@ def test_autotune_keeps_results_and_reports_choice(built_lib, oracles):
     before = dR.download()
     info = eng.autotune(dA, dB, dR)
     assert (info["tiny_cap"], info["small_cap"]) in {(16, 256), (32, 128), (32, 256), (64, 256), (64, 512)}
-    assert info["gemm_order"] in (0, 1) and info["recouple_ctas"] > 0
+    assert info["gemm_order"] in (0, 1) and info["recouple_ctas"] > 0 and info["recouple_min_blocks"] in (4, 5, 6, 8)
     assert info["ms_before"] > 0 and info["ms_after"] > 0
     eng.commutator(dA, dB, dR)
     assert np.array_equal(dR.download(), before)
