@@ -50,6 +50,129 @@ inline double sgn(int n) { return (n & 1) ? -1.0 : 1.0; }
 
 namespace {
 
+// one (n, l, j) of an me2j file: a proton / neutron pair of the pn basis
+struct IsoOrbit {
+  int n, l, j;
+};
+
+// the isospin orbits of an me2j file for eMax, in hk order
+std::vector<IsoOrbit> file_orbits(int emax) {
+  std::vector<IsoOrbit> v;
+  for (int e = 0; e <= emax; ++e)
+    for (int l = e % 2; l <= e; l += 2)
+      for (int j2 : {2 * l - 1, 2 * l + 1})
+        if (j2 >= 1) v.push_back(IsoOrbit{(e - l) / 2, l, j2});
+  return v;
+}
+
+// Visits every record of the me2j loop (src/interaction_IO.f90:320-352): isospin orbits
+// I1 >= I2, I3 <= I1 (I4 <= I2 when I3 == I1), equal parity, each J in the overlap of the
+// two couplings.  Each record holds four values: T=0, then T=1 with Mt = -1, 0, +1.
+template <class F>
+void for_each_record(const std::vector<IsoOrbit>& iso, F&& f) {
+  const int M = (int)iso.size();
+  for (int I1 = 0; I1 < M; ++I1)
+    for (int I2 = 0; I2 <= I1; ++I2)
+      for (int I3 = 0; I3 <= I1; ++I3) {
+        const int end = (I1 == I3) ? I2 : I3;
+        for (int I4 = 0; I4 <= end; ++I4) {
+          if ((iso[I1].l + iso[I2].l) % 2 != (iso[I3].l + iso[I4].l) % 2) continue;
+          const int jmin = std::max(std::abs(iso[I1].j - iso[I2].j), std::abs(iso[I3].j - iso[I4].j));
+          const int jmax = std::min(iso[I1].j + iso[I2].j, iso[I3].j + iso[I4].j);
+          for (int JT = jmin; JT <= jmax; JT += 2) f(I1, I2, I3, I4, JT);
+        }
+      }
+}
+
+int64_t record_values(const std::vector<IsoOrbit>& iso) {
+  int64_t n = 0;
+  for_each_record(iso, [&](int, int, int, int, int) { n += 4; });
+  return n;
+}
+
+// Seeded synthetic record values: T=0 and T=1 drawn from N(0, v_scale) times
+// exp(-(e1+e2+e3+e4)/eMax), T=1 shared by Mt = -1, 0, +1, zero where two identical orbits
+// would need J + T even.
+std::vector<double> synthetic_values(const imsrg::Layout& L, const std::vector<IsoOrbit>& iso, uint64_t seed,
+                                     double v_scale) {
+  const double emax = L.eMax > 0 ? (double)L.eMax : 1.0;
+  Normal rng(seed);
+  std::vector<double> v;
+  v.reserve((size_t)record_values(iso));
+  auto e_of = [&](int I) { return 2 * iso[I].n + iso[I].l; };
+  for_each_record(iso, [&](int I1, int I2, int I3, int I4, int JT) {
+    const double scale = v_scale * std::exp(-(e_of(I1) + e_of(I2) + e_of(I3) + e_of(I4)) / emax);
+    const int J = JT / 2;
+    double g0 = rng.gauss() * scale, g1 = rng.gauss() * scale;
+    if ((I1 == I2 || I3 == I4) && ((J + 0) % 2 == 0)) g0 = 0.0;
+    if ((I1 == I2 || I3 == I4) && ((J + 1) % 2 == 0)) g1 = 0.0;
+    v.push_back(g0); v.push_back(g1); v.push_back(g1); v.push_back(g1);
+  });
+  return v;
+}
+
+// The proton-neutron J-scheme two-body arrays from me2j record values
+// (src/interaction_IO.f90:398-555, without the centre-of-mass term of Htype 1): records whose
+// orbits are not all in the basis are skipped.
+void me2j_convert(const imsrg::Layout& L, const std::vector<IsoOrbit>& iso, const double* values, double* H) {
+  const int N = L.N, NJ = L.NJ;
+  std::vector<int> proton((size_t)iso.size(), -1);  // the basis index of the proton orbit of I
+  for (size_t I = 0; I < iso.size(); ++I)
+    for (int k = 0; k + 1 < N; ++k)
+      if (L.tz[k] == -1 && L.nn[k] == iso[I].n && L.ll[k] == iso[I].l && L.jj[k] == iso[I].j &&
+          L.tz[k + 1] == 1 && L.nn[k + 1] == iso[I].n && L.ll[k + 1] == iso[I].l && L.jj[k + 1] == iso[I].j) {
+        proton[I] = k;
+        break;
+      }
+  int64_t pos = 0;
+  for_each_record(iso, [&](int I1, int I2, int I3, int I4, int JT) {
+    const double* me = values + pos;
+    pos += 4;
+    if (proton[I1] < 0 || proton[I2] < 0 || proton[I3] < 0 || proton[I4] < 0) return;
+    const int J = JT / 2;
+    const int Par = (iso[I1].l + iso[I2].l) % 2;
+    for (int ax = proton[I1]; ax <= proton[I1] + 1; ++ax)
+      for (int bx = proton[I2]; bx <= proton[I2] + 1; ++bx)
+        for (int cx = proton[I3]; cx <= proton[I3] + 1; ++cx)
+          for (int dx = proton[I4]; dx <= proton[I4] + 1; ++dx) {
+            const int a = ax, b = bx, cc = cx, d = dx;
+            double pre2 = 1.0;
+            if (a == b) pre2 *= std::sqrt(0.5);
+            if (cc == d) pre2 *= std::sqrt(0.5);
+            // me2j files label isospin with the opposite sign
+            const int ta = -L.tz[a], tb = -L.tz[b], tc = -L.tz[cc], td = -L.tz[d];
+            if (tc + td != ta + tb) continue;
+            const int T = -(ta + tb) / 2;
+            const int q = L.block(JT, T, Par);
+            double V = 0.125 * (ta - tb) * (tc - td) * me[0] +
+                       ((ta + tb == -2) && (tc + td == -2) ? me[1] : 0.0) +
+                       ((ta + tb == 2) && (tc + td == 2) ? me[3] : 0.0) +
+                       0.125 * std::abs((ta - tb) * (tc - td)) * me[2];
+            V *= pre2;
+            const int C1 = L.con[a] + L.con[b], C2 = L.con[cc] + L.con[d];
+            static const int tab[3][3] = {{0, 1, 2}, {1, 3, 5}, {2, 5, 4}};
+            const int g = tab[C1][C2];
+            double pre = 1.0;
+            int i1, i2;
+            if (a > b) { i1 = L.pairpos[((size_t)b * N + a) * NJ + J]; pre = sgn(1 + (L.jj[a] + L.jj[b] - JT) / 2); }
+            else i1 = L.pairpos[((size_t)a * N + b) * NJ + J];
+            if (cc > d) { i2 = L.pairpos[((size_t)d * N + cc) * NJ + J]; pre *= sgn(1 + (L.jj[cc] + L.jj[d] - JT) / 2); }
+            else i2 = L.pairpos[((size_t)cc * N + d) * NJ + J];
+            if (i1 < 0 || i2 < 0) continue;
+            double* X = H + L.goff[q * 6 + g];
+            const int n1 = L.gn1[q * 6 + g];
+            if (g == 0 || g == 4 || g == 3) {
+              X[i2 + (int64_t)i1 * n1] = V * pre;
+              X[i1 + (int64_t)i2 * n1] = V * pre;
+            } else if (C1 > C2) {
+              X[i2 + (int64_t)i1 * n1] = V * pre;
+            } else {
+              X[i1 + (int64_t)i2 * n1] = V * pre;
+            }
+          }
+  });
+}
+
 imsrg_status synthetic(imsrg_ctx* ctx, uint64_t seed, double v_scale, bool bare, double* out) {
   if (!ctx || !out) return IMSRG_ERR_INVALID_ARGUMENT;
   Ctx* c = reinterpret_cast<Ctx*>(ctx);
@@ -62,73 +185,10 @@ imsrg_status synthetic(imsrg_ctx* ctx, uint64_t seed, double v_scale, bool bare,
     if (L.tz[k] != -1 || L.tz[k + 1] != 1 || L.nn[k] != L.nn[k + 1] || L.ll[k] != L.ll[k + 1] || L.jj[k] != L.jj[k + 1])
       return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "orbits are not in proton/neutron pairs (hk order)");
   std::vector<double> H((size_t)L.slab, 0.0);
-  const int M = N / 2;
-  const double emax = L.eMax > 0 ? (double)L.eMax : 1.0;
-  Normal rng(seed);
-  auto e_of = [&](int I) { return 2 * L.nn[2 * I] + L.ll[2 * I]; };
-  for (int I1 = 0; I1 < M; ++I1)
-    for (int I2 = 0; I2 <= I1; ++I2)
-      for (int I3 = 0; I3 <= I1; ++I3) {
-        const int end = (I1 == I3) ? I2 : I3;
-        for (int I4 = 0; I4 <= end; ++I4) {
-          const int l1 = L.ll[2 * I1], l2 = L.ll[2 * I2], l3 = L.ll[2 * I3], l4 = L.ll[2 * I4];
-          if ((l1 + l2) % 2 != (l3 + l4) % 2) continue;
-          const int j1 = L.jj[2 * I1], j2 = L.jj[2 * I2], j3 = L.jj[2 * I3], j4 = L.jj[2 * I4];
-          const int jmin = std::max(std::abs(j1 - j2), std::abs(j3 - j4));
-          const int jmax = std::min(j1 + j2, j3 + j4);
-          if (jmin > jmax) continue;
-          const int Par = (l1 + l2) % 2;
-          const double scale = v_scale * std::exp(-(e_of(I1) + e_of(I2) + e_of(I3) + e_of(I4)) / emax);
-          for (int JT = jmin; JT <= jmax; JT += 2) {
-            const int J = JT / 2;
-            double me[4];
-            double g0 = rng.gauss() * scale, g1 = rng.gauss() * scale;
-            // Pauli: an antisymmetric state of two identical orbits needs J + T odd
-            if ((I1 == I2 || I3 == I4) && ((J + 0) % 2 == 0)) g0 = 0.0;
-            if ((I1 == I2 || I3 == I4) && ((J + 1) % 2 == 0)) g1 = 0.0;
-            me[0] = g0; me[1] = g1; me[2] = g1; me[3] = g1;
-            for (int ax = 2 * I1; ax <= 2 * I1 + 1; ++ax)
-              for (int bx = 2 * I2; bx <= 2 * I2 + 1; ++bx)
-                for (int cx = 2 * I3; cx <= 2 * I3 + 1; ++cx)
-                  for (int dx = 2 * I4; dx <= 2 * I4 + 1; ++dx) {
-                    const int a = ax, b = bx, cc = cx, d = dx;
-                    double pre2 = 1.0;
-                    if (a == b) pre2 *= std::sqrt(0.5);
-                    if (cc == d) pre2 *= std::sqrt(0.5);
-                    // me2j files label isospin with the opposite sign
-                    const int ta = -L.tz[a], tb = -L.tz[b], tc = -L.tz[cc], td = -L.tz[d];
-                    if (tc + td != ta + tb) continue;
-                    const int T = -(ta + tb) / 2;
-                    const int q = L.block(JT, T, Par);
-                    double V = 0.125 * (ta - tb) * (tc - td) * me[0] +
-                               ((ta + tb == -2) && (tc + td == -2) ? me[1] : 0.0) +
-                               ((ta + tb == 2) && (tc + td == 2) ? me[3] : 0.0) +
-                               0.125 * std::abs((ta - tb) * (tc - td)) * me[2];
-                    V *= pre2;
-                    const int C1 = L.con[a] + L.con[b], C2 = L.con[cc] + L.con[d];
-                    static const int tab[3][3] = {{0, 1, 2}, {1, 3, 5}, {2, 5, 4}};
-                    const int g = tab[C1][C2];
-                    double pre = 1.0;
-                    int i1, i2;
-                    if (a > b) { i1 = L.pairpos[((size_t)b * N + a) * NJ + J]; pre = sgn(1 + (L.jj[a] + L.jj[b] - JT) / 2); }
-                    else i1 = L.pairpos[((size_t)a * N + b) * NJ + J];
-                    if (cc > d) { i2 = L.pairpos[((size_t)d * N + cc) * NJ + J]; pre *= sgn(1 + (L.jj[cc] + L.jj[d] - JT) / 2); }
-                    else i2 = L.pairpos[((size_t)cc * N + d) * NJ + J];
-                    if (i1 < 0 || i2 < 0) continue;
-                    double* X = H.data() + L.goff[q * 6 + g];
-                    const int n1 = L.gn1[q * 6 + g];
-                    if (g == 0 || g == 4 || g == 3) {
-                      X[i2 + (int64_t)i1 * n1] = V * pre;
-                      X[i1 + (int64_t)i2 * n1] = V * pre;
-                    } else if (C1 > C2) {
-                      X[i2 + (int64_t)i1 * n1] = V * pre;
-                    } else {
-                      X[i1 + (int64_t)i2 * n1] = V * pre;
-                    }
-                  }
-          }
-        }
-      }
+  std::vector<IsoOrbit> iso;
+  for (int k = 0; k < N; k += 2) iso.push_back(IsoOrbit{L.nn[k], L.ll[k], L.jj[k]});
+  const std::vector<double> values = synthetic_values(L, iso, seed, v_scale);
+  me2j_convert(L, iso, values.data(), H.data());
 
   // one-body kinetic energy (Htype 1), with the reference's FP32 intermediate literals
   const double hw = L.hw;
@@ -211,4 +271,51 @@ extern "C" imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t see
 extern "C" imsrg_status imsrg_synthetic_bare_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale,
                                                           double* out) {
   return synthetic(ctx, seed, v_scale, true, out);
+}
+
+namespace {
+imsrg_status check_pairs(Ctx* c, std::vector<IsoOrbit>& iso) {
+  const imsrg::Layout& L = c->L;
+  if (L.N % 2) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "me2j records need proton/neutron orbit pairs");
+  for (int k = 0; k < L.N; k += 2) {
+    if (L.tz[k] != -1 || L.tz[k + 1] != 1 || L.nn[k] != L.nn[k + 1] || L.ll[k] != L.ll[k + 1] ||
+        L.jj[k] != L.jj[k + 1])
+      return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "orbits are not in proton/neutron pairs (hk order)");
+    iso.push_back(IsoOrbit{L.nn[k], L.ll[k], L.jj[k]});
+  }
+  return IMSRG_OK;
+}
+}  // namespace
+
+extern "C" imsrg_status imsrg_synthetic_me2j_values(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* values,
+                                                    int64_t* n) {
+  if (!ctx || !n) return IMSRG_ERR_INVALID_ARGUMENT;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  std::vector<IsoOrbit> iso;
+  const imsrg_status st = check_pairs(c, iso);
+  if (st != IMSRG_OK) return st;
+  const int64_t count = record_values(iso);
+  if (!values) {
+    *n = count;
+    return IMSRG_OK;
+  }
+  if (*n < count) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "values buffer too small");
+  const std::vector<double> v = synthetic_values(c->L, iso, seed, v_scale);
+  std::memcpy(values, v.data(), sizeof(double) * v.size());
+  *n = count;
+  return IMSRG_OK;
+}
+
+extern "C" imsrg_status imsrg_me2j_to_slab(imsrg_ctx* ctx, const double* values, int64_t n, int32_t emax_file,
+                                           double* host_slab) {
+  if (!ctx || !values || !host_slab || emax_file < 0) return IMSRG_ERR_INVALID_ARGUMENT;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  std::vector<IsoOrbit> mine;
+  const imsrg_status st = check_pairs(c, mine);
+  if (st != IMSRG_OK) return st;
+  const std::vector<IsoOrbit> iso = file_orbits(emax_file);
+  if (record_values(iso) != n)
+    return c->fail(IMSRG_ERR_MISMATCH, "value count does not match the me2j records of emax_file");
+  me2j_convert(c->L, iso, values, host_slab);
+  return IMSRG_OK;
 }

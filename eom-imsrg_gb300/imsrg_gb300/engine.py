@@ -291,6 +291,25 @@ class Engine:
     def read_omega_checkpoint(self, G: SqOp, path: str):
         self._ck(self.L.imsrg_read_omega_checkpoint(self.h, G.h, str(path).encode()))
 
+    # ---------------------------------------------------------------- me2j interaction records
+    def synthetic_me2j_values(self, seed: int = 1, v_scale: float = 1.0) -> np.ndarray:
+        """The synthetic interaction as me2j record values (4 per record, file order)."""
+        n = C.c_int64()
+        self._ck(self.L.imsrg_synthetic_me2j_values(self.h, C.c_uint64(seed), float(v_scale), None, C.byref(n)))
+        out = np.zeros(n.value)
+        self._ck(self.L.imsrg_synthetic_me2j_values(self.h, C.c_uint64(seed), float(v_scale), out.ctypes.data,
+                                                    C.byref(n)))
+        return out
+
+    def me2j_to_slab(self, values: np.ndarray, emax_file: int, slab: np.ndarray | None = None) -> np.ndarray:
+        """read_me2j_interaction (src/interaction_IO.f90:282-557) of record values into the
+        two-body arrays of a host slab (a new zero slab by default)."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        out = np.zeros(self.slab) if slab is None else slab
+        self._ck(self.L.imsrg_me2j_to_slab(self.h, values.ctypes.data, int(values.size), int(emax_file),
+                                           out.ctypes.data))
+        return out
+
     # ---------------------------------------------------------------- Hartree-Fock
     def calc_hf(self, H: SqOp, max_iter: int = 1000):
         """calc_HF (src/HF_mod.f90:14-105): H (bare) becomes the normal-ordered HF-basis

@@ -281,6 +281,17 @@ imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v
  * and calculate_h0_harm_osc (src/main_IMSRG.f90:125-157): the kinetic energy in fhh/fpp/fph, V in
  * the two-body arrays, E0 = 0. */
 imsrg_status imsrg_synthetic_bare_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* host_slab);
+/* The interaction of the synthetic Hamiltonian as me2j record values: four per record (T=0, then
+ * T=1 with Mt = -1, 0, +1) in the loop order of read_me2j_interaction (src/interaction_IO.f90:
+ * 320-352) over this basis's isospin orbits.  values NULL: *n receives the count. */
+imsrg_status imsrg_synthetic_me2j_values(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* values, int64_t* n);
+/* read_me2j_interaction (src/interaction_IO.f90:282-557) from the record values of an me2j file
+ * for eMax_file (the caller decompresses and parses the text): the proton-neutron J-scheme
+ * two-body arrays of host_slab, for the records whose orbits are all in this basis.  The
+ * centre-of-mass term of Htype 1 is not added; the rest of the slab is untouched.
+ * IMSRG_ERR_MISMATCH when n is not the record count of eMax_file. */
+imsrg_status imsrg_me2j_to_slab(imsrg_ctx* ctx, const double* values, int64_t n, int32_t emax_file,
+                                double* host_slab);
 
 /* ---- Hartree-Fock and normal ordering (FP64).  The self-consistency loop runs on the host
  * (blocks of orbits sharing (l, j, tz), at most eMax/2+1 orbits each, cyclic Jacobi in place of

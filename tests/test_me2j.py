@@ -1,0 +1,68 @@
+"""me2j interaction records: the format and read_me2j_interaction's conversion
+(src/interaction_IO.f90:282-557) on the CPU.
+
+The synthetic Hamiltonian is built from seeded me2j record values through the same
+conversion, so converting those values reproduces its two-body part exactly; a file written
+in the me2j layout reads back to the values rounded to the format's 7 decimals; the records of
+a larger file that fall outside the basis are skipped."""
+import numpy as np
+import pytest
+
+from helpers import rel_err
+
+
+def _two_body(eng, slab):
+    b = eng.basis
+    A, P = b.nholes, b.norbits - b.nholes
+    return slab[1 + A * A + P * P + P * A:]
+
+
+@pytest.mark.parametrize("emax", [2, 4])
+def test_synthetic_values_reproduce_the_hamiltonian(built_lib, emax):
+    from imsrg_gb300 import Engine, make_basis
+    eng = Engine(make_basis(emax), device=-1)
+    vals = eng.synthetic_me2j_values(seed=5)
+    assert vals.size % 4 == 0 and np.count_nonzero(vals) > vals.size // 2
+    slab = eng.me2j_to_slab(vals, emax)
+    assert np.array_equal(_two_body(eng, slab), _two_body(eng, eng.synthetic_bare_hamiltonian(seed=5)))
+
+
+def test_file_round_trip(built_lib, tmp_path):
+    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300.me2j import read_me2j, write_me2j
+    eng = Engine(make_basis(4), device=-1)
+    vals = eng.synthetic_me2j_values(seed=6)
+    path = str(tmp_path / "synthetic_eMax04_hwHO020.me2j.gz")
+    write_me2j(path, vals)
+    back = read_me2j(path)
+    assert back.size == vals.size and np.abs(back - np.round(vals, 7)).max() < 1e-12
+    slab = eng.me2j_to_slab(back, 4)
+    ref = eng.synthetic_bare_hamiltonian(seed=6)
+    assert rel_err(_two_body(eng, slab), _two_body(eng, ref)) < 1e-6
+
+
+def test_larger_file_restricted_to_the_basis(built_lib, oracles):
+    """Records of an eMax=4 file read into the eMax=2 basis give the same elements as in the
+    eMax=4 basis"""
+    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300._lib import ImsrgError
+    big, small = Engine(make_basis(4), device=-1), Engine(make_basis(2), device=-1)
+    vals = big.synthetic_me2j_values(seed=7)
+    V4, V2 = big.me2j_to_slab(vals, 4), small.me2j_to_slab(vals, 4)
+    o4, o2 = oracles(4), oracles(2)
+    b2 = small.basis
+    # hk order: the eMax=2 orbits are the first ones of the eMax=4 basis
+    n = b2.norbits
+    checked = 0
+    for a in range(n):
+        for b in range(n):
+            for c in range(n):
+                for d in range(n):
+                    for J in range(0, 2 * int(b2.jj.max()) + 1, 2):
+                        v2 = o2.v_elem(V2, 1, a, b, c, d, J)
+                        assert abs(v2 - o4.v_elem(V4, 1, a, b, c, d, J)) < 1e-13
+                        checked += v2 != 0.0
+    assert checked > 100
+    with pytest.raises(ImsrgError) as e:
+        small.me2j_to_slab(vals[:-4], 4)
+    assert e.value.code == 5
