@@ -7,7 +7,8 @@
 //    v_scale * N(0,1) * exp(-(e1+e2+e3+e4)/eMax), the T=1 value shared by Mt=-1,0,+1
 //    (isospin symmetric), Pauli-forbidden records (identical orbits, J+T even) zero;
 //  * one-body part: the harmonic-oscillator kinetic energy with the intrinsic (1-1/A)
-//    factor (calculate_h0_harm_osc with Htype 1, src/basic_IMSRG.f90:2093-2191);
+//    factor (calculate_h0_harm_osc with Htype 1, src/basic_IMSRG.f90:2093-2191), and the
+//    two-body centre-of-mass term -p1.p2 hw/A that read_me2j_interaction adds for Htype 1;
 //  * normal ordering with respect to the reference state (normal_order,
 //    src/basic_IMSRG.f90:2419-2550), i.e. the HO-basis reference of calc_HO.
 #include <algorithm>
@@ -111,10 +112,47 @@ std::vector<double> synthetic_values(const imsrg::Layout& L, const std::vector<I
   return v;
 }
 
+// reduced_p / reduced_r (src/basic_IMSRG.f90:4567-4656): <a||p||b>, <a||r||b> of the HO
+// orbits in oscillator units
+double reduced_pr(const imsrg::Layout& L, int a, int b, bool momentum) {
+  const int la = L.ll[a], lb = L.ll[b], na = L.nn[a], nb = L.nn[b];
+  double c1 = 0.0, p1 = 0.0;
+  if (la == lb + 1) {
+    c1 = std::sqrt(lb + 1.0);
+    if (na == nb) p1 = (momentum ? -1.0 : 1.0) * std::sqrt(nb + lb + 1.5);
+    else if (na == nb - 1) p1 = -std::sqrt(nb * 1.0);
+  } else if (la == lb - 1) {
+    c1 = -std::sqrt(1.0 * lb);
+    if (na == nb) p1 = std::sqrt(nb + lb + 0.5);
+    else if (na == nb + 1) p1 = (momentum ? 1.0 : -1.0) * std::sqrt(nb + 1.0);
+  }
+  return p1 * c1;
+}
+
+// p1_p2 / r1_r2 (src/basic_IMSRG.f90:4445-4565): the normalised antisymmetrised J-coupled
+// matrix element of p1.p2 (or r1.r2) in oscillator units
+double two_body_dot(const imsrg::Layout& L, int a, int b, int c, int d, int J, bool momentum) {
+  const int ja = L.jj[a], jb = L.jj[b], jc = L.jj[c], jd = L.jj[d];
+  auto one = [&](int x, int y) {  // sqrt((jx+1)(jy+1)) (-1)^((3+2lx+jy)/2) {jx 1 jy; ly 1/2 lx} <x||.||y>
+    if (L.tz[x] != L.tz[y]) return 0.0;
+    return std::sqrt((L.jj[x] + 1.0) * (L.jj[y] + 1.0)) * sgn((3 + 2 * L.ll[x] + L.jj[y]) / 2) *
+           imsrg::sixj_racah(L.jj[x], 2, L.jj[y], 2 * L.ll[y], 1, 2 * L.ll[x]) * reduced_pr(L, x, y, momentum);
+  };
+  const double j_ac = one(a, c), j_bd = one(b, d), j_ad = one(a, d), j_bc = one(b, c);
+  const int s1 = momentum ? (jb - jc - J) / 2 : (jb + jc - J) / 2;
+  const int s2 = momentum ? (jb - jd - J) / 2 : (jb + jd - J) / 2;
+  const double v = sgn(s1) * imsrg::sixj_racah(ja, jb, J, jd, jc, 2) * j_ac * j_bd -
+                   sgn((jc + jd - J) / 2) * sgn(s2) * imsrg::sixj_racah(ja, jb, J, jc, jd, 2) * j_ad * j_bc;
+  return v / std::sqrt((1.0 + (a == b)) * (1.0 + (c == d)));
+}
+
 // The proton-neutron J-scheme two-body arrays from me2j record values
-// (src/interaction_IO.f90:398-555, without the centre-of-mass term of Htype 1): records whose
-// orbits are not all in the basis are skipped.
-void me2j_convert(const imsrg::Layout& L, const std::vector<IsoOrbit>& iso, const double* values, double* H) {
+// (src/interaction_IO.f90:398-555): records whose orbits are not all in the basis are skipped.
+// With htype 1 (the intrinsic Hamiltonian, Lawson beta 0) each element also receives the
+// two-body part of the centre-of-mass kinetic energy, -p1.p2 hw / A.
+void me2j_convert(const imsrg::Layout& L, const std::vector<IsoOrbit>& iso, const double* values, int htype,
+                  double* H) {
+  const double com = (htype == 1) ? L.hw / (L.Aprot + L.Aneut) : 0.0;
   const int N = L.N, NJ = L.NJ;
   std::vector<int> proton((size_t)iso.size(), -1);  // the basis index of the proton orbit of I
   for (size_t I = 0; I < iso.size(); ++I)
@@ -149,6 +187,7 @@ void me2j_convert(const imsrg::Layout& L, const std::vector<IsoOrbit>& iso, cons
                        ((ta + tb == 2) && (tc + td == 2) ? me[3] : 0.0) +
                        0.125 * std::abs((ta - tb) * (tc - td)) * me[2];
             V *= pre2;
+            if (com != 0.0) V -= two_body_dot(L, a, b, cc, d, JT, true) * com;
             const int C1 = L.con[a] + L.con[b], C2 = L.con[cc] + L.con[d];
             static const int tab[3][3] = {{0, 1, 2}, {1, 3, 5}, {2, 5, 4}};
             const int g = tab[C1][C2];
@@ -188,7 +227,7 @@ imsrg_status synthetic(imsrg_ctx* ctx, uint64_t seed, double v_scale, bool bare,
   std::vector<IsoOrbit> iso;
   for (int k = 0; k < N; k += 2) iso.push_back(IsoOrbit{L.nn[k], L.ll[k], L.jj[k]});
   const std::vector<double> values = synthetic_values(L, iso, seed, v_scale);
-  me2j_convert(L, iso, values.data(), H.data());
+  me2j_convert(L, iso, values.data(), 1, H.data());
 
   // one-body kinetic energy (Htype 1), with the reference's FP32 intermediate literals
   const double hw = L.hw;
@@ -307,8 +346,8 @@ extern "C" imsrg_status imsrg_synthetic_me2j_values(imsrg_ctx* ctx, uint64_t see
 }
 
 extern "C" imsrg_status imsrg_me2j_to_slab(imsrg_ctx* ctx, const double* values, int64_t n, int32_t emax_file,
-                                           double* host_slab) {
-  if (!ctx || !values || !host_slab || emax_file < 0) return IMSRG_ERR_INVALID_ARGUMENT;
+                                           int32_t htype, double* host_slab) {
+  if (!ctx || !values || !host_slab || emax_file < 0 || htype < 0 || htype > 1) return IMSRG_ERR_INVALID_ARGUMENT;
   Ctx* c = reinterpret_cast<Ctx*>(ctx);
   std::vector<IsoOrbit> mine;
   const imsrg_status st = check_pairs(c, mine);
@@ -316,6 +355,6 @@ extern "C" imsrg_status imsrg_me2j_to_slab(imsrg_ctx* ctx, const double* values,
   const std::vector<IsoOrbit> iso = file_orbits(emax_file);
   if (record_values(iso) != n)
     return c->fail(IMSRG_ERR_MISMATCH, "value count does not match the me2j records of emax_file");
-  me2j_convert(c->L, iso, values, host_slab);
+  me2j_convert(c->L, iso, values, htype, host_slab);
   return IMSRG_OK;
 }

@@ -113,7 +113,7 @@ SIGNATURES = {
     "imsrg_synthetic_hamiltonian": [_vp, _u64, _d, _vp],
     "imsrg_synthetic_bare_hamiltonian": [_vp, _u64, _d, _vp],
     "imsrg_synthetic_me2j_values": [_vp, _u64, _d, _vp, _pi64],
-    "imsrg_me2j_to_slab": [_vp, _vp, _i64, _i32, _vp],
+    "imsrg_me2j_to_slab": [_vp, _vp, _i64, _i32, _i32, _vp],
     "imsrg_neq": [_vp, _pi64],
     "imsrg_vectorize_slab": [_vp, _vp, _vp],
     "imsrg_repackage_slab": [_vp, _vp, _i32, _vp],

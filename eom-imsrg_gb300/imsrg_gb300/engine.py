@@ -301,13 +301,15 @@ class Engine:
                                                     C.byref(n)))
         return out
 
-    def me2j_to_slab(self, values: np.ndarray, emax_file: int, slab: np.ndarray | None = None) -> np.ndarray:
+    def me2j_to_slab(self, values: np.ndarray, emax_file: int, htype: int = 1,
+                     slab: np.ndarray | None = None) -> np.ndarray:
         """read_me2j_interaction (src/interaction_IO.f90:282-557) of record values into the
-        two-body arrays of a host slab (a new zero slab by default)."""
+        two-body arrays of a host slab (a new zero slab by default); htype 1 adds the
+        two-body centre-of-mass term -p1.p2 hw/A."""
         values = np.ascontiguousarray(values, dtype=np.float64)
         out = np.zeros(self.slab) if slab is None else slab
         self._ck(self.L.imsrg_me2j_to_slab(self.h, values.ctypes.data, int(values.size), int(emax_file),
-                                           out.ctypes.data))
+                                           int(htype), out.ctypes.data))
         return out
 
     # ---------------------------------------------------------------- Hartree-Fock

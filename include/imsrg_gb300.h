@@ -274,8 +274,8 @@ imsrg_status imsrg_read_omega_checkpoint(imsrg_ctx* ctx, imsrg_op* G, const char
 /* ---- input preparation (host, FP64): seeded synthetic Hamiltonian in the reference's
  * me2j -> pn J-scheme layout (read_me2j_interaction, src/interaction_IO.f90:282-557) plus the
  * harmonic-oscillator kinetic energy (calculate_h0_harm_osc, src/basic_IMSRG.f90:2093-2191),
- * normal ordered w.r.t. the reference state (normal_order, src/basic_IMSRG.f90:2419-2550).
- * Writes one host slab (herm = +1). */
+ * with the two-body centre-of-mass term of Htype 1 (-p1.p2 hw/A), normal ordered w.r.t. the
+ * reference state (normal_order, src/basic_IMSRG.f90:2419-2550).  Writes one host slab (herm = +1). */
 imsrg_status imsrg_synthetic_hamiltonian(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* host_slab);
 /* The same Hamiltonian before normal ordering, as calc_HF receives it after read_me2j_interaction
  * and calculate_h0_harm_osc (src/main_IMSRG.f90:125-157): the kinetic energy in fhh/fpp/fph, V in
@@ -287,10 +287,12 @@ imsrg_status imsrg_synthetic_bare_hamiltonian(imsrg_ctx* ctx, uint64_t seed, dou
 imsrg_status imsrg_synthetic_me2j_values(imsrg_ctx* ctx, uint64_t seed, double v_scale, double* values, int64_t* n);
 /* read_me2j_interaction (src/interaction_IO.f90:282-557) from the record values of an me2j file
  * for eMax_file (the caller decompresses and parses the text): the proton-neutron J-scheme
- * two-body arrays of host_slab, for the records whose orbits are all in this basis.  The
- * centre-of-mass term of Htype 1 is not added; the rest of the slab is untouched.
- * IMSRG_ERR_MISMATCH when n is not the record count of eMax_file. */
-imsrg_status imsrg_me2j_to_slab(imsrg_ctx* ctx, const double* values, int64_t n, int32_t emax_file,
+ * two-body arrays of host_slab, for the records whose orbits are all in this basis; the rest of
+ * the slab is untouched.  htype 1 (the intrinsic Hamiltonian, Lawson beta 0) adds the two-body
+ * centre-of-mass term -p1.p2 hw/A (p1_p2, src/basic_IMSRG.f90:4445-4504), htype 0 does not.
+ * The synthetic Hamiltonian uses htype 1.  IMSRG_ERR_MISMATCH when n is not the record count
+ * of eMax_file. */
+imsrg_status imsrg_me2j_to_slab(imsrg_ctx* ctx, const double* values, int64_t n, int32_t emax_file, int32_t htype,
                                 double* host_slab);
 
 /* ---- Hartree-Fock and normal ordering (FP64).  The self-consistency loop runs on the host

@@ -1853,5 +1853,7 @@ void orc_gamma_matrix(void* b, const double* op, int herm, const double* rho, do
 void orc_transform_2b_to_hf(void* b, double* op, const double* D) { transform_2b_to_hf(*(Basis*)b, op, D); }
 void orc_normal_order(void* b, const double* in, int herm, double* out) { normal_order(*(Basis*)b, in, herm, out); }
 int64_t orc_vectorize(void* b, const double* op, double* v) { return vectorize(*(Basis*)b, op, v); }
+double orc_p1_p2(void* b, int a, int bb, int c, int d, int J) { return dot12(*(Basis*)b, a, bb, c, d, J, true); }
+double orc_r1_r2(void* b, int a, int bb, int c, int d, int J) { return dot12(*(Basis*)b, a, bb, c, d, J, false); }
 
 }  // extern "C"

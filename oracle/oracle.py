@@ -93,6 +93,8 @@ def lib():
         "orc_transform_2b_to_hf": (None, [vp, _dp, _dp]),
         "orc_normal_order": (None, [vp, _dp, i, _dp]),
         "orc_vectorize": (i64, [vp, _dp, _dp]),
+        "orc_p1_p2": (d, [vp, i, i, i, i, i]),
+        "orc_r1_r2": (d, [vp, i, i, i, i, i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -282,6 +284,14 @@ class Oracle:
         out = np.zeros(self.slab)
         self.L.orc_normal_order(self.h, op, herm, out)
         return out
+
+    def p1_p2(self, a, b, c, d, J) -> float:
+        """p1_p2 (src/basic_IMSRG.f90:4445-4504)."""
+        return self.L.orc_p1_p2(self.h, a, b, c, d, J)
+
+    def r1_r2(self, a, b, c, d, J) -> float:
+        """r1_r2 (src/basic_IMSRG.f90:4506-4565)."""
+        return self.L.orc_r1_r2(self.h, a, b, c, d, J)
 
     def vectorize(self, op) -> np.ndarray:
         """vectorize (src/basic_IMSRG.f90:3929-3985)."""

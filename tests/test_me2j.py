@@ -66,3 +66,33 @@ def test_larger_file_restricted_to_the_basis(built_lib, oracles):
     with pytest.raises(ImsrgError) as e:
         small.me2j_to_slab(vals[:-4], 4)
     assert e.value.code == 5
+
+
+def test_centre_of_mass_term_matches_oracle(built_lib, oracles):
+    """htype 1 adds -p1.p2 hw/A to every element (p1_p2, src/basic_IMSRG.f90:4445-4504)"""
+    from imsrg_gb300 import Engine, make_basis
+    emax = 2
+    o, eng = oracles(emax), Engine(make_basis(emax), device=-1)
+    b = eng.basis
+    zero = np.zeros(eng.synthetic_me2j_values(seed=1).size)
+    com = eng.me2j_to_slab(zero, emax, htype=1)
+    assert not np.any(_two_body(eng, eng.me2j_to_slab(zero, emax, htype=0)))
+    f = -b.hw / (b.Aprot + b.Aneut)
+    n, checked = b.norbits, 0
+    for a in range(n):
+        for bb in range(n):
+            for c in range(n):
+                for d in range(n):
+                    if (b.ll[a] + b.ll[bb]) % 2 != (b.ll[c] + b.ll[d]) % 2 or b.itzp[a] + b.itzp[bb] != b.itzp[c] + b.itzp[d]:
+                        continue
+                    for J in range(abs(b.jj[a] - b.jj[bb]), b.jj[a] + b.jj[bb] + 1, 2):
+                        if not abs(b.jj[c] - b.jj[d]) <= J <= b.jj[c] + b.jj[d]:
+                            continue
+                        ref = f * o.p1_p2(a, bb, c, d, J)
+                        # v_elem adds sqrt(2) for identical orbits; p1_p2 is normalised
+                        norm = np.sqrt((1.0 + (a == bb)) * (1.0 + (c == d)))
+                        assert abs(o.v_elem(com, 1, a, bb, c, d, J) - ref * norm) < 1e-13, (a, bb, c, d, J)
+                        checked += ref != 0.0
+    assert checked > 50
+    # p.p and r.r share their angular structure: their elements are never both zero by symmetry alone
+    assert any(o.r1_r2(0, 2, 0, 2, J) != 0.0 for J in (0, 2, 4))
