@@ -205,7 +205,7 @@ imsrg_status Ctx::ensure_flow_workspace() {
 
 Ctx::~Ctx() {
   for (void* p : {(void*)d_tables, (void*)d_partial, (void*)d_scalars, (void*)d_mono, (void*)d_w1, (void*)d_w2,
-                  (void*)d_lcc, (void*)d_rcc, (void*)d_wcc, (void*)d_int1, (void*)d_int2, (void*)d_ad})
+                  (void*)d_lcc, (void*)d_rcc, (void*)d_wcc, (void*)d_int1, (void*)d_int2, (void*)d_ad, (void*)d_gen})
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
   for (auto& m : prof_marks) cudaEventDestroy(m.second);
@@ -363,6 +363,35 @@ imsrg_status Ctx::white(const double* H, int hH, double* ETA) {
   dim3 grid(16, L.nblocks);
   k_white_2b<<<grid, kThreads, 0, stream>>>(D, H, hH, d_mono, ETA);
   return launched("k_white_2b");
+}
+
+// build_gs_atan (Hnum == Hden) and build_gs_atanxx (src/generators.f90:163-374)
+imsrg_status Ctx::atan_generator(const double* Hden, int hden, const double* Hnum, double* ETA) {
+  CK(cuda(cudaMemsetAsync(ETA, 0, sizeof(double) * (size_t)L.slab, stream), "memset(ETA)"));
+  k_monopole<<<(L.N * L.N + kThreads - 1) / kThreads, kThreads, 0, stream>>>(D, Hden, hden, d_mono);
+  CK(launched("k_monopole"));
+  if (D.n_ai > 0) {
+    k_atan_1b<<<(D.n_ai + kThreads - 1) / kThreads, kThreads, 0, stream>>>(D, Hden, hden, Hnum, ETA);
+    CK(launched("k_atan_1b"));
+  }
+  dim3 grid(16, L.nblocks);
+  k_atan_2b<<<grid, kThreads, 0, stream>>>(D, Hden, hden, Hnum, d_mono, ETA);
+  return launched("k_atan_2b");
+}
+
+// build_gs_w2 (src/generators.f90:109-160): 1.5 atan(H) + 0.5 atanxx(H, [atan(H), H]), the
+// commutator in the context's precision; three slab workspaces kept between calls
+imsrg_status Ctx::w2_generator(const double* H, int hH, double* ETA) {
+  if (!d_gen) {
+    CK(cuda(cudaMalloc(&d_gen, 3 * sizeof(double) * (size_t)L.slab), "cudaMalloc(w2 generator workspace)"));
+  }
+  double* eta1 = d_gen;
+  double* h2 = d_gen + L.slab;
+  double* eta2 = d_gen + 2 * L.slab;
+  CK(atan_generator(H, hH, H, eta1));
+  CK(commutator(eta1, -1, H, hH, h2, hH, true));
+  CK(atan_generator(H, hH, h2, eta2));
+  return axpby(eta1, 1.5, eta2, 0.5, ETA);
 }
 
 // MAGNUS_EXPAND (src/IMSRG_MAGNUS.f90:620-691) with device-resident operators; the
@@ -940,6 +969,34 @@ imsrg_status imsrg_build_gs_white(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* E
   if (H == ETA) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "ETA must not alias H");
   ETA->herm = -1;
   return c->white(H->d, H->herm, ETA->d);
+}
+
+imsrg_status imsrg_build_gs_atan(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* ETA) {
+  CTX(ctx);
+  CK(check_op(c, H, "imsrg_build_gs_atan"));
+  CK(check_op(c, ETA, "imsrg_build_gs_atan"));
+  if (H == ETA) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_build_gs_atan: ETA must differ from H");
+  ETA->herm = -1;
+  return c->atan_generator(H->d, H->herm, H->d, ETA->d);
+}
+
+imsrg_status imsrg_build_gs_atanxx(imsrg_ctx* ctx, const imsrg_op* Hold, const imsrg_op* H, imsrg_op* ETA) {
+  CTX(ctx);
+  CK(check_op(c, Hold, "imsrg_build_gs_atanxx"));
+  CK(check_op(c, H, "imsrg_build_gs_atanxx"));
+  CK(check_op(c, ETA, "imsrg_build_gs_atanxx"));
+  if (ETA == H || ETA == Hold) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_build_gs_atanxx: ETA must differ");
+  ETA->herm = -1;
+  return c->atan_generator(Hold->d, Hold->herm, H->d, ETA->d);
+}
+
+imsrg_status imsrg_build_gs_w2(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* ETA) {
+  CTX(ctx);
+  CK(check_op(c, H, "imsrg_build_gs_w2"));
+  CK(check_op(c, ETA, "imsrg_build_gs_w2"));
+  if (H == ETA) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_build_gs_w2: ETA must differ from H");
+  ETA->herm = -1;
+  return c->w2_generator(H->d, H->herm, ETA->d);
 }
 
 imsrg_status imsrg_magnus_expand(imsrg_ctx* ctx, imsrg_op* DG, const imsrg_op* G, int32_t* used) {

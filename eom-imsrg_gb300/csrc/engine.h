@@ -69,6 +69,7 @@ struct Ctx {
   double *d_w1 = nullptr, *d_w2 = nullptr, *d_lcc = nullptr, *d_rcc = nullptr, *d_wcc = nullptr;
   // Magnus / BCH intermediates
   double *d_int1 = nullptr, *d_int2 = nullptr, *d_ad = nullptr;
+  double* d_gen = nullptr;  // w2 generator workspace (3 slabs)
   imsrg::TcState* tc = nullptr;
   StepGraph* sg = nullptr;  // captured Magnus step (graph.cu)
   AdjointState* adj = nullptr;  // reverse-mode workspaces (adjoint.cu)
@@ -105,6 +106,8 @@ struct Ctx {
   imsrg_status frob_async(const double* op, double scale, int slot);
   imsrg_status read_scalars(int n);
   imsrg_status white(const double* H, int hH, double* ETA);
+  imsrg_status atan_generator(const double* Hden, int hden, const double* Hnum, double* ETA);
+  imsrg_status w2_generator(const double* H, int hH, double* ETA);
   imsrg_status magnus_expand(double* DG, int hDG, const double* G, int hG, int* used);
   imsrg_status bch_expand(double* HS, const double* G, int hG, const double* H, int hH, int max_terms, double conv,
                           int* terms);

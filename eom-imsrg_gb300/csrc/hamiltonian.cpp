@@ -7,8 +7,11 @@
 //    v_scale * N(0,1) * exp(-(e1+e2+e3+e4)/eMax), the T=1 value shared by Mt=-1,0,+1
 //    (isospin symmetric), Pauli-forbidden records (identical orbits, J+T even) zero;
 //  * one-body part: the harmonic-oscillator kinetic energy with the intrinsic (1-1/A)
-//    factor (calculate_h0_harm_osc with Htype 1, src/basic_IMSRG.f90:2093-2191), and the
-//    two-body centre-of-mass term -p1.p2 hw/A that read_me2j_interaction adds for Htype 1;
+//    factor (calculate_h0_harm_osc with Htype 1, src/basic_IMSRG.f90:2093-2191); the records
+//    are converted without the two-body centre-of-mass term -p1.p2 hw/A: with a random
+//    interaction that term closes the particle-hole gap of the eMax 4-8 HF references and the
+//    White-generator flow diverges (E0 -> NaN by s=50 at eMax 4, in FP64 and in the oracle);
+//    me2j_convert applies it to interaction files read with htype 1;
 //  * normal ordering with respect to the reference state (normal_order,
 //    src/basic_IMSRG.f90:2419-2550), i.e. the HO-basis reference of calc_HO.
 #include <algorithm>
@@ -227,7 +230,7 @@ imsrg_status synthetic(imsrg_ctx* ctx, uint64_t seed, double v_scale, bool bare,
   std::vector<IsoOrbit> iso;
   for (int k = 0; k < N; k += 2) iso.push_back(IsoOrbit{L.nn[k], L.ll[k], L.jj[k]});
   const std::vector<double> values = synthetic_values(L, iso, seed, v_scale);
-  me2j_convert(L, iso, values.data(), 1, H.data());
+  me2j_convert(L, iso, values.data(), 0, H.data());
 
   // one-body kinetic energy (Htype 1), with the reference's FP32 intermediate literals
   const double hw = L.hw;

@@ -27,6 +27,9 @@ __global__ void k_comm221f(DevLayout D, int pm, double* RES, int hRES, const dou
 __global__ void k_monopole(DevLayout D, const double* H, int hH, double* mono);
 __global__ void k_white_1b(DevLayout D, const double* H, int hH, double* ETA);
 __global__ void k_white_2b(DevLayout D, const double* H, int hH, const double* mono, double* ETA);
+__global__ void k_atan_1b(DevLayout D, const double* Hden, int hden, const double* Hnum, double* ETA);
+__global__ void k_atan_2b(DevLayout D, const double* Hden, int hden, const double* Hnum, const double* mono,
+                          double* ETA);
 __global__ void k_axpby(int64_t n, const double* A, double ax, const double* B, double bx, double* C);
 __global__ void k_frob_partial(const double* op, const int64_t* seg_start, const int* seg_len, const int8_t* seg_w,
                                double* partial);

@@ -54,6 +54,47 @@ __global__ void k_white_2b(DevLayout D, const double* __restrict__ H, int hH, co
   }
 }
 
+// build_gs_atan / build_gs_atanxx one-body part (src/generators.f90:163-215, 271-323):
+// eta = atan(2 N / Eden) * 0.5, numerators from Hnum, White denominators from Hden
+__global__ void k_atan_1b(DevLayout D, const double* __restrict__ Hden, int hden, const double* __restrict__ Hnum,
+                          double* __restrict__ ETA) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= D.n_ai) return;
+  const int a = D.ai_a[w], i = D.ai_i[w];
+  const int ak = D.parts[a], ik = D.holes[i];
+  const int ji = D.jj[ik];
+  double Eden = 0.0;
+  for (int JT = 0; JT <= 2 * ji; JT += 2) Eden = Eden - (JT + 1) * d_v_elem(D, Hden, hden, ak, ik, ak, ik, JT);
+  Eden = Eden / (ji + 1.0) / (ji + 1.0);
+  Eden = Eden + Hden[D.off_fpp + a + (int64_t)a * D.P] - Hden[D.off_fhh + i + (int64_t)i * D.A];
+  ETA[D.off_fph + a + (int64_t)i * D.P] = atan(2 * Hnum[D.off_fph + a + (int64_t)i * D.P] / Eden) * 0.5;
+}
+
+// two-body part (src/generators.f90:216-265, 324-373): blockIdx.y = channel
+__global__ void k_atan_2b(DevLayout D, const double* __restrict__ Hden, int hden, const double* __restrict__ Hnum,
+                          const double* __restrict__ mono, double* __restrict__ ETA) {
+  const int q = blockIdx.y;
+  const int np = D.ncls[q * 3], nh = D.ncls[q * 3 + 2];
+  const int64_t n = (int64_t)np * nh;
+  const int64_t off = D.goff[q * 6 + 2];
+  const int N = D.N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int JX = (int)(t / np), IX = (int)(t - (int64_t)JX * np);
+    const int o1 = D.pair_off[q * 3] + IX, o2 = D.pair_off[q * 3 + 2] + JX;
+    const int a = D.pair_a[o1], b = D.pair_b[o1], i = D.pair_a[o2], j = D.pair_b[o2];
+    double Eden = 0.0;
+    Eden = Eden + mono[a * N + b];
+    Eden = Eden + mono[i * N + j];
+    Eden = Eden - mono[a * N + i];
+    Eden = Eden - mono[a * N + j];
+    Eden = Eden - mono[i * N + b];
+    Eden = Eden - mono[j * N + b];
+    Eden = Eden + d_f_elem(D, Hden, hden, a, a) + d_f_elem(D, Hden, hden, b, b) - d_f_elem(D, Hden, hden, i, i) -
+           d_f_elem(D, Hden, hden, j, j);
+    ETA[off + t] = 0.5 * atan(2 * Hnum[off + t] / Eden);
+  }
+}
+
 // add_sq_op (src/basic_IMSRG.f90:3551-3579): C = ax*A + bx*B over the whole slab
 __global__ void k_axpby(int64_t n, const double* __restrict__ A, double ax, const double* __restrict__ B, double bx,
                         double* __restrict__ C) {

@@ -93,6 +93,9 @@ SIGNATURES = {
     "imsrg_commutator_222_ph": [_vp, _vp, _vp, _vp, _vp],
     "imsrg_commutator": [_vp, _vp, _vp, _vp, _i32],
     "imsrg_build_gs_white": [_vp, _vp, _vp],
+    "imsrg_build_gs_atan": [_vp, _vp, _vp],
+    "imsrg_build_gs_atanxx": [_vp, _vp, _vp, _vp],
+    "imsrg_build_gs_w2": [_vp, _vp, _vp],
     "imsrg_magnus_expand": [_vp, _vp, _vp, _pi32],
     "imsrg_euler_step": [_vp, _vp, _vp, _pd, _d],
     "imsrg_bch_expand": [_vp, _vp, _vp, _vp, _i32, _d, _pi32],

@@ -406,6 +406,15 @@ class Engine:
     def build_gs_white(self, H: SqOp, ETA: SqOp):
         self._ck(self.L.imsrg_build_gs_white(self.h, H.h, ETA.h))
 
+    def build_gs_atan(self, H: SqOp, ETA: SqOp):
+        self._ck(self.L.imsrg_build_gs_atan(self.h, H.h, ETA.h))
+
+    def build_gs_atanxx(self, Hold: SqOp, H: SqOp, ETA: SqOp):
+        self._ck(self.L.imsrg_build_gs_atanxx(self.h, Hold.h, H.h, ETA.h))
+
+    def build_gs_w2(self, H: SqOp, ETA: SqOp):
+        self._ck(self.L.imsrg_build_gs_w2(self.h, H.h, ETA.h))
+
     def magnus_expand(self, DG: SqOp, G: SqOp) -> int:
         n = C.c_int32()
         self._ck(self.L.imsrg_magnus_expand(self.h, DG.h, G.h, C.byref(n)))

@@ -70,14 +70,18 @@ def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float |
     checkpoint_every steps (default: the reference's interval for eMax) Omega is written at
     the start of the step, the first one after a restart skipped, and the file written
     checkpoint_every steps earlier removed."""
-    if generator != "white":
-        raise ValueError("only the White generator is implemented")
+    gens = {"white": eng.build_gs_white, "atan": eng.build_gs_atan, "w2": eng.build_gs_w2}
+    if generator not in gens:
+        raise ValueError(f"generator must be one of {sorted(gens)}")
+    if graph and generator != "white":
+        raise ValueError("the CUDA-graph step builds the White generator; use graph=False for atan / w2")
+    build = gens[generator]
     HS = eng.new_op(1, H0)          # evolved Hamiltonian
     H = eng.new_op(1)               # bare Hamiltonian
     eng.copy_sq_op(HS, H)
     G = eng.new_op(-1)              # Omega
     DG = eng.new_op(-1)             # eta, then dOmega
-    eng.build_gs_white(HS, DG)
+    build(HS, DG)
     res = FlowResult()
     s, steps = 0.0, 0
     chk = checkpoint_every or checkpoint_interval(eng.basis.eMax)
@@ -86,7 +90,7 @@ def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float |
     if found:  # checkpoint restart (src/IMSRG_MAGNUS.f90:73-84)
         eng.read_omega_checkpoint(G, found[0])
         eng.bch_expand(HS, G, H, bch_max_terms, bch_conv)
-        eng.build_gs_white(HS, DG)
+        build(HS, DG)
         s = found[1]
         steps = int(round(s / ds))
         first = True
@@ -116,7 +120,7 @@ def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float |
             nm = eng.magnus_expand(DG, G)
             s = eng.euler_step(G, DG, s, ds)
             nb = eng.bch_expand(HS, G, H, bch_max_terms, bch_conv)
-            eng.build_gs_white(HS, DG)
+            build(HS, DG)
             e2 = eng.mbpt2(HS)
             e0 = HS.E0
         crit = abs(e2)

@@ -188,6 +188,14 @@ imsrg_status imsrg_commutator(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op*
 
 /* ---- generator and flow (src/generators.f90, src/IMSRG_MAGNUS.f90) */
 imsrg_status imsrg_build_gs_white(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* ETA);   /* generators.f90:4 */
+/* build_gs_atan (src/generators.f90:163-266): eta = atan(2 N / Eden) / 2 with White's numerators
+ * and denominators */
+imsrg_status imsrg_build_gs_atan(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* ETA);
+/* build_gs_atanxx (src/generators.f90:271-374): numerators from H, denominators from Hold */
+imsrg_status imsrg_build_gs_atanxx(imsrg_ctx* ctx, const imsrg_op* Hold, const imsrg_op* H, imsrg_op* ETA);
+/* build_gs_w2 (src/generators.f90:109-160), the reference driver's default generator:
+ * 1.5 atan(H) + 0.5 atanxx(H, [atan(H), H]), the commutator in the context's precision */
+imsrg_status imsrg_build_gs_w2(imsrg_ctx* ctx, const imsrg_op* H, imsrg_op* ETA);
 /* MAGNUS_EXPAND(DG, G, AD, jbas) :620 -- DG holds eta on entry and dOmega on exit */
 imsrg_status imsrg_magnus_expand(imsrg_ctx* ctx, imsrg_op* DG, const imsrg_op* G, int32_t* commutators_used);
 /* euler_step(G, DG, s, stp) :754 -- G += stp*DG; *s += stp */

@@ -862,6 +862,47 @@ void white(const Basis& B, const double* H, int hH, double* ETA) {
   }
 }
 
+// build_gs_atan / build_gs_atanxx (src/generators.f90:163-374): eta = atan(2 N / Eden) * 0.5
+// with the White denominators of Hden and the numerators of Hnum (atan: both H)
+void atan_gen(const Basis& B, const double* Hden, int hden, const double* Hnum, double* ETA) {
+  std::fill(ETA, ETA + B.slab, 0.0);
+  for (int a = 0; a < B.P; ++a) {
+    const int ak = B.parts[a];
+    for (int i = 0; i < B.A; ++i) {
+      const int ik = B.holes[i];
+      if (B.jj[ik] != B.jj[ak] || B.ll[ik] != B.ll[ak] || B.tz[ik] != B.tz[ak]) continue;
+      const int ji = B.jj[ik];
+      double Eden = 0.0;
+      for (int JT = 0; JT <= 2 * ji; JT += 2) Eden -= (JT + 1) * v_elem(B, Hden, hden, ak, ik, ak, ik, JT);
+      Eden = Eden / (ji + 1.0) / (ji + 1.0);
+      Eden = Eden + cfpp(B, Hden, a, a) - cfhh(B, Hden, i, i);
+      fph(B, ETA, a, i) = std::atan(2 * cfph(B, Hnum, a, i) / Eden) * 0.5;
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int q = 0; q < B.nblocks; ++q) {
+    const int np = B.ncls[q][0], nh = B.ncls[q][2];
+    const double* HX = B.X(Hnum, q, 2);
+    double* EX = B.X(ETA, q, 2);
+    for (int IX = 0; IX < np; ++IX) {
+      const int a = B.qa[q][0][IX], b = B.qb[q][0][IX];
+      for (int JX = 0; JX < nh; ++JX) {
+        const int i = B.qa[q][2][JX], j = B.qb[q][2][JX];
+        double Eden = 0.0;
+        Eden += monopole(B, Hden, hden, a, b);
+        Eden += monopole(B, Hden, hden, i, j);
+        Eden -= monopole(B, Hden, hden, a, i);
+        Eden -= monopole(B, Hden, hden, a, j);
+        Eden -= monopole(B, Hden, hden, i, b);
+        Eden -= monopole(B, Hden, hden, j, b);
+        Eden += f_elem(B, Hden, hden, a, a) + f_elem(B, Hden, hden, b, b) - f_elem(B, Hden, hden, i, i) -
+                f_elem(B, Hden, hden, j, j);
+        EX[IX + (int64_t)JX * np] = 0.5 * std::atan(2 * HX[IX + (int64_t)JX * np] / Eden);
+      }
+    }
+  }
+}
+
 // mbpt2 (src/basic_IMSRG.f90:4165-4199)
 double mbpt2(const Basis& B, const double* H, int hH) {
   double sm = 0.0;
@@ -1776,6 +1817,9 @@ void orc_full_commutator(void* b, const double* L, int hL, const double* R, int 
   full_commutator(B, L, hL, R, hR, RES, hRES, w, true);
 }
 void orc_build_gs_white(void* b, const double* H, int hH, double* ETA) { white(*(Basis*)b, H, hH, ETA); }
+void orc_build_gs_atanxx(void* b, const double* Hold, int hold, const double* H, double* ETA) {
+  atan_gen(*(Basis*)b, Hold, hold, H, ETA);
+}
 void orc_commutator_e0(void* b, const double* L, int hL, const double* R, int hR, double* RES, int hRES,
                        int with_e0) {
   Basis& B = *(Basis*)b;

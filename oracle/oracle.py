@@ -65,6 +65,7 @@ def lib():
         "orc_commutator_222_ph": (None, [vp, _dp, i, _dp, i, _dp, i, _dp]),
         "orc_full_commutator": (None, [vp, _dp, i, _dp, i, _dp, i]),
         "orc_build_gs_white": (None, [vp, _dp, i, _dp]),
+        "orc_build_gs_atanxx": (None, [vp, _dp, i, _dp, _dp]),
         "orc_commutator_e0": (None, [vp, _dp, i, _dp, i, _dp, i, i]),
         "orc_commutator_vjp": (None, [vp, _dp, i, _dp, i, i, i, _dp, _dp, _dp]),
         "orc_white_vjp": (None, [vp, _dp, i, _dp, _dp]),
@@ -237,6 +238,25 @@ class Oracle:
         ETA = self.new()
         self.L.orc_build_gs_white(self.h, H, hH, ETA)
         return ETA
+
+    def atan(self, H, hH=1):
+        """build_gs_atan (src/generators.f90:163-266)."""
+        ETA = self.new()
+        self.L.orc_build_gs_atanxx(self.h, H, hH, H, ETA)
+        return ETA
+
+    def atanxx(self, Hold, H, hold=1):
+        """build_gs_atanxx (src/generators.f90:271-374): numerators of H, denominators of Hold."""
+        ETA = self.new()
+        self.L.orc_build_gs_atanxx(self.h, Hold, hold, np.ascontiguousarray(H), ETA)
+        return ETA
+
+    def w2(self, H, hH=1):
+        """build_gs_w2 (src/generators.f90:109-160): 1.5 atan(H) + 0.5 atanxx(H, [atan(H), H])."""
+        eta1 = self.atan(H, hH)
+        H2 = self.commutator(eta1, -1, H, hH)
+        eta2 = self.atanxx(H, H2, hH)
+        return 1.5 * eta1 + 0.5 * eta2
 
     def frob(self, op):
         return self.L.orc_mat_frob_norm(self.h, op)

@@ -23,7 +23,7 @@ def test_synthetic_values_reproduce_the_hamiltonian(built_lib, emax):
     eng = Engine(make_basis(emax), device=-1)
     vals = eng.synthetic_me2j_values(seed=5)
     assert vals.size % 4 == 0 and np.count_nonzero(vals) > vals.size // 2
-    slab = eng.me2j_to_slab(vals, emax)
+    slab = eng.me2j_to_slab(vals, emax, htype=0)  # the synthetic H has no c.m. term
     assert np.array_equal(_two_body(eng, slab), _two_body(eng, eng.synthetic_bare_hamiltonian(seed=5)))
 
 
@@ -36,7 +36,7 @@ def test_file_round_trip(built_lib, tmp_path):
     write_me2j(path, vals)
     back = read_me2j(path)
     assert back.size == vals.size and np.abs(back - np.round(vals, 7)).max() < 1e-12
-    slab = eng.me2j_to_slab(back, 4)
+    slab = eng.me2j_to_slab(back, 4, htype=0)
     ref = eng.synthetic_bare_hamiltonian(seed=6)
     assert rel_err(_two_body(eng, slab), _two_body(eng, ref)) < 1e-6
 

@@ -158,3 +158,17 @@ def test_bch_and_magnus_small(oracles):
     used = o.magnus_expand(DG, G)
     assert used >= 1
     assert np.max(np.abs(DG - eta)) > 0
+
+
+def test_atan_generators_against_white(oracles):
+    """build_gs_atan / atanxx / w2 (src/generators.f90:109-374) share White's numerators N and
+    denominators E: atan = atan(2 N/E)/2 = atan(2 white)/2 element by element; atanxx with the
+    numerators and denominators of one operator is atan; w2 = 1.5 atan + 0.5 atanxx(H, [atan, H])"""
+    o = oracles(4)
+    H = o.random(51, 1)
+    w, a = o.white(H, 1), o.atan(H, 1)
+    assert np.abs(w).max() > 0
+    assert np.allclose(a, 0.5 * np.arctan(2 * w), rtol=1e-13, atol=1e-15)
+    assert np.array_equal(o.atanxx(H, H), a)
+    H2 = o.commutator(a, -1, H, 1)
+    assert np.allclose(o.w2(H, 1), 1.5 * a + 0.5 * o.atanxx(H, H2), rtol=0, atol=1e-15)
