@@ -27,6 +27,7 @@
 
 #include "../../include/imsrg_gb300.h"
 #include "engine.h"
+#include "linalg.h"
 #include "pair_groups.h"
 
 using namespace imsrg;
@@ -183,6 +184,25 @@ __global__ void k_hf_transform_2b(DevLayout D, HFDev H, double* op, int herm, co
 }
 
 // ---------------------------------------------------------------- host helpers
+// C = A^T B A for n x n column-major matrices
+std::vector<double> sandwich(int n, const std::vector<double>& A, const std::vector<double>& B) {
+  std::vector<double> BA((size_t)n * n, 0.0), C((size_t)n * n, 0.0);
+  for (int j = 0; j < n; ++j)
+    for (int k = 0; k < n; ++k)
+      for (int i = 0; i < n; ++i) BA[i + (size_t)j * n] += B[i + (size_t)k * n] * A[k + (size_t)j * n];
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s += A[k + (size_t)i * n] * BA[k + (size_t)j * n];
+      C[i + (size_t)j * n] = s;
+    }
+  return C;
+}
+
+}  // namespace
+
+namespace imsrg {
+
 // Symmetric eigenproblem of a small n x n matrix (column-major): cyclic Jacobi with the
 // rotation formulas of Rutishauser (Golub and Van Loan, Matrix Computations, sec. 8.5).
 // Eigenvalues ascending in w, eigenvectors in the columns of V.
@@ -235,22 +255,7 @@ void jacobi_eigen(int n, std::vector<double> A, std::vector<double>& w, std::vec
   V.swap(Vs);
 }
 
-// C = A^T B A for n x n column-major matrices
-std::vector<double> sandwich(int n, const std::vector<double>& A, const std::vector<double>& B) {
-  std::vector<double> BA((size_t)n * n, 0.0), C((size_t)n * n, 0.0);
-  for (int j = 0; j < n; ++j)
-    for (int k = 0; k < n; ++k)
-      for (int i = 0; i < n; ++i) BA[i + (size_t)j * n] += B[i + (size_t)k * n] * A[k + (size_t)j * n];
-  for (int j = 0; j < n; ++j)
-    for (int i = 0; i < n; ++i) {
-      double s = 0.0;
-      for (int k = 0; k < n; ++k) s += A[k + (size_t)i * n] * BA[k + (size_t)j * n];
-      C[i + (size_t)j * n] = s;
-    }
-  return C;
-}
-
-}  // namespace
+}  // namespace imsrg
 
 #define CKH(expr)                 \
   do {                            \

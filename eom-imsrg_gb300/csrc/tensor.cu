@@ -15,6 +15,7 @@
 #include "engine.h"
 #include "kernels.h"
 #include "tensor.h"
+#include "tensor_state.h"
 
 using namespace imsrg;
 
@@ -35,60 +36,6 @@ __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* R, int hR, in
 __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* Wx, const double* Wy, int J3, int J4,
                                   int qa, int qb, int hL, int hR, double* RES);
 }  // namespace imsrg
-
-// output slot of the second product of a tensor ladder problem (TcOut::f64 index)
-constexpr int kTensorOpW3 = 7;
-
-// device state of one (rank, dpar) layout
-struct TensorState {
-  TLayout T;
-  DevTLayout DT{};
-  void* tables = nullptr;
-  const GemmProb* pphh_p = nullptr;
-  const GemmTile* pphh_t = nullptr;
-  int n_pphh_t = 0;
-  // per cross-coupled block: GEMM problems (Wx, Wy) and their tile range
-  const GemmProb* cb_p = nullptr;
-  const GemmTile* cb_t = nullptr;
-  std::vector<int> cb_tile_start, cb_tile_n;
-  const int64_t* seg_start = nullptr;
-  const int* seg_len = nullptr;
-  const int8_t* seg_w = nullptr;
-  int nseg = 0;
-  double *w1 = nullptr, *w2 = nullptr;           // tensor-shaped ladder intermediates
-  double *ccx = nullptr, *ccr = nullptr;         // cross-coupled tensor blocks
-  double *wx = nullptr, *wy = nullptr;           // recoupling products
-  double *bch_a = nullptr, *bch_b = nullptr;     // BCH_TENSOR terms
-  // split-BF16 tensor-core form of the ladder's products through pp pairs (mixed modes):
-  // one single-term problem per product, the first product of a (block, class pair) into
-  // w1, the second into w3; the products through hh pairs (K = nhh) stay FP64 into w2
-  int tc_S = 0;
-  __nv_bfloat16* tc_buf = nullptr;
-  int64_t tc_slice_rows = 0, tc_slice_elems = 0;
-  CUtensorMap tc_map;
-  void* tc_tables = nullptr;
-  const TcSplitOp* tc_ops = nullptr;
-  const SplitChunk* tc_chunks = nullptr;
-  const TcProb* tc_probs = nullptr;
-  const TcTile* tc_tiles = nullptr;
-  const GemmProb* hh_p = nullptr;
-  const GemmTile* hh_t = nullptr;
-  int tc_nchunks = 0, tc_ntiles = 0, n_hh_t = 0;
-  double* w3 = nullptr;
-  // particle-hole products on the same tensor cores: the cross-coupled L of every channel is
-  // split once per commutator (LCC rows, K = nph); per cross-coupled tensor block, CCR and CCX
-  // are split into shared regions of the buffer and Wx = hL LCC(qa) CCR, Wy = CCX LCC(qb)^T run
-  // as single-term problems
-  int ph_lcc_nchunks = 0;
-  std::vector<int> ph_chunk_start, ph_chunk_n, ph_tile_start, ph_tile_n;  // per block
-};
-
-struct imsrg_tensor {
-  double* d = nullptr;
-  int herm = 1;
-  TensorState* ts = nullptr;
-  Ctx* owner = nullptr;
-};
 
 namespace {
 
@@ -142,7 +89,7 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
   CKT(ensure_workspace());
   const auto pphh = build_tensor_pphh_problems(T, L);
   const auto pphh_tiles = build_tiles(pphh, 64, 64);
-  // per cross-coupled block: Wx = hL LCC(qa) CCR and Wy = CCX LCC(qb)^T
+  // per cross-coupled block: Wx = -LCC(qa) CCR and Wy = CCX LCC(qb)^T
   std::vector<GemmProb> cbp;
   std::vector<GemmTile> cbt;
   for (size_t b = 0; b < T.cb_J3.size(); ++b) {
@@ -155,7 +102,7 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
       GemmTerm& t = p.t[0];
       t.a_id = kOpLCC; t.a_off = L.cc_off[qa]; t.lda = r1; t.ta = 0;
       t.b_id = kOpRCC; t.b_off = 0; t.ldb = nb1; t.tb = 0;
-      t.K = nb1; t.alpha = kAlphaHL;
+      t.K = nb1; t.alpha = kAlphaNeg | kAlphaOne;
       ps.push_back(p);
     }
     if (nb2 && T.cb_J3[b] != T.cb_J4[b]) {
@@ -299,7 +246,7 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
   for (size_t op = lcc_op0; op < ops.size(); ++op) add_chunks((int)op);
   S.ph_lcc_nchunks = (int)chunks.size() - ladder_nchunks;
   // per block: CCR (src 0, its columns, K = nb1) and CCX (src 1, its rows, K = nb2) into two
-  // regions shared by all blocks, then Wx = hL LCC(qa) CCR and Wy = CCX LCC(qb)^T
+  // regions shared by all blocks, then Wx = -LCC(qa) CCR and Wy = CCX LCC(qb)^T
   const TLayout& TT = S.T;
   int ccr_tiles_max = 0, ccx_tiles_max = 0;
   for (size_t b = 0; b < TT.cb_J3.size(); ++b) {
@@ -332,7 +279,7 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
       o.src = 0; o.src_off = 0; o.rows = r2; o.K = nb1; o.nkb = (nb1 + BKk - 1) / BKk; o.tile_base = ccr_base;
       ops.push_back(o);
       add_chunks((int)ops.size() - 1);
-      add_prob(nb1, TcTermDesc{lcc_tile[qa], ccr_base, kSignHL}, kOpW1);
+      add_prob(nb1, TcTermDesc{lcc_tile[qa], ccr_base, kSignNeg}, kOpW1);
     }
     if (doy && r1 && r2) {
       TcSplitOp o{};

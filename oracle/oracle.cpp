@@ -1720,6 +1720,7 @@ void white_vjp(const Basis& B, const double* H, int hH, const double* ETAb, doub
 namespace {
 #include "oracle_tensor.inc"
 #include "oracle_hf.inc"
+#include "oracle_eom.inc"
 }  // namespace
 
 // ====================================================================== C interface
@@ -1899,5 +1900,31 @@ void orc_normal_order(void* b, const double* in, int herm, double* out) { normal
 int64_t orc_vectorize(void* b, const double* op, double* v) { return vectorize(*(Basis*)b, op, v); }
 double orc_p1_p2(void* b, int a, int bb, int c, int d, int J) { return dot12(*(Basis*)b, a, bb, c, d, J, true); }
 double orc_r1_r2(void* b, int a, int bb, int c, int d, int J) { return dot12(*(Basis*)b, a, bb, c, d, J, false); }
+
+// ---- EOM-IMSRG ladder operators (oracle_eom.inc)
+void* orc_eom_create(void* t) { return new EomMap(build_eom_map(*(TBasis*)t)); }
+void orc_eom_destroy(void* m) { delete (EomMap*)m; }
+int64_t orc_eom_dim(void* m, int64_t* n1b) {
+  *n1b = ((EomMap*)m)->n1b;
+  return ((EomMap*)m)->n;
+}
+void orc_eom_map(void* m, int64_t* pos, int8_t* kind, int8_t* phase, int64_t* mirror) {
+  const EomMap& M = *(EomMap*)m;
+  for (int64_t k = 0; k < M.n; ++k) { pos[k] = M.pos[k]; kind[k] = M.kind[k]; phase[k] = M.phase[k]; mirror[k] = M.mirror[k]; }
+}
+void orc_eom_unwrap(void* t, void* m, const double* v, double* X) { eom_unwrap(*(TBasis*)t, *(EomMap*)m, v, X); }
+void orc_eom_rewrap(void* m, const double* X, double* v) { eom_rewrap(*(EomMap*)m, X, v); }
+double orc_eom_bf1(void* t, const double* A, int hA, const double* X, int a, int b) {
+  return eom_bf1(*(TBasis*)t, A, hA, X, a, b);
+}
+double orc_eom_bf2(void* t, const double* A, int hA, const double* X, int a, int b, int c, int d, int J1, int J2) {
+  return eom_bf2(*(TBasis*)t, A, hA, X, a, b, c, d, J1, J2);
+}
+double orc_pphh_ladder_elem(void* t, const double* X, int a, int b, int c, int d, int J1, int J2) {
+  return pphh_ladder_elem(*(TBasis*)t, X, a, b, c, d, J1, J2);
+}
+void orc_eom_matvec(void* t, void* m, const double* H, const double* v, double* w) {
+  eom_matvec(*(TBasis*)t, *(EomMap*)m, H, v, w);
+}
 
 }  // extern "C"

@@ -19,6 +19,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_bp = np.ctypeslib.ndpointer(dtype=np.int8, flags="C_CONTIGUOUS")
 _lib = None
 
 
@@ -96,6 +98,16 @@ def lib():
         "orc_vectorize": (i64, [vp, _dp, _dp]),
         "orc_p1_p2": (d, [vp, i, i, i, i, i]),
         "orc_r1_r2": (d, [vp, i, i, i, i, i]),
+        "orc_eom_create": (vp, [vp]),
+        "orc_eom_destroy": (None, [vp]),
+        "orc_eom_dim": (i64, [vp, C.POINTER(C.c_int64)]),
+        "orc_eom_map": (None, [vp, _lp, _bp, _bp, _lp]),
+        "orc_eom_unwrap": (None, [vp, vp, _dp, _dp]),
+        "orc_eom_rewrap": (None, [vp, _dp, _dp]),
+        "orc_eom_bf1": (d, [vp, _dp, i, _dp, i, i]),
+        "orc_eom_bf2": (d, [vp, _dp, i, _dp, i, i, i, i, i, i]),
+        "orc_pphh_ladder_elem": (d, [vp, _dp, i, i, i, i, i, i]),
+        "orc_eom_matvec": (None, [vp, vp, _dp, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -488,3 +500,63 @@ class TensorOracle:
     def bf2(self, A, hA, B, hB, a, b, c, d, J1, J2):
         return self.L.orc_tensor_bf2(self.h, A, hA, B, hB, a, b, c, d, J1, J2)
 
+
+class EomOracle:
+    """EOM-IMSRG ladder operators of rank `rank` / parity change `dpar` (doubled) on a scalar
+    Oracle's basis (test-only): the amplitude vector of unwrap_tensor / rewrap_tensor
+    (src/EOM_IMSRG.f90:1039-1340), the known-answer formulas of the reference's EOM
+    scalar-tensor test and the matrix-vector product of matvec_nonzeroX_prod (:518-556)."""
+
+    def __init__(self, o: "Oracle", rank: int, dpar: int = 0):
+        self.t = TensorOracle(o, rank, dpar)
+        self.o, self.L = o, o.L
+        self.m = self.L.orc_eom_create(self.t.h)
+        n1b = C.c_int64()
+        self.n = int(self.L.orc_eom_dim(self.m, C.byref(n1b)))
+        self.n1b = int(n1b.value)
+
+    def __del__(self):
+        try:
+            self.L.orc_eom_destroy(self.m)
+        except Exception:
+            pass
+
+    def amplitude_map(self):
+        pos, mir = np.zeros(self.n, np.int64), np.zeros(self.n, np.int64)
+        kind, ph = np.zeros(self.n, np.int8), np.zeros(self.n, np.int8)
+        self.L.orc_eom_map(self.m, pos, kind, ph, mir)
+        return dict(pos=pos, kind=kind, phase=ph, mirror=mir)
+
+    def unwrap(self, v):
+        X = self.t.new()
+        self.L.orc_eom_unwrap(self.t.h, self.m, np.ascontiguousarray(v, dtype=np.float64), X)
+        return X
+
+    def rewrap(self, X):
+        v = np.zeros(self.n)
+        self.L.orc_eom_rewrap(self.m, X, v)
+        return v
+
+    def bf1(self, H, X, a, b):
+        return self.L.orc_eom_bf1(self.t.h, H, 1, X, a, b)
+
+    def bf2(self, H, X, a, b, c, d, J1, J2):
+        return self.L.orc_eom_bf2(self.t.h, H, 1, X, a, b, c, d, J1, J2)
+
+    def pphh(self, X, a, b, c, d, J1, J2):
+        return self.L.orc_pphh_ladder_elem(self.t.h, X, a, b, c, d, J1, J2)
+
+    def matvec(self, H, v):
+        w = np.zeros(self.n)
+        self.L.orc_eom_matvec(self.t.h, self.m, H, np.ascontiguousarray(v, dtype=np.float64), w)
+        return w
+
+    def matrix(self, H):
+        """The dense EOM matrix, column k = matvec of the k-th unit vector."""
+        M = np.zeros((self.n, self.n))
+        e = np.zeros(self.n)
+        for k in range(self.n):
+            e[k] = 1.0
+            M[:, k] = self.matvec(H, e)
+            e[k] = 0.0
+        return M

@@ -4,7 +4,8 @@ The reference tests TS_commutator_* against its own J-coupled expressions
 scalar_tensor_1body_comm / scalar_tensor_2body_comm (src/brute_force_testing.f90:912-1056,
 2159-2247, 3223-3393).  The oracle restates both; here every one-body element and a seeded
 sample of two-body elements agree to 1e-10 for random operators (scalar anti-hermitian, as
-Omega in BCH_TENSOR; tensor hermitian or anti-hermitian; ranks 1 and 2).
+Omega in BCH_TENSOR, and hermitian, as H in the EOM product; tensor hermitian or
+anti-hermitian; ranks 0, 1 and 2).
 """
 import numpy as np
 import pytest
@@ -33,10 +34,10 @@ def _samples(o, rank, n, seed):
     return out
 
 
-@pytest.mark.parametrize("emax,rank,hB,n2", [(2, 4, 1, 25), (2, 2, -1, 25), (4, 4, 1, 6)])
-def test_scalar_tensor_commutator_known_answers(oracles, emax, rank, hB, n2):
+@pytest.mark.parametrize("emax,rank,hA,hB,n2", [(2, 4, -1, 1, 25), (2, 2, -1, -1, 25), (4, 4, -1, 1, 6),
+                                                (2, 0, 1, 1, 25), (2, 2, 1, -1, 25), (2, 4, 1, 1, 25)])
+def test_scalar_tensor_commutator_known_answers(oracles, emax, rank, hA, hB, n2):
     o, t = _tensor(oracles, emax, rank)
-    hA = -1
     A, B = o.random(3, hA), t.random(4, hB)
     RES = t.commutator(A, hA, B, hB)
     hR = -hA * hB
