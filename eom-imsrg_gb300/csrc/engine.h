@@ -19,6 +19,7 @@ struct TcState;
 struct StepGraph;
 struct AdjointState;
 struct TensorState;
+struct imsrg_eom;
 struct HFState;
 
 // MAGNUS_EXPAND coefficients as the literals of src/IMSRG_MAGNUS.f90:646
@@ -138,6 +139,11 @@ struct Ctx {
                                  int pieces);
   imsrg_status tensor_frob(TensorState& S, const double* op, double scale, int slot);
   imsrg_status bch_tensor(TensorState& S, const double* G, int hG, double* HS, int max_terms, double conv, int* terms);
+  // EOM-IMSRG ladder operators (eom.cu)
+  imsrg_status eom_matvec(imsrg_eom& E, const double* H, const double* d_v, double* d_w);
+  imsrg_status eom_matvec_host(imsrg_eom& E, const double* H, const double* v, double* w);
+  imsrg_status eom_lanczos(imsrg_eom& E, const double* H, int nev, double tol, int max_restarts, double* energies,
+                           double* vectors, int32_t* matvecs, int32_t* restarts);
 
   // Hartree-Fock and normal ordering (hf.cu)
   imsrg_status hf_prepare();

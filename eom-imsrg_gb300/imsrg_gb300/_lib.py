@@ -110,6 +110,15 @@ SIGNATURES = {
     "imsrg_tensor_commutator": [_vp, _vp, _vp, _vp, _i32],
     "imsrg_bch_tensor": [_vp, _vp, _vp, _i32, _d, _pi32],
     "imsrg_tensor_frob_norm": [_vp, _vp, _pd],
+    "imsrg_eom_create": [_vp, _i32, _i32, _pvp],
+    "imsrg_eom_destroy": [_vp, _vp],
+    "imsrg_eom_dim": [_vp, _vp, _pi64, _pi64],
+    "imsrg_eom_amplitude_map": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "imsrg_eom_matvec": [_vp, _vp, _vp, _vp, _vp],
+    "imsrg_eom_matvec_device": [_vp, _vp, _vp, _vp, _vp],
+    "imsrg_eom_unwrap": [_vp, _vp, _vp, _vp],
+    "imsrg_eom_rewrap": [_vp, _vp, _vp, _vp],
+    "imsrg_eom_lanczos": [_vp, _vp, _vp, _i32, _d, _i32, _vp, _vp, _pi32, _pi32],
     "imsrg_commutator_vjp": [_vp, _vp, _vp, _vp, _vp, _vp, _i32],
     "imsrg_white_vjp": [_vp, _vp, _vp, _vp],
     "imsrg_dot_sq_op": [_vp, _vp, _vp, _pd],

@@ -253,6 +253,45 @@ imsrg_status imsrg_bch_tensor(imsrg_ctx* ctx, const imsrg_op* G, imsrg_tensor* H
 /* mat_frob_norm of a tensor operator (src/basic_IMSRG.f90:4056-4087) */
 imsrg_status imsrg_tensor_frob_norm(imsrg_ctx* ctx, const imsrg_tensor* t, double* out);
 
+/* ---- EOM-IMSRG excitation ("ladder") operators (calculate_excited_states,
+ * src/EOM_IMSRG.f90:13-98).  A ladder operator of rank rank2/2 and parity change dpar2 (0 or 2)
+ * is a tensor whose only amplitudes are fph and the pp-hh arrays tgam(3) / tgam(7), stored with
+ * lam(1) = 1 (an amplitude <pp J1|X|hh J2> with J1 > J2 sits in tgam(7) of block (J2, J1),
+ * phase 1).  Amplitude vectors are ordered as unwrap_tensor / rewrap_tensor order them
+ * (src/EOM_IMSRG.f90:1039-1340): fph of allowed (particle, hole) pairs, particles outer; then
+ * per block the tgam(3) elements row by row and, for J1 < J2, the tgam(7) elements row by row,
+ * pairs of identical orbits skipped at odd J. */
+typedef struct imsrg_eom imsrg_eom;
+/* on a host-only context (device < 0) only imsrg_eom_dim and imsrg_eom_amplitude_map work */
+imsrg_status imsrg_eom_create(imsrg_ctx* ctx, int32_t rank2, int32_t dpar2, imsrg_eom** out);
+imsrg_status imsrg_eom_destroy(imsrg_ctx* ctx, imsrg_eom* eom);
+/* the amplitude count N (sps + tps of LANCZOS_DIAGONALIZE, src/EOM_IMSRG.f90:199-262) and the
+ * number of one-body (1p1h) amplitudes, which come first */
+imsrg_status imsrg_eom_dim(imsrg_ctx* ctx, const imsrg_eom* eom, int64_t* n, int64_t* n1b);
+/* per amplitude: slab position, kind (0 fph, 1 tgam(3), 2 tgam(7)), (-1)^((J1-J2)/2) of its block
+ * for kind 2, and the slab position of the transposed copy unwrap_tensor writes for J1 == J2
+ * blocks (-1 otherwise); any pointer may be NULL */
+imsrg_status imsrg_eom_amplitude_map(imsrg_ctx* ctx, const imsrg_eom* eom, int64_t* pos, int8_t* kind, int8_t* phase,
+                                     int64_t* mirror);
+/* matvec_nonzeroX_prod (src/EOM_IMSRG.f90:518-556): w = rewrap([H, unwrap(v)]) for a hermitian
+ * scalar H, the product of the EOM_TS_commutator_* routines (src/EOM_TS_commutators.f90), in
+ * the context's precision.  v, w: N host doubles (the _device form: N device doubles). */
+imsrg_status imsrg_eom_matvec(imsrg_ctx* ctx, imsrg_eom* eom, const imsrg_op* H, const double* v, double* w);
+imsrg_status imsrg_eom_matvec_device(imsrg_ctx* ctx, imsrg_eom* eom, const imsrg_op* H, const double* d_v, double* d_w);
+/* unwrap_tensor of host amplitudes into a tensor of the same rank / parity (herm set to 1), and
+ * rewrap_tensor back to host amplitudes */
+imsrg_status imsrg_eom_unwrap(imsrg_ctx* ctx, imsrg_eom* eom, const double* v, imsrg_tensor* X);
+imsrg_status imsrg_eom_rewrap(imsrg_ctx* ctx, imsrg_eom* eom, const imsrg_tensor* X, double* v);
+/* LANCZOS_DIAGONALIZE (src/EOM_IMSRG.f90:164-334): the nev eigenvalues of smallest magnitude of
+ * the EOM matrix (the excitation energies, ladder_ops(i)%E0), ascending; vectors (N x nev,
+ * column-major, may be NULL) receives the normalised amplitude vectors.  Thick-restart Lanczos
+ * with 5 nev basis vectors; converged when |beta s| <= tol |theta| for every wanted pair (the
+ * reference: dsaupd, which = 'SM', tol 1e-10, 500 iterations).  IMSRG_ERR_NOT_CONVERGED after
+ * max_restarts restarts (the results of the last one are still written). */
+imsrg_status imsrg_eom_lanczos(imsrg_ctx* ctx, imsrg_eom* eom, const imsrg_op* H, int32_t nev, double tol,
+                               int32_t max_restarts, double* energies, double* vectors, int32_t* matvecs,
+                               int32_t* restarts);
+
 /* ---- reverse mode (FP64) for adjoint derivatives of a flow (no counterpart in the
  * reference, which has no derivative code).  Each call ACCUMULATES into its outputs:
  * Lb += d<RESb, [L,R]>/dL and Rb += d<RESb, [L,R]>/dR for the FP64 commutator of

@@ -87,3 +87,17 @@ def test_decoupled_product_is_symmetric(oracles):
     assert np.abs(M - M.T).max() <= 1e-12 * np.abs(M).max()
     Mf = e.matrix(H)
     assert np.abs(Mf - Mf.T).max() > 1e-3 * np.abs(Mf).max()
+
+
+@pytest.mark.parametrize("emax,rank,dpar", [(2, 0, 0), (2, 4, 0), (4, 2, 0), (4, 2, 2), (4, 6, 2)])
+def test_library_amplitude_map_matches_oracle(built_lib, oracles, emax, rank, dpar):
+    """imsrg_eom_amplitude_map (host-only context) equals the oracle's unwrap_tensor order."""
+    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300.eom import LadderSpace
+    eng = Engine(make_basis(emax), device=-1)
+    space = LadderSpace(eng, rank, dpar)
+    _, e = _eom(oracles, emax, rank, dpar)
+    assert (space.n, space.n1b) == (e.n, e.n1b)
+    got, ref = space.amplitude_map(), e.amplitude_map()
+    for k in ("pos", "kind", "phase", "mirror"):
+        assert np.array_equal(got[k], ref[k]), k

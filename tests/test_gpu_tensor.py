@@ -13,8 +13,8 @@ TOL = 1e-10
 PIECES = [1 | 8, 2, 4, 16, 32, 64, 127]
 
 
-@pytest.mark.parametrize("emax,rank", [(2, 4), (4, 4), (4, 2)])
-@pytest.mark.parametrize("hA,hB", [(-1, 1), (-1, -1), (1, 1)])
+@pytest.mark.parametrize("emax,rank", [(2, 4), (4, 4), (4, 2), (4, 0)])
+@pytest.mark.parametrize("hA,hB", [(-1, 1), (-1, -1), (1, 1), (1, -1)])
 def test_tensor_commutator_pieces(oracles, engines, emax, rank, hA, hB):
     from oracle.oracle import TensorOracle
     o, eng = oracles(emax), engines(emax)
