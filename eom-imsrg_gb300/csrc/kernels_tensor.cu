@@ -455,10 +455,11 @@ __device__ __forceinline__ void recouple_loop(const DevLayout& D, const DevTLayo
 
 // ---------------------------------------------------------------- TS_commutator_222_ph
 // src/TS_commutators.f90:1529-1843 for one cross-coupled tensor block: every element of
-// Wx (and Wy) above 1e-6 in size recouples into the two-body tensor elements it feeds (ACCUMULATES)
+// Wx (and Wy) above thresh in size recouples into the two-body tensor elements it feeds (ACCUMULATES);
+// TS_commutator_222_ph uses thresh = 1e-6 (src/TS_commutators.f90:1562, 1714), the EOM product 0
 __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __restrict__ Wx,
                                   const double* __restrict__ Wy, int J3, int J4, int qa, int qb, int hL, int hR,
-                                  double* __restrict__ RES) {
+                                  double thresh, double* __restrict__ RES) {
   const int r1 = D.cc_rlen[qa], r2 = D.cc_rlen[qb];
   const int rank = T.rank;
   const double p34 = sqrt((J3 + 1.0) * (J4 + 1.0));
@@ -467,12 +468,12 @@ __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __res
        e += (int64_t)gridDim.x * blockDim.x) {
     const int JX = (int)(e / r1), IX = (int)(e - (int64_t)JX * r1);
     const double X = Wx[e], Y = Wy ? Wy[e] : 0.0;
-    if (fabs(X) <= 1e-6 && fabs(Y) <= 1e-6) continue;
+    if (fabs(X) <= thresh && fabs(Y) <= thresh) continue;
     const int d = D.cc_ra[D.cc_row_off[qa] + IX], a = D.cc_rb[D.cc_row_off[qa] + IX];
     const int c = D.cc_ra[D.cc_row_off[qb] + JX], b = D.cc_rb[D.cc_row_off[qb] + JX];
     const int ja = D.jj[a], jb = D.jj[b], jc = D.jj[c], jd = D.jj[d];
     const double pabcd = d_sgn((ja + jb + jc + jd) >> 1);
-    if (fabs(X) > 1e-6) {
+    if (fabs(X) > thresh) {
       const int J1min = abs(ja - jb), J1max = ja + jb, J2min = abs(jc - jd), J2max = jc + jd;
       if (b >= a) {
         if (d >= c) {
@@ -500,7 +501,7 @@ __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __res
         }
       }
     }
-    if (fabs(Y) > 1e-6) {
+    if (fabs(Y) > thresh) {
       const int J1min = abs(jd - jb), J1max = jd + jb, J2min = abs(jc - ja), J2max = jc + ja;
       if (b >= d) {
         if (a >= c) {

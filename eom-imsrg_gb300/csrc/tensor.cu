@@ -34,7 +34,7 @@ __global__ void k_ts_pphh_update(int64_t n, int64_t off, double* RES, const doub
 __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* R, int hR, int J3, int J4, int qa, int qb, int term,
                           double scale, double* out);
 __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* Wx, const double* Wy, int J3, int J4,
-                                  int qa, int qb, int hL, int hR, double* RES);
+                                  int qa, int qb, int hL, int hR, double thresh, double* RES);
 }  // namespace imsrg
 
 namespace {
@@ -324,6 +324,7 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
   CKT(ensure_workspace());
   const DevTLayout& T = S.DT;
   const int hRES = -hL * hR;
+  const double thresh = (pieces & kTensorExactPh) ? 0.0 : 1e-6;
   if (L.cc_size) CKT(pandya(Lp, hL, d_lcc));
   const int nob = T.n_ob;
   if (pieces & 1) {
@@ -433,7 +434,7 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       CKT(tc_gemm_on(S.tc_map, S.tc_slice_rows, S.tc_probs, S.tc_tiles + S.ph_tile_start[b], S.ph_tile_n[b], out, hL,
                      hR));
       k_ts222ph_scatter<<<grid_n((int64_t)r1 * r2), 256, 0, stream>>>(D, T, S.wx, doy ? S.wy : nullptr, J3, J4, qa,
-                                                                      qb, hL, hR, RES);
+                                                                      qb, hL, hR, thresh, RES);
       CKT(launched("k_ts222ph_scatter"));
     }
   } else if (pieces & 64) {
@@ -464,7 +465,7 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
         CKT(launched("k_gemm_fp64(tensor ph)"));
       }
       k_ts222ph_scatter<<<grid_n((int64_t)r1 * r2), 256, 0, stream>>>(D, T, S.wx, doy ? S.wy : nullptr, J3, J4, qa,
-                                                                      qb, hL, hR, RES);
+                                                                      qb, hL, hR, thresh, RES);
       CKT(launched("k_ts222ph_scatter"));
     }
   }

@@ -20,6 +20,10 @@ using imsrg::TcSplitOp;
 using imsrg::TcTile;
 using imsrg::TLayout;
 
+// pieces flag of Ctx::tensor_commutator: recouple every nonzero Wx / Wy element of TS_222_ph
+// (the EOM product) instead of those above 1e-6 (TS_commutator_222_ph)
+constexpr int kTensorExactPh = 512;
+
 // output slot of the second product of a tensor ladder problem (TcOut::f64 index)
 constexpr int kTensorOpW3 = 7;
 

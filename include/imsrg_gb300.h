@@ -243,7 +243,9 @@ imsrg_status imsrg_tensor_upload_slab(imsrg_ctx* ctx, imsrg_tensor* t, const dou
 imsrg_status imsrg_tensor_download_slab(imsrg_ctx* ctx, const imsrg_tensor* t, double* host);
 /* [L (scalar), R (tensor)] -> RES (RES->herm = -L->herm * R->herm), FP64.  pieces: 1 TS_111,
  * 2 TS_121, 4 TS_211, 8 TS_122, 16 TS_212, 32 TS_222_pp_hh + TS_221, 64 TS_222_ph
- * (src/TS_commutators.f90); 127 = the full commutator.  111 and 122 assign, the rest accumulate. */
+ * (src/TS_commutators.f90); 127 = the full commutator.  111 and 122 assign, the rest accumulate.
+ * + 512: TS_222_ph recouples every nonzero product element instead of those above 1e-6 in size
+ * (src/TS_commutators.f90:1562, 1714), as the EOM product does. */
 imsrg_status imsrg_tensor_commutator(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_tensor* R, imsrg_tensor* RES,
                                      int32_t pieces);
 /* BCH_TENSOR: HS <- e^G HS e^-G for a hermitian tensor HS and an anti-hermitian scalar G; stops when
