@@ -13,9 +13,12 @@
 // elements are X's and whose stored de-excitation elements are h times their images, so that
 // X = (S(+1) + S(-1)) / 2 as operators and [H, X] = ([H, S(+1)] + [H, S(-1)]) / 2.  Both
 // S(h) are written by one gather kernel from the amplitude vector and both results are read
-// back by one kernel; the commutators are the tensor engine's, in the context's precision, with
-// every particle-hole product recoupled (EOM_TS_commutator_222_ph has no 1e-6 cut, and the cut
-// would make the product depend on the scale of v).
+// back by one kernel.  The commutators run in the tensor engine's excitation mode: only the
+// terms with a nonzero (fph, pp-hh) operand of S(h) and only the fph and pp-hh outputs are
+// computed (the ladder's remaining products are small and stay FP64; the rest follows the
+// context's precision), and every particle-hole product is recoupled
+// (EOM_TS_commutator_222_ph has no 1e-6 cut, and a cut would make the product depend on the
+// scale of v).
 //
 // The eigensolver is a thick-restart Lanczos with full reorthogonalisation on the host
 // (ncv = 5 nev basis vectors, the nev Ritz values of smallest magnitude kept, convergence
@@ -214,8 +217,8 @@ imsrg_status Ctx::eom_matvec(imsrg_eom& E, const double* Hd, const double* d_v, 
   const int g = grid_of(E.n);
   k_eom_pack<<<g, 256, 0, stream>>>(E.n, E.d_pos, E.d_kind, E.d_phase, E.d_mirror, d_v, E.d_S[0], E.d_S[1]);
   CKE(launched("k_eom_pack"));
-  CKE(tensor_commutator(*E.ts, Hd, 1, E.d_S[0], 1, E.d_Y[0], 127 | kTensorExactPh));
-  CKE(tensor_commutator(*E.ts, Hd, 1, E.d_S[1], -1, E.d_Y[1], 127 | kTensorExactPh));
+  CKE(tensor_commutator(*E.ts, Hd, 1, E.d_S[0], 1, E.d_Y[0], 127 | kTensorExcitation));
+  CKE(tensor_commutator(*E.ts, Hd, 1, E.d_S[1], -1, E.d_Y[1], 127 | kTensorExcitation));
   k_eom_unpack<<<g, 256, 0, stream>>>(E.n, E.d_pos, E.d_kind, E.d_phase, E.d_Y[0], E.d_Y[1], d_w);
   return launched("k_eom_unpack");
 }

@@ -308,9 +308,23 @@ __global__ void k_ts221(DevLayout D, DevTLayout T, const double* __restrict__ w1
 
 // ---------------------------------------------------------------- TS_commutator_122 / 212
 // src/TS_commutators.f90:555-663 (ASSIGNS) and :666-806 (ACCUMULATES): one thread per two-body element
+// element x of a segment list (binary search over the prefix counts); x itself without one
+__device__ __forceinline__ int64_t d_seg_elem(const ElemSegs& sg, int64_t x) {
+  if (!sg.n) return x;
+  int lo = 0, hi = sg.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sg.pre[mid] <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return sg.off[lo] + (x - sg.pre[lo]);
+}
+
 __global__ void k_ts122(DevLayout D, DevTLayout T, const double* __restrict__ L, int hL, const double* __restrict__ R,
-                        int hR, double* __restrict__ RES) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T.n2b; e += (int64_t)gridDim.x * blockDim.x) {
+                        int hR, double* __restrict__ RES, ElemSegs sg) {
+  const int64_t ntot = sg.n ? sg.pre[sg.n] : T.n2b;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < ntot; x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = d_seg_elem(sg, x);
     int q, g, a, b, c, d;
     d_tdecode(D, T, e, q, g, a, b, c, d);
     const int J1 = T.J1[q], J2 = T.J2[q];
@@ -336,9 +350,11 @@ __global__ void k_ts122(DevLayout D, DevTLayout T, const double* __restrict__ L,
 }
 
 __global__ void k_ts212(DevLayout D, DevTLayout T, const double* __restrict__ L, int hL, const double* __restrict__ R,
-                        int hR, double* __restrict__ RES) {
+                        int hR, double* __restrict__ RES, ElemSegs sg) {
   const int rank = T.rank;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T.n2b; e += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t ntot = sg.n ? sg.pre[sg.n] : T.n2b;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < ntot; x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = d_seg_elem(sg, x);
     int q, g, a, b, c, d;
     d_tdecode(D, T, e, q, g, a, b, c, d);
     const int J1 = T.J1[q], J2 = T.J2[q];
@@ -380,7 +396,7 @@ __global__ void k_ts_pphh_update(int64_t n, int64_t off, double* __restrict__ RE
 // term 1 fills CCX (r1 x nb2: rows (a,b) of channel qa, ph columns (p,h) of channel qb),
 // term 2 fills CCR (nb1 x r2: ph columns (p,h) of qa, rows (b,a) of qb); out is scaled by `scale`.
 __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* __restrict__ R, int hR, int J3, int J4, int qa,
-                          int qb, int term, double scale, double* __restrict__ out) {
+                          int qb, int term, double scale, int exc, double* __restrict__ out) {
   const int r1 = D.cc_rlen[qa], r2 = D.cc_rlen[qb];
   const int nb1 = D.cc_nph[qa], nb2 = D.cc_nph[qb];
   const int64_t n = term == 1 ? (int64_t)r1 * nb2 : (int64_t)nb1 * r2;
@@ -398,7 +414,11 @@ __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* __restrict__ 
       b = D.cc_ra[D.cc_row_off[qb] + col]; a = D.cc_rb[D.cc_row_off[qb] + col];
     }
     double val = 0.0;
-    if (((D.ll[a] + D.ll[h]) & 1) == ((D.ll[b] + D.ll[p] + dp) & 1) && D.tz[a] + D.tz[h] == D.tz[b] + D.tz[p]) {
+    // an excitation operator has only (pp,hh) and (hh,pp) elements: the pairs (a,h) and (p,b) read
+    // below must be of opposite classes
+    const int ca = D.con[a] + D.con[h], cb = D.con[p] + D.con[b];
+    const bool live = !exc || (ca == 0 && cb == 2) || (ca == 2 && cb == 0);
+    if (live && ((D.ll[a] + D.ll[h]) & 1) == ((D.ll[b] + D.ll[p] + dp) & 1) && D.tz[a] + D.tz[h] == D.tz[b] + D.tz[p]) {
       const int ja = D.jj[a], jb = D.jj[b], jp = D.jj[p], jh = D.jj[h];
       double sm = 0.0;
       for (int Ja = abs(ja - jh); Ja <= ja + jh; Ja += 2)
@@ -440,7 +460,12 @@ __device__ __forceinline__ bool d_odd(int J) { return ((J >> 1) & 1) == 1; }
 template <class C>
 __device__ __forceinline__ void recouple_loop(const DevLayout& D, const DevTLayout& T, double* RES, int J3, int J4,
                                               int o1, int o2, int i1, int i2, bool skip_o, bool skip_i, int n1, int n2,
-                                              int n3, int n4, double p34, C coef, int a, int b, int c, int d) {
+                                              int n3, int n4, double p34, C coef, int a, int b, int c, int d,
+                                              int exc) {
+  if (exc) {  // only the (pp,hh) and (hh,pp) outputs are wanted
+    const int g = d_tg(D.con[a] + D.con[b], D.con[c] + D.con[d]);
+    if (g != 2 && g != 6) return;
+  }
   for (int J1 = o1; J1 <= o2; J1 += 2) {
     if (skip_o && d_odd(J1)) continue;
     const double p134 = p34 * sqrt(J1 + 1.0);
@@ -459,7 +484,7 @@ __device__ __forceinline__ void recouple_loop(const DevLayout& D, const DevTLayo
 // TS_commutator_222_ph uses thresh = 1e-6 (src/TS_commutators.f90:1562, 1714), the EOM product 0
 __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __restrict__ Wx,
                                   const double* __restrict__ Wy, int J3, int J4, int qa, int qb, int hL, int hR,
-                                  double thresh, double* __restrict__ RES) {
+                                  double thresh, int exc, double* __restrict__ RES) {
   const int r1 = D.cc_rlen[qa], r2 = D.cc_rlen[qb];
   const int rank = T.rank;
   const double p34 = sqrt((J3 + 1.0) * (J4 + 1.0));
@@ -478,26 +503,26 @@ __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __res
       if (b >= a) {
         if (d >= c) {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, a == b, c == d, ja, jd, jb, jc, p34,
-                        [&](int, int J2) { return d_sgn((jb + jd + J2) >> 1) * ph34 * hL * X; }, a, b, c, d);
+                        [&](int, int J2) { return d_sgn((jb + jd + J2) >> 1) * ph34 * hL * X; }, a, b, c, d, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == d, a == b, jd, ja, jc, jb, p34,
-                        [&](int J1, int) { return -d_sgn((jc + ja + J1 + rank) >> 1) * hR * X; }, c, d, a, b);
+                        [&](int J1, int) { return -d_sgn((jc + ja + J1 + rank) >> 1) * hR * X; }, c, d, a, b, exc);
         } else {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, a == b, false, ja, jd, jb, jc, p34,
-                        [&](int, int) { return d_sgn((jb + jc) >> 1) * ph34 * hL * X; }, a, b, d, c);
+                        [&](int, int) { return d_sgn((jb + jc) >> 1) * ph34 * hL * X; }, a, b, d, c, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, false, a == b, jd, ja, jc, jb, p34,
-                        [&](int, int) { return d_sgn((ja - jd + rank) >> 1) * hR * X; }, d, c, a, b);
+                        [&](int, int) { return d_sgn((ja - jd + rank) >> 1) * hR * X; }, d, c, a, b, exc);
         }
       } else {
         if (d >= c) {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, false, c == d, ja, jd, jb, jc, p34,
-                        [&](int J1, int J2) { return d_sgn((ja + jd + J1 + J2) >> 1) * ph34 * hL * X; }, b, a, c, d);
+                        [&](int J1, int J2) { return d_sgn((ja + jd + J1 + J2) >> 1) * ph34 * hL * X; }, b, a, c, d, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == d, false, jd, ja, jc, jb, p34,
-                        [&](int J1, int J2) { return d_sgn((jc - jb + J1 + J2 + rank) >> 1) * hR * X; }, c, d, b, a);
+                        [&](int J1, int J2) { return d_sgn((jc - jb + J1 + J2 + rank) >> 1) * hR * X; }, c, d, b, a, exc);
         } else {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, false, false, ja, jd, jb, jc, p34,
-                        [&](int J1, int) { return d_sgn((ja + jc + J1) >> 1) * ph34 * hL * X; }, b, a, d, c);
+                        [&](int J1, int) { return d_sgn((ja + jc + J1) >> 1) * ph34 * hL * X; }, b, a, d, c, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, false, false, jd, ja, jc, jb, p34,
-                        [&](int, int J2) { return d_sgn((jb - jd + J2 + rank) >> 1) * hR * X; }, d, c, b, a);
+                        [&](int, int J2) { return d_sgn((jb - jd + J2 + rank) >> 1) * hR * X; }, d, c, b, a, exc);
         }
       }
     }
@@ -506,26 +531,26 @@ __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __res
       if (b >= d) {
         if (a >= c) {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, d == b, c == a, jd, ja, jb, jc, p34,
-                        [&](int, int J2) { return d_sgn((jc + ja + J2) >> 1) * hL * Y; }, d, b, c, a);
+                        [&](int, int J2) { return d_sgn((jc + ja + J2) >> 1) * hL * Y; }, d, b, c, a, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == a, b == d, ja, jd, jc, jb, p34,
-                        [&](int J1, int) { return d_sgn((jd - jb + J1 + rank) >> 1) * ph34 * hR * Y; }, c, a, d, b);
+                        [&](int J1, int) { return d_sgn((jd - jb + J1 + rank) >> 1) * ph34 * hR * Y; }, c, a, d, b, exc);
         } else {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, d == b, c == a, jd, ja, jb, jc, p34,
-                        [&](int, int) { return -hL * Y; }, d, b, a, c);
+                        [&](int, int) { return -hL * Y; }, d, b, a, c, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, a == c, b == d, ja, jd, jc, jb, p34,
-                        [&](int, int) { return pabcd * ph34 * d_sgn(rank >> 1) * hR * Y; }, a, c, d, b);
+                        [&](int, int) { return pabcd * ph34 * d_sgn(rank >> 1) * hR * Y; }, a, c, d, b, exc);
         }
       } else {
         if (a >= c) {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, b == d, a == c, jd, ja, jb, jc, p34,
-                        [&](int J1, int J2) { return -pabcd * d_sgn((J1 + J2) >> 1) * hL * Y; }, b, d, c, a);
+                        [&](int J1, int J2) { return -pabcd * d_sgn((J1 + J2) >> 1) * hL * Y; }, b, d, c, a, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == a, b == d, ja, jd, jc, jb, p34,
-                        [&](int J1, int J2) { return d_sgn((J1 + J2 + rank) >> 1) * ph34 * hR * Y; }, c, a, b, d);
+                        [&](int J1, int J2) { return d_sgn((J1 + J2 + rank) >> 1) * ph34 * hR * Y; }, c, a, b, d, exc);
         } else {
           recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, b == d, a == c, jd, ja, jb, jc, p34,
-                        [&](int J1, int) { return d_sgn((jb + jd + J1) >> 1) * hL * Y; }, b, d, a, c);
+                        [&](int J1, int) { return d_sgn((jb + jd + J1) >> 1) * hL * Y; }, b, d, a, c, exc);
           recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, a == c, d == b, ja, jd, jc, jb, p34,
-                        [&](int, int J2) { return d_sgn((ja - jc + J2 + rank) >> 1) * ph34 * hR * Y; }, a, c, b, d);
+                        [&](int, int J2) { return d_sgn((ja - jc + J2 + rank) >> 1) * ph34 * hR * Y; }, a, c, b, d, exc);
         }
       }
     }
@@ -581,8 +606,10 @@ __device__ __forceinline__ float d_telem_f(const DevLayout& D, const DevTLayout&
 }  // namespace
 
 __global__ void k_ts122f(DevLayout D, DevTLayout T, const double* __restrict__ L, int hL, const double* __restrict__ R,
-                         int hR, double* __restrict__ RES) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T.n2b; e += (int64_t)gridDim.x * blockDim.x) {
+                         int hR, double* __restrict__ RES, ElemSegs sg) {
+  const int64_t ntot = sg.n ? sg.pre[sg.n] : T.n2b;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < ntot; x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = d_seg_elem(sg, x);
     int q, g, a, b, c, d;
     d_tdecode(D, T, e, q, g, a, b, c, d);
     const int J1 = T.J1[q], J2 = T.J2[q];
@@ -609,9 +636,11 @@ __global__ void k_ts122f(DevLayout D, DevTLayout T, const double* __restrict__ L
 }
 
 __global__ void k_ts212f(DevLayout D, DevTLayout T, const double* __restrict__ L, int hL, const double* __restrict__ R,
-                         int hR, double* __restrict__ RES) {
+                         int hR, double* __restrict__ RES, ElemSegs sg) {
   const int rank = T.rank;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T.n2b; e += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t ntot = sg.n ? sg.pre[sg.n] : T.n2b;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < ntot; x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = d_seg_elem(sg, x);
     int q, g, a, b, c, d;
     d_tdecode(D, T, e, q, g, a, b, c, d);
     const int J1 = T.J1[q], J2 = T.J2[q];

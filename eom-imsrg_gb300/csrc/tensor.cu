@@ -26,15 +26,19 @@ __global__ void k_ts121(DevLayout D, DevTLayout T, const double* L, int hL, cons
 __global__ void k_ts211(DevLayout D, DevTLayout T, const double* LCC, int hL, const double* R, int hR, double* RES,
                         int hRES);
 __global__ void k_ts221(DevLayout D, DevTLayout T, const double* w1, const double* w2, int pm, double* RES, int hRES);
-__global__ void k_ts122(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
-__global__ void k_ts212(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
-__global__ void k_ts122f(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
-__global__ void k_ts212f(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES);
+__global__ void k_ts122(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES,
+                        ElemSegs sg);
+__global__ void k_ts212(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES,
+                        ElemSegs sg);
+__global__ void k_ts122f(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES,
+                         ElemSegs sg);
+__global__ void k_ts212f(DevLayout D, DevTLayout T, const double* L, int hL, const double* R, int hR, double* RES,
+                         ElemSegs sg);
 __global__ void k_ts_pphh_update(int64_t n, int64_t off, double* RES, const double* w1, const double* w2);
 __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* R, int hR, int J3, int J4, int qa, int qb, int term,
-                          double scale, double* out);
+                          double scale, int exc, double* out);
 __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* Wx, const double* Wy, int J3, int J4,
-                                  int qa, int qb, int hL, int hR, double thresh, double* RES);
+                                  int qa, int qb, int hL, int hR, double thresh, int exc, double* RES);
 }  // namespace imsrg
 
 namespace {
@@ -89,6 +93,17 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
   CKT(ensure_workspace());
   const auto pphh = build_tensor_pphh_problems(T, L);
   const auto pphh_tiles = build_tiles(pphh, 64, 64);
+  const auto exc = build_tensor_pphh_problems(T, L, true);
+  const auto exc_tiles = build_tiles(exc, 64, 64);
+  // the (pp,hh) and (hh,pp) arrays of every block, relative to goff[0]
+  std::vector<int64_t> seg_off, seg_pre{0};
+  for (int q = 0; q < T.nblocks; ++q)
+    for (int g : {2, 6}) {
+      const int64_t n = (int64_t)T.n1[(size_t)q * 9 + g] * T.n2[(size_t)q * 9 + g];
+      if (!n) continue;
+      seg_off.push_back(T.goff[(size_t)q * 9 + g] - T.goff[0]);
+      seg_pre.push_back(seg_pre.back() + n);
+    }
   // per cross-coupled block: Wx = -LCC(qa) CCR and Wy = CCX LCC(qb)^T
   std::vector<GemmProb> cbp;
   std::vector<GemmTile> cbt;
@@ -138,12 +153,17 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
   pk.add(six_f, &d.six_f);
   pk.add(T.tnb_start, &d.tnb_start); pk.add(T.tnb_count, &d.tnb_count); pk.add(T.tnb_list, &d.tnb_list);
   pk.add(pphh, &st->pphh_p); pk.add(pphh_tiles, &st->pphh_t);
+  pk.add(exc, &st->exc_p); pk.add(exc_tiles, &st->exc_t);
+  pk.add(seg_off, &st->exc_segs.off); pk.add(seg_pre, &st->exc_segs.pre);
   pk.add(cbp, &st->cb_p); pk.add(cbt, &st->cb_t);
   pk.add(T.seg_start, &st->seg_start); pk.add(T.seg_len, &st->seg_len); pk.add(T.seg_w, &st->seg_w);
   CKT(cuda(cudaMalloc(&st->tables, pk.buf.size()), "cudaMalloc(tensor tables)"));
   CKT(cuda(cudaMemcpy(st->tables, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tensor tables)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(st->tables) + f.first;
   st->n_pphh_t = (int)pphh_tiles.size();
+  st->n_exc_t = (int)exc_tiles.size();
+  st->exc_segs.n = (int)seg_off.size();
+  st->exc_n2 = seg_pre.back();
   st->nseg = (int)T.seg_start.size();
   const size_t tb = sizeof(double) * (size_t)T.slab;
   for (double** p : {&st->w1, &st->w2, &st->bch_a, &st->bch_b}) {
@@ -324,7 +344,12 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
   CKT(ensure_workspace());
   const DevTLayout& T = S.DT;
   const int hRES = -hL * hR;
-  const double thresh = (pieces & kTensorExactPh) ? 0.0 : 1e-6;
+  const double thresh = (pieces & (kTensorExactPh | kTensorExcitation)) ? 0.0 : 1e-6;
+  // excitation mode: R has only fph and (pp,hh) / (hh,pp) elements and only the fph and
+  // (pp,hh) / (hh,pp) elements of RES are wanted (the EOM product)
+  const int exc = (pieces & kTensorExcitation) ? 1 : 0;
+  const ElemSegs segs = exc ? S.exc_segs : ElemSegs{};
+  const int64_t n2out = exc ? S.exc_n2 : (int64_t)T.n2b;
   if (L.cc_size) CKT(pandya(Lp, hL, d_lcc));
   const int nob = T.n_ob;
   if (pieces & 1) {
@@ -340,21 +365,21 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
     k_ts211<<<(nob * 32 + 255) / 256, 256, 0, stream>>>(D, T, d_lcc, hL, R, hR, RES, hRES);
     CKT(launched("k_ts211"));
   }
-  if ((pieces & 8) && T.n2b) {
+  if ((pieces & 8) && n2out) {
     if (precision != IMSRG_PREC_FP64)
-      k_ts122f<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+      k_ts122f<<<grid_n(n2out), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES, segs);
     else
-      k_ts122<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+      k_ts122<<<grid_n(n2out), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES, segs);
     CKT(launched("k_ts122"));
   }
-  if ((pieces & 16) && T.n2b) {
+  if ((pieces & 16) && n2out) {
     if (precision != IMSRG_PREC_FP64)
-      k_ts212f<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+      k_ts212f<<<grid_n(n2out), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES, segs);
     else
-      k_ts212<<<grid_n(T.n2b), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES);
+      k_ts212<<<grid_n(n2out), 256, 0, stream>>>(D, T, Lp, hL, R, hR, RES, segs);
     CKT(launched("k_ts212"));
   }
-  if ((pieces & 32) && precision != IMSRG_PREC_FP64) {  // split-BF16 products through pp pairs
+  if ((pieces & 32) && precision != IMSRG_PREC_FP64 && !exc) {  // split-BF16 products through pp pairs
     CKT(tensor_tc_prepare(S));
     const size_t tb = sizeof(double) * (size_t)T.slab;
     CKT(cuda(cudaMemsetAsync(S.w1, 0, tb, stream), "memset(tensor w1)"));
@@ -387,12 +412,13 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
     const size_t tb = sizeof(double) * (size_t)T.slab;
     CKT(cuda(cudaMemsetAsync(S.w1, 0, tb, stream), "memset(tensor w1)"));
     CKT(cuda(cudaMemsetAsync(S.w2, 0, tb, stream), "memset(tensor w2)"));
-    if (S.n_pphh_t) {
+    const int nt = exc ? S.n_exc_t : S.n_pphh_t;
+    if (nt) {
       GemmOperands ops{};
       ops.in[kOpL] = Lp; ops.in[kOpR] = R;
       ops.out[kOpW1] = S.w1; ops.out[kOpW2] = S.w2;
       ops.hL = hL; ops.hR = hR;
-      k_gemm_fp64<<<S.n_pphh_t, 256, 0, stream>>>(S.pphh_p, S.pphh_t, ops);
+      k_gemm_fp64<<<nt, 256, 0, stream>>>(exc ? S.exc_p : S.pphh_p, exc ? S.exc_t : S.pphh_t, ops);
       CKT(launched("k_gemm_fp64(tensor pphh)"));
     }
     if (T.n2b) {
@@ -416,14 +442,14 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       if (!dox && !doy) continue;
       if (dox) {
         k_tpandya<<<grid_n((int64_t)nb1 * r2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 2,
-                                                                 1.0 / std::sqrt(J3 + 1.0), S.ccr);
+                                                                 1.0 / std::sqrt(J3 + 1.0), exc, S.ccr);
         CKT(launched("k_tpandya"));
       } else {
         CKT(cuda(cudaMemsetAsync(S.wx, 0, sizeof(double) * (size_t)r1 * r2, stream), "memset(Wx)"));
       }
       if (doy) {
         k_tpandya<<<grid_n((int64_t)r1 * nb2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 1,
-                                                                 1.0 / std::sqrt(J4 + 1.0), S.ccx);
+                                                                 1.0 / std::sqrt(J4 + 1.0), exc, S.ccx);
         CKT(launched("k_tpandya"));
       }
       CKT(tc_split_on(S.tc_ops, S.tc_chunks + S.ph_chunk_start[b], S.ph_chunk_n[b], S.ccr, S.ccx, S.tc_buf,
@@ -434,7 +460,7 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       CKT(tc_gemm_on(S.tc_map, S.tc_slice_rows, S.tc_probs, S.tc_tiles + S.ph_tile_start[b], S.ph_tile_n[b], out, hL,
                      hR));
       k_ts222ph_scatter<<<grid_n((int64_t)r1 * r2), 256, 0, stream>>>(D, T, S.wx, doy ? S.wy : nullptr, J3, J4, qa,
-                                                                      qb, hL, hR, thresh, RES);
+                                                                      qb, hL, hR, thresh, exc, RES);
       CKT(launched("k_ts222ph_scatter"));
     }
   } else if (pieces & 64) {
@@ -446,14 +472,14 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       if (!dox && !doy) continue;
       if (dox) {
         k_tpandya<<<grid_n((int64_t)nb1 * r2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 2,
-                                                                 1.0 / std::sqrt(J3 + 1.0), S.ccr);
+                                                                 1.0 / std::sqrt(J3 + 1.0), exc, S.ccr);
         CKT(launched("k_tpandya"));
       } else {
         CKT(cuda(cudaMemsetAsync(S.wx, 0, sizeof(double) * (size_t)r1 * r2, stream), "memset(Wx)"));
       }
       if (doy) {
         k_tpandya<<<grid_n((int64_t)r1 * nb2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 1,
-                                                                 1.0 / std::sqrt(J4 + 1.0), S.ccx);
+                                                                 1.0 / std::sqrt(J4 + 1.0), exc, S.ccx);
         CKT(launched("k_tpandya"));
       }
       if (S.cb_tile_n[b]) {
@@ -465,7 +491,7 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
         CKT(launched("k_gemm_fp64(tensor ph)"));
       }
       k_ts222ph_scatter<<<grid_n((int64_t)r1 * r2), 256, 0, stream>>>(D, T, S.wx, doy ? S.wy : nullptr, J3, J4, qa,
-                                                                      qb, hL, hR, thresh, RES);
+                                                                      qb, hL, hR, thresh, exc, RES);
       CKT(launched("k_ts222ph_scatter"));
     }
   }

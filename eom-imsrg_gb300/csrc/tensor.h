@@ -58,7 +58,17 @@ std::string build_tlayout(TLayout& T, const Layout& L, int rank, int dpar);
 // TS_commutator_222_pp_hh's products as grouped-GEMM problems: per block and class pair,
 // W1 = L(q1)[c1,pp] R[pp,c2] - R[c1,pp] L(q2)[pp,c2] and W2 the same through hh pairs
 // (operands: kOpL scalar L, kOpR tensor R, outputs kOpW1 / kOpW2 in tensor layout)
-std::vector<GemmProb> build_tensor_pphh_problems(const TLayout& T, const Layout& L);
+// excitation_only keeps the terms whose R operand is a (pp,hh) or (hh,pp) array (the other
+// arrays of an EOM ladder operator are zero)
+std::vector<GemmProb> build_tensor_pphh_problems(const TLayout& T, const Layout& L, bool excitation_only = false);
+
+// a subset of the two-body elements of a tensor slab for the per-element kernels: segment s
+// covers elements off[s] .. off[s] + (pre[s+1] - pre[s]) - 1 (relative to goff[0]); n = 0 means all
+struct ElemSegs {
+  const int64_t* off = nullptr;
+  const int64_t* pre = nullptr;
+  int n = 0;
+};
 
 struct DevTLayout {
   int rank, dpar, nblocks, n_ob, six_nJ, six_nh, six_nhx;

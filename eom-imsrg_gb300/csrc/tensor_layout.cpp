@@ -160,7 +160,7 @@ std::string build_tlayout(TLayout& T, const Layout& L, int rank, int dpar) {
   return std::string();
 }
 
-std::vector<GemmProb> build_tensor_pphh_problems(const TLayout& T, const Layout& L) {
+std::vector<GemmProb> build_tensor_pphh_problems(const TLayout& T, const Layout& L, bool excitation_only) {
   std::vector<GemmProb> P;
   const int N = 0, TR = 1;
   for (int q = 0; q < T.nblocks; ++q) {
@@ -177,7 +177,8 @@ std::vector<GemmProb> build_tensor_pphh_problems(const TLayout& T, const Layout&
         p.c_id = side == 0 ? kOpW1 : kOpW2;
         p.c_off = T.goff[(size_t)q * 9 + g];
         p.M = M; p.N = Nn; p.ldc = M;
-        if (K1) {  // + L(qa)[c1,k] R[k,c2]
+        auto excitation = [](int g) { return g == 2 || g == 6; };
+        if (K1 && (!excitation_only || excitation(tg_of(k, c2)))) {  // + L(qa)[c1,k] R[k,c2]
           GemmTerm t{};
           if (c1 <= k) {
             t.a_id = kOpL; t.a_off = L.goff[qa * 6 + qx_of(c1, k)]; t.lda = L.ncls[qa][c1]; t.ta = N; t.alpha = kAlphaOne;
@@ -188,7 +189,7 @@ std::vector<GemmProb> build_tensor_pphh_problems(const TLayout& T, const Layout&
           t.K = K1;
           p.t[p.nterm++] = t;
         }
-        if (K2) {  // - R[c1,k] L(qb)[k,c2]
+        if (K2 && (!excitation_only || excitation(tg_of(c1, k)))) {  // - R[c1,k] L(qb)[k,c2]
           GemmTerm t{};
           t.a_id = kOpR; t.a_off = T.goff[(size_t)q * 9 + tg_of(c1, k)]; t.lda = M; t.ta = N;
           if (k <= c2) {

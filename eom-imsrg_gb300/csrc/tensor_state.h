@@ -12,6 +12,7 @@
 #include "tensor.h"
 
 using imsrg::DevTLayout;
+using imsrg::ElemSegs;
 using imsrg::GemmProb;
 using imsrg::GemmTile;
 using imsrg::SplitChunk;
@@ -23,6 +24,10 @@ using imsrg::TLayout;
 // pieces flag of Ctx::tensor_commutator: recouple every nonzero Wx / Wy element of TS_222_ph
 // (the EOM product) instead of those above 1e-6 (TS_commutator_222_ph)
 constexpr int kTensorExactPh = 512;
+// pieces flag: R is an excitation operator (fph and (pp,hh) / (hh,pp) elements only) and only
+// the fph and (pp,hh) / (hh,pp) elements of RES are computed (the rest of RES is undefined);
+// implies kTensorExactPh and runs the ladder's remaining products in FP64
+constexpr int kTensorExcitation = 1024;
 
 // output slot of the second product of a tensor ladder problem (TcOut::f64 index)
 constexpr int kTensorOpW3 = 7;
@@ -35,6 +40,12 @@ struct TensorState {
   const GemmProb* pphh_p = nullptr;
   const GemmTile* pphh_t = nullptr;
   int n_pphh_t = 0;
+  // excitation mode: the ladder terms with a (pp,hh) / (hh,pp) R operand and the output arrays
+  const GemmProb* exc_p = nullptr;
+  const GemmTile* exc_t = nullptr;
+  int n_exc_t = 0;
+  ElemSegs exc_segs;
+  int64_t exc_n2 = 0;
   // per cross-coupled block: GEMM problems (Wx, Wy) and their tile range
   const GemmProb* cb_p = nullptr;
   const GemmTile* cb_t = nullptr;

@@ -103,3 +103,18 @@ def test_excited_states_after_flow(engines, tmp_path):
     assert np.abs(E - ref).max() <= max(10 * asym, 1e-8) * np.abs(w).max(), (E, ref, asym)
     for dE, Etot, n1 in rows:
         assert abs(Etot - (dE + HS.E0)) < 1e-9 and 0.0 <= n1 <= 1.0 + 1e-12
+
+
+@pytest.mark.parametrize("mode,tol", [("bf16x6", 1e-5), ("bf16x3", 1e-4)])
+def test_eom_matvec_mixed_precision(oracles, mode, tol):
+    """The mixed modes run the product's particle-hole GEMMs on the split-BF16 tensor cores."""
+    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300.eom import LadderSpace
+    from oracle.oracle import EomOracle
+    o = oracles(4)
+    eng = Engine(make_basis(4), device=0, precision=mode)
+    e = EomOracle(o, 4, 0)
+    space = LadderSpace(eng, 4, 0)
+    H = eng.synthetic_hamiltonian(seed=5)
+    v = np.random.default_rng(9).standard_normal(space.n)
+    assert rel_err(space.matvec(eng.new_op(1, H), v), e.matvec(H, v)) < tol
