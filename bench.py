@@ -574,6 +574,85 @@ def observables_workload(args, local: int):
     }), flush=True)
 
 
+def eom_workload(args, local: int):
+    """EOM-IMSRG excited states (calculate_excited_states) after a mixed-precision Magnus flow:
+    calc_HF, graph steps to s=50, then the Lanczos for J^pi = 0+, 2+ and 3- (nev states each)
+    with the EOM product in FP64 and in the flow's mixed mode; wall time of each, the
+    energies' agreement, and the EOM product rate against the oracle's on the host cores."""
+    import numpy as np
+    from imsrg_gb300 import CONV, Engine, make_basis
+    from imsrg_gb300.eom import EOM_TOL, LadderSpace
+    from oracle import oracle as orc
+    emax = args.emax if args.emax is not None else 8
+    steps = int(round(args.s_end / args.ds))
+    b = make_basis(emax)
+    eng = Engine(b, device=local, precision=args.mode)
+    H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
+    st = flow_state(eng, H)
+    kw = dict(max_terms=args.obs_bch_max_terms, conv=CONV, graph=True, allow_unconverged=True)
+    t = time.perf_counter()
+    for _ in range(steps):
+        info = eng.magnus_step(*st, args.ds, **kw)
+    eng.synchronize()
+    t_flow = time.perf_counter() - t
+    HS_host = st[0].download()
+    del st
+    states = [(0, 0), (2, 0), (3, 1)]
+    nev = args.eom_states
+    res = {}
+    total = {}
+    for mode in ("fp64", args.mode):
+        e = Engine(b, device=local, precision=mode)
+        HS = e.new_op(1, HS_host)
+        for J, P in states:
+            sp = LadderSpace(e, 2 * J, 2 * P)
+            v = np.random.default_rng(0).standard_normal(sp.n)
+            sp.matvec(HS, v)  # warm-up (tables, workspaces)
+            t = time.perf_counter()
+            reps = 3
+            for _ in range(reps):
+                sp.matvec(HS, v)
+            t_mv = (time.perf_counter() - t) / reps
+            t = time.perf_counter()
+            E, V, inf = sp.lanczos(HS, nev, EOM_TOL)
+            t_lz = time.perf_counter() - t
+            key = f"{J}{'+-'[P]}"
+            res.setdefault(key, {"amplitudes": sp.n})[mode] = {
+                "energies_MeV": [float(x) for x in E], "n1p1h": [float(np.sum(V[:sp.n1b, i] ** 2)) for i in range(nev)],
+                "lanczos_s": t_lz, "matvecs": inf["matvecs"], "restarts": inf["restarts"], "matvec_ms": 1e3 * t_mv}
+            total[mode] = total.get(mode, 0.0) + t_lz
+            del sp
+        del HS, e
+    for key, r in res.items():
+        r["max_dE_keV"] = 1e3 * float(np.max(np.abs(np.array(r["fp64"]["energies_MeV"]) -
+                                                     np.array(r[args.mode]["energies_MeV"]))))
+    # the oracle's EOM product (two FP64 scalar-tensor commutators on all host cores), J=0+
+    o = orc.Oracle(b)
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    eo = orc.EomOracle(o, 0, 0)
+    v = np.random.default_rng(0).standard_normal(eo.n)
+    t = time.perf_counter()
+    eo.matvec(HS_host, v)
+    t_cpu = time.perf_counter() - t
+    gpu_mv = res["0+"][args.mode]["matvec_ms"] * 1e-3
+    print(json.dumps({
+        "metric": f"EOM-IMSRG excited states at eMax={emax}: Lanczos wall time, J^pi 0+ 2+ 3-, {nev} states each",
+        "value": total[args.mode], "unit": "s", "n_gpus": 1, "steps": len(states), "warmup": 1,
+        "ms_per_step": 1e3 * total[args.mode] / len(states), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": f"calc_HF, {steps} {args.mode} Magnus graph steps (ds={args.ds}) at eMax={emax} "
+                               f"({b.norbits} orbits), then calculate_excited_states for 0+, 2+, 3- (nev={nev}, "
+                               f"tol={EOM_TOL:.3g}, 5 nev Lanczos vectors) with the EOM product in FP64 and {args.mode}",
+                   "reference_state": hf_rec, "flow_s": t_flow, "E0": float(HS_host[0]),
+                   "mbpt2_final": info["mbpt2"], "lanczos_s_fp64": total["fp64"], "states": res,
+                   "eom_matvecs_per_s_gpu_0+": 1.0 / gpu_mv, "eom_matvecs_per_s_cpu_0+": 1.0 / t_cpu},
+        "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "EOM products/s (J=0+)", "cores": cores, "kind": "port",
+                         "sample": f"one EOM product for 0+ at eMax={emax} with the oracle (two FP64 scalar-tensor "
+                                   f"commutators, OpenMP x{cores})"},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -581,10 +660,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--emax", type=int, default=None, help="default 10 (flow), 6 (adjoint)")
-    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision", "hf-flow"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision", "hf-flow", "eom"])
     ap.add_argument("--precision-flow-steps", type=int, default=20)
     ap.add_argument("--obs-bch-max-terms", type=int, default=40)
     ap.add_argument("--adjoint-k", type=int, default=16)
+    ap.add_argument("--eom-states", type=int, default=4, help="eom workload: states per J^pi")
     ap.add_argument("--s-end", type=float, default=30.0, help="adjoint workload: flow length")
     ap.add_argument("--fd-components", type=int, default=None)
     ap.add_argument("--mode", default="bf16x6", choices=["bf16x3", "bf16x6"])
@@ -623,6 +703,12 @@ def main():
     if args.workload == "precision":
         if rank == 0:
             precision_workload(args, local)
+        return
+    if args.workload == "eom":
+        if rank == 0:
+            if args.s_end == 30.0:
+                args.s_end = 50.0
+            eom_workload(args, local)
         return
     if args.workload == "observables":
         if rank == 0:

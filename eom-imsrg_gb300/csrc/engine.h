@@ -142,6 +142,7 @@ struct Ctx {
   // EOM-IMSRG ladder operators (eom.cu)
   imsrg_status eom_matvec(imsrg_eom& E, const double* H, const double* d_v, double* d_w);
   imsrg_status eom_matvec_host(imsrg_eom& E, const double* H, const double* v, double* w);
+  imsrg_status eom_matvec_graph(imsrg_eom& E, const double* H);
   imsrg_status eom_lanczos(imsrg_eom& E, const double* H, int nev, double tol, int max_restarts, double* energies,
                            double* vectors, int32_t* matvecs, int32_t* restarts);
 

@@ -55,6 +55,10 @@ struct imsrg_eom {
   double* d_w = nullptr;
   double* d_S[2] = {nullptr, nullptr};
   double* d_Y[2] = {nullptr, nullptr};
+  // the product on d_v -> d_w as one CUDA graph (several hundred launches), for the H it was
+  // captured with
+  cudaGraphExec_t gexec = nullptr;
+  const double* g_H = nullptr;
 };
 
 namespace {
@@ -168,6 +172,7 @@ void build_map(const Layout& L, const TLayout& T, imsrg_eom& E) {
 }
 
 void release(imsrg_eom* E) {
+  if (E->gexec) cudaGraphExecDestroy(E->gexec);
   cudaFree(E->d_pos);
   cudaFree(E->d_mirror);
   cudaFree(E->d_kind);
@@ -223,11 +228,36 @@ imsrg_status Ctx::eom_matvec(imsrg_eom& E, const double* Hd, const double* d_v, 
   return launched("k_eom_unpack");
 }
 
+// the product d_v -> d_w through the CUDA graph captured for Hd (captured on first use, after
+// one direct run that also makes the workspaces; the operands are read when the graph runs)
+imsrg_status Ctx::eom_matvec_graph(imsrg_eom& E, const double* Hd) {
+  if (E.gexec && E.g_H == Hd) return cuda(cudaGraphLaunch(E.gexec, stream), "cudaGraphLaunch(eom)");
+  CKE(eom_matvec(E, Hd, E.d_v, E.d_w));
+  CKE(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize"));
+  if (E.gexec) {
+    cudaGraphExecDestroy(E.gexec);
+    E.gexec = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CKE(cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture(eom)"));
+  const imsrg_status s = eom_matvec(E, Hd, E.d_v, E.d_w);
+  const imsrg_status e = cuda(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture(eom)");
+  imsrg_status r = s != IMSRG_OK ? s : e;
+  if (r == IMSRG_OK) r = cuda(cudaGraphInstantiate(&E.gexec, g, 0), "cudaGraphInstantiate(eom)");
+  if (g) cudaGraphDestroy(g);
+  if (r != IMSRG_OK) {
+    E.gexec = nullptr;
+    return r;
+  }
+  E.g_H = Hd;
+  return IMSRG_OK;  // d_w already holds the direct run's product
+}
+
 // host vectors in and out
 imsrg_status Ctx::eom_matvec_host(imsrg_eom& E, const double* Hd, const double* v, double* w) {
   const size_t b = sizeof(double) * (size_t)E.n;
   CKE(cuda(cudaMemcpyAsync(E.d_v, v, b, cudaMemcpyHostToDevice, stream), "H2D eom vector"));
-  CKE(eom_matvec(E, Hd, E.d_v, E.d_w));
+  CKE(eom_matvec_graph(E, Hd));
   CKE(cuda(cudaMemcpyAsync(w, E.d_w, b, cudaMemcpyDeviceToHost, stream), "D2H eom vector"));
   return cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
 }

@@ -395,12 +395,48 @@ __global__ void k_ts_pphh_update(int64_t n, int64_t off, double* __restrict__ RE
 // src/cross_coupled.f90:1416-1634 for the cross-coupled tensor block (J3, J4, Tz, PAR):
 // term 1 fills CCX (r1 x nb2: rows (a,b) of channel qa, ph columns (p,h) of channel qb),
 // term 2 fills CCR (nb1 x r2: ph columns (p,h) of qa, rows (b,a) of qb); out is scaled by `scale`.
+namespace {
+// one element of the tensor Pandya transform (rows (a, b) / ph columns (p, h) as k_tpandya
+// reads them); exc: zero unless the tensor element read is (pp,hh) or (hh,pp)
+__device__ __forceinline__ double tpandya_at(const DevLayout& D, const DevTLayout& T, const double* __restrict__ R,
+                                             int hR, int J3, int J4, int term, int a, int b, int p, int h, double norm,
+                                             int exc) {
+  const int dp = T.dpar >> 1;
+  // an excitation operator has only (pp,hh) and (hh,pp) elements: the pairs (a,h) and (p,b) read
+  // below must be of opposite classes
+  const int ca = D.con[a] + D.con[h], cb = D.con[p] + D.con[b];
+  const bool live = !exc || (ca == 0 && cb == 2) || (ca == 2 && cb == 0);
+  if (!(live && ((D.ll[a] + D.ll[h]) & 1) == ((D.ll[b] + D.ll[p] + dp) & 1) && D.tz[a] + D.tz[h] == D.tz[b] + D.tz[p]))
+    return 0.0;
+  const int ja = D.jj[a], jb = D.jj[b], jp = D.jj[p], jh = D.jj[h];
+  double sm = 0.0;
+  for (int Ja = abs(ja - jh); Ja <= ja + jh; Ja += 2)
+    for (int Jb = abs(jp - jb); Jb <= jp + jb; Jb += 2) {
+      const double t = term == 1 ? d_telem(D, T, R, hR, a, h, p, b, Ja, Jb) : d_telem(D, T, R, hR, h, a, b, p, Ja, Jb);
+      if (t == 0.0) continue;
+      const double nj = term == 1 ? d_nine(T, ja, jb, J3, jh, jp, J4, Ja, Jb) : d_nine(T, jh, jp, J3, ja, jb, J4, Ja, Jb);
+      sm -= d_sgn(Jb >> 1) * sqrt((Ja + 1.0) * (Jb + 1.0)) * nj * t;
+    }
+  return term == 1 ? sm * d_sgn((jh + jb + J4) >> 1) * norm : sm * d_sgn((jp + ja + J4) >> 1) * norm * d_sgn((jp + jh) >> 1);
+}
+
+// the block of a flattened element index (prefix counts pre[0..n], pre[0] = 0)
+__device__ __forceinline__ int d_block_of(const int64_t* __restrict__ pre, int n, int64_t e) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+}  // namespace
+
 __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* __restrict__ R, int hR, int J3, int J4, int qa,
-                          int qb, int term, double scale, int exc, double* __restrict__ out) {
+                          int qb, int term, double scale, double* __restrict__ out) {
   const int r1 = D.cc_rlen[qa], r2 = D.cc_rlen[qb];
   const int nb1 = D.cc_nph[qa], nb2 = D.cc_nph[qb];
   const int64_t n = term == 1 ? (int64_t)r1 * nb2 : (int64_t)nb1 * r2;
-  const int dp = T.dpar >> 1, rank = T.rank;
   const double norm = sqrt((J3 + 1.0) * (J4 + 1.0)) * scale;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     int a, b, p, h;
@@ -413,25 +449,38 @@ __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* __restrict__ 
       p = D.cc_cp[D.cc_col_off[qa] + row]; h = D.cc_ch[D.cc_col_off[qa] + row];
       b = D.cc_ra[D.cc_row_off[qb] + col]; a = D.cc_rb[D.cc_row_off[qb] + col];
     }
-    double val = 0.0;
-    // an excitation operator has only (pp,hh) and (hh,pp) elements: the pairs (a,h) and (p,b) read
-    // below must be of opposite classes
-    const int ca = D.con[a] + D.con[h], cb = D.con[p] + D.con[b];
-    const bool live = !exc || (ca == 0 && cb == 2) || (ca == 2 && cb == 0);
-    if (live && ((D.ll[a] + D.ll[h]) & 1) == ((D.ll[b] + D.ll[p] + dp) & 1) && D.tz[a] + D.tz[h] == D.tz[b] + D.tz[p]) {
-      const int ja = D.jj[a], jb = D.jj[b], jp = D.jj[p], jh = D.jj[h];
-      double sm = 0.0;
-      for (int Ja = abs(ja - jh); Ja <= ja + jh; Ja += 2)
-        for (int Jb = abs(jp - jb); Jb <= jp + jb; Jb += 2) {
-          const double t = term == 1 ? d_telem(D, T, R, hR, a, h, p, b, Ja, Jb) : d_telem(D, T, R, hR, h, a, b, p, Ja, Jb);
-          if (t == 0.0) continue;
-          const double nj = term == 1 ? d_nine(T, ja, jb, J3, jh, jp, J4, Ja, Jb) : d_nine(T, jh, jp, J3, ja, jb, J4, Ja, Jb);
-          sm -= d_sgn(Jb >> 1) * sqrt((Ja + 1.0) * (Jb + 1.0)) * nj * t;
-        }
-      val = term == 1 ? sm * d_sgn((jh + jb + J4) >> 1) * norm
-                      : sm * d_sgn((jp + ja + J4) >> 1) * norm * d_sgn((jp + jh) >> 1);
+    out[e] = tpandya_at(D, T, R, hR, J3, J4, term, a, b, p, h, norm, 0);
+  }
+}
+
+// Excitation mode, all cross-coupled tensor blocks in one launch: per block, the packed CCR
+// (nb1 x nx, columns pe of qb, scale 1/sqrt(J3+1)) and then the packed CCX (ny x nb2, rows hp of
+// qa, scale 1/sqrt(J4+1)); pre: prefix counts of nb1 nx + ny nb2 over the blocks
+__global__ void k_tpandya_exc(DevLayout D, DevTLayout T, const double* __restrict__ R, int hR,
+                              const ExcBlock* __restrict__ blk, const int64_t* __restrict__ pre, int nblk,
+                              const int* __restrict__ pe, const int* __restrict__ hp, double* __restrict__ ccr,
+                              double* __restrict__ ccx) {
+  const int64_t n = pre[nblk];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int ib = d_block_of(pre, nblk, e);
+    const ExcBlock B = blk[ib];
+    const int64_t f = e - pre[ib];
+    const int qa = B.qa, qb = B.qb, nb1 = D.cc_nph[qa];
+    const double n34 = sqrt((B.J3 + 1.0) * (B.J4 + 1.0));
+    if (f < (int64_t)nb1 * B.nx) {  // CCR
+      const int c = (int)(f / nb1), row = (int)(f - (int64_t)c * nb1);
+      const int col = pe[B.xs + c];
+      const int p = D.cc_cp[D.cc_col_off[qa] + row], h = D.cc_ch[D.cc_col_off[qa] + row];
+      const int b = D.cc_ra[D.cc_row_off[qb] + col], a = D.cc_rb[D.cc_row_off[qb] + col];
+      ccr[B.ccr + f] = tpandya_at(D, T, R, hR, B.J3, B.J4, 2, a, b, p, h, n34 / sqrt(B.J3 + 1.0), 1);
+    } else {  // CCX
+      const int64_t g = f - (int64_t)nb1 * B.nx;
+      const int col = (int)(g / B.ny), r = (int)(g - (int64_t)col * B.ny);
+      const int row = hp[B.ys + r];
+      const int a = D.cc_ra[D.cc_row_off[qa] + row], b = D.cc_rb[D.cc_row_off[qa] + row];
+      const int p = D.cc_cp[D.cc_col_off[qb] + col], h = D.cc_ch[D.cc_col_off[qb] + col];
+      ccx[B.ccx + g] = tpandya_at(D, T, R, hR, B.J3, B.J4, 1, a, b, p, h, n34 / sqrt(B.J4 + 1.0), 1);
     }
-    out[e] = val;
   }
 }
 
@@ -482,78 +531,119 @@ __device__ __forceinline__ void recouple_loop(const DevLayout& D, const DevTLayo
 // src/TS_commutators.f90:1529-1843 for one cross-coupled tensor block: every element of
 // Wx (and Wy) above thresh in size recouples into the two-body tensor elements it feeds (ACCUMULATES);
 // TS_commutator_222_ph uses thresh = 1e-6 (src/TS_commutators.f90:1562, 1714), the EOM product 0
+namespace {
+// the recouplings of one (Wx, Wy) element pair, rows (d, a) of qa and (c, b) of qb
+__device__ __forceinline__ void ph_scatter_elem(const DevLayout& D, const DevTLayout& T, double* RES, int J3, int J4,
+                                                int qa, int qb, int IX, int JX, double X, double Y, int hL, int hR,
+                                                double thresh, int exc) {
+  const int rank = T.rank;
+  const double p34 = sqrt((J3 + 1.0) * (J4 + 1.0));
+  const double ph34 = d_sgn((J3 + J4) >> 1);
+  const int d = D.cc_ra[D.cc_row_off[qa] + IX], a = D.cc_rb[D.cc_row_off[qa] + IX];
+  const int c = D.cc_ra[D.cc_row_off[qb] + JX], b = D.cc_rb[D.cc_row_off[qb] + JX];
+  const int ja = D.jj[a], jb = D.jj[b], jc = D.jj[c], jd = D.jj[d];
+  const double pabcd = d_sgn((ja + jb + jc + jd) >> 1);
+  if (fabs(X) > thresh) {
+    const int J1min = abs(ja - jb), J1max = ja + jb, J2min = abs(jc - jd), J2max = jc + jd;
+    if (b >= a) {
+      if (d >= c) {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, a == b, c == d, ja, jd, jb, jc, p34,
+                      [&](int, int J2) { return d_sgn((jb + jd + J2) >> 1) * ph34 * hL * X; }, a, b, c, d, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == d, a == b, jd, ja, jc, jb, p34,
+                      [&](int J1, int) { return -d_sgn((jc + ja + J1 + rank) >> 1) * hR * X; }, c, d, a, b, exc);
+      } else {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, a == b, false, ja, jd, jb, jc, p34,
+                      [&](int, int) { return d_sgn((jb + jc) >> 1) * ph34 * hL * X; }, a, b, d, c, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, false, a == b, jd, ja, jc, jb, p34,
+                      [&](int, int) { return d_sgn((ja - jd + rank) >> 1) * hR * X; }, d, c, a, b, exc);
+      }
+    } else {
+      if (d >= c) {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, false, c == d, ja, jd, jb, jc, p34,
+                      [&](int J1, int J2) { return d_sgn((ja + jd + J1 + J2) >> 1) * ph34 * hL * X; }, b, a, c, d, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == d, false, jd, ja, jc, jb, p34,
+                      [&](int J1, int J2) { return d_sgn((jc - jb + J1 + J2 + rank) >> 1) * hR * X; }, c, d, b, a, exc);
+      } else {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, false, false, ja, jd, jb, jc, p34,
+                      [&](int J1, int) { return d_sgn((ja + jc + J1) >> 1) * ph34 * hL * X; }, b, a, d, c, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, false, false, jd, ja, jc, jb, p34,
+                      [&](int, int J2) { return d_sgn((jb - jd + J2 + rank) >> 1) * hR * X; }, d, c, b, a, exc);
+      }
+    }
+  }
+  if (fabs(Y) > thresh) {
+    const int J1min = abs(jd - jb), J1max = jd + jb, J2min = abs(jc - ja), J2max = jc + ja;
+    if (b >= d) {
+      if (a >= c) {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, d == b, c == a, jd, ja, jb, jc, p34,
+                      [&](int, int J2) { return d_sgn((jc + ja + J2) >> 1) * hL * Y; }, d, b, c, a, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == a, b == d, ja, jd, jc, jb, p34,
+                      [&](int J1, int) { return d_sgn((jd - jb + J1 + rank) >> 1) * ph34 * hR * Y; }, c, a, d, b, exc);
+      } else {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, d == b, c == a, jd, ja, jb, jc, p34,
+                      [&](int, int) { return -hL * Y; }, d, b, a, c, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, a == c, b == d, ja, jd, jc, jb, p34,
+                      [&](int, int) { return pabcd * ph34 * d_sgn(rank >> 1) * hR * Y; }, a, c, d, b, exc);
+      }
+    } else {
+      if (a >= c) {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, b == d, a == c, jd, ja, jb, jc, p34,
+                      [&](int J1, int J2) { return -pabcd * d_sgn((J1 + J2) >> 1) * hL * Y; }, b, d, c, a, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == a, b == d, ja, jd, jc, jb, p34,
+                      [&](int J1, int J2) { return d_sgn((J1 + J2 + rank) >> 1) * ph34 * hR * Y; }, c, a, b, d, exc);
+      } else {
+        recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, b == d, a == c, jd, ja, jb, jc, p34,
+                      [&](int J1, int) { return d_sgn((jb + jd + J1) >> 1) * hL * Y; }, b, d, a, c, exc);
+        recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, a == c, d == b, ja, jd, jc, jb, p34,
+                      [&](int, int J2) { return d_sgn((ja - jc + J2 + rank) >> 1) * ph34 * hR * Y; }, a, c, b, d, exc);
+      }
+    }
+  }
+}
+}  // namespace
+
 __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* __restrict__ Wx,
                                   const double* __restrict__ Wy, int J3, int J4, int qa, int qb, int hL, int hR,
                                   double thresh, int exc, double* __restrict__ RES) {
   const int r1 = D.cc_rlen[qa], r2 = D.cc_rlen[qb];
-  const int rank = T.rank;
-  const double p34 = sqrt((J3 + 1.0) * (J4 + 1.0));
-  const double ph34 = d_sgn((J3 + J4) >> 1);
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)r1 * r2;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int JX = (int)(e / r1), IX = (int)(e - (int64_t)JX * r1);
     const double X = Wx[e], Y = Wy ? Wy[e] : 0.0;
     if (fabs(X) <= thresh && fabs(Y) <= thresh) continue;
-    const int d = D.cc_ra[D.cc_row_off[qa] + IX], a = D.cc_rb[D.cc_row_off[qa] + IX];
-    const int c = D.cc_ra[D.cc_row_off[qb] + JX], b = D.cc_rb[D.cc_row_off[qb] + JX];
-    const int ja = D.jj[a], jb = D.jj[b], jc = D.jj[c], jd = D.jj[d];
-    const double pabcd = d_sgn((ja + jb + jc + jd) >> 1);
-    if (fabs(X) > thresh) {
-      const int J1min = abs(ja - jb), J1max = ja + jb, J2min = abs(jc - jd), J2max = jc + jd;
-      if (b >= a) {
-        if (d >= c) {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, a == b, c == d, ja, jd, jb, jc, p34,
-                        [&](int, int J2) { return d_sgn((jb + jd + J2) >> 1) * ph34 * hL * X; }, a, b, c, d, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == d, a == b, jd, ja, jc, jb, p34,
-                        [&](int J1, int) { return -d_sgn((jc + ja + J1 + rank) >> 1) * hR * X; }, c, d, a, b, exc);
-        } else {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, a == b, false, ja, jd, jb, jc, p34,
-                        [&](int, int) { return d_sgn((jb + jc) >> 1) * ph34 * hL * X; }, a, b, d, c, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, false, a == b, jd, ja, jc, jb, p34,
-                        [&](int, int) { return d_sgn((ja - jd + rank) >> 1) * hR * X; }, d, c, a, b, exc);
-        }
-      } else {
-        if (d >= c) {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, false, c == d, ja, jd, jb, jc, p34,
-                        [&](int J1, int J2) { return d_sgn((ja + jd + J1 + J2) >> 1) * ph34 * hL * X; }, b, a, c, d, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == d, false, jd, ja, jc, jb, p34,
-                        [&](int J1, int J2) { return d_sgn((jc - jb + J1 + J2 + rank) >> 1) * hR * X; }, c, d, b, a, exc);
-        } else {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, false, false, ja, jd, jb, jc, p34,
-                        [&](int J1, int) { return d_sgn((ja + jc + J1) >> 1) * ph34 * hL * X; }, b, a, d, c, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, false, false, jd, ja, jc, jb, p34,
-                        [&](int, int J2) { return d_sgn((jb - jd + J2 + rank) >> 1) * hR * X; }, d, c, b, a, exc);
-        }
-      }
+    ph_scatter_elem(D, T, RES, J3, J4, qa, qb, IX, JX, X, Y, hL, hR, thresh, exc);
+  }
+}
+
+// Excitation mode, all cross-coupled tensor blocks in one launch: per block, the elements of the
+// packed Wx (r1 x nx, columns pe of qb) and then of Wy (ny x r2, rows hp of qa) recouple, into
+// (pp,hh) and (hh,pp) outputs only; pre: prefix counts of r1 nx + ny r2 over the blocks
+__global__ void k_ts222ph_scatter_exc(DevLayout D, DevTLayout T, const ExcBlock* __restrict__ blk,
+                                      const int64_t* __restrict__ pre, int nblk, const int* __restrict__ pe,
+                                      const int* __restrict__ hp, const double* __restrict__ Wx,
+                                      const double* __restrict__ Wy, int hL, int hR, double* __restrict__ RES) {
+  const int64_t n = pre[nblk];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int ib = d_block_of(pre, nblk, e);
+    const ExcBlock B = blk[ib];
+    const int64_t f = e - pre[ib];
+    const int r1 = D.cc_rlen[B.qa];
+    int IX, JX;
+    double X = 0.0, Y = 0.0;
+    if (f < (int64_t)r1 * B.nx) {
+      const int c = (int)(f / r1);
+      IX = (int)(f - (int64_t)c * r1);
+      JX = pe[B.xs + c];
+      X = Wx[B.wx + f];
+    } else {
+      const int64_t g = f - (int64_t)r1 * B.nx;
+      JX = (int)(g / B.ny);
+      const int r = (int)(g - (int64_t)JX * B.ny);
+      IX = hp[B.ys + r];
+      Y = Wy[B.wy + g];
     }
-    if (fabs(Y) > thresh) {
-      const int J1min = abs(jd - jb), J1max = jd + jb, J2min = abs(jc - ja), J2max = jc + ja;
-      if (b >= d) {
-        if (a >= c) {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, d == b, c == a, jd, ja, jb, jc, p34,
-                        [&](int, int J2) { return d_sgn((jc + ja + J2) >> 1) * hL * Y; }, d, b, c, a, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == a, b == d, ja, jd, jc, jb, p34,
-                        [&](int J1, int) { return d_sgn((jd - jb + J1 + rank) >> 1) * ph34 * hR * Y; }, c, a, d, b, exc);
-        } else {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, d == b, c == a, jd, ja, jb, jc, p34,
-                        [&](int, int) { return -hL * Y; }, d, b, a, c, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, a == c, b == d, ja, jd, jc, jb, p34,
-                        [&](int, int) { return pabcd * ph34 * d_sgn(rank >> 1) * hR * Y; }, a, c, d, b, exc);
-        }
-      } else {
-        if (a >= c) {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, b == d, a == c, jd, ja, jb, jc, p34,
-                        [&](int J1, int J2) { return -pabcd * d_sgn((J1 + J2) >> 1) * hL * Y; }, b, d, c, a, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, c == a, b == d, ja, jd, jc, jb, p34,
-                        [&](int J1, int J2) { return d_sgn((J1 + J2 + rank) >> 1) * ph34 * hR * Y; }, c, a, b, d, exc);
-        } else {
-          recouple_loop(D, T, RES, J3, J4, J1min, J1max, J2min, J2max, b == d, a == c, jd, ja, jb, jc, p34,
-                        [&](int J1, int) { return d_sgn((jb + jd + J1) >> 1) * hL * Y; }, b, d, a, c, exc);
-          recouple_loop(D, T, RES, J3, J4, J2min, J2max, J1min, J1max, a == c, d == b, ja, jd, jc, jb, p34,
-                        [&](int, int J2) { return d_sgn((ja - jc + J2 + rank) >> 1) * ph34 * hR * Y; }, a, c, b, d, exc);
-        }
-      }
-    }
+    if (X == 0.0 && Y == 0.0) continue;
+    ph_scatter_elem(D, T, RES, B.J3, B.J4, B.qa, B.qb, IX, JX, X, Y, hL, hR, 0.0, 1);
   }
 }
 

@@ -36,7 +36,12 @@ __global__ void k_ts212f(DevLayout D, DevTLayout T, const double* L, int hL, con
                          ElemSegs sg);
 __global__ void k_ts_pphh_update(int64_t n, int64_t off, double* RES, const double* w1, const double* w2);
 __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* R, int hR, int J3, int J4, int qa, int qb, int term,
-                          double scale, int exc, double* out);
+                          double scale, double* out);
+__global__ void k_tpandya_exc(DevLayout D, DevTLayout T, const double* R, int hR, const ExcBlock* blk,
+                              const int64_t* pre, int nblk, const int* pe, const int* hp, double* ccr, double* ccx);
+__global__ void k_ts222ph_scatter_exc(DevLayout D, DevTLayout T, const ExcBlock* blk, const int64_t* pre, int nblk,
+                                      const int* pe, const int* hp, const double* Wx, const double* Wy, int hL, int hR,
+                                      double* RES);
 __global__ void k_ts222ph_scatter(DevLayout D, DevTLayout T, const double* Wx, const double* Wy, int J3, int J4,
                                   int qa, int qb, int hL, int hR, double thresh, int exc, double* RES);
 }  // namespace imsrg
@@ -95,6 +100,63 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
   const auto pphh_tiles = build_tiles(pphh, 64, 64);
   const auto exc = build_tensor_pphh_problems(T, L, true);
   const auto exc_tiles = build_tiles(exc, 64, 64);
+  // per cross-coupled channel, its rows (i, j) with i a particle and j a hole, and with i a hole
+  // and j a particle: the only columns of CCR and rows of CCX an excitation operator fills
+  std::vector<int> pe_off{0}, pe, hp_off{0}, hp;
+  for (int q = 0; q < L.ncc; ++q) {
+    for (int r = 0; r < L.cc_rlen[q]; ++r) {
+      const int i = L.cc_ra[L.cc_row_off[q] + r], j = L.cc_rb[L.cc_row_off[q] + r];
+      if (L.con[i] == 0 && L.con[j] == 1) pe.push_back(r);
+      if (L.con[i] == 1 && L.con[j] == 0) hp.push_back(r);
+    }
+    pe_off.push_back((int)pe.size());
+    hp_off.push_back((int)hp.size());
+  }
+  // excitation-mode particle-hole products of all cross-coupled tensor blocks, batched: the
+  // packed CCR / CCX of every block, Wx (r1 x npe(qb)) = -LCC(qa) CCR and Wy (nhp(qa) x r2) =
+  // CCX LCC(qb)^T as one grouped GEMM, each in its own region of four buffers
+  std::vector<ExcBlock> xblk;
+  std::vector<int64_t> xpre_p{0}, xpre_s{0};
+  std::vector<GemmProb> xbp;
+  int64_t o_ccr = 0, o_ccx = 0, o_wx = 0, o_wy = 0;
+  for (size_t b = 0; b < T.cb_J3.size(); ++b) {
+    const int qa = T.cb_qa[b], qb = T.cb_qb[b];
+    const int r1 = L.cc_rlen[qa], r2 = L.cc_rlen[qb], nb1 = L.cc_nph[qa], nb2 = L.cc_nph[qb];
+    const int nx = nb1 ? pe_off[qb + 1] - pe_off[qb] : 0;
+    const int ny = (nb2 && T.cb_J3[b] != T.cb_J4[b]) ? hp_off[qa + 1] - hp_off[qa] : 0;
+    if (!nx && !ny) continue;
+    ExcBlock B{T.cb_J3[b], T.cb_J4[b], qa, qb, nx, ny, pe_off[qb], hp_off[qa], o_ccr, o_ccx, o_wx, o_wy};
+    if (nx) {
+      GemmProb p{};
+      p.c_id = kOpW1; p.c_off = o_wx; p.M = r1; p.N = nx; p.ldc = r1; p.nterm = 1;
+      GemmTerm& t = p.t[0];
+      t.a_id = kOpLCC; t.a_off = L.cc_off[qa]; t.lda = r1; t.ta = 0;
+      t.b_id = kOpRCC; t.b_off = o_ccr; t.ldb = nb1; t.tb = 0;
+      t.K = nb1; t.alpha = kAlphaNeg | kAlphaOne;
+      xbp.push_back(p);
+    }
+    if (ny) {
+      GemmProb p{};
+      p.c_id = kOpW2; p.c_off = o_wy; p.M = ny; p.N = r2; p.ldc = ny; p.nterm = 1;
+      GemmTerm& t = p.t[0];
+      t.a_id = kOpWCC; t.a_off = o_ccx; t.lda = ny; t.ta = 0;
+      t.b_id = kOpLCC; t.b_off = L.cc_off[qb]; t.ldb = r2; t.tb = 1;
+      t.K = nb2; t.alpha = kAlphaOne;
+      xbp.push_back(p);
+    }
+    o_ccr += (int64_t)nb1 * nx; o_ccx += (int64_t)ny * nb2; o_wx += (int64_t)r1 * nx; o_wy += (int64_t)ny * r2;
+    xblk.push_back(B);
+    xpre_p.push_back(xpre_p.back() + (int64_t)nb1 * nx + (int64_t)ny * nb2);
+    xpre_s.push_back(xpre_s.back() + (int64_t)r1 * nx + (int64_t)ny * r2);
+  }
+  const auto xbt = build_tiles(xbp, 64, 64);
+  st->x_nblk = (int)xblk.size();
+  st->x_np = xpre_p.back();
+  st->x_ns = xpre_s.back();
+  st->x_n_t = (int)xbt.size();
+  st->x_sizes[0] = o_ccr; st->x_sizes[1] = o_ccx; st->x_sizes[2] = o_wx; st->x_sizes[3] = o_wy;
+  st->pe_off = pe_off;
+  st->hp_off = hp_off;
   // the (pp,hh) and (hh,pp) arrays of every block, relative to goff[0]
   std::vector<int64_t> seg_off, seg_pre{0};
   for (int q = 0; q < T.nblocks; ++q)
@@ -155,6 +217,9 @@ imsrg_status Ctx::tensor_state(int rank, int dpar, TensorState** out) {
   pk.add(pphh, &st->pphh_p); pk.add(pphh_tiles, &st->pphh_t);
   pk.add(exc, &st->exc_p); pk.add(exc_tiles, &st->exc_t);
   pk.add(seg_off, &st->exc_segs.off); pk.add(seg_pre, &st->exc_segs.pre);
+  pk.add(pe, &st->d_pe); pk.add(hp, &st->d_hp);
+  pk.add(xbp, &st->x_p); pk.add(xbt, &st->x_t);
+  pk.add(xblk, &st->x_blk); pk.add(xpre_p, &st->x_pre_p); pk.add(xpre_s, &st->x_pre_s);
   pk.add(cbp, &st->cb_p); pk.add(cbt, &st->cb_t);
   pk.add(T.seg_start, &st->seg_start); pk.add(T.seg_len, &st->seg_len); pk.add(T.seg_w, &st->seg_w);
   CKT(cuda(cudaMalloc(&st->tables, pk.buf.size()), "cudaMalloc(tensor tables)"));
@@ -190,7 +255,8 @@ void Ctx::tensor_release() {
     }
     TensorState* s = it->second.get();
     for (void* p : {(void*)s->w1, (void*)s->w2, (void*)s->ccx, (void*)s->ccr, (void*)s->wx, (void*)s->wy,
-                    (void*)s->bch_a, (void*)s->bch_b, s->tables, (void*)s->tc_buf, s->tc_tables, (void*)s->w3})
+                    (void*)s->bch_a, (void*)s->bch_b, s->tables, (void*)s->tc_buf, s->tc_tables, (void*)s->w3,
+                    (void*)s->x_buf[0], (void*)s->x_buf[1], (void*)s->x_buf[2], (void*)s->x_buf[3]})
       if (p) cudaFree(p);
     it = reg.erase(it);
   }
@@ -430,7 +496,28 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       CKT(launched("k_ts221"));
     }
   }
-  if ((pieces & 64) && precision != IMSRG_PREC_FP64) {  // split-BF16 cross-coupled products
+  if ((pieces & 64) && exc) {  // excitation mode: packed CCR / CCX of all blocks, FP64 products
+    if (S.x_nblk) {
+      if (!S.x_buf[0])
+        for (int k = 0; k < 4; ++k)
+          CKT(cuda(cudaMalloc(&S.x_buf[k], sizeof(double) * (size_t)std::max<int64_t>(S.x_sizes[k], 1)),
+                   "cudaMalloc(excitation ph buffers)"));
+      k_tpandya_exc<<<grid_n(S.x_np), 256, 0, stream>>>(D, T, R, hR, S.x_blk, S.x_pre_p, S.x_nblk, S.d_pe, S.d_hp,
+                                                         S.x_buf[0], S.x_buf[1]);
+      CKT(launched("k_tpandya_exc"));
+      if (S.x_n_t) {
+        GemmOperands ops{};
+        ops.in[kOpLCC] = d_lcc; ops.in[kOpRCC] = S.x_buf[0]; ops.in[kOpWCC] = S.x_buf[1];
+        ops.out[kOpW1] = S.x_buf[2]; ops.out[kOpW2] = S.x_buf[3];
+        ops.hL = hL; ops.hR = hR;
+        k_gemm_fp64<<<S.x_n_t, 256, 0, stream>>>(S.x_p, S.x_t, ops);
+        CKT(launched("k_gemm_fp64(tensor ph, excitation)"));
+      }
+      k_ts222ph_scatter_exc<<<grid_n(S.x_ns), 256, 0, stream>>>(D, T, S.x_blk, S.x_pre_s, S.x_nblk, S.d_pe, S.d_hp,
+                                                                 S.x_buf[2], S.x_buf[3], hL, hR, RES);
+      CKT(launched("k_ts222ph_scatter_exc"));
+    }
+  } else if ((pieces & 64) && precision != IMSRG_PREC_FP64) {  // split-BF16 cross-coupled products
     CKT(tensor_tc_prepare(S));
     const TLayout& H = S.T;
     CKT(tc_split_on(S.tc_ops, S.tc_chunks + S.tc_nchunks, S.ph_lcc_nchunks, d_lcc, nullptr, S.tc_buf,
@@ -442,14 +529,14 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       if (!dox && !doy) continue;
       if (dox) {
         k_tpandya<<<grid_n((int64_t)nb1 * r2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 2,
-                                                                 1.0 / std::sqrt(J3 + 1.0), exc, S.ccr);
+                                                                 1.0 / std::sqrt(J3 + 1.0), S.ccr);
         CKT(launched("k_tpandya"));
       } else {
         CKT(cuda(cudaMemsetAsync(S.wx, 0, sizeof(double) * (size_t)r1 * r2, stream), "memset(Wx)"));
       }
       if (doy) {
         k_tpandya<<<grid_n((int64_t)r1 * nb2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 1,
-                                                                 1.0 / std::sqrt(J4 + 1.0), exc, S.ccx);
+                                                                 1.0 / std::sqrt(J4 + 1.0), S.ccx);
         CKT(launched("k_tpandya"));
       }
       CKT(tc_split_on(S.tc_ops, S.tc_chunks + S.ph_chunk_start[b], S.ph_chunk_n[b], S.ccr, S.ccx, S.tc_buf,
@@ -472,14 +559,14 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       if (!dox && !doy) continue;
       if (dox) {
         k_tpandya<<<grid_n((int64_t)nb1 * r2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 2,
-                                                                 1.0 / std::sqrt(J3 + 1.0), exc, S.ccr);
+                                                                 1.0 / std::sqrt(J3 + 1.0), S.ccr);
         CKT(launched("k_tpandya"));
       } else {
         CKT(cuda(cudaMemsetAsync(S.wx, 0, sizeof(double) * (size_t)r1 * r2, stream), "memset(Wx)"));
       }
       if (doy) {
         k_tpandya<<<grid_n((int64_t)r1 * nb2), 256, 0, stream>>>(D, T, R, hR, J3, J4, qa, qb, 1,
-                                                                 1.0 / std::sqrt(J4 + 1.0), exc, S.ccx);
+                                                                 1.0 / std::sqrt(J4 + 1.0), S.ccx);
         CKT(launched("k_tpandya"));
       }
       if (S.cb_tile_n[b]) {

@@ -70,6 +70,15 @@ struct ElemSegs {
   int n = 0;
 };
 
+// one cross-coupled tensor block of the excitation-mode particle-hole products: packed CCR
+// (nb1 x nx) over the (particle, hole) rows of qb listed from xs, packed CCX (ny x nb2) over the
+// (hole, particle) rows of qa listed from ys, and the offsets of CCR, CCX, Wx (r1 x nx) and
+// Wy (ny x r2) in their buffers (nx = 0 / ny = 0: no Wx / Wy)
+struct ExcBlock {
+  int J3, J4, qa, qb, nx, ny, xs, ys;
+  int64_t ccr, ccx, wx, wy;
+};
+
 struct DevTLayout {
   int rank, dpar, nblocks, n_ob, six_nJ, six_nh, six_nhx;
   int64_t off_fhh, off_fpp, off_fph, slab, n2b;

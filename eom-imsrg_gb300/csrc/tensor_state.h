@@ -13,6 +13,7 @@
 
 using imsrg::DevTLayout;
 using imsrg::ElemSegs;
+using imsrg::ExcBlock;
 using imsrg::GemmProb;
 using imsrg::GemmTile;
 using imsrg::SplitChunk;
@@ -46,6 +47,21 @@ struct TensorState {
   int n_exc_t = 0;
   ElemSegs exc_segs;
   int64_t exc_n2 = 0;
+  // excitation-mode particle-hole products: per cross-coupled channel the (particle, hole) and
+  // (hole, particle) rows (host offsets, device lists) and per tensor block the packed GEMMs
+  std::vector<int> pe_off, hp_off;
+  const int* d_pe = nullptr;
+  const int* d_hp = nullptr;
+  // ... batched over the blocks: ExcBlock table, prefix counts of the Pandya and scatter
+  // elements, the grouped GEMM, and the CCR / CCX / Wx / Wy buffers (allocated on first use)
+  const ExcBlock* x_blk = nullptr;
+  const int64_t* x_pre_p = nullptr;
+  const int64_t* x_pre_s = nullptr;
+  const GemmProb* x_p = nullptr;
+  const GemmTile* x_t = nullptr;
+  int x_nblk = 0, x_n_t = 0;
+  int64_t x_np = 0, x_ns = 0, x_sizes[4] = {0, 0, 0, 0};
+  double* x_buf[4] = {nullptr, nullptr, nullptr, nullptr};
   // per cross-coupled block: GEMM problems (Wx, Wy) and their tile range
   const GemmProb* cb_p = nullptr;
   const GemmTile* cb_t = nullptr;
