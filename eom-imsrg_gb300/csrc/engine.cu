@@ -431,7 +431,7 @@ imsrg_status Ctx::magnus_expand(double* DG, int hDG, const double* G, int hG, in
 
 // BCH_EXPAND (src/IMSRG_MAGNUS.f90:149-234)
 imsrg_status Ctx::bch_expand(double* HS, const double* G, int hG, const double* H, int hH, int max_terms,
-                             double conv, int* terms) {
+                             double conv, int* terms, bool cr) {
   CK(ensure_workspace());
   CK(ensure_flow_workspace());
   const size_t sb = sizeof(double) * (size_t)L.slab;
@@ -441,7 +441,7 @@ imsrg_status Ctx::bch_expand(double* HS, const double* G, int hG, const double* 
   double coef = 1.0;
   int iw;
   for (iw = 2; iw <= max_terms; ++iw) {
-    coef = coef / (iw - 1.0);
+    coef = cr ? coef / iw : coef / (iw - 1.0);  // CR_EXPAND: 1/n! on ad^(n-1)(H)
     const double* ad = (iw == 2) ? H : ((iw & 1) ? d_int2 : d_ad);
     double* out = (iw & 1) ? d_ad : d_int2;
     CK(commutator(G, hG, ad, hH, out, hH, true));
@@ -451,8 +451,8 @@ imsrg_status Ctx::bch_expand(double* HS, const double* G, int hG, const double* 
     if (h_scalars[0] < conv) break;
   }
   *terms = (iw > max_terms) ? max_terms - 1 : iw - 1;
-  if (iw > max_terms) return fail(IMSRG_ERR_NOT_CONVERGED, "BCH series did not converge within max_terms");
-  return IMSRG_OK;
+  if (iw > max_terms && !cr) return fail(IMSRG_ERR_NOT_CONVERGED, "BCH series did not converge within max_terms");
+  return IMSRG_OK;  // CR_EXPAND ends after max_terms without an error, as the reference does
 }
 
 // ====================================================================== C ABI
@@ -1029,6 +1029,21 @@ imsrg_status imsrg_bch_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, c
   HS->herm = H->herm;
   int t = 0;
   imsrg_status s = c->bch_expand(HS->d, G->d, G->herm, H->d, H->herm, max_terms, conv, &t);
+  if (terms_used) *terms_used = t;
+  return s;
+}
+
+imsrg_status imsrg_cr_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H, int32_t max_terms,
+                             double conv, int32_t* terms_used) {
+  CTX(ctx);
+  CK(check_op(c, HS, "imsrg_cr_expand"));
+  CK(check_op(c, G, "imsrg_cr_expand"));
+  CK(check_op(c, H, "imsrg_cr_expand"));
+  if (HS == G || HS == H) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "HS must not alias G or H");
+  if (max_terms < 2) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "max_terms must be >= 2");
+  HS->herm = H->herm;
+  int t = 0;
+  imsrg_status s = c->bch_expand(HS->d, G->d, G->herm, H->d, H->herm, max_terms, conv, &t, true);
   if (terms_used) *terms_used = t;
   return s;
 }

@@ -110,8 +110,9 @@ struct Ctx {
   imsrg_status atan_generator(const double* Hden, int hden, const double* Hnum, double* ETA);
   imsrg_status w2_generator(const double* H, int hH, double* ETA);
   imsrg_status magnus_expand(double* DG, int hDG, const double* G, int hG, int* used);
+  // cr: CR_EXPAND's coefficients 1/n! (src/IMSRG_MAGNUS.f90:532-617) and no error after max_terms
   imsrg_status bch_expand(double* HS, const double* G, int hG, const double* H, int hH, int max_terms, double conv,
-                          int* terms);
+                          int* terms, bool cr = false);
 
   // one Magnus step, eager or replayed from a CUDA graph (graph.cu)
   imsrg_status magnus_step(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,

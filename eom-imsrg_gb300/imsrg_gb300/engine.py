@@ -430,6 +430,12 @@ class Engine:
         self._ck(self.L.imsrg_bch_expand(self.h, HS.h, G.h, H.h, int(max_terms), float(conv), C.byref(n)))
         return n.value
 
+    def cr_expand(self, HS: SqOp, G: SqOp, H: SqOp, max_terms: int = 14, conv: float = CONV) -> int:
+        """CR_EXPAND (src/IMSRG_MAGNUS.f90:532-617): HS = sum_n ad_G^n(H) / (n+1)!."""
+        n = C.c_int32()
+        self._ck(self.L.imsrg_cr_expand(self.h, HS.h, G.h, H.h, int(max_terms), float(conv), C.byref(n)))
+        return n.value
+
     def magnus_step(self, HS: SqOp, G: SqOp, DG: SqOp, H: SqOp, ds: float, max_terms: int = 40, conv: float = CONV,
                     graph: bool = True, wait: bool = True, allow_unconverged: bool = False):
         """One step of magnus_decouple (MAGNUS_EXPAND, euler_step, BCH_EXPAND, White, MBPT2).

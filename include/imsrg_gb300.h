@@ -205,6 +205,11 @@ imsrg_status imsrg_euler_step(imsrg_ctx* ctx, imsrg_op* G, const imsrg_op* DG, d
  * max_terms (the reference STOPs after 40). */
 imsrg_status imsrg_bch_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H, int32_t max_terms,
                               double conv, int32_t* terms_used);
+/* CR_EXPAND(HS, G, H, jbas, quads) :532 -- HS = H + [G,H]/2! + [G,[G,H]]/3! + ..., the operator of
+ * the completely renormalised triples (src/main_IMSRG.f90:310); stops when a term's norm times its
+ * coefficient drops below conv or after max_terms (the reference: 14, 1e-6), without an error. */
+imsrg_status imsrg_cr_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H, int32_t max_terms,
+                             double conv, int32_t* terms_used);
 
 /* One step of magnus_decouple (src/IMSRG_MAGNUS.f90:47-110): MAGNUS_EXPAND(DG, G),
  * euler_step(G, DG, ds), BCH_EXPAND(HS, G, H, max_terms, conv), build_gs_white(HS, DG) and

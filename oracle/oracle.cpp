@@ -952,13 +952,15 @@ int magnus_expand(const Basis& B, double* DG, const double* G, Work& w) {
 
 // BCH_EXPAND (src/IMSRG_MAGNUS.f90:149-234): HS = exp(G) H exp(-G).  Returns terms used,
 // or -1 when the series did not converge within max_terms (the reference STOPs at 40).
-int bch_expand(const Basis& B, double* HS, const double* G, const double* H, int max_terms, double conv, Work& w) {
+// cr: CR_EXPAND (src/IMSRG_MAGNUS.f90:532-617), coef = coef/iw, no failure after max_terms
+int bch_expand(const Basis& B, double* HS, const double* G, const double* H, int max_terms, double conv, Work& w,
+               bool cr = false) {
   std::vector<double> INT1(B.slab), INT2(H, H + B.slab), AD(B.slab);
   std::copy(H, H + B.slab, HS);
   double coef = 1.0;
   int iw;
   for (iw = 2; iw <= max_terms; ++iw) {
-    coef = coef / (iw - 1.0);
+    coef = cr ? coef / iw : coef / (iw - 1.0);
     std::copy(HS, HS + B.slab, INT1.begin());
     AD = INT2;
     std::fill(INT2.begin(), INT2.end(), 0.0);
@@ -966,6 +968,7 @@ int bch_expand(const Basis& B, double* HS, const double* G, const double* H, int
     add_op(B, INT1.data(), 1.0, INT2.data(), coef, HS);
     if (frob(B, INT2.data()) * coef < conv) break;
   }
+  if (cr) return (iw > max_terms) ? max_terms - 1 : iw - 1;
   return (iw > max_terms) ? -1 : iw - 1;
 }
 
@@ -1848,6 +1851,11 @@ int orc_bch_expand(void* b, double* HS, const double* G, const double* H, int ma
   Basis& B = *(Basis*)b;
   Work w(B);
   return bch_expand(B, HS, G, H, max_terms, conv, w);
+}
+int orc_cr_expand(void* b, double* HS, const double* G, const double* H, int max_terms, double conv) {
+  Basis& B = *(Basis*)b;
+  Work w(B);
+  return bch_expand(B, HS, G, H, max_terms, conv, w, true);
 }
 double orc_bf_0body(void* b, const double* A, int hA, const double* Bo, int hB) { return bf0(*(Basis*)b, A, hA, Bo, hB); }
 double orc_bf_1body(void* b, const double* A, int hA, const double* Bo, int hB, int a, int bb) {

@@ -89,6 +89,7 @@ def lib():
         "orc_add_sq_op": (None, [vp, _dp, d, _dp, d, _dp]),
         "orc_magnus_expand": (i, [vp, _dp, _dp]),
         "orc_bch_expand": (i, [vp, _dp, _dp, _dp, i, d]),
+        "orc_cr_expand": (i, [vp, _dp, _dp, _dp, i, d]),
         "orc_bf_0body": (d, [vp, _dp, i, _dp, i]),
         "orc_bf_1body": (d, [vp, _dp, i, _dp, i, i, i]),
         "orc_bf_2body": (d, [vp, _dp, i, _dp, i, i, i, i, i, i]),
@@ -283,6 +284,12 @@ class Oracle:
     def bch_expand(self, G, H, max_terms=40, conv=BCH_CONV):
         HS = self.new()
         n = self.L.orc_bch_expand(self.h, HS, G, H, max_terms, conv)
+        return HS, n
+
+    def cr_expand(self, G, H, max_terms=14, conv=BCH_CONV):
+        """CR_EXPAND (src/IMSRG_MAGNUS.f90:532-617): sum_n ad_G^n(H) / (n+1)!."""
+        HS = self.new()
+        n = self.L.orc_cr_expand(self.h, HS, G, H, max_terms, conv)
         return HS, n
 
     # brute force ---------------------------------------------------------

@@ -104,3 +104,17 @@ def test_generator_norms_flow(oracles, engines, emax):
     dHS = eng.new_op(1)
     assert eng.bch_expand(dHS, dG, dH) == n
     _check("bch", dHS.download(), HS, o)
+
+
+@pytest.mark.parametrize("emax", [2, 4])
+def test_cr_expand(oracles, engines, emax):
+    """CR_EXPAND (src/IMSRG_MAGNUS.f90:532-617) against the oracle: same terms, 1e-10."""
+    o, eng = oracles(emax), engines(emax)
+    G = o.random(81, -1) * 0.05
+    H = o.random(82, 1)
+    ref, n = o.cr_expand(G, H, 14, 1e-6)
+    dG, dH, dHS = eng.new_op(-1, G), eng.new_op(1, H), eng.new_op(1)
+    assert eng.cr_expand(dHS, dG, dH, 14, 1e-6) == n
+    assert rel_err(dHS.download(), ref) < TOL
+    # the capped series ends without an error
+    assert eng.cr_expand(dHS, eng.new_op(-1, G * 40), dH, 14, 1e-30) == 13

@@ -172,3 +172,24 @@ def test_atan_generators_against_white(oracles):
     assert np.array_equal(o.atanxx(H, H), a)
     H2 = o.commutator(a, -1, H, 1)
     assert np.allclose(o.w2(H, 1), 1.5 * a + 0.5 * o.atanxx(H, H2), rtol=0, atol=1e-15)
+
+
+def test_cr_expand_series(oracles):
+    """CR_EXPAND (src/IMSRG_MAGNUS.f90:532-617): H + [G,H]/2! + [G,[G,H]]/3! + ... with the
+    reference's stop (term norm times coefficient below conv) and at most 13 nested commutators."""
+    o = oracles(2)
+    G = o.random(71, -1) * 0.05
+    H = o.random(72, 1)
+    CR, n = o.cr_expand(G, H, 14, 1e-6)
+    ref, ad, coef = H.copy(), H.copy(), 1.0
+    for k in range(2, 15):
+        coef /= k
+        ad = o.commutator(G, -1, ad, 1)
+        ref += coef * ad
+        if o.frob(ad) * coef < 1e-6:
+            break
+    assert n == k - 1
+    assert np.allclose(CR, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+    # capped series: no error, all 13 terms
+    CR2, n2 = o.cr_expand(G * 40, H, 14, 1e-30)
+    assert n2 == 13 and np.all(np.isfinite(CR2))
