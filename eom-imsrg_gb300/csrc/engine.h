@@ -140,6 +140,8 @@ struct Ctx {
                                  int pieces);
   imsrg_status tensor_frob(TensorState& S, const double* op, double scale, int slot);
   imsrg_status bch_tensor(TensorState& S, const double* G, int hG, double* HS, int max_terms, double conv, int* terms);
+  // perturbative triples after the flow (triples.cu)
+  imsrg_status restore_triples(const double* H, const double* OM, double* e3, int64_t* items);
   // EOM-IMSRG ladder operators (eom.cu)
   imsrg_status eom_matvec(imsrg_eom& E, const double* H, const double* d_v, double* d_w);
   imsrg_status eom_matvec_host(imsrg_eom& E, const double* H, const double* v, double* w);

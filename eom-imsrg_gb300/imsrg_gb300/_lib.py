@@ -111,6 +111,7 @@ SIGNATURES = {
     "imsrg_tensor_commutator": [_vp, _vp, _vp, _vp, _i32],
     "imsrg_bch_tensor": [_vp, _vp, _vp, _i32, _d, _pi32],
     "imsrg_tensor_frob_norm": [_vp, _vp, _pd],
+    "imsrg_restore_triples": [_vp, _vp, _vp, _pd, _pi64],
     "imsrg_eom_create": [_vp, _i32, _i32, _pvp],
     "imsrg_eom_destroy": [_vp, _vp],
     "imsrg_eom_dim": [_vp, _vp, _pi64, _pi64],

@@ -430,6 +430,13 @@ class Engine:
         self._ck(self.L.imsrg_bch_expand(self.h, HS.h, G.h, H.h, int(max_terms), float(conv), C.byref(n)))
         return n.value
 
+    def restore_triples(self, H: SqOp, OM: SqOp):
+        """restore_triples (src/IMSRG_MAGNUS.f90:767-902): the triples correction and the number of
+        (ppp, hhh) pairs summed."""
+        e3, n = C.c_double(), C.c_int64()
+        self._ck(self.L.imsrg_restore_triples(self.h, H.h, OM.h, C.byref(e3), C.byref(n)))
+        return e3.value, n.value
+
     def cr_expand(self, HS: SqOp, G: SqOp, H: SqOp, max_terms: int = 14, conv: float = CONV) -> int:
         """CR_EXPAND (src/IMSRG_MAGNUS.f90:532-617): HS = sum_n ad_G^n(H) / (n+1)!."""
         n = C.c_int32()

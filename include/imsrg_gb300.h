@@ -260,6 +260,14 @@ imsrg_status imsrg_bch_tensor(imsrg_ctx* ctx, const imsrg_op* G, imsrg_tensor* H
 /* mat_frob_norm of a tensor operator (src/basic_IMSRG.f90:4056-4087) */
 imsrg_status imsrg_tensor_frob_norm(imsrg_ctx* ctx, const imsrg_tensor* t, double* out);
 
+/* ---- perturbative triples (restore_triples, src/IMSRG_MAGNUS.f90:767-902; the driver's
+ * 'trips' option, src/main_IMSRG.f90:296-315): the correction summed over the three-body basis
+ * of enumerate_three_body (src/basic_IMSRG.f90:4215-4420) of W^2/D (Jtot+1), W the three-body
+ * element of [OM, H] (commutator_223_single, src/commutators.f90:928-1325) and D the
+ * Epstein-Nesbet denominator with two-body monopoles.  H hermitian (the flowed or the CR_EXPAND
+ * Hamiltonian), OM anti-hermitian (Omega).  items (may be NULL): (ppp, hhh) pairs summed. FP64. */
+imsrg_status imsrg_restore_triples(imsrg_ctx* ctx, const imsrg_op* H, const imsrg_op* OM, double* e3, int64_t* items);
+
 /* ---- EOM-IMSRG excitation ("ladder") operators (calculate_excited_states,
  * src/EOM_IMSRG.f90:13-98).  A ladder operator of rank rank2/2 and parity change dpar2 (0 or 2)
  * is a tensor whose only amplitudes are fph and the pp-hh arrays tgam(3) / tgam(7), stored with

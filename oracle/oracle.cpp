@@ -1724,6 +1724,7 @@ namespace {
 #include "oracle_tensor.inc"
 #include "oracle_hf.inc"
 #include "oracle_eom.inc"
+#include "oracle_triples.inc"
 }  // namespace
 
 // ====================================================================== C interface
@@ -1933,6 +1934,22 @@ double orc_pphh_ladder_elem(void* t, const double* X, int a, int b, int c, int d
 }
 void orc_eom_matvec(void* t, void* m, const double* H, const double* v, double* w) {
   eom_matvec(*(TBasis*)t, *(EomMap*)m, H, v, w);
+}
+
+// ---- perturbative triples (oracle_triples.inc)
+int orc_three_channels(void* b, int* J, int* Tz, int* P, int* nppp, int* nhhh) {
+  const std::vector<ThreeChannel> ch = enumerate_three_body(*(Basis*)b);
+  for (size_t q = 0; q < ch.size(); ++q) {
+    if (J) { J[q] = ch[q].J; Tz[q] = ch[q].Tz; P[q] = ch[q].P; nppp[q] = (int)ch[q].ppp.size(); nhhh[q] = (int)ch[q].hhh.size(); }
+  }
+  return (int)ch.size();
+}
+double orc_comm223(void* b, const double* L, int hL, const double* R, int hR, int p, int q, int r, int s, int t, int u,
+                   int Jtot, int jpq, int jst) {
+  return comm223(*(Basis*)b, L, hL, R, hR, p, q, r, s, t, u, Jtot, jpq, jst);
+}
+double orc_restore_triples(void* b, const double* H, const double* OM, int chan) {
+  return restore_triples(*(Basis*)b, H, OM, chan);
 }
 
 }  // extern "C"

@@ -99,6 +99,9 @@ def lib():
         "orc_vectorize": (i64, [vp, _dp, _dp]),
         "orc_p1_p2": (d, [vp, i, i, i, i, i]),
         "orc_r1_r2": (d, [vp, i, i, i, i, i]),
+        "orc_three_channels": (i, [vp, vp, vp, vp, vp, vp]),
+        "orc_comm223": (d, [vp, _dp, i, _dp, i] + [i] * 9),
+        "orc_restore_triples": (d, [vp, _dp, _dp, i]),
         "orc_eom_create": (vp, [vp]),
         "orc_eom_destroy": (None, [vp]),
         "orc_eom_dim": (i64, [vp, C.POINTER(C.c_int64)]),
@@ -301,6 +304,22 @@ class Oracle:
 
     def bf_2body(self, A, hA, B, hB, a, b, c, d, J):
         return self.L.orc_bf_2body(self.h, A, hA, B, hB, a, b, c, d, J)
+
+    # ---- perturbative triples (src/IMSRG_MAGNUS.f90:767-902)
+    def three_channels(self):
+        """enumerate_three_body: per channel (Jtot, Tz, parity, #ppp, #hhh)."""
+        n = self.L.orc_three_channels(self.h, None, None, None, None, None)
+        arrs = [np.zeros(n, np.int32) for _ in range(5)]
+        self.L.orc_three_channels(self.h, *[a.ctypes.data for a in arrs])
+        return dict(zip(("J", "Tz", "P", "nppp", "nhhh"), arrs))
+
+    def comm223(self, L, hL, R, hR, p, q, r, s, t, u, Jtot, jpq, jst):
+        """commutator_223_single (src/commutators.f90:928-1325)."""
+        return self.L.orc_comm223(self.h, L, hL, R, hR, p, q, r, s, t, u, Jtot, jpq, jst)
+
+    def restore_triples(self, H, OM, chan=-1):
+        """restore_triples: the triples correction of H (herm +1) and Omega (herm -1)."""
+        return self.L.orc_restore_triples(self.h, H, OM, int(chan))
 
     # ---- Hartree-Fock input preparation (src/HF_mod.f90)
     def sp_blocks(self) -> list:
