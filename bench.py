@@ -653,6 +653,63 @@ def eom_workload(args, local: int):
     }), flush=True)
 
 
+def triples_workload(args, local: int):
+    """The driver's triples step (src/main_IMSRG.f90:294-318) after a mixed-precision Magnus flow:
+    calc_HF, bf16x6 graph steps to s=50, then restore_triples of (H0, Omega) and of
+    (CR_EXPAND(Omega, H0), Omega) on the GPU in FP64, and the first by the oracle on all host
+    cores (the CPU baseline)."""
+    from imsrg_gb300 import CONV, Engine, make_basis
+    from oracle import oracle as orc
+    emax = args.emax if args.emax is not None else 8
+    steps = int(round(args.s_end / args.ds))
+    b = make_basis(emax)
+    eng = Engine(b, device=local, precision=args.mode)
+    H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
+    st = flow_state(eng, H)
+    kw = dict(max_terms=args.obs_bch_max_terms, conv=CONV, graph=True, allow_unconverged=True)
+    t = time.perf_counter()
+    for _ in range(steps):
+        eng.magnus_step(*st, args.ds, **kw)
+    eng.synchronize()
+    t_flow = time.perf_counter() - t
+    E0 = st[0].E0
+    OM = st[1].download()
+    del st
+    e64 = Engine(b, device=local, precision="fp64")
+    dH, dG = e64.new_op(1, H), e64.new_op(-1, OM)
+    e64.restore_triples(dH, dG)  # warm-up
+    t = time.perf_counter()
+    corr, items = e64.restore_triples(dH, dG)
+    t_gpu = time.perf_counter() - t
+    CR = e64.new_op(1)
+    t = time.perf_counter()
+    n_cr = e64.cr_expand(CR, dG, dH, 14, CONV)
+    corr_cr, _ = e64.restore_triples(CR, dG)
+    e64.synchronize()
+    t_cr = time.perf_counter() - t
+    o = orc.Oracle(b)
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    t = time.perf_counter()
+    corr_cpu = o.restore_triples(H, OM)
+    t_cpu = time.perf_counter() - t
+    print(json.dumps({
+        "metric": f"Magnus triples correction at eMax={emax}, wall time", "value": t_gpu, "unit": "s",
+        "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * t_gpu, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"calc_HF, {steps} {args.mode} Magnus graph steps (ds={args.ds}) at eMax={emax} "
+                               f"({b.norbits} orbits), then restore_triples(H0, Omega) (FP64, {items} ppp-hhh pairs) "
+                               "and the completely renormalised form with CR_EXPAND",
+                   "reference_state": hf_rec, "flow_s": t_flow, "E0": E0, "triples_MeV": corr,
+                   "E0_plus_triples": E0 + corr, "cr_triples_MeV": corr_cr, "cr_expand_terms": n_cr,
+                   "cr_triples_s": t_cr, "triples_cpu_MeV": corr_cpu,
+                   "rel_diff_gpu_cpu": abs(corr - corr_cpu) / max(abs(corr_cpu), 1e-300),
+                   "cpu_s": t_cpu, "cpu_over_gpu": t_cpu / t_gpu},
+        "cpu_baseline": {"value": t_cpu, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"the same restore_triples at eMax={emax} with the oracle (FP64, OpenMP x{cores})"},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -660,7 +717,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--emax", type=int, default=None, help="default 10 (flow), 6 (adjoint)")
-    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision", "hf-flow", "eom"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision", "hf-flow", "eom",
+                                                     "triples"])
     ap.add_argument("--precision-flow-steps", type=int, default=20)
     ap.add_argument("--obs-bch-max-terms", type=int, default=40)
     ap.add_argument("--adjoint-k", type=int, default=16)
@@ -703,6 +761,12 @@ def main():
     if args.workload == "precision":
         if rank == 0:
             precision_workload(args, local)
+        return
+    if args.workload == "triples":
+        if rank == 0:
+            if args.s_end == 30.0:
+                args.s_end = 50.0
+            triples_workload(args, local)
         return
     if args.workload == "eom":
         if rank == 0:

@@ -12,8 +12,10 @@
 //        multiplicity factors (6 for three equal orbits, 2 for two) of both triples.
 //
 // One thread per (channel, ppp, hhh) item evaluates the denominator once and W for every
-// allowed (Jab, Jij); the 6j symbols, whose fourth or fifth argument reaches 3 jmax, come from
-// Racah's single-sum formula over a log-factorial table.  Each block reduces its items and adds
+// allowed (Jab, Jij).  Every 6j symbol of the nine terms has three single-particle j, one
+// three-body total (up to 3 jmax) and two pair couplings, so one table {j1 j2 x; J j3 y}, filled
+// on the device by Racah's single-sum formula over a log-factorial table (165 MB at eMax=10),
+// serves them all through the column symmetry of the 6j symbol.  Each block reduces its items and adds
 // one partial into the result.  The reference's cuts are kept: the terms with a single
 // two-body factor outside the J sums skip orbits where both factors are below 1e-8.
 #include <cuda_runtime.h>
@@ -53,6 +55,10 @@ struct DevTriples {
   const double* lf;    // log(n!), n < kLogFact
   const double* mono;  // twobody_monopole(a, b) of H, N x N
   const double* fdiag; // f(a, a) of H
+  // 6j {j1 j2 x; J j3 y}: j1, j2, j3 single-particle (h = (j-1)/2 < nh), J a three-body total
+  // (hJ < nJ), x, y pair couplings (x/2, y/2 < nx)
+  const double* six;
+  int nh, nJ, nx;
 };
 
 __device__ __forceinline__ double dsgn(int n) { return (n & 1) ? -1.0 : 1.0; }
@@ -76,8 +82,22 @@ __device__ double d_sixj(const double* __restrict__ lf, int j1, int j2, int j3, 
   return s;
 }
 
+__global__ void k_six_table(const double* __restrict__ lf, int nh, int nJ, int nx, double* __restrict__ out) {
+  const int64_t n = (int64_t)nh * nh * nh * nJ * nx * nx;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = e;
+    const int y = (int)(r % nx); r /= nx;
+    const int x = (int)(r % nx); r /= nx;
+    const int hJ = (int)(r % nJ); r /= nJ;
+    const int h3 = (int)(r % nh); r /= nh;
+    const int h2 = (int)(r % nh);
+    const int h1 = (int)(r / nh);
+    out[e] = d_sixj(lf, 2 * h1 + 1, 2 * h2 + 1, 2 * x, 2 * hJ + 1, 2 * h3 + 1, 2 * y);
+  }
+}
+
 // commutator_223_single (src/commutators.f90:928-1325): <(pq)jpq r; J| [L, R] |(st)jst u; J>
-__device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, const double* __restrict__ L, int hL,
+__device__ double d_comm223(const DevLayout& D, const DevTriples& T, const double* __restrict__ L, int hL,
                             const double* __restrict__ R, int hR, int ip, int iq, int ir, int is, int it, int iu,
                             int J, int jpq, int jst) {
   const int jp = D.jj[ip], jq = D.jj[iq], jr = D.jj[ir], js = D.jj[is], jt = D.jj[it], ju = D.jj[iu];
@@ -86,7 +106,12 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
   const int N = D.N;
   auto vL = [&](int a, int b, int c, int d, int Jx) { return d_v_elem(D, L, hL, a, b, c, d, Jx); };
   auto vR = [&](int a, int b, int c, int d, int Jx) { return d_v_elem(D, R, hR, a, b, c, d, Jx); };
-  auto six = [&](int a, int b, int c, int d, int e, int f) { return d_sixj(lf, a, b, c, d, e, f); };
+  // 6j symbols from the table: {a b c; J e f} directly, {a b c; d J f} = {b a c; J d f}
+  auto six4 = [&](int a, int b, int c, int Jx, int e, int f) {
+    return T.six[(((((int64_t)(a >> 1) * T.nh + (b >> 1)) * T.nh + (e >> 1)) * T.nJ + (Jx >> 1)) * T.nx + (c >> 1)) *
+                     T.nx + (f >> 1)];
+  };
+  auto six5 = [&](int a, int b, int c, int d, int Jx, int f) { return six4(b, a, c, Jx, d, f); };
   auto same = [&](int a, int tx, int lx, int t1, int t2, int l1, int l2) {
     return D.tz[a] + tx == t1 + t2 && ((D.ll[a] + lx) & 1) == ((l1 + l2) & 1);
   };
@@ -101,7 +126,7 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       if (fabs(V1) < 1e-8 && fabs(V2) < 1e-8) continue;
       const int lo = max(max(abs(jq - jr), abs(ja - ju)), abs(jp - J)), hi = min(min(jq + jr, ja + ju), jp + J);
       for (int J2 = lo; J2 <= hi; J2 += 2)
-        sm += dsgn((ja - ju) / 2) * (J2 + 1.0) * six(jq, jp, jpq, J, jr, J2) * six(ja, jp, jst, J, ju, J2) *
+        sm += dsgn((ja - ju) / 2) * (J2 + 1.0) * six4(jq, jp, jpq, J, jr, J2) * six4(ja, jp, jst, J, ju, J2) *
               (V1 * vL(iq, ir, a, iu, J2) - V2 * vR(iq, ir, a, iu, J2));
     }
     tot += sm * dsgn((jq - jr) / 2);
@@ -114,12 +139,12 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       const int lo = max(max(abs(jp - ja), abs(jt - ju)), abs(js - J)), hi = min(min(jp + ja, jt + ju), js + J);
       const int lo2 = max(max(abs(jq - jr), abs(ja - js)), abs(jp - J)), hi2 = min(min(jq + jr, ja + js), jp + J);
       for (int J1 = lo; J1 <= hi; J1 += 2) {
-        const double other = (J1 + 1.0) * dsgn(J1 / 2) * six(jt, js, jst, J, ju, J1);
+        const double other = (J1 + 1.0) * dsgn(J1 / 2) * six4(jt, js, jst, J, ju, J1);
         if (other == 0.0) continue;
         const double r1 = vR(ip, a, it, iu, J1), l1 = vL(ip, a, it, iu, J1);
         double sub = 0.0;
         for (int J2 = lo2; J2 <= hi2; J2 += 2)
-          sub += (J2 + 1.0) * six(jq, jp, jpq, J, jr, J2) * six(jp, ja, J1, js, J, J2) *
+          sub += (J2 + 1.0) * six4(jq, jp, jpq, J, jr, J2) * six5(jp, ja, J1, js, J, J2) *
                  (r1 * vL(iq, ir, a, is, J2) - l1 * vR(iq, ir, a, is, J2));
         sm += sub * dsgn((ja + ju) / 2) * other;
       }
@@ -134,12 +159,12 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       const int lo = max(max(abs(jp - ja), abs(js - ju)), abs(jt - J)), hi = min(min(jp + ja, js + ju), jt + J);
       const int lo2 = max(max(abs(jq - jr), abs(ja - jt)), abs(jp - J)), hi2 = min(min(jq + jr, ja + jt), jp + J);
       for (int J1 = lo; J1 <= hi; J1 += 2) {
-        const double other = (J1 + 1.0) * six(js, jt, jst, J, ju, J1);
+        const double other = (J1 + 1.0) * six4(js, jt, jst, J, ju, J1);
         if (other == 0.0) continue;
         const double r1 = vR(ip, a, iu, is, J1), l1 = vL(ip, a, iu, is, J1);
         double sub = 0.0;
         for (int J2 = lo2; J2 <= hi2; J2 += 2)
-          sub += (J2 + 1.0) * six(jq, jp, jpq, J, jr, J2) * six(jp, ja, J1, jt, J, J2) *
+          sub += (J2 + 1.0) * six4(jq, jp, jpq, J, jr, J2) * six5(jp, ja, J1, jt, J, J2) *
                  (r1 * vL(iq, ir, a, it, J2) - l1 * vR(iq, ir, a, it, J2));
         sm += sub * dsgn((ja + js) / 2) * other;
       }
@@ -156,8 +181,8 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       if (fabs(V1) < 1e-8 && fabs(V2) < 1e-8) continue;
       const int lo = max(max(abs(jp - jr), abs(ja - ju)), abs(J - jq)), hi = min(min(jp + jr, ja + ju), J + jq);
       for (int J2 = lo; J2 <= hi; J2 += 2)
-        sm += dsgn((ja + ju) / 2) * (J2 + 1.0) * dsgn(J2 / 2) * six(jp, jq, jpq, J, jr, J2) *
-              six(ja, jq, jst, J, ju, J2) * (V1 * vL(ir, ip, a, iu, J2) - V2 * vR(ir, ip, a, iu, J2));
+        sm += dsgn((ja + ju) / 2) * (J2 + 1.0) * dsgn(J2 / 2) * six4(jp, jq, jpq, J, jr, J2) *
+              six4(ja, jq, jst, J, ju, J2) * (V1 * vL(ir, ip, a, iu, J2) - V2 * vR(ir, ip, a, iu, J2));
     }
     tot += sm * dsgn((jpq + jp + jq) / 2);
   }
@@ -169,12 +194,12 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       const int lo = max(max(abs(jq - ja), abs(jt - ju)), abs(js - J)), hi = min(min(jq + ja, jt + ju), js + J);
       const int lo2 = max(max(abs(jp - jr), abs(ja - js)), abs(jq - J)), hi2 = min(min(jp + jr, ja + js), jq + J);
       for (int J1 = lo; J1 <= hi; J1 += 2) {
-        const double other = (J1 + 1.0) * dsgn(J1 / 2) * six(jt, js, jst, J, ju, J1);
+        const double other = (J1 + 1.0) * dsgn(J1 / 2) * six4(jt, js, jst, J, ju, J1);
         if (other == 0.0) continue;
         const double r1 = vR(iq, a, it, iu, J1), l1 = vL(iq, a, it, iu, J1);
         double sub = 0.0;
         for (int J2 = lo2; J2 <= hi2; J2 += 2)
-          sub += dsgn(J2 / 2) * (J2 + 1.0) * six(jp, jq, jpq, J, jr, J2) * six(jq, ja, J1, js, J, J2) *
+          sub += dsgn(J2 / 2) * (J2 + 1.0) * six4(jp, jq, jpq, J, jr, J2) * six5(jq, ja, J1, js, J, J2) *
                  (r1 * vL(ir, ip, a, is, J2) - l1 * vR(ir, ip, a, is, J2));
         sm += sub * dsgn((ja + ju) / 2) * other;
       }
@@ -189,12 +214,12 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       const int lo = max(max(abs(jq - ja), abs(js - ju)), abs(jt - J)), hi = min(min(jq + ja, js + ju), jt + J);
       const int lo2 = max(max(abs(jp - jr), abs(ja - jt)), abs(jq - J)), hi2 = min(min(jp + jr, ja + jt), jq + J);
       for (int J1 = lo; J1 <= hi; J1 += 2) {
-        const double other = (J1 + 1.0) * six(js, jt, jst, J, ju, J1);
+        const double other = (J1 + 1.0) * six4(js, jt, jst, J, ju, J1);
         if (other == 0.0) continue;
         const double r1 = vR(iq, a, iu, is, J1), l1 = vL(iq, a, iu, is, J1);
         double sub = 0.0;
         for (int J2 = lo2; J2 <= hi2; J2 += 2)
-          sub += dsgn(J2 / 2) * (J2 + 1.0) * six(jp, jq, jpq, J, jr, J2) * six(jq, ja, J1, jt, J, J2) *
+          sub += dsgn(J2 / 2) * (J2 + 1.0) * six4(jp, jq, jpq, J, jr, J2) * six5(jq, ja, J1, jt, J, J2) *
                  (r1 * vL(ir, ip, a, it, J2) - l1 * vR(ir, ip, a, it, J2));
         sm += sub * dsgn((ja - js) / 2) * other;
       }
@@ -207,7 +232,7 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       if (!same(a, tr, lr, ts, tt, ls, lt)) continue;
       const int ja = D.jj[a];
       if (!dtri(ju, ja, jpq) || !dtri(jr, ja, jst)) continue;
-      sm += dsgn((ja - ju) / 2) * six(jr, ja, jst, ju, J, jpq) *
+      sm += dsgn((ja - ju) / 2) * six5(jr, ja, jst, ju, J, jpq) *
             (vR(ir, a, is, it, jst) * vL(ip, iq, a, iu, jpq) - vL(ir, a, is, it, jst) * vR(ip, iq, a, iu, jpq));
     }
     tot += sm * dsgn(jpq / 2);
@@ -222,8 +247,8 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       if (fabs(V1) < 1e-8 && fabs(V2) < 1e-8) continue;
       const int lo = max(max(abs(ja - jr), abs(jt - ju)), abs(js - J)), hi = min(min(ja + jr, jt + ju), js + J);
       for (int J1 = lo; J1 <= hi; J1 += 2)
-        sm += dsgn((ja + ju) / 2) * dsgn(J1 / 2) * (J1 + 1.0) * six(jt, js, jst, J, ju, J1) *
-              six(jr, ja, J1, js, J, jpq) * (vR(ir, a, it, iu, J1) * V1 - vL(ir, a, it, iu, J1) * V2);
+        sm += dsgn((ja + ju) / 2) * dsgn(J1 / 2) * (J1 + 1.0) * six4(jt, js, jst, J, ju, J1) *
+              six5(jr, ja, J1, js, J, jpq) * (vR(ir, a, it, iu, J1) * V1 - vL(ir, a, it, iu, J1) * V2);
     }
     tot += sm * dsgn((jpq + js + jt) / 2);
   }
@@ -237,7 +262,7 @@ __device__ double d_comm223(const DevLayout& D, const double* __restrict__ lf, c
       if (fabs(V1) < 1e-8 && fabs(V2) < 1e-8) continue;
       const int lo = max(max(abs(ja - jr), abs(js - ju)), abs(jt - J)), hi = min(min(ja + jr, js + ju), jt + J);
       for (int J1 = lo; J1 <= hi; J1 += 2)
-        sm += dsgn((ja - js) / 2) * (J1 + 1.0) * six(js, jt, jst, J, ju, J1) * six(jr, ja, J1, jt, J, jpq) *
+        sm += dsgn((ja - js) / 2) * (J1 + 1.0) * six4(js, jt, jst, J, ju, J1) * six5(jr, ja, J1, jt, J, jpq) *
               (vR(ir, a, iu, is, J1) * V1 - vL(ir, a, iu, is, J1) * V2);
     }
     tot += sm * dsgn((jst - jpq) / 2);
@@ -293,7 +318,7 @@ __global__ void __launch_bounds__(128) k_triples(DevLayout D, DevTriples T, cons
       if (!dtri(C.J, jc, jab) || (a == b && ((jab >> 1) & 1))) continue;
       for (int jij = abs(ji - jj); jij <= ji + jj; jij += 2) {
         if (!dtri(C.J, jk, jij) || (i == j && ((jij >> 1) & 1))) continue;
-        const double w = d_comm223(D, T.lf, OM, -1, H, 1, a, b, c, i, j, k, C.J, jab, jij);
+        const double w = d_comm223(D, T, OM, -1, H, 1, a, b, c, i, j, k, C.J, jab, jij);
         acc += w * w / den * (C.J + 1.0);
       }
     }
@@ -358,12 +383,16 @@ imsrg_status Ctx::restore_triples(const double* H, const double* OM, double* e3,
   for (int n = 2; n < kLogFact; ++n) lf[n] = lf[n - 1] + std::log((double)n);
   // one allocation for the tables and the scratch
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const int nh = (jmax + 1) / 2, nJ = (3 * jmax + 1) / 2, nx = jmax + 1;
+  const int64_t nsix = (int64_t)nh * nh * nh * nJ * nx * nx;
   const size_t bc = al(sizeof(TriChan) * chans.size()), bp = al(sizeof(int16_t) * ppp.size()),
                bh = al(sizeof(int16_t) * hhh.size()), bl = al(sizeof(double) * kLogFact),
-               bm = al(sizeof(double) * (size_t)N * N), bf = al(sizeof(double) * N), bo = al(sizeof(double));
+               bm = al(sizeof(double) * (size_t)N * N), bf = al(sizeof(double) * N), bo = al(sizeof(double)),
+               bs = al(sizeof(double) * (size_t)nsix);
   char* buf = nullptr;
-  CKR(cuda(cudaMalloc(&buf, bc + bp + bh + bl + bm + bf + bo), "cudaMalloc(triples)"));
+  CKR(cuda(cudaMalloc(&buf, bc + bp + bh + bl + bm + bf + bo + bs), "cudaMalloc(triples)"));
   DevTriples T{};
+  T.nh = nh; T.nJ = nJ; T.nx = nx;
   char* o = buf;
   T.chan = reinterpret_cast<const TriChan*>(o);
   imsrg_status st = cuda(cudaMemcpyAsync(o, chans.data(), sizeof(TriChan) * chans.size(), cudaMemcpyHostToDevice, stream),
@@ -388,9 +417,17 @@ imsrg_status Ctx::restore_triples(const double* H, const double* OM, double* e3,
   T.fdiag = fd;
   o += bf;
   double* d_out = reinterpret_cast<double*>(o);
+  o += bo;
+  double* six = reinterpret_cast<double*>(o);
+  T.six = six;
   T.nchan = (int)chans.size();
   T.nitems = nit;
   if (st == IMSRG_OK) st = cuda(cudaMemsetAsync(d_out, 0, sizeof(double), stream), "memset(triples)");
+  if (st == IMSRG_OK) {
+    k_six_table<<<(int)std::max<int64_t>(1, std::min<int64_t>((nsix + 255) / 256, 152 * 32)), 256, 0, stream>>>(
+        T.lf, nh, nJ, nx, six);
+    st = launched("k_six_table");
+  }
   if (st == IMSRG_OK) {
     k_triples_prep<<<(N * N + 255) / 256, 256, 0, stream>>>(D, H, mono, fd);
     st = launched("k_triples_prep");

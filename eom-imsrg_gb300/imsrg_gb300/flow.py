@@ -128,3 +128,38 @@ def magnus_decouple(eng: Engine, H0: np.ndarray, ds: float = 0.5, s_max: float |
     if ops is not None:
         ops.update(HS=HS, G=G)
     return res
+
+
+def magnus_triples(eng: Engine, H0: np.ndarray, G, E0: float, kind: str = "y", prefix: str | None = None,
+                   output_dir: str = ".") -> tuple:
+    """The driver's triples step after the flow (src/main_IMSRG.f90:294-318): restore_triples of
+    the flow's starting Hamiltonian H0 (host slab) and Omega G (device operator), kind 'y', or of
+    CR_EXPAND(Omega, H0) and Omega, kind 'C' (completely renormalised).  Returns
+    (E0, E0 + correction); with prefix set, writes them to <output_dir>/<prefix>_magnus_triples.dat
+    or _magnus_cr_triples.dat as the reference does ('(2(e15.7))')."""
+    if kind not in ("y", "C"):
+        raise ValueError("kind must be 'y' or 'C'")
+    H = eng.new_op(1, H0)
+    if kind == "C":
+        CR = eng.new_op(1)
+        eng.cr_expand(CR, G, H, 14, CONV)
+        H = CR
+    corr, _ = eng.restore_triples(H, G)
+    if prefix is not None:
+        name = f"{prefix.strip()}_magnus_triples.dat" if kind == "y" else f"{prefix.strip()}_magnus_cr_triples.dat"
+        with open(os.path.join(output_dir, name), "w") as f:
+            f.write(f"{_e15_7(E0)}{_e15_7(E0 + corr)}\n")
+    return E0, E0 + corr
+
+
+def _e15_7(x: float) -> str:
+    """Fortran's e15.7 edit descriptor: 0.ddddddd E+xx, right-justified in 15 columns."""
+    if x == 0.0:
+        return f"{'0.0000000E+00':>15}"
+    exp = int(np.floor(np.log10(abs(x)))) + 1
+    v = round(abs(x) / 10.0 ** exp, 7)
+    if v >= 1.0:  # rounding carried into a new digit
+        v /= 10.0
+        exp += 1
+    s = f"{'-' if x < 0 else ''}0.{int(round(v * 1e7)):07d}E{'+' if exp >= 0 else '-'}{abs(exp):02d}"
+    return f"{s:>15}"

@@ -32,3 +32,12 @@ def test_checkpoint_names_follow_the_reference():
     assert omega_checkpoint_name(p, 12.5) == "chi2b_srg0625_eMax08_hwHO020_s12.500.bin"
     assert omega_checkpoint_name(p, 2.5) == "chi2b_srg0625_eMax08_hwHO020_s2.5000.bin"
     assert omega_checkpoint_name("synth_eMax10_hw20_x", 24.0) == "synth_eMax10_hw20_s24.000.bin"
+
+
+def test_fortran_e15_7_format():
+    from imsrg_gb300.flow import _e15_7
+    assert _e15_7(-12.3456789) == " -0.1234568E+02"
+    assert _e15_7(123.45678949) == "  0.1234568E+03"
+    assert _e15_7(9.99999999) == "  0.1000000E+02"
+    assert _e15_7(-0.000123456789) == " -0.1234568E-03"
+    assert _e15_7(0.0) == "  0.0000000E+00"

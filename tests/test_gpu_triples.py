@@ -40,3 +40,19 @@ def test_triples_after_flow(oracles, engines):
     cr_ref, _ = o.cr_expand(OM, H0, 14)
     e3cr, _ = eng.restore_triples(CR, G)
     assert abs(e3cr - o.restore_triples(cr_ref, OM)) <= 1e-10 * abs(e3cr)
+
+
+def test_magnus_triples_files(engines, tmp_path):
+    """The driver's output files: E0 and E0 + correction in e15.7."""
+    from imsrg_gb300.flow import magnus_decouple, magnus_triples
+    eng = engines(2)
+    H0 = eng.synthetic_hamiltonian(seed=2)
+    ops = {}
+    res = magnus_decouple(eng, H0, max_steps=10, ops=ops)
+    E0, Et = magnus_triples(eng, H0, ops["G"], res.E0, "y", prefix="t", output_dir=str(tmp_path))
+    E0c, Ec = magnus_triples(eng, H0, ops["G"], res.E0, "C", prefix="t", output_dir=str(tmp_path))
+    assert E0 == E0c == res.E0 and Et < E0 and Ec < E0
+    for name, v in (("t_magnus_triples.dat", Et), ("t_magnus_cr_triples.dat", Ec)):
+        line = (tmp_path / name).read_text().rstrip("\n")
+        assert len(line) == 30
+        assert abs(float(line[15:]) - v) <= 1e-6 * abs(v)
