@@ -11,7 +11,8 @@
 //   D  = -(e_a + e_b + e_c - e_i - e_j - e_k + the 15 two-body monopoles) times the
 //        multiplicity factors (6 for three equal orbits, 2 for two) of both triples.
 //
-// One thread per (channel, ppp, hhh) item evaluates the denominator once and W for every
+// One thread per (channel, ppp, hhh) item (the kernel can split the orbit sums of the nine terms
+// over a lane group, which measured slower) evaluates the denominator once and W for every
 // allowed (Jab, Jij).  Every 6j symbol of the nine terms has three single-particle j, one
 // three-body total (up to 3 jmax) and two pair couplings, so one table {j1 j2 x; J j3 y}, filled
 // on the device by Racah's single-sum formula over a log-factorial table (165 MB at eMax=10),
@@ -99,7 +100,8 @@ __global__ void k_six_table(const double* __restrict__ lf, int nh, int nJ, int n
 // commutator_223_single (src/commutators.f90:928-1325): <(pq)jpq r; J| [L, R] |(st)jst u; J>
 __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const double* __restrict__ L, int hL,
                             const double* __restrict__ R, int hR, int ip, int iq, int ir, int is, int it, int iu,
-                            int J, int jpq, int jst) {
+                            int J, int jpq, int jst, int lane, int nlanes) {
+  // this lane's share: the orbits a = lane, lane + nlanes, ... of every term's sum
   const int jp = D.jj[ip], jq = D.jj[iq], jr = D.jj[ir], js = D.jj[is], jt = D.jj[it], ju = D.jj[iu];
   const int tp = D.tz[ip], tq = D.tz[iq], tr = D.tz[ir], ts = D.tz[is], tt = D.tz[it], tu = D.tz[iu];
   const int lp = D.ll[ip], lq = D.ll[iq], lr = D.ll[ir], ls = D.ll[is], lt = D.ll[it], lu = D.ll[iu];
@@ -118,7 +120,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   double tot = 0.0;
   {  // 1
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tp, lp, ts, tt, ls, lt)) continue;
       const int ja = D.jj[a];
       if (!dtri(jp, ja, jst)) continue;
@@ -133,7 +135,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 2
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tp, lp, tu, tt, lu, lt)) continue;
       const int ja = D.jj[a];
       const int lo = max(max(abs(jp - ja), abs(jt - ju)), abs(js - J)), hi = min(min(jp + ja, jt + ju), js + J);
@@ -153,7 +155,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 3
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tp, lp, tu, ts, lu, ls)) continue;
       const int ja = D.jj[a];
       const int lo = max(max(abs(jp - ja), abs(js - ju)), abs(jt - J)), hi = min(min(jp + ja, js + ju), jt + J);
@@ -173,7 +175,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 4
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tq, lq, tt, ts, lt, ls)) continue;
       const int ja = D.jj[a];
       if (!dtri(jq, ja, jst)) continue;
@@ -188,7 +190,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 5
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tq, lq, tt, tu, lt, lu)) continue;
       const int ja = D.jj[a];
       const int lo = max(max(abs(jq - ja), abs(jt - ju)), abs(js - J)), hi = min(min(jq + ja, jt + ju), js + J);
@@ -208,7 +210,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 6
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tq, lq, ts, tu, ls, lu)) continue;
       const int ja = D.jj[a];
       const int lo = max(max(abs(jq - ja), abs(js - ju)), abs(jt - J)), hi = min(min(jq + ja, js + ju), jt + J);
@@ -228,7 +230,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 7
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tr, lr, ts, tt, ls, lt)) continue;
       const int ja = D.jj[a];
       if (!dtri(ju, ja, jpq) || !dtri(jr, ja, jst)) continue;
@@ -239,7 +241,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 8
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tr, lr, tu, tt, lu, lt)) continue;
       const int ja = D.jj[a];
       if (!dtri(js, ja, jpq)) continue;
@@ -254,7 +256,7 @@ __device__ double d_comm223(const DevLayout& D, const DevTriples& T, const doubl
   }
   {  // 9
     double sm = 0.0;
-    for (int a = 0; a < N; ++a) {
+    for (int a = lane; a < N; a += nlanes) {
       if (!same(a, tr, lr, tu, ts, lu, ls)) continue;
       const int ja = D.jj[a];
       if (!dtri(ja, jt, jpq)) continue;
@@ -289,12 +291,21 @@ __global__ void k_triples_prep(DevLayout D, const double* __restrict__ H, double
   }
 }
 
+// kLanes lanes per (channel, ppp, hhh) item, splitting the orbit sums of the nine terms
+template <int kLanes>
 __global__ void __launch_bounds__(128) k_triples(DevLayout D, DevTriples T, const double* __restrict__ H,
                                                  const double* __restrict__ OM, double* __restrict__ out) {
   __shared__ double red[128];
+  const int lane = threadIdx.x & (kLanes - 1);
+  constexpr int kPerBlock = 128 / kLanes;
+  // the lane groups of a warp run different items (different loop counts): each group
+  // shuffles among its own lanes only
+  const unsigned gmask = ((1u << kLanes) - 1u) << ((threadIdx.x & 31) & ~(kLanes - 1));
   double acc = 0.0;
   const int N = D.N;
-  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < T.nitems; x += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t ng = (int64_t)gridDim.x * kPerBlock;
+  // the loop bounds are uniform over each lane group, so every shuffle sees the group's lanes
+  for (int64_t x = blockIdx.x * (int64_t)kPerBlock + threadIdx.x / kLanes; x < T.nitems; x += ng) {
     int lo = 0, hi = T.nchan - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -318,8 +329,9 @@ __global__ void __launch_bounds__(128) k_triples(DevLayout D, DevTriples T, cons
       if (!dtri(C.J, jc, jab) || (a == b && ((jab >> 1) & 1))) continue;
       for (int jij = abs(ji - jj); jij <= ji + jj; jij += 2) {
         if (!dtri(C.J, jk, jij) || (i == j && ((jij >> 1) & 1))) continue;
-        const double w = d_comm223(D, T, OM, -1, H, 1, a, b, c, i, j, k, C.J, jab, jij);
-        acc += w * w / den * (C.J + 1.0);
+        double w = d_comm223(D, T, OM, -1, H, 1, a, b, c, i, j, k, C.J, jab, jij, lane, kLanes);
+        for (int o = kLanes / 2; o > 0; o >>= 1) w += __shfl_xor_sync(gmask, w, o, kLanes);
+        if (lane == 0) acc += w * w / den * (C.J + 1.0);
       }
     }
   }
@@ -433,8 +445,9 @@ imsrg_status Ctx::restore_triples(const double* H, const double* OM, double* e3,
     st = launched("k_triples_prep");
   }
   if (st == IMSRG_OK) {
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nit + 127) / 128, 152 * 16));
-    k_triples<<<grid, 128, 0, stream>>>(D, T, H, OM, d_out);
+    constexpr int kLanes = 1;  // measured at eMax=8: 1 lane 1.07 s, 4 lanes 1.40 s, 32 lanes 1.50 s
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nit + 128 / kLanes - 1) / (128 / kLanes), 152 * 16));
+    k_triples<kLanes><<<grid, 128, 0, stream>>>(D, T, H, OM, d_out);
     st = launched("k_triples");
   }
   if (st == IMSRG_OK) st = cuda(cudaMemcpyAsync(e3, d_out, sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H triples");
