@@ -208,6 +208,7 @@ Ctx::~Ctx() {
                   (void*)d_lcc, (void*)d_rcc, (void*)d_wcc, (void*)d_int1, (void*)d_int2, (void*)d_ad, (void*)d_gen})
     if (p) cudaFree(p);
   if (h_scalars) cudaFreeHost(h_scalars);
+  quads_release();
   for (auto& m : prof_marks) cudaEventDestroy(m.second);
   for (auto e : prof_pool) cudaEventDestroy(e);
   if (ev_begin) cudaEventDestroy(ev_begin);
@@ -431,9 +432,15 @@ imsrg_status Ctx::magnus_expand(double* DG, int hDG, const double* G, int hG, in
 
 // BCH_EXPAND (src/IMSRG_MAGNUS.f90:149-234)
 imsrg_status Ctx::bch_expand(double* HS, const double* G, int hG, const double* H, int hH, int max_terms,
-                             double conv, int* terms, bool cr) {
+                             double conv, int* terms, bool cr, bool quads) {
   CK(ensure_workspace());
   CK(ensure_flow_workspace());
+  double* int3 = nullptr;  // quads: the correction added to the next nested commutator
+  if (quads) {
+    CK(quads_prepare());
+    int3 = quads_int3();
+    CK(cuda(cudaMemsetAsync(int3, 0, sizeof(double) * (size_t)L.slab, stream), "memset(INT3)"));
+  }
   const size_t sb = sizeof(double) * (size_t)L.slab;
   CK(cuda(cudaMemcpyAsync(HS, H, sb, cudaMemcpyDeviceToDevice, stream), "copy HS"));
   // ad^(n-1)(H) and ad^n(H) alternate between two buffers; the commutator assigns every
@@ -445,6 +452,10 @@ imsrg_status Ctx::bch_expand(double* HS, const double* G, int hG, const double* 
     const double* ad = (iw == 2) ? H : ((iw & 1) ? d_int2 : d_ad);
     double* out = (iw & 1) ? d_ad : d_int2;
     CK(commutator(G, hG, ad, hH, out, hH, true));
+    if (quads) {
+      CK(axpby(out, 1.0, int3, 1.0, out));
+      CK(restore_quadrupoles(ad, hH, G, hG, int3));
+    }
     CK(axpby(HS, 1.0, out, coef, HS));
     CK(frob_async(out, coef, 0));
     CK(read_scalars(1));
@@ -1029,6 +1040,21 @@ imsrg_status imsrg_bch_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, c
   HS->herm = H->herm;
   int t = 0;
   imsrg_status s = c->bch_expand(HS->d, G->d, G->herm, H->d, H->herm, max_terms, conv, &t);
+  if (terms_used) *terms_used = t;
+  return s;
+}
+
+imsrg_status imsrg_bch_expand_quads(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H,
+                                    int32_t max_terms, double conv, int32_t* terms_used) {
+  CTX(ctx);
+  CK(check_op(c, HS, "imsrg_bch_expand_quads"));
+  CK(check_op(c, G, "imsrg_bch_expand_quads"));
+  CK(check_op(c, H, "imsrg_bch_expand_quads"));
+  if (HS == G || HS == H) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "HS must not alias G or H");
+  if (max_terms < 2) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "max_terms must be >= 2");
+  HS->herm = H->herm;
+  int t = 0;
+  imsrg_status s = c->bch_expand(HS->d, G->d, G->herm, H->d, H->herm, max_terms, conv, &t, false, true);
   if (terms_used) *terms_used = t;
   return s;
 }

@@ -20,6 +20,7 @@ struct StepGraph;
 struct AdjointState;
 struct TensorState;
 struct imsrg_eom;
+struct QuadState;
 struct HFState;
 
 // MAGNUS_EXPAND coefficients as the literals of src/IMSRG_MAGNUS.f90:646
@@ -75,6 +76,7 @@ struct Ctx {
   StepGraph* sg = nullptr;  // captured Magnus step (graph.cu)
   AdjointState* adj = nullptr;  // reverse-mode workspaces (adjoint.cu)
   HFState* hf = nullptr;        // Hartree-Fock tables (hf.cu)
+  QuadState* qs = nullptr;      // quadrupole restoration of BCH_EXPAND (quads.cu)
   std::vector<double*> op_pool;  // slabs of destroyed operators, reused by imsrg_op_create
   // kernel launches issued (cumulative) and optional per-phase CUDA-event timing
   int64_t launches = 0;
@@ -110,9 +112,14 @@ struct Ctx {
   imsrg_status atan_generator(const double* Hden, int hden, const double* Hnum, double* ETA);
   imsrg_status w2_generator(const double* H, int hH, double* ETA);
   imsrg_status magnus_expand(double* DG, int hDG, const double* G, int hG, int* used);
-  // cr: CR_EXPAND's coefficients 1/n! (src/IMSRG_MAGNUS.f90:532-617) and no error after max_terms
+  // cr: CR_EXPAND's coefficients 1/n! (src/IMSRG_MAGNUS.f90:532-617) and no error after max_terms;
+  // quads: BCH_EXPAND with quads = 'y' (restore_quadrupoles after every nested commutator)
   imsrg_status bch_expand(double* HS, const double* G, int hG, const double* H, int hH, int max_terms, double conv,
-                          int* terms, bool cr = false);
+                          int* terms, bool cr = false, bool quads = false);
+  imsrg_status quads_prepare();
+  void quads_release();
+  double* quads_int3();
+  imsrg_status restore_quadrupoles(const double* X, int hX, const double* OM, int hOM, double* RES);
 
   // one Magnus step, eager or replayed from a CUDA graph (graph.cu)
   imsrg_status magnus_step(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,

@@ -430,6 +430,16 @@ class Engine:
         self._ck(self.L.imsrg_bch_expand(self.h, HS.h, G.h, H.h, int(max_terms), float(conv), C.byref(n)))
         return n.value
 
+    def bch_expand_quads(self, HS: SqOp, G: SqOp, H: SqOp, max_terms: int = 40, conv: float = CONV) -> int:
+        """BCH_EXPAND with quads = 'y' (src/IMSRG_MAGNUS.f90:149-234, 908-1132)."""
+        n = C.c_int32()
+        self._ck(self.L.imsrg_bch_expand_quads(self.h, HS.h, G.h, H.h, int(max_terms), float(conv), C.byref(n)))
+        return n.value
+
+    def restore_quadrupoles(self, X: SqOp, OM: SqOp, RES: SqOp):
+        """restore_quadrupoles (src/IMSRG_MAGNUS.f90:908-1070): RES = its pp-hh arrays."""
+        self._ck(self.L.imsrg_restore_quadrupoles(self.h, X.h, OM.h, RES.h))
+
     def restore_triples(self, H: SqOp, OM: SqOp):
         """restore_triples (src/IMSRG_MAGNUS.f90:767-902): the triples correction and the number of
         (ppp, hhh) pairs summed."""

@@ -205,6 +205,14 @@ imsrg_status imsrg_euler_step(imsrg_ctx* ctx, imsrg_op* G, const imsrg_op* DG, d
  * max_terms (the reference STOPs after 40). */
 imsrg_status imsrg_bch_expand(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H, int32_t max_terms,
                               double conv, int32_t* terms_used);
+/* BCH_EXPAND with quads = 'y': after every nested commutator the correction of
+ * restore_quadrupoles (:908-1132) from the previous term is added, then rebuilt from the operator
+ * just commuted (FP64 intermediates and insertions; the commutators in the context's precision). */
+imsrg_status imsrg_bch_expand_quads(imsrg_ctx* ctx, imsrg_op* HS, const imsrg_op* G, const imsrg_op* H,
+                                    int32_t max_terms, double conv, int32_t* terms_used);
+/* restore_quadrupoles(X, OM, w1, w2, RES) :908 -- RES = 0 except its pp-hh arrays, which it assigns;
+ * RES->herm = 1 */
+imsrg_status imsrg_restore_quadrupoles(imsrg_ctx* ctx, const imsrg_op* X, const imsrg_op* OM, imsrg_op* RES);
 /* CR_EXPAND(HS, G, H, jbas, quads) :532 -- HS = H + [G,H]/2! + [G,[G,H]]/3! + ..., the operator of
  * the completely renormalised triples (src/main_IMSRG.f90:310); stops when a term's norm times its
  * coefficient drops below conv or after max_terms (the reference: 14, 1e-6), without an error. */

@@ -1725,6 +1725,7 @@ namespace {
 #include "oracle_hf.inc"
 #include "oracle_eom.inc"
 #include "oracle_triples.inc"
+#include "oracle_quads.inc"
 }  // namespace
 
 // ====================================================================== C interface
@@ -1950,6 +1951,16 @@ double orc_comm223(void* b, const double* L, int hL, const double* R, int hR, in
 }
 double orc_restore_triples(void* b, const double* H, const double* OM, int chan) {
   return restore_triples(*(Basis*)b, H, OM, chan);
+}
+
+// ---- quadrupoles in BCH_EXPAND (oracle_quads.inc)
+void orc_restore_quadrupoles(void* b, const double* X, int hX, const double* OM, int hOM, double* RES) {
+  restore_quadrupoles(*(Basis*)b, X, hX, OM, hOM, RES);
+}
+int orc_bch_expand_quads(void* b, double* HS, const double* G, const double* H, int max_terms, double conv) {
+  Basis& B = *(Basis*)b;
+  Work w(B);
+  return bch_expand_quads(B, HS, G, H, max_terms, conv, w);
 }
 
 }  // extern "C"

@@ -100,6 +100,8 @@ def lib():
         "orc_p1_p2": (d, [vp, i, i, i, i, i]),
         "orc_r1_r2": (d, [vp, i, i, i, i, i]),
         "orc_three_channels": (i, [vp, vp, vp, vp, vp, vp]),
+        "orc_restore_quadrupoles": (None, [vp, _dp, i, _dp, i, _dp]),
+        "orc_bch_expand_quads": (i, [vp, _dp, _dp, _dp, i, d]),
         "orc_comm223": (d, [vp, _dp, i, _dp, i] + [i] * 9),
         "orc_restore_triples": (d, [vp, _dp, _dp, i]),
         "orc_eom_create": (vp, [vp]),
@@ -304,6 +306,19 @@ class Oracle:
 
     def bf_2body(self, A, hA, B, hB, a, b, c, d, J):
         return self.L.orc_bf_2body(self.h, A, hA, B, hB, a, b, c, d, J)
+
+    # ---- quadrupoles (src/IMSRG_MAGNUS.f90:908-1132)
+    def restore_quadrupoles(self, X, hX, OM, hOM):
+        """restore_quadrupoles: the pp-hh arrays it assigns (zero elsewhere)."""
+        RES = self.new()
+        self.L.orc_restore_quadrupoles(self.h, X, hX, OM, hOM, RES)
+        return RES
+
+    def bch_expand_quads(self, G, H, max_terms=40, conv=BCH_CONV):
+        """BCH_EXPAND with quads = 'y'."""
+        HS = self.new()
+        n = self.L.orc_bch_expand_quads(self.h, HS, G, H, max_terms, conv)
+        return HS, n
 
     # ---- perturbative triples (src/IMSRG_MAGNUS.f90:767-902)
     def three_channels(self):

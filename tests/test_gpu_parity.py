@@ -118,3 +118,18 @@ def test_cr_expand(oracles, engines, emax):
     assert rel_err(dHS.download(), ref) < TOL
     # the capped series ends without an error
     assert eng.cr_expand(dHS, eng.new_op(-1, G * 40), dH, 14, 1e-30) == 13
+
+
+@pytest.mark.parametrize("emax", [2, 4])
+def test_quadrupoles(oracles, engines, emax):
+    """restore_quadrupoles and BCH_EXPAND with quads = 'y' (src/IMSRG_MAGNUS.f90:149-234, 908-1132)
+    against the oracle, FP64, 1e-10."""
+    o, eng = oracles(emax), engines(emax)
+    X, OM = o.random(93, 1), o.random(94, -1) * 0.05
+    dX, dOM, dQ = eng.new_op(1, X), eng.new_op(-1, OM), eng.new_op(1)
+    eng.restore_quadrupoles(dX, dOM, dQ)
+    assert rel_err(dQ.download(), o.restore_quadrupoles(X, 1, OM, -1)) < TOL
+    ref, n = o.bch_expand_quads(OM, X, 40, 1e-6)
+    dHS = eng.new_op(1)
+    assert eng.bch_expand_quads(dHS, dOM, dX, 40, 1e-6) == n
+    assert rel_err(dHS.download(), ref) < TOL

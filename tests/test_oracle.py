@@ -193,3 +193,25 @@ def test_cr_expand_series(oracles):
     # capped series: no error, all 13 terms
     CR2, n2 = o.cr_expand(G * 40, H, 14, 1e-30)
     assert n2 == 13 and np.all(np.isfinite(CR2))
+
+
+def test_restore_quadrupoles_structure(oracles):
+    """restore_quadrupoles (src/IMSRG_MAGNUS.f90:908-1070): with a zero Omega the quadrupole BCH
+    reduces to H, and its change of H(s) shrinks with Omega (at first order through the ladder
+    products the reference's workspace holds in channels without pp or hh pairs, at second order
+    elsewhere)."""
+    o = oracles(4)
+    b = o.basis
+    X, OM = o.random(91, 1), o.random(92, -1) * 0.05
+    Q = o.restore_quadrupoles(X, 1, OM, -1)
+    ref, _ = o.bch_expand(OM, X)
+    hq, _ = o.bch_expand_quads(OM, X)
+    assert np.count_nonzero(Q) > 0
+    assert np.abs(hq - ref).max() > 0.0
+    h0, n0 = o.bch_expand_quads(OM * 0.0, X)
+    assert n0 == 1 and np.array_equal(h0, X)
+    # halving Omega at least halves the difference
+    hq2, _ = o.bch_expand_quads(OM * 0.5, X)
+    ref2, _ = o.bch_expand(OM * 0.5, X)
+    r = np.abs(hq2 - ref2).max() / np.abs(hq - ref).max()
+    assert 0.1 < r < 0.55
