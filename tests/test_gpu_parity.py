@@ -125,7 +125,7 @@ def test_quadrupoles(oracles, engines, emax):
     """restore_quadrupoles and BCH_EXPAND with quads = 'y' (src/IMSRG_MAGNUS.f90:149-234, 908-1132)
     against the oracle, FP64, 1e-10."""
     o, eng = oracles(emax), engines(emax)
-    X, OM = o.random(93, 1), o.random(94, -1) * 0.05
+    X, OM = o.random(93, 1), o.random(94, -1) * 0.02
     dX, dOM, dQ = eng.new_op(1, X), eng.new_op(-1, OM), eng.new_op(1)
     eng.restore_quadrupoles(dX, dOM, dQ)
     assert rel_err(dQ.download(), o.restore_quadrupoles(X, 1, OM, -1)) < TOL
