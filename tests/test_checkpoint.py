@@ -41,3 +41,9 @@ def test_fortran_e15_7_format():
     assert _e15_7(9.99999999) == "  0.1000000E+02"
     assert _e15_7(-0.000123456789) == " -0.1234568E-03"
     assert _e15_7(0.0) == "  0.0000000E+00"
+
+
+def test_fortran_e_formats():
+    from imsrg_gb300.ode import _e_fmt
+    assert _e_fmt(114.357603550025, 17, 9) == "  0.114357604E+03"
+    assert _e_fmt(-0.0001234, 15, 7) == " -0.1234000E-03"
