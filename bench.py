@@ -725,7 +725,8 @@ def main():
     ap.add_argument("--eom-states", type=int, default=4, help="eom workload: states per J^pi")
     ap.add_argument("--s-end", type=float, default=30.0, help="adjoint workload: flow length")
     ap.add_argument("--fd-components", type=int, default=None)
-    ap.add_argument("--mode", default="bf16x6", choices=["bf16x3", "bf16x6"])
+    ap.add_argument("--mode", default=None, choices=["bf16x3", "bf16x6"],
+                    help="mixed mode: default bf16x3 for the flow (the headline), bf16x6 for the other workloads")
     ap.add_argument("--ds", type=float, default=0.5)
     ap.add_argument("--bch-max-terms", type=int, default=11, help="BCH_EXPAND max_terms (10 nested commutators)")
     ap.add_argument("--bch-conv", type=float, default=1e-8)
@@ -738,6 +739,8 @@ def main():
                     help="reference state of the flow: calc_HF (default) or calc_HO")
     args = ap.parse_args()
     args.e2e_steps = max(1, args.e2e_steps)
+    if args.mode is None:
+        args.mode = "bf16x3" if args.workload == "flow" else "bf16x6"
     world, rank, local, pg = dist_setup()
 
     if args.emax is None and args.workload == "flow":
