@@ -59,6 +59,7 @@ struct imsrg_eom {
   // captured with
   cudaGraphExec_t gexec = nullptr;
   const double* g_H = nullptr;
+  int g_prec = -1;  // the context's precision at capture (the kernels differ between modes)
 };
 
 namespace {
@@ -228,10 +229,12 @@ imsrg_status Ctx::eom_matvec(imsrg_eom& E, const double* Hd, const double* d_v, 
   return launched("k_eom_unpack");
 }
 
-// the product d_v -> d_w through the CUDA graph captured for Hd (captured on first use, after
-// one direct run that also makes the workspaces; the operands are read when the graph runs)
+// the product d_v -> d_w through the CUDA graph captured for Hd and the context's precision
+// (captured on first use, after one direct run that also makes the workspaces; the operands are
+// read when the graph runs)
 imsrg_status Ctx::eom_matvec_graph(imsrg_eom& E, const double* Hd) {
-  if (E.gexec && E.g_H == Hd) return cuda(cudaGraphLaunch(E.gexec, stream), "cudaGraphLaunch(eom)");
+  if (E.gexec && E.g_H == Hd && E.g_prec == (int)precision)
+    return cuda(cudaGraphLaunch(E.gexec, stream), "cudaGraphLaunch(eom)");
   CKE(eom_matvec(E, Hd, E.d_v, E.d_w));
   CKE(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize"));
   if (E.gexec) {
@@ -250,6 +253,7 @@ imsrg_status Ctx::eom_matvec_graph(imsrg_eom& E, const double* Hd) {
     return r;
   }
   E.g_H = Hd;
+  E.g_prec = (int)precision;
   return IMSRG_OK;  // d_w already holds the direct run's product
 }
 

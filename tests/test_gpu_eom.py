@@ -118,3 +118,25 @@ def test_eom_matvec_mixed_precision(oracles, mode, tol):
     H = eng.synthetic_hamiltonian(seed=5)
     v = np.random.default_rng(9).standard_normal(space.n)
     assert rel_err(space.matvec(eng.new_op(1, H), v), e.matvec(H, v)) < tol
+
+
+def test_eom_graph_follows_precision_and_h(oracles):
+    """The replayed product is recaptured when the context's precision or the H operator changes."""
+    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300.eom import LadderSpace
+    from oracle.oracle import EomOracle
+    o = oracles(4)
+    eng = Engine(make_basis(4), device=0)
+    e = EomOracle(o, 2, 0)
+    space = LadderSpace(eng, 2, 0)
+    H1, H2 = eng.synthetic_hamiltonian(seed=6), eng.synthetic_hamiltonian(seed=7)
+    d1, d2 = eng.new_op(1, H1), eng.new_op(1, H2)
+    v = np.random.default_rng(2).standard_normal(space.n)
+    r1, r2 = e.matvec(H1, v), e.matvec(H2, v)
+    for _ in range(2):
+        assert rel_err(space.matvec(d1, v), r1) < 1e-10
+    assert rel_err(space.matvec(d2, v), r2) < 1e-10
+    eng.set_precision("bf16x6")
+    assert rel_err(space.matvec(d2, v), r2) < 1e-5
+    eng.set_precision("fp64")
+    assert rel_err(space.matvec(d2, v), r2) < 1e-10
