@@ -710,6 +710,47 @@ def triples_workload(args, local: int):
     }), flush=True)
 
 
+def ode_workload(args, local: int):
+    """The traditional flow (decouple_hamiltonian, src/IMSRG_ODE.f90:9-178): calc_HF, then the
+    Adams integration of dH/ds = [eta, H] over intervals of 0.1 until |MBPT2| < 1e-6 (or s=s_end),
+    once with the device derivative and once with the oracle's (all host cores), same integrator."""
+    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300.ode import decouple_hamiltonian
+    from oracle import oracle as orc
+    emax = args.emax if args.emax is not None else 4
+    b = make_basis(emax)
+    eng = Engine(b, device=local, precision="fp64")
+    H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
+    s_max = args.s_end
+    t = time.perf_counter()
+    res = decouple_hamiltonian(eng, H, s_max=s_max)
+    t_gpu = time.perf_counter() - t
+    o = orc.Oracle(b)
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+
+    def oracle_derivative(s, y):
+        Hs = eng.repackage(y, 1)
+        return eng.vectorize(o.commutator(o.white(Hs, 1), -1, Hs, 1))
+
+    t = time.perf_counter()
+    ref = decouple_hamiltonian(eng, H, s_max=s_max, derivative=oracle_derivative)
+    t_cpu = time.perf_counter() - t
+    print(json.dumps({
+        "metric": f"traditional ODE flow at eMax={emax}, wall time", "value": t_gpu, "unit": "s", "n_gpus": 1,
+        "steps": len(res.steps) - 1, "warmup": 0, "ms_per_step": 1e3 * t_gpu / max(len(res.steps) - 1, 1),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"calc_HF, then decouple_hamiltonian at eMax={emax} ({b.norbits} orbits): Adams "
+                               f"(Shampine-Gordon) integration, relerr = abserr = 1e-6, intervals of 0.1 up to "
+                               f"s={s_max:g} or |MBPT2| < 1e-6; device derivative vs the oracle's, same integrator",
+                   "reference_state": hf_rec, "s_end": res.steps[-1][1], "E0": res.E0, "E0_cpu": ref.E0,
+                   "dE0_keV": 1e3 * abs(res.E0 - ref.E0), "derivatives": res.evaluations,
+                   "derivatives_cpu": ref.evaluations, "gpu_s": t_gpu, "cpu_s": t_cpu, "cpu_over_gpu": t_cpu / t_gpu},
+        "cpu_baseline": {"value": t_cpu, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"the same flow with the oracle's derivative (FP64, OpenMP x{cores})"},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -718,7 +759,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--emax", type=int, default=None, help="default 10 (flow), 6 (adjoint)")
     ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision", "hf-flow", "eom",
-                                                     "triples"])
+                                                     "triples", "ode"])
     ap.add_argument("--precision-flow-steps", type=int, default=20)
     ap.add_argument("--obs-bch-max-terms", type=int, default=40)
     ap.add_argument("--adjoint-k", type=int, default=16)
@@ -764,6 +805,12 @@ def main():
     if args.workload == "precision":
         if rank == 0:
             precision_workload(args, local)
+        return
+    if args.workload == "ode":
+        if rank == 0:
+            if args.s_end == 30.0:
+                args.s_end = 20.0
+            ode_workload(args, local)
         return
     if args.workload == "triples":
         if rank == 0:
