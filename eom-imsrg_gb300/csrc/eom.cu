@@ -15,8 +15,8 @@
 // S(h) are written by one gather kernel from the amplitude vector and both results are read
 // back by one kernel.  The commutators run in the tensor engine's excitation mode: only the
 // terms with a nonzero (fph, pp-hh) operand of S(h) and only the fph and pp-hh outputs are
-// computed (the ladder's remaining products are small and stay FP64; the rest follows the
-// context's precision), and every particle-hole product is recoupled
+// computed (their GEMMs in FP64, or FP32 in the mixed modes, with the 122 / 212 sums), and every
+// particle-hole product is recoupled
 // (EOM_TS_commutator_222_ph has no 1e-6 cut, and a cut would make the product depend on the
 // scale of v).
 //

@@ -37,6 +37,8 @@ __global__ void k_ts212f(DevLayout D, DevTLayout T, const double* L, int hL, con
 __global__ void k_ts_pphh_update(int64_t n, int64_t off, double* RES, const double* w1, const double* w2);
 __global__ void k_tpandya(DevLayout D, DevTLayout T, const double* R, int hR, int J3, int J4, int qa, int qb, int term,
                           double scale, double* out);
+// FP32 SIMT form of k_gemm_fp64 (FP64 operands and results), gemm_tc.cu
+__global__ void k_gemm_f32(const GemmProb* probs, const GemmTile* tiles, GemmOperands ops);
 __global__ void k_tpandya_exc(DevLayout D, DevTLayout T, const double* R, int hR, const ExcBlock* blk,
                               const int64_t* pre, int nblk, const int* pe, const int* hp, double* ccr, double* ccx);
 __global__ void k_ts222ph_scatter_exc(DevLayout D, DevTLayout T, const ExcBlock* blk, const int64_t* pre, int nblk,
@@ -484,8 +486,13 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       ops.in[kOpL] = Lp; ops.in[kOpR] = R;
       ops.out[kOpW1] = S.w1; ops.out[kOpW2] = S.w2;
       ops.hL = hL; ops.hR = hR;
-      k_gemm_fp64<<<nt, 256, 0, stream>>>(exc ? S.exc_p : S.pphh_p, exc ? S.exc_t : S.pphh_t, ops);
-      CKT(launched("k_gemm_fp64(tensor pphh)"));
+      if (exc && precision != IMSRG_PREC_FP64) {  // mixed modes: the excitation ladder in FP32
+        k_gemm_f32<<<nt, 256, 0, stream>>>(S.exc_p, S.exc_t, ops);
+        CKT(launched("k_gemm_f32(tensor pphh, excitation)"));
+      } else {
+        k_gemm_fp64<<<nt, 256, 0, stream>>>(exc ? S.exc_p : S.pphh_p, exc ? S.exc_t : S.pphh_t, ops);
+        CKT(launched("k_gemm_fp64(tensor pphh)"));
+      }
     }
     if (T.n2b) {
       k_ts_pphh_update<<<grid_n(T.n2b), 256, 0, stream>>>(T.n2b, S.T.goff.empty() ? 0 : S.T.goff[0], RES, S.w1, S.w2);
@@ -496,7 +503,7 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
       CKT(launched("k_ts221"));
     }
   }
-  if ((pieces & 64) && exc) {  // excitation mode: packed CCR / CCX of all blocks, FP64 products
+  if ((pieces & 64) && exc) {  // excitation mode: packed CCR / CCX of all blocks (FP32 products in mixed modes)
     if (S.x_nblk) {
       if (!S.x_buf[0])
         for (int k = 0; k < 4; ++k)
@@ -510,8 +517,13 @@ imsrg_status Ctx::tensor_commutator(TensorState& S, const double* Lp, int hL, co
         ops.in[kOpLCC] = d_lcc; ops.in[kOpRCC] = S.x_buf[0]; ops.in[kOpWCC] = S.x_buf[1];
         ops.out[kOpW1] = S.x_buf[2]; ops.out[kOpW2] = S.x_buf[3];
         ops.hL = hL; ops.hR = hR;
-        k_gemm_fp64<<<S.x_n_t, 256, 0, stream>>>(S.x_p, S.x_t, ops);
-        CKT(launched("k_gemm_fp64(tensor ph, excitation)"));
+        if (precision != IMSRG_PREC_FP64) {  // mixed modes: FP32 products
+          k_gemm_f32<<<S.x_n_t, 256, 0, stream>>>(S.x_p, S.x_t, ops);
+          CKT(launched("k_gemm_f32(tensor ph, excitation)"));
+        } else {
+          k_gemm_fp64<<<S.x_n_t, 256, 0, stream>>>(S.x_p, S.x_t, ops);
+          CKT(launched("k_gemm_fp64(tensor ph, excitation)"));
+        }
       }
       k_ts222ph_scatter_exc<<<grid_n(S.x_ns), 256, 0, stream>>>(D, T, S.x_blk, S.x_pre_s, S.x_nblk, S.d_pe, S.d_hp,
                                                                  S.x_buf[2], S.x_buf[3], hL, hR, RES);

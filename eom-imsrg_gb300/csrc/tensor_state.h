@@ -27,7 +27,8 @@ using imsrg::TLayout;
 constexpr int kTensorExactPh = 512;
 // pieces flag: R is an excitation operator (fph and (pp,hh) / (hh,pp) elements only) and only
 // the fph and (pp,hh) / (hh,pp) elements of RES are computed (the rest of RES is undefined);
-// implies kTensorExactPh and runs the ladder's remaining products in FP64
+// implies kTensorExactPh; its ladder and particle-hole products run in FP64, or as FP32 SIMT
+// GEMMs in the mixed modes
 constexpr int kTensorExcitation = 1024;
 
 // output slot of the second product of a tensor ladder problem (TcOut::f64 index)
