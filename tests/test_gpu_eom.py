@@ -107,7 +107,7 @@ def test_excited_states_after_flow(engines, tmp_path):
 
 @pytest.mark.parametrize("mode,tol", [("bf16x6", 1e-5), ("bf16x3", 1e-4)])
 def test_eom_matvec_mixed_precision(oracles, mode, tol):
-    """The mixed modes run the product's particle-hole GEMMs on the split-BF16 tensor cores."""
+    """In the mixed modes the product's GEMMs run as FP32 SIMT tiles and the 122 / 212 sums in FP32."""
     from imsrg_gb300 import Engine, make_basis
     from imsrg_gb300.eom import LadderSpace
     from oracle.oracle import EomOracle
