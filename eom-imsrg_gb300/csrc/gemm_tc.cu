@@ -1060,7 +1060,7 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
     tc->recouple_minb = bm;
     if (st != IMSRG_OK) break;
     int br = tc->recouple_ctas;
-    for (int mult : {4, 8, 16, 32}) {
+    for (int mult : {4, 8, 16, 32, 64, 128}) {
       tc->recouple_ctas = tc->num_sms * mult;
       float ms;
       if ((st = time_one(&ms)) != IMSRG_OK) break;

@@ -268,7 +268,7 @@ imsrg_status imsrg_bch_tensor(imsrg_ctx* ctx, const imsrg_op* G, imsrg_tensor* H
 /* mat_frob_norm of a tensor operator (src/basic_IMSRG.f90:4056-4087) */
 imsrg_status imsrg_tensor_frob_norm(imsrg_ctx* ctx, const imsrg_tensor* t, double* out);
 
-/* ---- perturbative triples (restore_triples, src/IMSRG_MAGNUS.f90:767-902; the driver's
+/* ---- perturbative triples (restore_triples, src/IMSRG_MAGNUS.f90:767-902; the main program's
  * 'trips' option, src/main_IMSRG.f90:296-315): the correction summed over the three-body basis
  * of enumerate_three_body (src/basic_IMSRG.f90:4215-4420) of W^2/D (Jtot+1), W the three-body
  * element of [OM, H] (commutator_223_single, src/commutators.f90:928-1325) and D the
