@@ -1049,23 +1049,20 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
       if (ms < best) { best = ms; bt = c[0]; bs = c[1]; }
     }
     if (st != IMSRG_OK || (st = tc_g122_partition(bt, bs)) != IMSRG_OK) break;
-    // recoupling: launch-bounds variant, then CTAs
-    int bm = tc->recouple_minb;
+    // recoupling: launch-bounds variant and CTA count together (the best CTA count depends on
+    // how many CTAs of the variant are resident)
+    int bm = tc->recouple_minb, br = tc->recouple_ctas;
     for (int minb : {4, 5, 6, 8}) {
-      tc->recouple_minb = minb;
-      float ms;
-      if ((st = time_one(&ms)) != IMSRG_OK) break;
-      if (ms < best) { best = ms; bm = minb; }
+      for (int mult : {4, 8, 16, 32, 64, 128}) {
+        tc->recouple_minb = minb;
+        tc->recouple_ctas = tc->num_sms * mult;
+        float ms;
+        if ((st = time_one(&ms)) != IMSRG_OK) break;
+        if (ms < best) { best = ms; bm = minb; br = tc->recouple_ctas; }
+      }
+      if (st != IMSRG_OK) break;
     }
     tc->recouple_minb = bm;
-    if (st != IMSRG_OK) break;
-    int br = tc->recouple_ctas;
-    for (int mult : {4, 8, 16, 32, 64, 128}) {
-      tc->recouple_ctas = tc->num_sms * mult;
-      float ms;
-      if ((st = time_one(&ms)) != IMSRG_OK) break;
-      if (ms < best) { best = ms; br = tc->recouple_ctas; }
-    }
     tc->recouple_ctas = br;
     if (st != IMSRG_OK) break;
     // GEMM tile order
