@@ -169,27 +169,32 @@ def find_blas_dgemm():
     return None, False, "built-in blocked dgemm", None
 
 
-def cpu_commutators(emax: int, n_warm: int, n_steps: int, seed: int = 1):
-    """Time the CPU restatement of the reference on one [eta, H] commutator per step."""
+def cpu_commutators(emax: int, n_warm: int, n_steps: int, seed: int = 1, reference: str = "hf"):
+    """Time the CPU restatement of the reference (the oracle) on one [eta, H] commutator per
+    step.  Only the oracle runs here: it builds the same seeded bare Hamiltonian as the
+    library, brings it to the same reference state (calc_HF, or calc_HO) and its White
+    generator, untimed; the timed region is the commutators alone."""
     from oracle import oracle as orc
-    from imsrg_gb300 import Engine, make_basis
+    from imsrg_gb300.basis import make_basis
     b = make_basis(emax)
-    host = Engine(b, device=-1)
-    H = host.synthetic_hamiltonian(seed=seed)
     o = orc.Oracle(b)
     cores = os.cpu_count() or 1
     orc.set_threads(cores)
     addr, ilp64, blas_name, keep = find_blas_dgemm()
     if addr:
         orc.use_blas_dgemm(addr, ilp64)
+    t = time.perf_counter()
+    bare = o.synthetic_bare_hamiltonian(seed=seed)
+    H = (o.calc_hf(bare) if reference == "hf" else o.calc_ho(bare))[0]
     eta = o.white(H, 1)
+    prep_s = time.perf_counter() - t
     for _ in range(n_warm):
         o.commutator(eta, -1, H, 1, 1)
     t = time.perf_counter()
     for _ in range(n_steps):
         o.commutator(eta, -1, H, 1, 1)
     dt = time.perf_counter() - t
-    return dt, cores, blas_name, keep
+    return dt, cores, blas_name, keep, {"reference": reference, "E0": float(H[0]), "prepare_s": prep_s}
 
 
 def prepared_hamiltonian(eng, reference: str, seed: int = 1, time_transform: bool = False):
@@ -232,24 +237,36 @@ def algorithmic_work(eng, mode: str, phase: str):
     """Algorithmic bytes (or FLOPs) of one launch of a phase at this basis.
 
     Bytes count each array the phase must touch once: FP64 operators (8 B), the FP32
-    particle-hole products Z and Y (4 B each, wcc_size elements), the split-BF16 operand
-    slices (2 B per slice).  FLOPs are 2 M N K of the reference's dgemm calls times the
-    number of slice products."""
-    S = {"bf16x3": 3, "bf16x6": 6, "fp64": 1}[mode]          # slice products per GEMM
-    slices = {"bf16x3": 2, "bf16x6": 3, "fp64": 1}[mode]
+    recoupling input X (4 B, wcc_size elements; for the recoupling itself the distinct
+    elements it reads, counted by the library), the split operand slices (2 B BF16, 4 B TF32
+    per slice).  FLOPs are 2 M N K of the products times the number of slice products."""
+    import numpy as np
+    S = {"bf16x3": 3, "bf16x6": 6, "tf32x3": 3, "fp64": 1}[mode]  # slice products per GEMM
+    slices = {"bf16x3": 2, "bf16x6": 3, "tf32x3": 2, "fp64": 1}[mode]
+    esize = 4 if mode == "tf32x3" else 2                           # bytes per operand value
     info = eng.block_info()
     A = eng.basis.nholes
     P = eng.basis.norbits - A
     n2b = eng.slab - (1 + A * A + P * P + P * A)
     cc = eng.cc_info()
-    if phase == "recouple":   # read Z and Y once, read and write the 2b part of RES
-        return "hbm", 2 * 4 * eng.wcc_size + 2 * 8 * n2b
+    if phase == "recouple":   # counted exactly from the quadruples: distinct X reads (FP32), the
+        #                        RES elements read and written (FP64), the kernel's index data
+        v = [C.c_int64() for _ in range(4)]
+        eng._ck(eng.L.imsrg_recouple_traffic(eng.h, *[C.byref(x) for x in v]))
+        x_reads, x_distinct, res_elems, aux = (x.value for x in v)
+        return "hbm", 4 * x_distinct + 16 * res_elems + aux
+    if phase == "mirror":     # the upper triangle of every square array read, the lower written
+        sq = sum(n * (n - 1) // 2 for g in ("npp", "nph", "nhh") for n in (int(x) for x in info[g]))
+        return "hbm", 16 * sq
     if phase == "c122":       # read L and R once, write the 2b part of RES
         return "hbm", 2 * 8 * eng.slab + 8 * n2b
-    if phase == "ph_gemm":    # Z and Y written once in FP32 (the products have K <= nph)
-        return "hbm", 2 * 4 * eng.wcc_size
-    if phase == "pphh_gemm":  # sum 2 M N K over the K = npp products, times slice products
-        f = 0
+    if phase == "ph_gemm":    # X written once in FP32 (one product of four terms per channel, K = nph),
+        #                       its split operands (row-signed and row-swapped LCC, RCC) read once
+        return "hbm", 4 * eng.wcc_size + 2 * 2 * esize * slices * int((cc["rlen"] * cc["nph"]).sum())
+    if phase == "pphh_gemm":  # the merged tensor-core launch: sum 2 M N K over the K = npp ladder
+        #                       products and the four K = nph products of X per cross-coupled
+        #                       channel, times the slice products
+        f = 4 * 2 * int((cc["rlen"].astype(np.int64) ** 2 * cc["nph"]).sum()) if mode != "fp64" else 0
         for q in range(eng.nblocks):
             np_, nb, nh = int(info["npp"][q]), int(info["nph"][q]), int(info["nhh"][q])
             if np_ == 0:
@@ -258,7 +275,7 @@ def algorithmic_work(eng, mode: str, phase: str):
             f += 2 * nb * nb * np_ + 2 * 2 * np_ * nb * np_ + 2 * 2 * nb * nh * np_
         return "tensor", f * S
     if phase == "pandya":     # two operators read, their CC slices written (standard and row-swapped)
-        return "hbm", 2 * 8 * eng.slab + 2 * 2 * 2 * slices * int((cc["rlen"] * cc["nph"]).sum())
+        return "hbm", 2 * 8 * eng.slab + 2 * 2 * esize * slices * int((cc["rlen"] * cc["nph"]).sum())
     return None, None
 
 
@@ -272,19 +289,35 @@ def flow_state(eng, H):
     return HS, G, DG, dH
 
 
+def flow_workload_name(args, norbits: int) -> str:
+    """The benchmark workload, named the same way by both arms."""
+    return (f"Magnus flow at eMax={args.emax} ({norbits} orbits, 16O-like), seeded synthetic Hamiltonian after "
+            f"calc_{args.reference.upper()}, White generator, ds={args.ds}; a Magnus step = MAGNUS_EXPAND + "
+            f"euler_step + BCH_EXPAND (<= {args.bch_max_terms - 1} nested commutators or term norm < "
+            f"{args.bch_conv:g}) + generator + MBPT2; unit: one full IMSRG(2) commutator")
+
+
 def reference_arm(args):
-    """The CPU restatement of the reference (FP64, OpenMP on all host cores, BLAS dgemm)."""
-    dt, cores, blas, _ = cpu_commutators(args.emax, args.warmup, args.steps)
+    """The CPU restatement of the reference (FP64, OpenMP on all host cores, BLAS dgemm).
+
+    A step is one full commutator [eta, H] on the flow's starting state, the unit of the
+    metric: the commutator's cost does not depend on its operands' values, so the K
+    commutators are a bounded sample of the flow's commutators.  Only the oracle is loaded."""
+    from imsrg_gb300.basis import make_basis
+    dt, cores, blas, _, state = cpu_commutators(args.emax, args.warmup, args.steps, reference=args.reference)
     v = args.steps / dt
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"[eta,H] IMSRG(2) commutators, eMax={args.emax}", "emax": args.emax,
+        "config": {"workload": flow_workload_name(args, make_basis(args.emax).norbits), "emax": args.emax,
+                   "ds": args.ds, "step": "one full commutator [eta, H] of the flow (a bounded sample)",
                    "path": "CPU restatement of the reference (FP64, OpenMP)", "blas": blas,
-                   "step": "one full commutator (the unit of the reference's Magnus/BCH loop)"},
+                   "reference_state": state,
+                   "inputs": "the oracle's own seeded synthetic Hamiltonian and calc_HF (no product library loaded)"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full commutators at eMax={args.emax}"},
+                         "sample": f"{args.steps} full commutators [eta, H] at eMax={args.emax} on the "
+                                   f"{args.reference.upper()} state"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -364,7 +397,7 @@ def precision_workload(args, local: int):
     H = None
     out = {}
     ref = {}
-    for mode in ("fp64", "bf16x6", "bf16x3"):
+    for mode in ("fp64", "bf16x6", "bf16x3", "tf32x3"):
         eng = Engine(b, device=local, precision=mode)
         if H is None:
             H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
@@ -404,7 +437,7 @@ def precision_workload(args, local: int):
         "dtype": "bf16", "data": "synthetic",
         "config": {"workload": f"[eta,H] and a Magnus flow (ds={args.ds}) at eMax={emax} ({b.norbits} orbits)",
                    "reference_state": hf_rec, "modes": out,
-                   "not_built": "FP8 and TF32-compensated products (only split-BF16 is implemented)"},
+                   "not_built": "FP8 products"},
     }), flush=True)
 
 
@@ -766,12 +799,13 @@ def main():
     ap.add_argument("--eom-states", type=int, default=4, help="eom workload: states per J^pi")
     ap.add_argument("--s-end", type=float, default=30.0, help="adjoint workload: flow length")
     ap.add_argument("--fd-components", type=int, default=None)
-    ap.add_argument("--mode", default=None, choices=["bf16x3", "bf16x6"],
+    ap.add_argument("--mode", default=None, choices=["bf16x3", "bf16x6", "tf32x3"],
                     help="mixed mode: default bf16x3 for the flow (the headline), bf16x6 for the other workloads")
     ap.add_argument("--ds", type=float, default=0.5)
     ap.add_argument("--bch-max-terms", type=int, default=11, help="BCH_EXPAND max_terms (10 nested commutators)")
     ap.add_argument("--bch-conv", type=float, default=1e-8)
-    ap.add_argument("--fp64-steps", type=int, default=3, help="FP64 graph steps (rate and |dE0|); 0 skips")
+    ap.add_argument("--fp64-steps", type=int, default=-1,
+                    help="FP64 graph steps (rate and |dE0|); -1: the W + K steps of the timed flow; 0 skips")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
@@ -879,12 +913,16 @@ def main():
     value = comm_all / (ms_max * 1e-3)
     timed = {"steps": K, "commutators": n_comm, "unconverged_bch_steps": c1["unconverged"] - c0["unconverged"],
              "s_end": args.ds * (W + K)}
+    # the mixed flow's state at the end of the timed region (s = ds * (W + K))
+    hs_end, eta_end = st[0].download(), st[2].download()
     del st
-    # ---- plain FP64 GPU path: the same flow, same graph step; rate and |dE0|, ||dH(s)||
+    # ---- plain FP64 GPU path: the same flow, same graph step; its rate, and |dE0|, ||dH(s)||
+    #      against the mixed flow at the end of the timed region (the default runs the FP64 flow
+    #      for the same W + K steps) or after --fp64-steps steps
     cmp = {}
     fp64_rate = None
-    if args.fp64_steps > 0:
-        F = args.fp64_steps
+    F = (W + K) if args.fp64_steps < 0 else args.fp64_steps
+    if F > 0:
         eng64 = Engine(b, device=local, precision="fp64")
         st64 = flow_state(eng64, H)
         eng64.magnus_step(*st64, args.ds, allow_unconverged=True, **step_kw)
@@ -896,24 +934,28 @@ def main():
             ms64 = eng64.timer_end()
             k1 = eng64.magnus_step_counters()
             fp64_rate = (k1["commutators"] - k0["commutators"]) / (ms64 * 1e-3)
-        stm = flow_state(eng, H)
-        for _ in range(F):
-            eng.magnus_step(*stm, args.ds, allow_unconverged=True, **step_kw)
-        hs_m, hs_64 = stm[0].download(), st64[0].download()
-        cmp = {"flow_steps": F, "E0_mixed": float(hs_m[0]), "E0_fp64": float(hs_64[0]),
+        if F == W + K:
+            hs_m, eta_m = hs_end, eta_end
+        else:
+            stm = flow_state(eng, H)
+            for _ in range(F):
+                eng.magnus_step(*stm, args.ds, allow_unconverged=True, **step_kw)
+            hs_m, eta_m = stm[0].download(), stm[2].download()
+            del stm
+        hs_64 = st64[0].download()
+        cmp = {"flow_steps": F, "s_compared": args.ds * F, "E0_mixed": float(hs_m[0]), "E0_fp64": float(hs_64[0]),
                "dE0_keV": abs(float(hs_m[0] - hs_64[0])) * 1e3,
                "dH_frob_rel": float(np.linalg.norm(hs_m - hs_64) / np.linalg.norm(hs_64))}
         # one commutator [eta, H(s)] in both precisions on identical inputs
-        dR = eng.new_op(1)
+        dR, dEm, dHm = eng.new_op(1), eng.new_op(-1, eta_m), eng.new_op(1, hs_m)
         dR64 = eng64.new_op(1)
-        eng.commutator(stm[2], stm[0], dR)
-        dE64, dHs64 = eng64.new_op(-1, stm[2].download()), eng64.new_op(1, hs_m)
+        eng.commutator(dEm, dHm, dR)
+        dE64, dHs64 = eng64.new_op(-1, eta_m), eng64.new_op(1, hs_m)
         eng64.commutator(dE64, dHs64, dR64)
         r_m, r_64 = dR.download(), dR64.download()
         cmp.update({"commutator_dE0_keV": abs(float(r_m[0] - r_64[0])) * 1e3,
                     "commutator_max_rel_err": float(np.max(np.abs(r_m - r_64)) / np.max(np.abs(r_64)))})
-        del st64, dR64, dE64, dHs64, eng64
-        del stm
+        del st64, dR64, dE64, dHs64, eng64, dR, dEm, dHm
 
     # ---- end to end through the C ABI: the flow kept in pinned host memory; every step
     # uploads H, Omega, eta and downloads H(s), Omega, eta around imsrg_magnus_step
@@ -988,24 +1030,22 @@ def main():
     # ---- CPU restatement of the reference on the host cores (rank 0, N=1)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        dt, cores, blas, _ = cpu_commutators(args.emax, 0, args.cpu_steps)
+        dt, cores, blas, _, state = cpu_commutators(args.emax, 0, args.cpu_steps, reference=args.reference)
         cpu = {"value": args.cpu_steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{args.cpu_steps} full [eta,H] commutators at eMax={args.emax} "
-                         f"(FP64 restatement, OpenMP x{cores}, {blas})"}
+               "sample": f"{args.cpu_steps} full [eta,H] commutators at eMax={args.emax} on the "
+                         f"{state['reference'].upper()} state (FP64 restatement, OpenMP x{cores}, {blas})"}
 
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16", "data": "synthetic",
+            "dtype": "tf32" if args.mode == "tf32x3" else "bf16", "data": "synthetic",
             "config": {
-                "workload": f"Magnus flow steps at eMax={args.emax} ({b.norbits} orbits, 16O-like), seeded "
-                            "synthetic Hamiltonian, White generator; one step = MAGNUS_EXPAND + euler_step + "
-                            f"BCH_EXPAND (<= {args.bch_max_terms - 1} nested commutators or term norm < "
-                            f"{args.bch_conv:g}) + generator + MBPT2, one CUDA-graph replay",
+                "workload": flow_workload_name(args, b.norbits),
                 "emax": args.emax, "ds": args.ds,
-                "precision": f"{args.mode}: split-BF16 tcgen05 channel GEMMs, FP32 accumulate, FP32 gathers, "
-                             "FP64 operators, E0 and norms",
+                "step": "one Magnus step, one CUDA-graph replay",
+                "precision": f"{args.mode}: " + ("TF32-compensated" if args.mode == "tf32x3" else "split-BF16") +
+                             " tcgen05 channel GEMMs, FP32 accumulate, FP32 gathers, FP64 operators, E0 and norms",
                 "parallelism": f"replicas x{world}",
                 "l2": "inputs larger than L2 (0.27 GiB per operator, 0.78 GiB Z and Y each)",
                 "reference_state": hf_rec, "autotune": tune,

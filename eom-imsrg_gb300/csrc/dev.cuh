@@ -185,27 +185,54 @@ __device__ __forceinline__ bool d_vref_f(const DevLayout& D, int a, int b, int c
   return true;
 }
 
-// FP64 -> FP32 by truncation with integer instructions only (no FP64 pipe); values below
-// FP32's normal range flush to zero.  The discarded bits are below FP32 precision, which
-// is the precision the mixed kernels work in.
+// FP64 -> FP32 with integer instructions only (GB300's FP64 pipe, which the hardware
+// conversion would use, runs at ~1/64 of the FP32 rate).  Rounds to nearest, ties to
+// even, as IEEE 754 binary64 -> binary32 conversion does:
+//   - NaN stays NaN (quiet, with the top payload bits), +-Inf stays +-Inf;
+//   - magnitudes that round above FLT_MAX become +-Inf (the rounding carry runs from the
+//     mantissa into the exponent, and exponent field 255 with a zero mantissa is Inf);
+//   - magnitudes below FP32's normal range round to FP32 subnormals k * 2^-149, or +-0.
 __device__ __forceinline__ float f64_to_f32(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7FF);
-  if (e < 1023 - 126) return 0.0f;
   const unsigned int sign = (unsigned int)(b >> 63) << 31;
-  const unsigned int fe = (unsigned int)(e - 1023 + 127);
-  const unsigned int mant = (unsigned int)((b >> 29) & 0x7FFFFF);
-  return __uint_as_float(sign | (fe << 23) | mant);
+  const int e = (int)((b >> 52) & 0x7FF);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (m ? 0x400000u | (unsigned int)(m >> 29) : 0u));
+  if (e >= 1023 - 126) {  // FP32 normal range (or overflow): keep 23 mantissa bits, round off 29
+    if (e > 1023 + 127) return __uint_as_float(sign | 0x7F800000u);
+    unsigned int v = ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(m >> 29);
+    const unsigned int rest = (unsigned int)(m & 0x1FFFFFFFu);
+    v += (rest > 0x10000000u || (rest == 0x10000000u && (v & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | v);
+  }
+  // |x| = sig * 2^(e-1075) with sig = 2^52 + m; in units of 2^-149 that is sig >> (926 - e).
+  // A shift of 54 or more leaves less than half a unit (sig < 2^53): the result is +-0.
+  const int shift = 926 - e;
+  if (shift >= 54) return __uint_as_float(sign);
+  const unsigned long long sig = m | (1ull << 52);
+  unsigned int k = (unsigned int)(sig >> shift);
+  const unsigned long long rest = sig & ((1ull << shift) - 1ull), half = 1ull << (shift - 1);
+  k += (rest > half || (rest == half && (k & 1u))) ? 1u : 0u;  // k = 2^23 encodes the smallest normal
+  return __uint_as_float(sign | k);
 }
 
-// FP32 -> FP64 (exact) with integer instructions only; zero and subnormals map to zero
+// FP32 -> FP64 (exact) with integer instructions only: zeros keep their sign, subnormals
+// are normalised, Inf and NaN (with its payload) carry over.
 __device__ __forceinline__ double f32_to_f64(float f) {
   const unsigned int u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
   const unsigned int e = (u >> 23) & 0xFF;
-  if (e == 0) return 0.0;
-  const unsigned long long b = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)(e + 1023 - 127) << 52) |
-                               ((unsigned long long)(u & 0x7FFFFF) << 29);
-  return __longlong_as_double((long long)b);
+  const unsigned int m = u & 0x7FFFFF;
+  if (e == 0xFF) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull | ((unsigned long long)m << 29)));
+  if (e == 0) {
+    if (m == 0) return __longlong_as_double((long long)sign);
+    // m * 2^-149 with its leading bit p (0..22) moved into the implicit bit
+    const int p = 31 - __clz((int)m);
+    const unsigned long long mant = (unsigned long long)(m ^ (1u << p)) << (52 - p);
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(p - 149 + 1023) << 52) | mant));
+  }
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023 - 127) << 52) |
+                                          ((unsigned long long)m << 29)));
 }
 
 __device__ __forceinline__ float d_f_elem_f(const DevLayout& D, const double* op, int herm, int a, int b) {

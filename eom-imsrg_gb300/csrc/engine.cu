@@ -126,6 +126,34 @@ imsrg_status Ctx::upload_tables() {
   pphh_tiles = build_tiles(pphh_probs, 64, 64);
   wcc_probs = build_wcc_problems(l.ncc, l.cc_rlen, l.cc_nph, l.cc_off, l.wcc_off);
   wcc_tiles = build_tiles(wcc_probs, 64, 64);
+  // 222_pp_hh intermediates: every W1 / W2 problem writes its whole array, so only the arrays
+  // no problem writes (channels without pp or without hh pairs), and E0 and the one-body
+  // part, are cleared before the products (src/commutators.f90:581-768 leaves them zero)
+  for (int w = 0; w < 2; ++w) {
+    std::vector<char> covered((size_t)l.nblocks * 6, 0);
+    for (const GemmProb& p : pphh_probs)
+      if (p.c_id == (w ? kOpW2 : kOpW1))
+        for (int k = 0; k < l.nblocks * 6; ++k)
+          if (l.goff[k] == p.c_off && p.M == l.gn1[k] && p.N == l.gn2[k] && p.M * (int64_t)p.N > 0) covered[k] = 1;
+    std::vector<int64_t>& runs = w ? zero_runs_w2 : zero_runs_w1;
+    runs.clear();
+    auto add = [&](int64_t a, int64_t n) {
+      if (n <= 0) return;
+      if (!runs.empty() && runs[runs.size() - 2] + runs.back() == a) runs.back() += n;
+      else { runs.push_back(a); runs.push_back(n); }
+    };
+    add(0, l.goff[0]);
+    for (int k = 0; k < l.nblocks * 6; ++k)
+      if (!covered[k]) add(l.goff[k], (int64_t)l.gn1[k] * l.gn2[k]);
+    // one CTA per run of at most 32768 elements (k_zero_runs)
+    std::vector<int64_t> split;
+    for (size_t r = 0; r < runs.size(); r += 2)
+      for (int64_t o = 0; o < runs[r + 1]; o += 32768) {
+        split.push_back(runs[r] + o);
+        split.push_back(std::min<int64_t>(32768, runs[r + 1] - o));
+      }
+    runs.swap(split);
+  }
   // Frobenius-norm segments: chunks of at most 64K elements inside one array
   std::vector<int64_t> s_start;
   std::vector<int> s_len;
@@ -161,6 +189,9 @@ imsrg_status Ctx::upload_tables() {
   pk.add(s_start, &seg_s); pk.add(s_len, &seg_l); pk.add(s_w, &seg_w);
   const int4* ut = nullptr;
   pk.add(upd_tiles, &ut);
+  const int64_t *zr1 = nullptr, *zr2 = nullptr;
+  pk.add(zero_runs_w1, &zr1);
+  pk.add(zero_runs_w2, &zr2);
 
   CK(cuda(cudaMalloc(&d_tables, pk.buf.size()), "cudaMalloc(tables)"));
   CK(cuda(cudaMemcpy(d_tables, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tables)"));
@@ -168,6 +199,8 @@ imsrg_status Ctx::upload_tables() {
   d_pphh_probs = pp_p; d_pphh_tiles = pp_t; d_wcc_probs = wc_p; d_wcc_tiles = wc_t;
   d_seg_start = seg_s; d_seg_len = seg_l; d_seg_w = seg_w;
   d_upd_tiles = ut;
+  d_zero_runs_w1 = zr1;
+  d_zero_runs_w2 = zr2;
   partial_capacity = std::max(nseg, l.nblocks) + 64;
   CK(cuda(cudaMalloc(&d_partial, sizeof(double) * partial_capacity), "cudaMalloc(partials)"));
   CK(cuda(cudaMalloc(&d_scalars, sizeof(double) * 64), "cudaMalloc(scalars)"));
@@ -213,6 +246,8 @@ Ctx::~Ctx() {
   for (auto e : prof_pool) cudaEventDestroy(e);
   if (ev_begin) cudaEventDestroy(ev_begin);
   if (ev_end) cudaEventDestroy(ev_end);
+  if (ev_ext_in) cudaEventDestroy(ev_ext_in);
+  if (ev_ext_out) cudaEventDestroy(ev_ext_out);
   if (stream) cudaStreamSynchronize(stream);
   for (double* p : op_pool) cudaFree(p);
   tc_release();
@@ -255,22 +290,21 @@ imsrg_status Ctx::c122(const double* Lp, int hL, const double* Rp, int hR, doubl
   return launched("k_comm122");
 }
 
-imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* w1, double* w2,
-                       bool upper_f32) {
-  const size_t sb = sizeof(double) * (size_t)L.slab;
-  CK(cuda(cudaMemsetAsync(w1, 0, sb, stream), "memset(w1)"));
-  CK(cuda(cudaMemsetAsync(w2, 0, sb, stream), "memset(w2)"));
-  if (precision != IMSRG_PREC_FP64) {
-    CK(tc_pphh(Lp, hL, Rp, hR, w1, w2));
-  } else if (!pphh_tiles.empty()) {
-    GemmOperands ops{};
-    ops.in[kOpL] = Lp; ops.in[kOpR] = Rp;
-    ops.out[kOpW1] = w1; ops.out[kOpW2] = w2;
-    ops.hL = hL; ops.hR = hR;
-    k_gemm_fp64<<<(int)pphh_tiles.size(), 256, 0, stream>>>(d_pphh_probs, d_pphh_tiles, ops);
-    CK(launched("k_gemm_fp64(pphh)"));
+// w1, w2 of 222_pp_hh: the parts no product writes are cleared
+imsrg_status Ctx::pphh_clear(double* w1, double* w2) {
+  if (!zero_runs_w1.empty()) {
+    k_zero_runs<<<(int)zero_runs_w1.size() / 2, 256, 0, stream>>>(w1, d_zero_runs_w1);
+    CK(launched("k_zero_runs"));
   }
-  mark(kPhasePphhGemm);
+  if (!zero_runs_w2.empty()) {
+    k_zero_runs<<<(int)zero_runs_w2.size() / 2, 256, 0, stream>>>(w2, d_zero_runs_w2);
+    CK(launched("k_zero_runs"));
+  }
+  return IMSRG_OK;
+}
+
+// RES += W1 - W2 - pm (W1 - W2)^T on the square arrays, RES += W1 - W2 on the others
+imsrg_status Ctx::pphh_accumulate(int hL, int hR, double* RES, const double* w1, const double* w2, bool upper_f32) {
   if (!upd_tiles.empty()) {
     if (upper_f32) {
       k_pphh_update_f<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (float)(hL * hR));
@@ -282,6 +316,23 @@ imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, doubl
   }
   mark(kPhasePphhUpdate);
   return IMSRG_OK;
+}
+
+imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* w1, double* w2,
+                       bool upper_f32) {
+  CK(pphh_clear(w1, w2));
+  if (precision != IMSRG_PREC_FP64) {
+    CK(tc_pphh(Lp, hL, Rp, hR, w1, w2));
+  } else if (!pphh_tiles.empty()) {
+    GemmOperands ops{};
+    ops.in[kOpL] = Lp; ops.in[kOpR] = Rp;
+    ops.out[kOpW1] = w1; ops.out[kOpW2] = w2;
+    ops.hL = hL; ops.hR = hR;
+    k_gemm_fp64<<<(int)pphh_tiles.size(), 256, 0, stream>>>(d_pphh_probs, d_pphh_tiles, ops);
+    CK(launched("k_gemm_fp64(pphh)"));
+  }
+  mark(kPhasePphhGemm);
+  return pphh_accumulate(hL, hR, RES, w1, w2, upper_f32);
 }
 
 imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2, bool f32) {
@@ -511,6 +562,8 @@ imsrg_status imsrg_ctx_create(const imsrg_basis* b, int32_t device, imsrg_ctx** 
   }
   imsrg_status s = c->cuda(cudaSetDevice(device), "cudaSetDevice");
   if (s == IMSRG_OK) s = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (s == IMSRG_OK) s = c->cuda(cudaEventCreateWithFlags(&c->ev_ext_in, cudaEventDisableTiming), "cudaEventCreate");
+  if (s == IMSRG_OK) s = c->cuda(cudaEventCreateWithFlags(&c->ev_ext_out, cudaEventDisableTiming), "cudaEventCreate");
   if (s == IMSRG_OK) s = c->upload_tables();
   if (s != IMSRG_OK) {
     delete c;
@@ -588,7 +641,7 @@ imsrg_status imsrg_cc_info(const imsrg_ctx* ctx, int32_t* rlen, int32_t* nph, in
 
 imsrg_status imsrg_set_precision(imsrg_ctx* ctx, int32_t mode) {
   CTX(ctx);
-  if (mode != IMSRG_PREC_FP64 && mode != IMSRG_PREC_BF16X3 && mode != IMSRG_PREC_BF16X6)
+  if (mode != IMSRG_PREC_FP64 && mode != IMSRG_PREC_BF16X3 && mode != IMSRG_PREC_BF16X6 && mode != IMSRG_PREC_TF32X3)
     return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "unknown precision mode");
   if (mode != IMSRG_PREC_FP64) CK(c->tc_prepare(mode));
   c->precision = mode;
@@ -599,6 +652,19 @@ imsrg_status imsrg_synchronize(imsrg_ctx* ctx) {
   CTX(ctx);
   CK(c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"));
   return c->tc_error();
+}
+
+imsrg_status imsrg_set_wait_limit(imsrg_ctx* ctx, int64_t nanoseconds) {
+  CTX(ctx);
+  if (nanoseconds < 0) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_set_wait_limit: negative limit");
+  c->tc_wait_ns = nanoseconds ? (unsigned long long)nanoseconds : 2000000000ull;
+  return IMSRG_OK;
+}
+
+imsrg_status imsrg_test_unarmed_stage(imsrg_ctx* ctx, int32_t enable) {
+  CTX(ctx);
+  c->tc_unarmed_next = enable ? 1 : 0;
+  return IMSRG_OK;
 }
 
 imsrg_status imsrg_launch_count(imsrg_ctx* ctx, int64_t* count) {
@@ -835,6 +901,32 @@ imsrg_status imsrg_mat_frob_norm(imsrg_ctx* ctx, const imsrg_op* op, double* out
   CK(c->read_scalars(1));
   *out = c->h_scalars[0];
   return IMSRG_OK;
+}
+
+imsrg_status imsrg_check_conversions(imsrg_ctx* ctx, const double* host_x, const float* host_y, int64_t n,
+                                     float* out_f32, double* out_f64) {
+  CTX(ctx);
+  if (n < 0 || (n > 0 && (!host_x || !host_y || !out_f32 || !out_f64))) return IMSRG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return IMSRG_OK;
+  void* d = nullptr;
+  const size_t bx = sizeof(double) * (size_t)n, by = sizeof(float) * (size_t)n;
+  CK(c->cuda(cudaMalloc(&d, bx + by + 2 * by + 2 * bx), "cudaMalloc(conversion check)"));
+  // [x: n doubles | out_f64: 2n doubles | y: n floats | out_f32: 2n floats]
+  double* dx = static_cast<double*>(d);
+  double* dd = dx + n;
+  float* dy = reinterpret_cast<float*>(dd + 2 * n);
+  float* df = dy + n;
+  imsrg_status st = c->cuda(cudaMemcpyAsync(dx, host_x, bx, cudaMemcpyHostToDevice, c->stream), "H2D x");
+  if (st == IMSRG_OK) st = c->cuda(cudaMemcpyAsync(dy, host_y, by, cudaMemcpyHostToDevice, c->stream), "H2D y");
+  if (st == IMSRG_OK) {
+    k_convert_check<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, c->stream>>>(dx, dy, n, df, dd);
+    st = c->launched("k_convert_check");
+  }
+  if (st == IMSRG_OK) st = c->cuda(cudaMemcpyAsync(out_f32, df, 2 * by, cudaMemcpyDeviceToHost, c->stream), "D2H f32");
+  if (st == IMSRG_OK) st = c->cuda(cudaMemcpyAsync(out_f64, dd, 2 * bx, cudaMemcpyDeviceToHost, c->stream), "D2H f64");
+  if (st == IMSRG_OK) st = c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  cudaFree(d);
+  return st;
 }
 
 imsrg_status imsrg_mbpt2(imsrg_ctx* ctx, const imsrg_op* H, double* out) {

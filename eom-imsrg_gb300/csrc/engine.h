@@ -39,6 +39,7 @@ enum Phase : int {
   kPhase221 = 8,
   kPhasePhGemm = 9,
   kPhaseRecouple = 10,
+  kPhaseMirror = 11,
 };
 
 struct Ctx {
@@ -67,12 +68,20 @@ struct Ctx {
   double* d_mono = nullptr;
   std::vector<int4> upd_tiles;
   const int4* d_upd_tiles = nullptr;
+  // (start, length) runs of w1 / w2 that no 222_pp_hh product writes
+  std::vector<int64_t> zero_runs_w1, zero_runs_w2;
+  const int64_t* d_zero_runs_w1 = nullptr;
+  const int64_t* d_zero_runs_w2 = nullptr;
   // commutator workspaces (w1, w2: sq_op shaped; LCC/RCC: CCX; WCC: rlen x rlen blocks)
   double *d_w1 = nullptr, *d_w2 = nullptr, *d_lcc = nullptr, *d_rcc = nullptr, *d_wcc = nullptr;
   // Magnus / BCH intermediates
   double *d_int1 = nullptr, *d_int2 = nullptr, *d_ad = nullptr;
   double* d_gen = nullptr;  // w2 generator workspace (3 slabs)
   imsrg::TcState* tc = nullptr;
+  // limit of every bounded device wait of the tensor-core kernels (imsrg_set_wait_limit), and the
+  // one-shot test switch that leaves one pipeline stage of the next GEMM launch unarmed
+  unsigned long long tc_wait_ns = 2000000000ull;
+  int tc_unarmed_next = 0;
   StepGraph* sg = nullptr;  // captured Magnus step (graph.cu)
   AdjointState* adj = nullptr;  // reverse-mode workspaces (adjoint.cu)
   HFState* hf = nullptr;        // Hartree-Fock tables (hf.cu)
@@ -84,6 +93,9 @@ struct Ctx {
   std::vector<std::pair<int, cudaEvent_t>> prof_marks;
   std::vector<cudaEvent_t> prof_pool;
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  // order a call on a caller's stream (imsrg_mat_frob_norm_noalloc) after the context's queued
+  // work, and the context's later work after it
+  cudaEvent_t ev_ext_in = nullptr, ev_ext_out = nullptr;
   void mark(int phase);
 
   ~Ctx();
@@ -101,6 +113,8 @@ struct Ctx {
   imsrg_status c122(const double* L, int hL, const double* R, int hR, double* RES, int hRES);
   imsrg_status pphh(const double* L, int hL, const double* R, int hR, double* RES, double* w1, double* w2,
                     bool upper_f32 = false);
+  imsrg_status pphh_clear(double* w1, double* w2);
+  imsrg_status pphh_accumulate(int hL, int hR, double* RES, const double* w1, const double* w2, bool upper_f32);
   imsrg_status c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2, bool f32);
   imsrg_status ensure_wcc();
   imsrg_status ph(const double* lcc, int hL, const double* rcc, int hR, double* RES, int hRES, double* wcc);
@@ -174,13 +188,16 @@ struct Ctx {
   imsrg_status tc_commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
   void tc_release();
   imsrg_status tc_gemm_on(const CUtensorMap& map, int64_t slice_rows, const imsrg::TcProb* probs,
-                          const imsrg::TcTile* tiles, int ntiles, imsrg::TcOut out, int hL, int hR);
+                          const imsrg::TcTile* tiles, int ntiles, imsrg::TcOut out, int hL, int hR, int wmax = 128);
   imsrg_status tc_encode_map(CUtensorMap* map, void* buf, int64_t total_rows);
   imsrg_status tc_split_on(const imsrg::TcSplitOp* ops, const imsrg::SplitChunk* chunks, int nchunks, const double* L,
-                           const double* R, __nv_bfloat16* buf, int64_t slice_elems);
-  int tc_slices() const;  // bf16 slices of the tensor-core path (0 before tc_prepare)
+                           const double* R, void* buf, int64_t slice_elems);
+  int tc_slices() const;      // operand slices of the tensor-core path (0 before tc_prepare)
+  int tc_tile_k() const;      // K values per 128-byte tile row of the operand slices (64 BF16, 32 TF32)
+  int tc_elem_bytes() const;  // bytes per operand value (2 BF16, 4 TF32)
+  int tc_kind() const;        // operand type of the slices (0 BF16, 1 TF32)
   imsrg_status tc_g122_partition(int tiny_cap, int small_cap);
-  imsrg_status tc_set_gemm_order(int order);
+  imsrg_status tc_set_tiles(int wmax, bool narrow, int order);
   imsrg_status tc_autotune(const double* L, int hL, const double* R, int hR, double* RES, imsrg_tune_info* info);
 };
 

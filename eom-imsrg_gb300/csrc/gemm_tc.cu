@@ -23,16 +23,17 @@
 #include "engine.h"
 #include "kernels.h"
 #include "pair_groups.h"
+#include "recouple.h"
+#include "split.cuh"
 #include "tc.h"
 
 namespace imsrg {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;
-constexpr int TILE_BYTES = BM * BK * 2;  // 16 KiB, identical for A and B tiles
+constexpr int BM = 128;
+constexpr int TILE_BYTES = BM * 128;  // 128 rows of 128 bytes: 16 KiB, one TMA box
 constexpr int NUM_THREADS = 320;  // TMA warp, MMA warp, 8 epilogue warps
-constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -60,16 +61,16 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait on a barrier phase.  Returns false (after recording `code`) on timeout or
-// when another role has already aborted.
+// Bounded wait on a barrier phase.  Returns false (after recording `code`) when it has waited
+// more than limit_ns, or when another role has already aborted.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err,
-                                          int code) {
+                                          int code, unsigned long long limit_ns) {
   if (mbar_test(bar, parity)) return true;
   const unsigned long long t0 = globaltimer();
   while (true) {
     if (mbar_test(bar, parity)) return true;
     if (*abort_flag) return false;
-    if (globaltimer() - t0 > kWaitLimitNs) {
+    if (globaltimer() - t0 > limit_ns) {
       atomicCAS(err, 0, code);
       *abort_flag = 1;
       return false;
@@ -96,18 +97,37 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
   return d;
 }
 
-// instruction descriptor, kind::f16: BF16 A/B, FP32 D, both K-major, M=128, N=128
-__host__ __device__ constexpr uint32_t umma_idesc(bool negate_a) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((negate_a ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
+// Operand element kinds of the tensor-core products: split-BF16 (tcgen05.mma kind::f16, A and
+// B both BF16) or split-TF32 (kind::tf32, FP32 words rounded to TF32).  A tile row is 128
+// bytes in both: 64 BF16 or 32 TF32 values of K, and one MMA consumes 32 bytes of it (K = 16
+// BF16 or 8 TF32), so the shared-memory descriptors step the same way.
+enum TcKind : int { kKindBF16 = 0, kKindTF32 = 1 };
+constexpr int kMmaPerRow = 4;  // MMAs per 128-byte tile row
+
+// instruction descriptor (kind::f16 / kind::tf32): FP32 D (bits 4-5 = 1), A and B types in
+// bits 7-9 / 10-12 (BF16 = 1, TF32 = 2), both K-major, N >> 3 at bit 17 (the tile's width n,
+// a multiple of 16 up to 256), M >> 4 at bit 24 (M = 128)
+template <int KIND>
+__host__ __device__ constexpr uint32_t umma_idesc(bool negate_a, int n) {
+  constexpr uint32_t t = KIND == kKindTF32 ? 2u : 1u;
+  return (1u << 4) | (t << 7) | (t << 10) | ((negate_a ? 1u : 0u) << 13) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(BM >> 4) << 24);
 }
 
+template <int KIND>
 __device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          tmem_d),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
-      : "memory");
+  if constexpr (KIND == kKindTF32)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -151,26 +171,36 @@ struct SliceProducts<3> {
   __device__ static int b(int p) { return (p == 2) ? 2 : (p == 1 || p == 4) ? 1 : 0; }
 };
 
-template <int S>
-constexpr int stages_for() { return S == 2 ? 3 : 2; }
-
-template <int S>
+// A stage holds S A boxes (128 rows) and S B tiles of WMAX rows (WMAX / 128 boxes each).
+template <int S, int WMAX>
+constexpr int stage_bytes() { return S * TILE_BYTES * (1 + WMAX / 128); }
+template <int S, int WMAX>
+constexpr int stages_for() {
+  return (200 * 1024) / stage_bytes<S, WMAX>() > 4 ? 4 : (200 * 1024) / stage_bytes<S, WMAX>();
+}
+template <int S, int WMAX>
 constexpr size_t smem_bytes() {
-  return (size_t)stages_for<S>() * 2 * S * TILE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+  return (size_t)stages_for<S, WMAX>() * stage_bytes<S, WMAX>() + 1024 /*align*/ + 256 /*barriers*/;
 }
 
 }  // namespace
 
-template <int S>
+// WMAX: the widest tile (128 or 256 columns); each tile carries its own width (TcTile::w), which
+// goes into the instruction descriptor, so one launch mixes wide and narrow tiles.
+template <int S, int KIND, int WMAX>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmap, int64_t slice_rows, const TcProb* __restrict__ probs,
-              const TcTile* __restrict__ tiles, int ntiles, TcOut out, int hL, int hR, int* err) {
-  constexpr int ST = stages_for<S>();
+              const TcTile* __restrict__ tiles, int ntiles, TcOut out, int hL, int hR, int* err,
+              unsigned long long wait_ns, int unarmed_it) {
+  constexpr int ST = stages_for<S, WMAX>();
+  static_assert(ST >= 2, "at least two pipeline stages");
   constexpr int NP = SliceProducts<S>::n;
+  constexpr int BBYTES = TILE_BYTES * (WMAX / 128);  // one B slice of a stage
+  constexpr int SBYTES = stage_bytes<S, WMAX>();
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* ring = smem;  // stage s: A slices [S] then B slices [S], 16 KiB each
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)ST * 2 * S * TILE_BYTES);
+  uint8_t* ring = smem;  // stage s: A slices [S] (16 KiB each), then B slices [S] (BBYTES each)
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)ST * SBYTES);
   uint64_t* empty = full + ST;
   uint64_t* tfull = empty + ST;
   uint64_t* tempty = tfull + 2;
@@ -192,9 +222,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     *consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {  // 2 accumulators x 128 FP32 columns
+  if (warp == 1) {  // 2 accumulators x WMAX FP32 columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(2 * BN)
+                 "r"(2 * WMAX)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -211,19 +241,25 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         const TcTile tile = tiles[t];
         const TcProb& P = probs[tile.prob];
+        const int nbox = (tile.w + 127) >> 7;  // B boxes of this tile (1, or 2 for tiles wider than 128)
         for (int term = 0; term < P.nterm && ok; ++term) {
           const int abase = P.t[term].a_tile + (tile.m0 / BM) * P.nkb;
-          const int bbase = P.t[term].b_tile + (tile.n0 / BN) * P.nkb;
+          const int bbase = P.t[term].b_tile + (tile.n0 >> 7) * P.nkb;
           for (int kb = 0; kb < P.nkb; ++kb, ++it) {
             const int s = it % ST;
-            if (!mbar_wait(&empty[s], ((it / ST) & 1) ^ 1, abort_flag, err, 1)) { ok = false; break; }
-            mbar_expect_tx(&full[s], (uint32_t)(2 * S * TILE_BYTES));
-            uint8_t* stage = ring + (size_t)s * 2 * S * TILE_BYTES;
+            if (!mbar_wait(&empty[s], ((it / ST) & 1) ^ 1, abort_flag, err, 1, wait_ns)) { ok = false; break; }
+            // test switch (imsrg_test_unarmed_stage): CTA 0 leaves this stage unarmed -- no copy
+            // is issued for it and nothing arrives on its barrier -- so the MMA warp's bounded
+            // wait on it runs out
+            if (it == unarmed_it && blockIdx.x == 0) continue;
+            mbar_expect_tx(&full[s], (uint32_t)(S * (1 + nbox) * TILE_BYTES));
+            uint8_t* stage = ring + (size_t)s * SBYTES;
             for (int sl = 0; sl < S; ++sl) {
               tma_load_2d(smem_u32(stage + (size_t)sl * TILE_BYTES), &tmap, 0,
                           (int)(sl * slice_rows + (int64_t)(abase + kb) * BM), &full[s]);
-              tma_load_2d(smem_u32(stage + (size_t)(S + sl) * TILE_BYTES), &tmap, 0,
-                          (int)(sl * slice_rows + (int64_t)(bbase + kb) * BN), &full[s]);
+              for (int bx = 0; bx < nbox; ++bx)
+                tma_load_2d(smem_u32(stage + (size_t)S * TILE_BYTES + (size_t)sl * BBYTES + (size_t)bx * TILE_BYTES),
+                            &tmap, 0, (int)(sl * slice_rows + (int64_t)(bbase + bx * P.nkb + kb) * BM), &full[s]);
             }
           }
         }
@@ -233,7 +269,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const unsigned long long t0 = globaltimer();
         for (int j = *consumed; j < it; ++j) {
           while (!mbar_test(&full[j % ST], (j / ST) & 1)) {
-            if (globaltimer() - t0 > kWaitLimitNs) break;
+            if (globaltimer() - t0 > wait_ns) break;
           }
         }
       }
@@ -247,24 +283,24 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const TcTile tile = tiles[t];
         const TcProb& P = probs[tile.prob];
         const int acc = local & 1;
-        if (!mbar_wait(&tempty[acc], ((local >> 1) & 1) ^ 1, abort_flag, err, 2)) { ok = false; break; }
+        if (!mbar_wait(&tempty[acc], ((local >> 1) & 1) ^ 1, abort_flag, err, 2, wait_ns)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t d_tmem = tmem_base + (uint32_t)(acc * BN);
+        const uint32_t d_tmem = tmem_base + (uint32_t)(acc * WMAX);
         bool first = true;
         for (int term = 0; term < P.nterm && ok; ++term) {
-          const uint32_t idesc = umma_idesc(term_negated(P.t[term].sign, hL, hR));
+          const uint32_t idesc = umma_idesc<KIND>(term_negated(P.t[term].sign, hL, hR), tile.w);
           for (int kb = 0; kb < P.nkb; ++kb, ++it) {
             const int s = it % ST;
-            if (!mbar_wait(&full[s], (it / ST) & 1, abort_flag, err, 3)) { ok = false; break; }
+            if (!mbar_wait(&full[s], (it / ST) & 1, abort_flag, err, 3, wait_ns)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t stage = smem_u32(ring + (size_t)s * 2 * S * TILE_BYTES);
+            const uint32_t stage = smem_u32(ring + (size_t)s * SBYTES);
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
               const uint32_t a0 = stage + (uint32_t)(SliceProducts<S>::a(p) * TILE_BYTES);
-              const uint32_t b0 = stage + (uint32_t)((S + SliceProducts<S>::b(p)) * TILE_BYTES);
+              const uint32_t b0 = stage + (uint32_t)(S * TILE_BYTES + SliceProducts<S>::b(p) * BBYTES);
 #pragma unroll
-              for (int ks = 0; ks < BK / 16; ++ks) {
-                umma(d_tmem, umma_desc(a0 + ks * 32), umma_desc(b0 + ks * 32), idesc, first ? 0u : 1u);
+              for (int ks = 0; ks < kMmaPerRow; ++ks) {
+                umma<KIND>(d_tmem, umma_desc(a0 + ks * 32), umma_desc(b0 + ks * 32), idesc, first ? 0u : 1u);
                 first = false;
               }
             }
@@ -278,18 +314,18 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   } else {
     // ------------------------------------------------------------ epilogue (warps 2..9)
     const int quad = warp & 3;          // TMEM lanes 32*quad .. 32*quad+31
-    const int half = (warp - 2) >> 2;   // accumulator columns 64*half .. 64*half+63
+    const int half = (warp - 2) >> 2;   // accumulator columns 32*(2c+half) .. +31, c = 0, 1, ...
     int local = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++local) {
       const TcTile tile = tiles[t];
       const TcProb& P = probs[tile.prob];
       const int acc = local & 1;
-      if (!mbar_wait(&tfull[acc], (local >> 1) & 1, abort_flag, err, 4)) break;
+      if (!mbar_wait(&tfull[acc], (local >> 1) & 1, abort_flag, err, 4, wait_ns)) break;
       tc_fence_after();
       const int m = tile.m0 + quad * 32 + lane;
-      for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
+      for (int c0 = half * 32; c0 < tile.w; c0 += 64) {
         uint32_t r[32];
-        tmem_ld32(tmem_base + (uint32_t)(acc * BN + c0) + ((uint32_t)(quad * 32) << 16), r);
+        tmem_ld32(tmem_base + (uint32_t)(acc * WMAX + c0) + ((uint32_t)(quad * 32) << 16), r);
         if (m < P.M) {
           if (P.out_f32) {
             float* C = (P.out_f32 == 1 ? out.f32 : out.f32b) + P.c_off;
@@ -319,45 +355,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   tc_fence_after();
   __syncwarp();
   if (warp == 1)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(2 * BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(2 * WMAX) : "memory");
 }
 
 // ---------------------------------------------------------------- operand split
-// FP64 columns of the stored arrays -> S bf16 slices, K-major 128x64 tiles.
-template <int S>
-__global__ void k_split_cols(const TcSplitOp* __restrict__ ops, const int64_t* __restrict__ prefix, int nops,
-                             const double* __restrict__ L, const double* __restrict__ R, __nv_bfloat16* __restrict__ buf,
-                             int64_t slice_elems) {
-  const int64_t total = prefix[nops];
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nops;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (prefix[mid] <= e) lo = mid; else hi = mid;
-    }
-    while (prefix[lo + 1] <= e) ++lo;
-    const TcSplitOp& o = ops[lo];
-    const int64_t loc = e - prefix[lo];
-    const int r = (int)(loc / o.K), k = (int)(loc - (int64_t)r * o.K);
-    const float x = f64_to_f32((o.src == 0 ? L : R)[o.src_off + k + (int64_t)r * o.K]);
-    const int64_t dst = ((int64_t)(o.tile_base + (r / BM) * o.nkb + k / BK) * BM + (r % BM)) * BK + (k % BK);
-    float rem = x;
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-      const __nv_bfloat16 h = __float2bfloat16_rn(rem);
-      buf[s * slice_elems + dst] = h;
-      rem -= __bfloat162float(h);
-    }
-  }
-}
-
 // Chunked split: one block per run of rows of one operand, each thread converts 8
-// consecutive k of one row and writes 16-byte bf16 vectors into every slice.
-template <int S>
+// consecutive k of one row and writes them as one vector (16 bytes of BF16, 32 of TF32) into
+// every slice.  T: the operand type (split.cuh).
+template <int S, typename T>
 __global__ void __launch_bounds__(256) k_split_chunks(const TcSplitOp* __restrict__ ops,
                                                       const SplitChunk* __restrict__ chunks,
                                                       const double* __restrict__ L, const double* __restrict__ R,
-                                                      __nv_bfloat16* __restrict__ buf, int64_t slice_elems) {
+                                                      void* __restrict__ bufv, int64_t slice_elems) {
+  T* buf = static_cast<T*>(bufv);
   const SplitChunk ch = chunks[blockIdx.x];
   const TcSplitOp o = ops[ch.op];
   const double* src = (o.src == 0 ? L : R) + o.src_off;
@@ -374,16 +384,15 @@ __global__ void __launch_bounds__(256) k_split_chunks(const TcSplitOp* __restric
       x[u] = (k0 + u < o.K)
                  ? f64_to_f32(o.trans ? src[r + (int64_t)(k0 + u) * o.ld] : src[k0 + u + (int64_t)r * o.K])
                  : 0.0f;
-    const int64_t dst = ((int64_t)(o.tile_base + (r / BM) * o.nkb + k0 / BK) * BM + (r % BM)) * BK + (k0 % BK);
+    const int64_t dst = split_offset<T>(o.tile_base, o.nkb, r, k0);
 #pragma unroll
     for (int sl = 0; sl < S; ++sl) {
-      __align__(16) __nv_bfloat16 h[8];
+      __align__(32) T h[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        h[u] = __float2bfloat16_rn(x[u]);
-        x[u] -= __bfloat162float(h[u]);
-      }
-      *reinterpret_cast<uint4*>(buf + sl * slice_elems + dst) = *reinterpret_cast<const uint4*>(h);
+      for (int u = 0; u < 8; ++u) h[u] = SplitElem<T>::take(x[u]);
+      uint4* d = reinterpret_cast<uint4*>(buf + sl * slice_elems + dst);
+#pragma unroll
+      for (int v = 0; v < (int)(8 * sizeof(T) / 16); ++v) d[v] = reinterpret_cast<const uint4*>(h)[v];
     }
   }
 }
@@ -456,9 +465,13 @@ using namespace imsrg;
 
 namespace imsrg {
 
+cudaError_t tc_gemm_smem_attrs(int S, int kind);
+
 struct TcState {
   int S = 0;
-  __nv_bfloat16* buf = nullptr;
+  int kind = kKindBF16;  // operand type of the slices (TcKind)
+  int tile_k = 64;       // K values per 128-byte tile row: 64 BF16, 32 TF32
+  void* buf = nullptr;
   int64_t slice_rows = 0, slice_elems = 0;
   int total_tiles = 0;
   CUtensorMap tmap;
@@ -469,7 +482,7 @@ struct TcState {
   std::vector<TcTile> pphh_tiles;
   std::vector<GemmProb> small_probs;
   std::vector<GemmTile> small_tiles;
-  // particle-hole: Z(q) = hL LCC RCC^T - hR RCC LCC^T
+  // particle-hole: X(q) = phi phi Z - pm Zs with Z(q) = hL LCC RCC^T - hR RCC LCC^T (recouple.cu)
   std::vector<int> cc_tile_L, cc_tile_R, cc_tile_Ls, cc_tile_Rs, cc_nkb, swap_row;
   std::vector<TcProb> z_probs;
   std::vector<TcTile> z_tiles;
@@ -488,12 +501,22 @@ struct TcState {
   const int* d_cc_tile_Ls = nullptr;
   const int* d_cc_tile_Rs = nullptr;
   const int* d_swap_row = nullptr;
-  float* zbuf = nullptr;
-  float* ybuf = nullptr;
+  float* zbuf = nullptr;  // X, the recoupling input (FP32, wcc layout)
   int* d_err = nullptr;
-  // orbit quadruples (i<=j, k<=l) of the particle-hole recoupling, j fastest
+  // orbit quadruples (i<=j, k<=l) of the particle-hole recoupling, j fastest, and the
+  // recoupling's groups / tasks / staged 6j blocks
   std::vector<uint64_t> quads;
   const uint64_t* d_quads = nullptr;
+  RecouplePlan rc;
+  std::vector<int> xcol;              // X column offset of every pair and J' (recouple.cu)
+  const int* d_xcol = nullptr;
+  int recouple_kind = 0;              // 0: by (i, k, l) groups (k_recouple_g), 1: per quadruple (k_recouple_q)
+  int recouple_minb = 6;              // launch-bounds variant of k_recouple_q
+  int recouple_ctas = 0;              // CTAs of k_recouple_q
+  const RcTask* d_rc_tasks = nullptr;
+  const RcGroup* d_rc_groups = nullptr;
+  const RcTriple* d_rc_triples = nullptr;
+  const float* d_rc_table = nullptr;
   std::vector<SplitChunk> chunks;
   const SplitChunk* d_chunks = nullptr;
   // commutator_122 by pair groups: sub-blocks of at most g122_small elements go one per warp,
@@ -507,11 +530,17 @@ struct TcState {
   int g122_ntiny = 0, g122_nwarp = 0, g122_ncta = 0;
   PairGroupsDev g122_t{}, g122_w{}, g122_c{};
   int g122_tiny_cap = 64, g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
-  // tuned launch parameters (imsrg_autotune): CTAs of the recoupling kernel, GEMM tile order
-  int recouple_ctas = 152 * 16;
-  int recouple_minb = 4;  // launch-bounds variant of k_recouple_y
+  // tuned launch parameters (imsrg_autotune): GEMM tile order and shape
   int gemm_order = 0;  // 0: longest K first, 1: problem order
-  std::vector<TcTile> pphh_tiles_lpt, z_tiles_lpt;
+  int wmax = 128;      // widest output tile of the persistent GEMM (128 or 256 columns)
+  bool narrow = true;  // last column tile of a problem only as wide as needed (multiple of 16)
+  // the merged list of one commutator: the K = npp ladder problems, then the X problems, in one
+  // persistent launch (tile lists in device memory sized for the largest tile count)
+  std::vector<TcProb> all_probs;
+  std::vector<TcTile> all_tiles;
+  const TcProb* d_all_probs = nullptr;
+  TcTile* d_tile_mem = nullptr;  // [pphh tiles | X tiles | merged tiles]
+  size_t tile_cap_pphh = 0, tile_cap_z = 0, tile_cap_all = 0;
   std::vector<int> g_start, g_n, g_orb, g_b1, g_b2, g_blk_off;
   float* g122_fb = nullptr;  // f(x, y) of L and R on every (l, j, tz) block
   int num_sms = 148;
@@ -527,11 +556,14 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
 
 int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
-std::vector<TcTile> make_tiles(const std::vector<TcProb>& probs) {
+// the output tiles of a problem list: 128 rows by up to wmax columns (narrow: the last
+// column tile only as wide as its columns need, in steps of 16), longest K first
+std::vector<TcTile> make_tiles(const std::vector<TcProb>& probs, int wmax, bool narrow) {
   std::vector<TcTile> t;
   for (int p = 0; p < (int)probs.size(); ++p)
     for (int m0 = 0; m0 < probs[p].M; m0 += BM)
-      for (int n0 = 0; n0 < probs[p].N; n0 += BN) t.push_back(TcTile{p, m0, n0, 0});
+      for (int n0 = 0; n0 < probs[p].N; n0 += wmax)
+        t.push_back(TcTile{p, m0, n0, tc_tile_width(probs[p].N, n0, wmax, narrow)});
   std::stable_sort(t.begin(), t.end(), [&](const TcTile& a, const TcTile& b) {
     return probs[a.prob].nkb * probs[a.prob].nterm > probs[b.prob].nkb * probs[b.prob].nterm;
   });
@@ -557,23 +589,27 @@ void Ctx::tc_release() {
   if (tc->buf) cudaFree(tc->buf);
   if (tc->d_mem) cudaFree(tc->d_mem);
   if (tc->zbuf) cudaFree(tc->zbuf);
-  if (tc->ybuf) cudaFree(tc->ybuf);
   if (tc->d_err) cudaFree(tc->d_err);
   if (tc->g122_fb) cudaFree(tc->g122_fb);
   if (tc->d_g122_tasks) cudaFree(tc->d_g122_tasks);
+  if (tc->d_tile_mem) cudaFree(tc->d_tile_mem);
   delete tc;
   tc = nullptr;
 }
 
 imsrg_status Ctx::tc_prepare(int mode) {
   const int S = (mode == IMSRG_PREC_BF16X6) ? 3 : 2;
-  if (tc && tc->S == S) return IMSRG_OK;
+  const int kind = (mode == IMSRG_PREC_TF32X3) ? kKindTF32 : kKindBF16;
+  if (tc && tc->S == S && tc->kind == kind) return IMSRG_OK;
   tc_release();
   int cc_major = 0;
   cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, device);
   if (cc_major < 10) return fail(IMSRG_ERR_UNSUPPORTED, "tensor-core path needs a Blackwell (sm_10x) GPU");
   tc = new TcState();
   tc->S = S;
+  tc->kind = kind;
+  tc->tile_k = kind == kKindTF32 ? 32 : 64;
+  const int BK = tc->tile_k;
   cudaDeviceGetAttribute(&tc->num_sms, cudaDevAttrMultiProcessorCount, device);
   const Layout& l = L;
   int tiles = 0;
@@ -640,15 +676,17 @@ imsrg_status Ctx::tc_prepare(int mode) {
       prob(nb, nh, 5, nb, TcTermDesc{T(q, 0, 1), T(q, 1, 2), hl}, 2, TcTermDesc{T(q, 1, 1), T(q, 0, 2), ng | hr});
     }
   }
-  tc->pphh_tiles = make_tiles(tc->pphh_probs);
   // K = nhh products (all W2 arrays), from the FP64 problem list
   for (const GemmProb& p : pphh_probs)
     if (p.c_id == kOpW2) tc->small_probs.push_back(p);
   tc->small_tiles = build_tiles(tc->small_probs, 64, 64);
 
-  // ---- particle-hole: LCC / RCC rows r, K = nph, each also with its rows swapped
-  //      (row r(a,b) holding row r(b,a)); Z(q) = hL LCC RCC^T - hR RCC LCC^T and its
-  //      row-swapped copy Y(q) = hL LCCs RCC^T - hR RCCs LCC^T
+  // ---- particle-hole: LCC / RCC rows r, K = nph, written by the Pandya pass with the row
+  //      sign phi(r), and the same rows unsigned at the swapped position (row r(a,b) holding
+  //      row r(b,a)): phiL, phiR, Ls, Rs.  One FP32 product per channel,
+  //        X = hL phiL phiR^T - hR phiR phiL^T - hR Ls Rs^T + hL Rs Ls^T
+  //          = phi phi Z - pm Z(s, s),   Z = hL LCC RCC^T - hR RCC LCC^T, pm = hL hR,
+  //      is the input of the recoupling (recouple.cu).
   tc->cc_tile_L.assign(l.ncc, 0);
   tc->cc_tile_R.assign(l.ncc, 0);
   tc->cc_tile_Ls.assign(l.ncc, 0);
@@ -672,19 +710,16 @@ imsrg_status Ctx::tc_prepare(int mode) {
     tc->cc_tile_R[q] = tiles; tiles += blk;
     tc->cc_tile_Ls[q] = tiles; tiles += blk;
     tc->cc_tile_Rs[q] = tiles; tiles += blk;
-    for (int which = 0; which < 2; ++which) {
-      TcProb p{};
-      p.M = r; p.N = r; p.nkb = nkb; p.nterm = 2;
-      const int aL = which ? tc->cc_tile_Ls[q] : tc->cc_tile_L[q];
-      const int aR = which ? tc->cc_tile_Rs[q] : tc->cc_tile_R[q];
-      p.t[0] = TcTermDesc{aL, tc->cc_tile_R[q], hl};
-      p.t[1] = TcTermDesc{aR, tc->cc_tile_L[q], ng | hr};
-      p.out_f32 = 1 + which;  // 1 -> Z, 2 -> Y
-      p.c_id = 0; p.c_off = l.wcc_off[q]; p.ldc = r;
-      tc->z_probs.push_back(p);
-    }
+    TcProb p{};
+    p.M = r; p.N = r; p.nkb = nkb; p.nterm = 4;
+    p.t[0] = TcTermDesc{tc->cc_tile_L[q], tc->cc_tile_R[q], hl};
+    p.t[1] = TcTermDesc{tc->cc_tile_R[q], tc->cc_tile_L[q], ng | hr};
+    p.t[2] = TcTermDesc{tc->cc_tile_Ls[q], tc->cc_tile_Rs[q], ng | hr};
+    p.t[3] = TcTermDesc{tc->cc_tile_Rs[q], tc->cc_tile_Ls[q], hl};
+    p.out_f32 = 1;
+    p.c_id = 0; p.c_off = l.wcc_off[q]; p.ldc = r;
+    tc->z_probs.push_back(p);
   }
-  tc->z_tiles = make_tiles(tc->z_probs);
   tc->total_tiles = tiles;
   if (l.JM + 1 > 26) return fail(IMSRG_ERR_UNSUPPORTED, "mixed recoupling supports 2j <= 25 (eMax <= 12)");
   // ---- commutator_122 tasks: the group pairs G1 <= G2 of each channel
@@ -735,13 +770,15 @@ imsrg_status Ctx::tc_prepare(int mode) {
   tc->slice_elems = tc->slice_rows * BK;
   if ((int64_t)S * tc->slice_rows >= (int64_t)1 << 31) return fail(IMSRG_ERR_UNSUPPORTED, "operand buffer too large for 32-bit TMA rows");
 
-  const size_t bytes = sizeof(__nv_bfloat16) * (size_t)S * tc->slice_elems;
+  const size_t bytes = (size_t)tc_elem_bytes() * (size_t)S * tc->slice_elems;
   CK_TC(cuda(cudaMalloc(&tc->buf, std::max<size_t>(bytes, 256)), "cudaMalloc(tc operands)"));
   CK_TC(cuda(cudaMemset(tc->buf, 0, std::max<size_t>(bytes, 256)), "memset(tc operands)"));
-  CK_TC(cuda(cudaMalloc(&tc->zbuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(Z)"));
-  CK_TC(cuda(cudaMemset(tc->zbuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(Z)"));
-  CK_TC(cuda(cudaMalloc(&tc->ybuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(Y)"));
-  CK_TC(cuda(cudaMemset(tc->ybuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(Y)"));
+  {
+    const std::string e = build_recouple_plan(l, tc->quads, tc->rc);
+    if (!e.empty()) return fail(IMSRG_ERR_UNSUPPORTED, e);
+  }
+  CK_TC(cuda(cudaMalloc(&tc->zbuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(X)"));
+  CK_TC(cuda(cudaMemset(tc->zbuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(X)"));
   CK_TC(cuda(cudaMalloc(&tc->d_err, sizeof(int)), "cudaMalloc(err)"));
   CK_TC(cuda(cudaMalloc(&tc->g122_fb, sizeof(float) * 2 * std::max(tc->g122_nblk2, 1)), "cudaMalloc(122 blocks)"));
   CK_TC(cuda(cudaMemset(tc->d_err, 0, sizeof(int)), "memset(err)"));
@@ -749,11 +786,12 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->split_ops, &tc->d_split_ops);
   pk.add(tc->split_prefix, &tc->d_split_prefix);
   pk.add(tc->pphh_probs, &tc->d_pphh_probs);
-  pk.add(tc->pphh_tiles, &tc->d_pphh_tiles);
   pk.add(tc->small_probs, &tc->d_small_probs);
   pk.add(tc->small_tiles, &tc->d_small_tiles);
   pk.add(tc->z_probs, &tc->d_z_probs);
-  pk.add(tc->z_tiles, &tc->d_z_tiles);
+  tc->all_probs = tc->pphh_probs;
+  for (TcProb p : tc->z_probs) tc->all_probs.push_back(p);
+  pk.add(tc->all_probs, &tc->d_all_probs);
   pk.add(tc->cc_tile_L, &tc->d_cc_tile_L);
   pk.add(tc->cc_tile_R, &tc->d_cc_tile_R);
   pk.add(tc->cc_nkb, &tc->d_cc_nkb);
@@ -761,6 +799,12 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->cc_tile_Rs, &tc->d_cc_tile_Rs);
   pk.add(tc->swap_row, &tc->d_swap_row);
   pk.add(tc->quads, &tc->d_quads);
+  tc->xcol = build_xcol(l);
+  pk.add(tc->xcol, &tc->d_xcol);
+  pk.add(tc->rc.tasks, &tc->d_rc_tasks);
+  pk.add(tc->rc.groups, &tc->d_rc_groups);
+  pk.add(tc->rc.triples, &tc->d_rc_triples);
+  pk.add(tc->rc.table, &tc->d_rc_table);
   pk.add(tc->chunks, &tc->d_chunks);
   pk.add(tc->g_start, &tc->g122_w.spb_start);
   pk.add(tc->g_n, &tc->g122_w.spb_n);
@@ -776,50 +820,94 @@ imsrg_status Ctx::tc_prepare(int mode) {
              "cudaMalloc(122 tasks)"));
   tc->g122_t = tc->g122_c = tc->g122_w;
   CK_TC(tc_g122_partition(tc->g122_tiny_cap, tc->g122_small));
-  tc->recouple_ctas = tc->num_sms * 16;
-  tc->pphh_tiles_lpt = tc->pphh_tiles;
-  tc->z_tiles_lpt = tc->z_tiles;
+  tc->recouple_ctas = tc->num_sms * 32;
+  // tile lists: the most tiles come with 128-wide tiles
+  tc->tile_cap_pphh = make_tiles(tc->pphh_probs, 128, false).size();
+  tc->tile_cap_z = make_tiles(tc->z_probs, 128, false).size();
+  tc->tile_cap_all = tc->tile_cap_pphh + tc->tile_cap_z;
+  CK_TC(cuda(cudaMalloc(&tc->d_tile_mem, sizeof(TcTile) * std::max<size_t>(tc->tile_cap_all * 2, 1)),
+             "cudaMalloc(GEMM tiles)"));
+  tc->d_pphh_tiles = tc->d_tile_mem;
+  tc->d_z_tiles = tc->d_tile_mem + tc->tile_cap_pphh;
+  CK_TC(tc_set_tiles(tc->wmax, tc->narrow, tc->gemm_order));
 
   // tensor map over the whole operand buffer: rows of 64 bf16 (128 bytes), box 64 x 128
   CK_TC(tc_encode_map(&tc->tmap, tc->buf, (int64_t)S * tc->slice_rows));
-  const size_t sm = S == 2 ? smem_bytes<2>() : smem_bytes<3>();
-  if (S == 2)
-    CK_TC(cuda(cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem attr"));
-  else
-    CK_TC(cuda(cudaFuncSetAttribute(k_tc_gemm<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem attr"));
+  CK_TC(cuda(recouple_g_smem_attr(tc->rc.smem_bytes), "smem attr (recoupling)"));
+  CK_TC(cuda(tc_gemm_smem_attrs(S, kind), "smem attr (tensor-core GEMM)"));
   return IMSRG_OK;
 }
 
 imsrg_status Ctx::tc_gemm(const TcProb* probs, const TcTile* tiles, int ntiles, TcOut out, int hL, int hR) {
-  return tc_gemm_on(tc->tmap, tc->slice_rows, probs, tiles, ntiles, out, hL, hR);
+  return tc_gemm_on(tc->tmap, tc->slice_rows, probs, tiles, ntiles, out, hL, hR, tc->wmax);
 }
 
 int Ctx::tc_slices() const { return tc ? tc->S : 0; }
+int Ctx::tc_tile_k() const { return tc ? tc->tile_k : 64; }
+int Ctx::tc_elem_bytes() const { return (tc && tc->kind == kKindTF32) ? 4 : 2; }
+int Ctx::tc_kind() const { return tc ? tc->kind : kKindBF16; }
 
-// the persistent split-BF16 GEMM over any operand buffer of this context's slice count
+namespace {
+template <int S, int KIND, int WMAX>
+void launch_tc_gemm(int grid, cudaStream_t st, const CUtensorMap& map, int64_t slice_rows, const TcProb* probs,
+                    const TcTile* tiles, int ntiles, TcOut out, int hL, int hR, int* err, unsigned long long wait_ns,
+                    int unarmed) {
+  k_tc_gemm<S, KIND, WMAX><<<grid, NUM_THREADS, smem_bytes<S, WMAX>(), st>>>(map, slice_rows, probs, tiles, ntiles,
+                                                                           out, hL, hR, err, wait_ns, unarmed);
+}
+template <int S, int KIND, int WMAX>
+cudaError_t set_gemm_smem() {
+  return cudaFuncSetAttribute(k_tc_gemm<S, KIND, WMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem_bytes<S, WMAX>());
+}
+}  // namespace
+
+// the kernel instances of one slice count and operand type: widest tile 128, and 256 where two
+// stages of S x (16 + 32) KiB fit (S = 2)
+cudaError_t imsrg::tc_gemm_smem_attrs(int S, int kind) {
+  cudaError_t e;
+  if (kind == kKindTF32) {
+    if ((e = set_gemm_smem<2, kKindTF32, 128>()) != cudaSuccess) return e;
+    return set_gemm_smem<2, kKindTF32, 256>();
+  }
+  if (S == 3) return set_gemm_smem<3, kKindBF16, 128>();
+  if ((e = set_gemm_smem<2, kKindBF16, 128>()) != cudaSuccess) return e;
+  return set_gemm_smem<2, kKindBF16, 256>();
+}
+
+// the persistent tensor-core GEMM over any operand buffer of this context's slice count and
+// operand type; the tile list must have been built for the widest tile wmax
 imsrg_status Ctx::tc_gemm_on(const CUtensorMap& map, int64_t slice_rows, const TcProb* probs, const TcTile* tiles,
-                             int ntiles, TcOut out, int hL, int hR) {
+                             int ntiles, TcOut out, int hL, int hR, int wmax) {
   if (ntiles == 0) return IMSRG_OK;
+  if (wmax != 128 && !(wmax == 256 && tc->S == 2)) return fail(IMSRG_ERR_INVALID_ARGUMENT, "unsupported tile width");
   const int grid = std::min(ntiles, tc->num_sms);
-  if (tc->S == 2)
-    k_tc_gemm<2><<<grid, NUM_THREADS, smem_bytes<2>(), stream>>>(map, slice_rows, probs, tiles, ntiles, out, hL, hR,
-                                                                  tc->d_err);
+  const int unarmed = tc_unarmed_next ? 0 : -1;  // one-shot test switch
+  tc_unarmed_next = 0;
+  auto go = [&](auto launcher) {
+    launcher(grid, stream, map, slice_rows, probs, tiles, ntiles, out, hL, hR, tc->d_err, tc_wait_ns, unarmed);
+  };
+  if (tc->kind == kKindTF32)
+    wmax == 256 ? go(launch_tc_gemm<2, kKindTF32, 256>) : go(launch_tc_gemm<2, kKindTF32, 128>);
+  else if (tc->S == 2)
+    wmax == 256 ? go(launch_tc_gemm<2, kKindBF16, 256>) : go(launch_tc_gemm<2, kKindBF16, 128>);
   else
-    k_tc_gemm<3><<<grid, NUM_THREADS, smem_bytes<3>(), stream>>>(map, slice_rows, probs, tiles, ntiles, out, hL, hR,
-                                                                  tc->d_err);
+    go(launch_tc_gemm<3, kKindBF16, 128>);
   return launched("k_tc_gemm");
 }
 
-// rows of 64 bf16 (128 bytes) over total_rows rows, box 64 x 128, 128-byte swizzle
+// rows of 128 bytes over total_rows rows, box 128 bytes x 128 rows, 128-byte swizzle.  The map
+// moves bytes: it is described as rows of 64 BF16 values for BF16 and TF32 operands alike
+// (the swizzle permutes 16-byte chunks by row and does not depend on the element type).
 imsrg_status Ctx::tc_encode_map(CUtensorMap* map, void* buf, int64_t total_rows) {
   void* fn = nullptr;
   cudaDriverEntryPointQueryResult q;
   CK_TC(cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
              "cudaGetDriverEntryPointByVersion"));
   if (!fn || q != cudaDriverEntryPointSuccess) return fail(IMSRG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  const cuuint64_t gdim[2] = {(cuuint64_t)BK, (cuuint64_t)std::max<int64_t>(total_rows, BM)};
-  const cuuint64_t gstride[1] = {(cuuint64_t)(BK * sizeof(__nv_bfloat16))};
-  const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
+  const cuuint64_t gdim[2] = {64, (cuuint64_t)std::max<int64_t>(total_rows, BM)};
+  const cuuint64_t gstride[1] = {128};
+  const cuuint32_t box[2] = {64, (cuuint32_t)BM};
   const cuuint32_t estride[2] = {1, 1};
   CUresult r = reinterpret_cast<EncodeTiledFn>(fn)(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, buf, gdim, gstride, box,
                                                     estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -831,23 +919,21 @@ imsrg_status Ctx::tc_encode_map(CUtensorMap* map, void* buf, int64_t total_rows)
 
 // operand split of any op / chunk list into a buffer of this context's slice count
 imsrg_status Ctx::tc_split_on(const TcSplitOp* ops, const SplitChunk* chunks, int nchunks, const double* Lp,
-                              const double* Rp, __nv_bfloat16* buf, int64_t slice_elems) {
+                              const double* Rp, void* buf, int64_t slice_elems) {
   if (nchunks == 0) return IMSRG_OK;
-  if (tc->S == 2)
-    k_split_chunks<2><<<nchunks, 256, 0, stream>>>(ops, chunks, Lp, Rp, buf, slice_elems);
+  if (tc->kind == kKindTF32)
+    k_split_chunks<2, float><<<nchunks, 256, 0, stream>>>(ops, chunks, Lp, Rp, buf, slice_elems);
+  else if (tc->S == 2)
+    k_split_chunks<2, __nv_bfloat16><<<nchunks, 256, 0, stream>>>(ops, chunks, Lp, Rp, buf, slice_elems);
   else
-    k_split_chunks<3><<<nchunks, 256, 0, stream>>>(ops, chunks, Lp, Rp, buf, slice_elems);
+    k_split_chunks<3, __nv_bfloat16><<<nchunks, 256, 0, stream>>>(ops, chunks, Lp, Rp, buf, slice_elems);
   return launched("k_split_chunks");
 }
 
 imsrg_status Ctx::tc_pphh(const double* Lp, int hL, const double* Rp, int hR, double* w1, double* w2) {
   if (!tc->chunks.empty()) {
     const int grid = (int)tc->chunks.size();
-    if (tc->S == 2)
-      k_split_chunks<2><<<grid, 256, 0, stream>>>(tc->d_split_ops, tc->d_chunks, Lp, Rp, tc->buf, tc->slice_elems);
-    else
-      k_split_chunks<3><<<grid, 256, 0, stream>>>(tc->d_split_ops, tc->d_chunks, Lp, Rp, tc->buf, tc->slice_elems);
-    CK_TC(launched("k_split_chunks"));
+    CK_TC(tc_split_on(tc->d_split_ops, tc->d_chunks, grid, Lp, Rp, tc->buf, tc->slice_elems));
   }
   mark(kPhasePphhSplit);
   TcOut out{};
@@ -874,7 +960,10 @@ imsrg_status Ctx::tc_error() {
   CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize"));
   if (e) {
     cudaMemsetAsync(tc->d_err, 0, sizeof(int), stream);
-    return fail(IMSRG_ERR_CUDA, "tensor-core GEMM wait timed out (code " + std::to_string(e) + ")");
+    static const char* role[] = {"", "producer (stage free)", "MMA (accumulator free)", "MMA (stage loaded)",
+                                 "epilogue (accumulator ready)"};
+    return fail(IMSRG_ERR_TIMEOUT, std::string("tensor-core GEMM: a bounded wait ran out in the ") +
+                                       (e >= 1 && e <= 4 ? role[e] : "kernel") + " (code " + std::to_string(e) + ")");
   }
   return IMSRG_OK;
 }
@@ -889,15 +978,30 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
                                 bool with_e0) {
   const int64_t ncc = L.cc_size;
   mark(kPhaseStart);
+  // operands of both tensor-core products: the Pandya tiles (particle-hole) and the split
+  // columns of the ladder arrays; then one persistent launch computes the K = npp ladder
+  // products W1 and the recoupling input X over the merged tile list
   if (ncc) {
     const int grid = (int)std::min<int64_t>((ncc + 255) / 256, 152 * 16);
-    launch_pandya_tc(tc->S, grid, stream, D, Rp, hR, tc->buf, tc->slice_elems, tc->d_cc_tile_R, tc->d_cc_tile_Rs,
+    launch_pandya_tc(tc->S, tc->kind, grid, stream, D, Rp, hR, tc->buf, tc->slice_elems, tc->d_cc_tile_R, tc->d_cc_tile_Rs,
                      tc->d_cc_nkb, tc->d_swap_row);
-    launch_pandya_tc(tc->S, grid, stream, D, Lp, hL, tc->buf, tc->slice_elems, tc->d_cc_tile_L, tc->d_cc_tile_Ls,
+    launch_pandya_tc(tc->S, tc->kind, grid, stream, D, Lp, hL, tc->buf, tc->slice_elems, tc->d_cc_tile_L, tc->d_cc_tile_Ls,
                      tc->d_cc_nkb, tc->d_swap_row);
     CK_TC(launched("k_pandya_tc"));
   }
   mark(kPhasePandya);
+  CK_TC(pphh_clear(d_w1, d_w2));
+  if (!tc->chunks.empty()) CK_TC(tc_split_on(tc->d_split_ops, tc->d_chunks, (int)tc->chunks.size(), Lp, Rp, tc->buf,
+                                             tc->slice_elems));
+  mark(kPhasePphhSplit);
+  {
+    TcOut out{};
+    out.f64[kOpW1] = d_w1;
+    out.f64[kOpW2] = d_w2;
+    out.f32 = tc->zbuf;
+    CK_TC(tc_gemm(tc->d_all_probs, tc->d_tile_mem + tc->tile_cap_all, (int)tc->all_tiles.size(), out, hL, hR));
+  }
+  mark(kPhasePphhGemm);
   if (with_e0) CK_TC(e0(Lp, hL, Rp, hR, RES, nullptr));
   CK_TC(c111(Lp, hL, Rp, hR, RES));
   CK_TC(c121(Lp, hL, Rp, hR, RES, hRES));
@@ -931,25 +1035,36 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     }
   }
   mark(kPhase122);
-  CK_TC(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2, true));
+  if (!tc->small_tiles.empty()) {  // the K = nhh products (W2) on FP32 SIMT
+    GemmOperands ops{};
+    ops.in[kOpL] = Lp; ops.in[kOpR] = Rp;
+    ops.out[kOpW1] = d_w1; ops.out[kOpW2] = d_w2;
+    ops.hL = hL; ops.hR = hR;
+    k_gemm_f32<<<(int)tc->small_tiles.size(), 256, 0, stream>>>(tc->d_small_probs, tc->d_small_tiles, ops);
+    CK_TC(launched("k_gemm_f32"));
+  }
+  mark(kPhasePphhSmall);
+  CK_TC(pphh_accumulate(hL, hR, RES, d_w1, d_w2, true));
   CK_TC(c221(hL, hR, RES, hRES, d_w1, d_w2, true));
   mark(kPhase221);
-  TcOut zo{};
-  zo.f32 = tc->zbuf;
-  zo.f32b = tc->ybuf;
-  CK_TC(tc_gemm(tc->d_z_probs, tc->d_z_tiles, (int)tc->z_tiles.size(), zo, hL, hR));
-  mark(kPhasePhGemm);
   if (!tc->quads.empty()) {
-    const int64_t nq = (int64_t)tc->quads.size();
-    const int grid = (int)std::min<int64_t>((nq + 255) / 256, tc->recouple_ctas);
-    launch_recouple_y(tc->recouple_minb, grid, stream, D, tc->d_quads, nq, tc->zbuf, tc->ybuf, RES, hL * hR);
-    CK_TC(launched("k_recouple_y"));
+    if (tc->recouple_kind == 0) {
+      launch_recouple_g(tc->rc, stream, D, tc->d_rc_tasks, tc->d_rc_groups, tc->d_rc_triples, tc->d_rc_table,
+                        tc->d_quads, tc->d_xcol, tc->zbuf, RES);
+      CK_TC(launched("k_recouple_g"));
+    } else {
+      const int64_t nq = (int64_t)tc->quads.size();
+      const int grid = (int)std::min<int64_t>((nq + 255) / 256, tc->recouple_ctas);
+      launch_recouple_q(tc->recouple_minb, grid, stream, D, tc->d_quads, nq, tc->d_xcol, tc->zbuf, RES);
+      CK_TC(launched("k_recouple_q"));
+    }
   }
+  mark(kPhaseRecouple);
   if (!upd_tiles.empty()) {
     k_mirror_square<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, hRES);
     CK_TC(launched("k_mirror_square"));
   }
-  mark(kPhaseRecouple);
+  mark(kPhaseMirror);
   return IMSRG_OK;
 }
 
@@ -989,33 +1104,44 @@ imsrg_status Ctx::tc_g122_partition(int tiny_cap, int small_cap) {
   return IMSRG_OK;
 }
 
-// Order of the persistent GEMM tile lists: 0 = longest K first, 1 = problem order.
-imsrg_status Ctx::tc_set_gemm_order(int order) {
-  auto sorted = [&](const std::vector<TcTile>& lpt) {
-    std::vector<TcTile> t = lpt;
+// Tile lists of the persistent GEMMs for a tile shape and order: widest tile wmax (128, or 256
+// with two slices), narrow last column tiles or not, and order 0 = longest K first (LPT),
+// 1 = problem order.  No output element depends on these choices.
+imsrg_status Ctx::tc_set_tiles(int wmax, bool narrow, int order) {
+  if (wmax != 128 && !(wmax == 256 && tc->S == 2)) return fail(IMSRG_ERR_INVALID_ARGUMENT, "unsupported tile width");
+  auto build = [&](const std::vector<TcProb>& probs) {
+    std::vector<TcTile> t = make_tiles(probs, wmax, narrow);
     if (order == 1)
       std::stable_sort(t.begin(), t.end(), [](const TcTile& a, const TcTile& b) {
         return a.prob != b.prob ? a.prob < b.prob : (a.m0 != b.m0 ? a.m0 < b.m0 : a.n0 < b.n0);
       });
     return t;
   };
-  tc->pphh_tiles = sorted(tc->pphh_tiles_lpt);
-  tc->z_tiles = sorted(tc->z_tiles_lpt);
-  if (!tc->pphh_tiles.empty())
-    CK_TC(cuda(cudaMemcpyAsync(const_cast<TcTile*>(tc->d_pphh_tiles), tc->pphh_tiles.data(),
-                               sizeof(TcTile) * tc->pphh_tiles.size(), cudaMemcpyHostToDevice, stream),
-               "cudaMemcpyAsync(GEMM tiles)"));
-  if (!tc->z_tiles.empty())
-    CK_TC(cuda(cudaMemcpyAsync(const_cast<TcTile*>(tc->d_z_tiles), tc->z_tiles.data(),
-                               sizeof(TcTile) * tc->z_tiles.size(), cudaMemcpyHostToDevice, stream),
-               "cudaMemcpyAsync(GEMM tiles)"));
+  tc->pphh_tiles = build(tc->pphh_probs);
+  tc->z_tiles = build(tc->z_probs);
+  tc->all_tiles = build(tc->all_probs);
+  if (tc->pphh_tiles.size() > tc->tile_cap_pphh || tc->z_tiles.size() > tc->tile_cap_z ||
+      tc->all_tiles.size() > tc->tile_cap_all)
+    return fail(IMSRG_ERR_MISMATCH, "GEMM tile list larger than its allocation");
+  TcTile* d_all = tc->d_tile_mem + tc->tile_cap_all;
+  auto put = [&](TcTile* dst, const std::vector<TcTile>& v) -> imsrg_status {
+    if (v.empty()) return IMSRG_OK;
+    return cuda(cudaMemcpyAsync(dst, v.data(), sizeof(TcTile) * v.size(), cudaMemcpyHostToDevice, stream),
+                "cudaMemcpyAsync(GEMM tiles)");
+  };
+  CK_TC(put(tc->d_tile_mem, tc->pphh_tiles));
+  CK_TC(put(tc->d_tile_mem + tc->tile_cap_pphh, tc->z_tiles));
+  CK_TC(put(d_all, tc->all_tiles));
   CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize(GEMM tiles)"));
+  tc->wmax = wmax;
+  tc->narrow = narrow;
   tc->gemm_order = order;
   return IMSRG_OK;
 }
 
 // Times one mixed commutator [L, R] per candidate launch configuration on this basis and keeps
-// the fastest, one knob at a time (122 task caps, recoupling CTAs, GEMM tile order).  Every
+// the fastest: the 122 task caps, the recoupling kernel, then the tensor-core GEMM's tile shape
+// and order jointly.  Every
 // candidate computes the same result: no output element depends on the partition, the grid or
 // the tile order.  A captured Magnus-step graph is dropped, so the next step re-captures it.
 imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR, double* RES, imsrg_tune_info* info) {
@@ -1049,38 +1175,56 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
       if (ms < best) { best = ms; bt = c[0]; bs = c[1]; }
     }
     if (st != IMSRG_OK || (st = tc_g122_partition(bt, bs)) != IMSRG_OK) break;
-    // recoupling: launch-bounds variant and CTA count together (the best CTA count depends on
-    // how many CTAs of the variant are resident)
-    int bm = tc->recouple_minb, br = tc->recouple_ctas;
-    for (int minb : {4, 5, 6, 8}) {
-      for (int mult : {4, 8, 16, 32, 64, 128}) {
-        tc->recouple_minb = minb;
-        tc->recouple_ctas = tc->num_sms * mult;
-        float ms;
-        if ((st = time_one(&ms)) != IMSRG_OK) break;
-        if (ms < best) { best = ms; bm = minb; br = tc->recouple_ctas; }
-      }
-      if (st != IMSRG_OK) break;
-    }
-    tc->recouple_minb = bm;
-    tc->recouple_ctas = br;
-    if (st != IMSRG_OK) break;
-    // GEMM tile order
-    int bo = tc->gemm_order;
-    for (int order : {0, 1}) {
-      if ((st = tc_set_gemm_order(order)) != IMSRG_OK) break;
+    // recoupling: by groups, or per quadruple with its launch-bounds variant and CTA count (the
+    // kernels sum every output in the same order, so the choice leaves the result unchanged)
+    {
+      int bk = tc->recouple_kind, bm = tc->recouple_minb, bc = tc->recouple_ctas;
+      tc->recouple_kind = 0;
       float ms;
       if ((st = time_one(&ms)) != IMSRG_OK) break;
-      if (ms < best) { best = ms; bo = order; }
+      if (ms < best) { best = ms; bk = 0; }
+      tc->recouple_kind = 1;
+      for (int minb : {4, 6, 8}) {
+        for (int mult : {16, 32, 64}) {
+          tc->recouple_minb = minb;
+          tc->recouple_ctas = tc->num_sms * mult;
+          if ((st = time_one(&ms)) != IMSRG_OK) break;
+          if (ms < best) { best = ms; bk = 1; bm = minb; bc = tc->recouple_ctas; }
+        }
+        if (st != IMSRG_OK) break;
+      }
+      if (st != IMSRG_OK) break;
+      tc->recouple_kind = bk;
+      tc->recouple_minb = bm;
+      tc->recouple_ctas = bc;
     }
-    if (st != IMSRG_OK || (st = tc_set_gemm_order(bo)) != IMSRG_OK) break;
+    // tensor-core GEMM: tile shape (widest tile, narrow last tiles) and tile order, jointly
+    {
+      int bw = tc->wmax, bo = tc->gemm_order;
+      bool bn = tc->narrow;
+      for (int wmax : {128, 256}) {
+        if (wmax == 256 && tc->S != 2) continue;
+        for (int narrow = 0; narrow < 2 && st == IMSRG_OK; ++narrow)
+          for (int order : {0, 1}) {
+            if ((st = tc_set_tiles(wmax, narrow != 0, order)) != IMSRG_OK) break;
+            float ms;
+            if ((st = time_one(&ms)) != IMSRG_OK) break;
+            if (ms < best) { best = ms; bw = wmax; bn = narrow != 0; bo = order; }
+          }
+        if (st != IMSRG_OK) break;
+      }
+      if (st != IMSRG_OK || (st = tc_set_tiles(bw, bn, bo)) != IMSRG_OK) break;
+    }
     float after = 0.0f;
     if ((st = time_one(&after)) != IMSRG_OK) break;
     if (info) {
       info->tiny_cap = tc->g122_tiny_cap;
       info->small_cap = tc->g122_small;
-      info->recouple_ctas = tc->recouple_ctas;
-      info->recouple_min_blocks = tc->recouple_minb;
+      info->recouple_kind = tc->recouple_kind;
+      info->recouple_min_blocks = tc->recouple_kind ? tc->recouple_minb : 0;
+      info->recouple_ctas = tc->recouple_kind ? tc->recouple_ctas : (int32_t)tc->rc.tasks.size();
+      info->gemm_wmax = tc->wmax;
+      info->gemm_narrow = tc->narrow ? 1 : 0;
       info->gemm_order = tc->gemm_order;
       info->ms_before = base;
       info->ms_after = after;
@@ -1090,6 +1234,22 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
   cudaEventDestroy(e1);
   if (st == IMSRG_OK) graph_release();
   return st;
+}
+
+extern "C" imsrg_status imsrg_recouple_traffic(imsrg_ctx* ctx, int64_t* x_reads, int64_t* x_distinct,
+                                               int64_t* res_elems, int64_t* aux_bytes) {
+  if (!ctx || !x_reads || !x_distinct || !res_elems || !aux_bytes) return IMSRG_ERR_INVALID_ARGUMENT;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  if (c->device < 0) return c->fail(IMSRG_ERR_UNSUPPORTED, "host-only context (device < 0)");
+  if (c->precision == IMSRG_PREC_FP64) return c->fail(IMSRG_ERR_UNSUPPORTED, "the recoupling kernel runs in the mixed modes");
+  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(IMSRG_ERR_CUDA, "cudaSetDevice");
+  CK_TC(c->tc_prepare(c->precision));
+  const RecoupleTraffic t = recouple_traffic(c->L, c->tc->quads, c->tc->rc);
+  *x_reads = t.x_reads;
+  *x_distinct = t.x_distinct;
+  *res_elems = t.res_elems;
+  *aux_bytes = t.aux_bytes;
+  return IMSRG_OK;
 }
 
 extern "C" imsrg_status imsrg_autotune(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES,

@@ -36,13 +36,15 @@ __global__ void k_frob_partial(const double* op, const int64_t* seg_start, const
 __global__ void k_sum_sqrt(const double* partial, int n, double scale, double* out);
 __global__ void k_mbpt2_partial(DevLayout D, const double* H, int hH, double* partial);
 __global__ void k_sum(const double* partial, int n, double* out);
+__global__ void k_zero_runs(double* x, const int64_t* runs);
+__global__ void k_convert_check(const double* x, const float* y, int64_t n, float* out_f32, double* out_f64);
 
 __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOperands ops);
 
 // mixed-precision companions (kernels_mixed.cu)
-void launch_pandya_tc(int S, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
-                      __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s,
-                      const int* nkb, const int* swap_row);
+void launch_pandya_tc(int S, int kind, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
+                      void* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s, const int* nkb,
+                      const int* swap_row);
 __global__ void k_comm122f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
 __global__ void k_comm122_fblocks(DevLayout D, PairGroupsDev G, int nspb, int nblk2, const double* L, int hL,
                                   const double* R, int hR, float* FB);
@@ -55,10 +57,5 @@ __global__ void k_comm122_groups_cta(DevLayout D, PairGroupsDev G, int nmax4, in
 __global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
                                 float pm);
 __global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);
-// k_recouple_y with launch bounds (256, min_blocks), min_blocks 4, 5, 6 or 8
-void launch_recouple_y(int min_blocks, int grid, cudaStream_t st, const DevLayout& D, const uint64_t* quads,
-                       int64_t nquads, const float* Z, const float* Y, double* RES, int pm);
-__global__ void k_comm222ph_z(DevLayout D, const float* Z, double* RES, int hRES);
-__global__ void k_recouple_quad(DevLayout D, const uint64_t* quads, int64_t nquads, const float* Z, double* RES, int hRES);
 
 }  // namespace imsrg

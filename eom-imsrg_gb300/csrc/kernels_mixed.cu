@@ -6,6 +6,7 @@
 #include "dev.cuh"
 #include "kernels.h"
 #include "pair_groups.h"
+#include "split.cuh"
 
 namespace imsrg {
 
@@ -17,15 +18,18 @@ __device__ __forceinline__ float d_sixjf(const DevLayout& D, int j1, int j2, int
 }
 
 // Pandya transform (calculate_cross_coupled, src/cross_coupled.f90:1190-1300) in FP32,
-// written straight into the K-major split-BF16 operand tiles of the cross-coupled GEMM:
+// written straight into the K-major split operand tiles (BF16 or TF32, split.cuh) of the
+// cross-coupled GEMM:
 // row r of the tile block of channel q, column ph.  Threads run along ph so the writes
 // into each 128-byte tile row are contiguous.
-// Each element is written twice: at row r of the operand tiles and at row s(r) of the
-// row-swapped copy, s(r(a,b)) = r(b,a), which feeds the row-swapped product Y.
-template <int S>
-__global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm, __nv_bfloat16* __restrict__ buf,
+// Each element is written twice: at row r of the operand tiles, times the row sign
+// phi(r(a,b)) = (-1)^((ja+jb)/2), and unsigned at row s(r) of the row-swapped copy,
+// s(r(a,b)) = r(b,a).  The recoupling input X (gemm_tc.cu) is built from both.
+template <int S, typename T>
+__global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm, void* __restrict__ bufv,
                             int64_t slice_elems, const int* __restrict__ tile_base, const int* __restrict__ tile_base_s,
                             const int* __restrict__ nkb, const int* __restrict__ swap_row) {
+  T* buf = static_cast<T*>(bufv);
   const int64_t total = D.cc_size;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = D.ncc;
@@ -56,27 +60,30 @@ __global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm
       val = sm * (((jh + jb + JC) & 2) ? -1.0f : 1.0f) * sqrtf((float)(JC + 1));
     }
     const int rs = swap_row[D.cc_row_off[q] + r];
-    const int64_t dst =
-        ((int64_t)(tile_base[q] + (r >> 7) * nkb[q] + (nbx >> 6)) * 128 + (r & 127)) * 64 + (nbx & 63);
-    const int64_t dsts =
-        ((int64_t)(tile_base_s[q] + (rs >> 7) * nkb[q] + (nbx >> 6)) * 128 + (rs & 127)) * 64 + (nbx & 63);
+    const int64_t dst = split_offset<T>(tile_base[q], nkb[q], r, nbx);
+    const int64_t dsts = split_offset<T>(tile_base_s[q], nkb[q], rs, nbx);
+    const bool flip = ((ja + jb) & 2) != 0;  // phi(r) = -1
     float rem = val;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      const __nv_bfloat16 hv = __float2bfloat16_rn(rem);
-      buf[s * slice_elems + dst] = hv;
+      const T hv = SplitElem<T>::take(rem);
+      buf[s * slice_elems + dst] = flip ? SplitElem<T>::neg(hv) : hv;
       buf[s * slice_elems + dsts] = hv;
-      rem -= __bfloat162float(hv);
     }
   }
 }
-void launch_pandya_tc(int S, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
-                      __nv_bfloat16* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s,
-                      const int* nkb, const int* swap_row) {
-  if (S == 2)
-    k_pandya_tc<2><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s, nkb, swap_row);
+void launch_pandya_tc(int S, int kind, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
+                      void* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s, const int* nkb,
+                      const int* swap_row) {
+  if (kind == 1)
+    k_pandya_tc<2, float><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s, nkb,
+                                                     swap_row);
+  else if (S == 2)
+    k_pandya_tc<2, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s,
+                                                             nkb, swap_row);
   else
-    k_pandya_tc<3><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s, nkb, swap_row);
+    k_pandya_tc<3, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s,
+                                                             nkb, swap_row);
 }
 
 // commutator_122 (src/commutators.f90:283-396), FP32 arithmetic -- ASSIGNS every 2b element
@@ -174,7 +181,7 @@ __global__ void __launch_bounds__(256) k_pphh_update_f(DevLayout D, const int4* 
       const int i = i0 + tx, j = j0 + r;
       if (i < n1 && j < n2) {
         const int64_t e = base + i + (int64_t)j * n1;
-        RES[e] = f32_to_f64(f64_to_f32(RES[e]) + (f64_to_f32(w1[e]) - f64_to_f32(w2[e])));
+        RES[e] += f32_to_f64(f64_to_f32(w1[e]) - f64_to_f32(w2[e]));
       }
     }
     return;
@@ -193,7 +200,7 @@ __global__ void __launch_bounds__(256) k_pphh_update_f(DevLayout D, const int4* 
     const int i = i0 + tx, j = j0 + r;
     if (i < n1 && j < n1 && i <= j) {
       const int64_t e = base + i + (int64_t)j * n1;
-      RES[e] = f32_to_f64(f64_to_f32(RES[e]) + (Xa[r][tx] - Xb[tx][r] * pm));
+      RES[e] += f32_to_f64(Xa[r][tx] - Xb[tx][r] * pm);
     }
   }
 }
@@ -221,257 +228,6 @@ __global__ void __launch_bounds__(256) k_mirror_square(DevLayout D, const int4* 
       const double v = T[tx][r];
       RES[base + i + (int64_t)j * n1] = __longlong_as_double(__double_as_longlong(v) ^ (long long)flip);
     }
-  }
-}
-
-// commutator_222_ph recoupling (src/commutators.f90:804-921) reading the antisymmetrised
-// cross-coupled product Z(q) = hL LCC RCC^T - hR RCC LCC^T (FP32), which folds the
-// reference's four WCC reads per J' into two.  ACCUMULATES into RES.
-__global__ void k_comm222ph_z(DevLayout D, const float* __restrict__ Z, double* __restrict__ RES, int hRES) {
-  // element-by-element form of the same recoupling (kept for reference and tests)
-  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < D.n_unique; u += (int64_t)gridDim.x * blockDim.x) {
-    int q, g, IX, JX;
-    d_unique_decode(D, u, q, g, IX, JX);
-    const int c1 = (g < 3) ? 0 : (g == 4 ? 2 : 1);
-    const int c2 = (g == 0) ? 0 : ((g == 1 || g == 3) ? 1 : 2);
-    const int o1 = D.pair_off[q * 3 + c1] + IX, o2 = D.pair_off[q * 3 + c2] + JX;
-    const int i = D.pair_a[o1], j = D.pair_b[o1], k = D.pair_a[o2], l = D.pair_b[o2];
-    const int ji = D.jj[i], jj = D.jj[j], jk = D.jj[k], jl = D.jj[l];
-    const int Jtot = D.lamJ[q];
-    const int N = D.N, NJ = D.NJ;
-    const float phase = ((ji + jj + jk + jl) & 2) ? -1.0f : 1.0f;
-    float sm = 0.0f;
-    {
-      const int Tz = abs(D.tz[i] - D.tz[k]) >> 1;
-      const int PAR = (D.ll[i] + D.ll[k]) & 1;
-      const int jmin = max(abs(jj - jl), abs(ji - jk)), jmax = min(jj + jl, ji + jk);
-      float acc = 0.0f;
-      for (int JP = jmin; JP <= jmax; JP += 2) {
-        const int qx = (JP >> 1) + Tz * (D.JM + 1) + PAR * 2 * (D.JM + 1);
-        const float* W = Z + D.wcc_off[qx];
-        const int64_t rl = D.cc_rlen[qx];
-        const int h = JP >> 1;
-        const int64_t rjl = D.ccr[(j * N + l) * NJ + h], rik = D.ccr[(i * N + k) * NJ + h];
-        const int64_t gjl = D.ccr[(l * N + j) * NJ + h], gik = D.ccr[(k * N + i) * NJ + h];
-        if ((rjl | rik | gjl | gik) < 0) continue;
-        acc += (W[gik + rjl * rl] + phase * W[gjl + rik * rl]) * d_sixjf(D, ji, jj, Jtot, jl, jk, JP);
-      }
-      sm -= (((jl + jk + Jtot) & 2) ? -1.0f : 1.0f) * acc;
-    }
-    {
-      const int Tz = abs(D.tz[i] - D.tz[l]) >> 1;
-      const int PAR = (D.ll[i] + D.ll[l]) & 1;
-      const int jmin = max(abs(ji - jl), abs(jj - jk)), jmax = min(ji + jl, jj + jk);
-      for (int JP = jmin; JP <= jmax; JP += 2) {
-        const int qx = (JP >> 1) + Tz * (D.JM + 1) + PAR * 2 * (D.JM + 1);
-        const float* W = Z + D.wcc_off[qx];
-        const int64_t rl = D.cc_rlen[qx];
-        const int h = JP >> 1;
-        const int64_t ril = D.ccr[(i * N + l) * NJ + h], rjk = D.ccr[(j * N + k) * NJ + h];
-        const int64_t gil = D.ccr[(l * N + i) * NJ + h], gjk = D.ccr[(k * N + j) * NJ + h];
-        if ((ril | rjk | gil | gjk) < 0) continue;
-        sm += (W[gil + rjk * rl] + phase * W[gjk + ril * rl]) * d_sixjf(D, ji, jj, Jtot, jk, jl, JP);
-      }
-    }
-    double v = (double)sm;
-    if (i == j) v *= .70710678118;
-    if (k == l) v *= .70710678118;
-    const int kk = q * 6 + g;
-    double* X = RES + D.goff[kk];
-    const int n1 = D.gn1[kk];
-    const double nv = X[IX + (int64_t)JX * n1] + v;
-    X[IX + (int64_t)JX * n1] = nv;
-    if (g == 0 || g == 3 || g == 4) X[JX + (int64_t)IX * n1] = nv * hRES;
-  }
-}
-
-// commutator_222_ph recoupling organised by orbit quadruple: one thread per (i<=j, k<=l)
-// with matching Tz and parity.  The J'-sums of the direct and exchange terms do not
-// depend on the output J, so each Z(J') pair is read once and reused for every J the two
-// pairs share (the reference re-reads them for each J).  Quadruples are ordered with j
-// fastest so the reads Z[(l,j),(i,k)] and Z[(k,j),(i,l)] are consecutive across a warp.
-// ACCUMULATES into RES (and refreshes the mirrored element of square arrays).
-constexpr int kMaxJp = 26;  // J' values per term: at most jmax+1 (2j <= 25 for eMax <= 12)
-__global__ void k_recouple_quad(DevLayout D, const uint64_t* __restrict__ quads, int64_t nquads,
-                                const float* __restrict__ Z, double* __restrict__ RES, int hRES) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nquads; t += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t qd = quads[t];
-    const int i = (int)(qd & 0xFFFF), j = (int)((qd >> 16) & 0xFFFF), k = (int)((qd >> 32) & 0xFFFF),
-              l = (int)((qd >> 48) & 0xFFFF);
-    const int ji = D.jj[i], jj = D.jj[j], jk = D.jj[k], jl = D.jj[l];
-    const int N = D.N, NJ = D.NJ;
-    const float phase = ((ji + jj + jk + jl) & 2) ? -1.0f : 1.0f;
-    // direct term inputs: zd(J') = Z[(k,i),(j,l)] + phase Z[(l,j),(i,k)]
-    float zd[kMaxJp], ze[kMaxJp];
-    const int dlo = max(abs(jj - jl), abs(ji - jk)), dhi = min(jj + jl, ji + jk);
-    {
-      const int Tz = abs(D.tz[i] - D.tz[k]) >> 1, PAR = (D.ll[i] + D.ll[k]) & 1;
-      for (int JP = dlo, n = 0; JP <= dhi && n < kMaxJp; JP += 2, ++n) {
-        const int qx = (JP >> 1) + Tz * (D.JM + 1) + PAR * 2 * (D.JM + 1);
-        const float* W = Z + D.wcc_off[qx];
-        const int64_t rl = D.cc_rlen[qx];
-        const int h = JP >> 1;
-        const int64_t rjl = D.ccr[(j * N + l) * NJ + h], rik = D.ccr[(i * N + k) * NJ + h];
-        const int64_t gjl = D.ccr[(l * N + j) * NJ + h], gik = D.ccr[(k * N + i) * NJ + h];
-        zd[n] = ((rjl | rik | gjl | gik) < 0) ? 0.0f : W[gik + rjl * rl] + phase * W[gjl + rik * rl];
-      }
-    }
-    // exchange term inputs: ze(J') = Z[(l,i),(j,k)] + phase Z[(k,j),(i,l)]
-    const int elo = max(abs(ji - jl), abs(jj - jk)), ehi = min(ji + jl, jj + jk);
-    {
-      const int Tz = abs(D.tz[i] - D.tz[l]) >> 1, PAR = (D.ll[i] + D.ll[l]) & 1;
-      for (int JP = elo, n = 0; JP <= ehi && n < kMaxJp; JP += 2, ++n) {
-        const int qx = (JP >> 1) + Tz * (D.JM + 1) + PAR * 2 * (D.JM + 1);
-        const float* W = Z + D.wcc_off[qx];
-        const int64_t rl = D.cc_rlen[qx];
-        const int h = JP >> 1;
-        const int64_t ril = D.ccr[(i * N + l) * NJ + h], rjk = D.ccr[(j * N + k) * NJ + h];
-        const int64_t gil = D.ccr[(l * N + i) * NJ + h], gjk = D.ccr[(k * N + j) * NJ + h];
-        ze[n] = ((ril | rjk | gil | gjk) < 0) ? 0.0f : W[gil + rjk * rl] + phase * W[gjk + ril * rl];
-      }
-    }
-    // 6j blocks {ji jj J; jl jk J'} (direct) and {ji jj J; jk jl J'} (exchange)
-    const int nh = D.sj_nh;
-    const int kd = (((ji >> 1) * nh + (jj >> 1)) * nh + (jl >> 1)) * nh + (jk >> 1);
-    const int ke = (((ji >> 1) * nh + (jj >> 1)) * nh + (jk >> 1)) * nh + (jl >> 1);
-    const float* sjd = D.sj_valf + D.sj_off[kd];
-    const float* sje = D.sj_valf + D.sj_off[ke];
-    const int d3 = D.sj_j3min[kd], d6 = D.sj_j6min[kd], dn6 = D.sj_n6[kd];
-    const int e3 = D.sj_j3min[ke], e6 = D.sj_j6min[ke], en6 = D.sj_n6[ke];
-    const int C1 = D.con[i] + D.con[j], C2 = D.con[k] + D.con[l];
-    const int g = (C1 == 0) ? C2 : (C1 == 1 ? (C2 == 1 ? 3 : 5) : 4);
-    const bool square = (C1 == C2);
-    const int T = D.tz[i] + D.tz[j], P = (D.ll[i] + D.ll[j]) & 1;
-    const float pre = ((i == j) ? .70710678118f : 1.0f) * ((k == l) ? .70710678118f : 1.0f);
-    const int Jlo = max(abs(ji - jj), abs(jk - jl)), Jhi = min(ji + jj, jk + jl);
-    for (int J = Jlo; J <= Jhi; J += 2) {
-      float sd = 0.0f, se = 0.0f;
-      {
-        // valid J' for this J: triangles (ji,jj,J) hold; (jl,jk,J) and the J' range of zd
-        // every (J, J') here satisfies the four triangles: J lies in both pair ranges and
-        // J' in the direct range, whose lower ends are this 6j block's j3min / j6min
-        const float* row = sjd + ((J - d3) >> 1) * dn6 + ((dlo - d6) >> 1);
-        const int n = min((dhi - dlo) / 2 + 1, kMaxJp);
-        for (int m = 0; m < n; ++m) sd += row[m] * zd[m];
-      }
-      {
-        const float* row = sje + ((J - e3) >> 1) * en6 + ((elo - e6) >> 1);
-        const int n = min((ehi - elo) / 2 + 1, kMaxJp);
-        for (int m = 0; m < n; ++m) se += row[m] * ze[m];
-      }
-      const float sm = -(((jl + jk + J) & 2) ? -1.0f : 1.0f) * sd + se;
-      const int q = 3 * J + (T + 2) + P;
-      const int kk = q * 6 + g;
-      const int IX = D.pairpos[(i * N + j) * NJ + (J >> 1)], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
-      double* X = RES + D.goff[kk];
-      const int n1 = D.gn1[kk];
-      const double nv = X[IX + (int64_t)JX * n1] + (double)(sm * pre);
-      X[IX + (int64_t)JX * n1] = nv;
-      if (square) X[JX + (int64_t)IX * n1] = nv * hRES;
-    }
-  }
-}
-
-// Recoupling with the row-swapped copy Y(r(a,b), c) = Z(r(b,a), c).  Using the
-// antisymmetry Z(x,y) = -pm Z(y,x), the four reads per J' become
-//   direct   : -pm Y[(l,j),(k,i)] + phase Z[(l,j),(i,k)]
-//   exchange : -pm Y[(k,j),(l,i)] + phase Z[(k,j),(i,l)]
-// whose rows advance with j; quadruples are ordered j fastest and the J' and J loops are
-// warp-uniform, so each warp reads consecutive rows of one channel matrix and writes
-// consecutive rows of one RES column.  Upper triangles only (mirror pass afterwards).
-// kMinBlocks: the resident-CTA hint of the launch bounds (registers traded for occupancy),
-// one of the choices of the autotuner
-template <int kMinBlocks>
-__global__ void __launch_bounds__(256, kMinBlocks) k_recouple_y(DevLayout D, const uint64_t* __restrict__ quads, int64_t nquads,
-                                                    const float* __restrict__ Z, const float* __restrict__ Y,
-                                                    double* __restrict__ RES, int pm) {
-  const int lane = threadIdx.x & 31;
-  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int N = D.N, NJ = D.NJ, JM = D.JM;
-  const float fpm = (float)pm;
-  for (int64_t w = gw; w * 32 < nquads; w += nw) {
-    const int64_t t = w * 32 + lane;
-    const bool act = t < nquads;
-    const uint64_t qd = act ? quads[t] : 0ull;
-    const int i = (int)(qd & 0xFFFF), j = (int)((qd >> 16) & 0xFFFF), k = (int)((qd >> 32) & 0xFFFF),
-              l = (int)((qd >> 48) & 0xFFFF);
-    const int ji = D.jj[i], jj = D.jj[j], jk = D.jj[k], jl = D.jj[l];
-    const float phase = ((ji + jj + jk + jl) & 2) ? -1.0f : 1.0f;
-    const int dlo = act ? max(abs(jj - jl), abs(ji - jk)) : 1 << 20, dhi = act ? min(jj + jl, ji + jk) : -1;
-    const int elo = act ? max(abs(ji - jl), abs(jj - jk)) : 1 << 20, ehi = act ? min(ji + jl, jj + jk) : -1;
-    float zd[kMaxJp], ze[kMaxJp];
-    {
-      const int Tz = abs(D.tz[i] - D.tz[k]) >> 1, PAR = (D.ll[i] + D.ll[k]) & 1;
-      const int wlo = __reduce_min_sync(0xffffffffu, dlo), whi = __reduce_max_sync(0xffffffffu, dhi);
-      for (int JP = wlo; JP <= whi; JP += 2) {
-        if (JP < dlo || JP > dhi) continue;
-        const int qx = (JP >> 1) + Tz * (JM + 1) + PAR * 2 * (JM + 1);
-        const int64_t off = D.wcc_off[qx];
-        const int64_t rl = D.cc_rlen[qx];
-        const int h = JP >> 1;
-        const int64_t rlj = D.ccr_t[(l * NJ + h) * N + j], rki = D.ccr[(k * N + i) * NJ + h];
-        const int64_t rik = D.ccr[(i * N + k) * NJ + h];
-        zd[(JP - dlo) >> 1] = -fpm * Y[off + rlj + rki * rl] + phase * Z[off + rlj + rik * rl];
-      }
-    }
-    {
-      const int Tz = abs(D.tz[i] - D.tz[l]) >> 1, PAR = (D.ll[i] + D.ll[l]) & 1;
-      const int wlo = __reduce_min_sync(0xffffffffu, elo), whi = __reduce_max_sync(0xffffffffu, ehi);
-      for (int JP = wlo; JP <= whi; JP += 2) {
-        if (JP < elo || JP > ehi) continue;
-        const int qx = (JP >> 1) + Tz * (JM + 1) + PAR * 2 * (JM + 1);
-        const int64_t off = D.wcc_off[qx];
-        const int64_t rl = D.cc_rlen[qx];
-        const int h = JP >> 1;
-        const int64_t rkj = D.ccr_t[(k * NJ + h) * N + j], rli = D.ccr[(l * N + i) * NJ + h];
-        const int64_t ril = D.ccr[(i * N + l) * NJ + h];
-        ze[(JP - elo) >> 1] = -fpm * Y[off + rkj + rli * rl] + phase * Z[off + rkj + ril * rl];
-      }
-    }
-    const int nh = D.sj_nh;
-    const int kd = (((ji >> 1) * nh + (jj >> 1)) * nh + (jl >> 1)) * nh + (jk >> 1);
-    const int ke = (((ji >> 1) * nh + (jj >> 1)) * nh + (jk >> 1)) * nh + (jl >> 1);
-    const float* sjd = D.sj_valf + D.sj_off[kd];
-    const float* sje = D.sj_valf + D.sj_off[ke];
-    const int d3 = D.sj_j3min[kd], d6 = D.sj_j6min[kd], dn6 = D.sj_n6[kd];
-    const int e3 = D.sj_j3min[ke], e6 = D.sj_j6min[ke], en6 = D.sj_n6[ke];
-    const int C1 = D.con[i] + D.con[j], C2 = D.con[k] + D.con[l];
-    const int g = (C1 == 0) ? C2 : (C1 == 1 ? (C2 == 1 ? 3 : 5) : 4);
-    const int T = D.tz[i] + D.tz[j], P = (D.ll[i] + D.ll[j]) & 1;
-    const float pre = ((i == j) ? .70710678118f : 1.0f) * ((k == l) ? .70710678118f : 1.0f);
-    const int Jlo = act ? max(abs(ji - jj), abs(jk - jl)) : 1 << 20, Jhi = act ? min(ji + jj, jk + jl) : -1;
-    const int wJlo = __reduce_min_sync(0xffffffffu, Jlo), wJhi = __reduce_max_sync(0xffffffffu, Jhi);
-    const int nd = (dhi - dlo) / 2 + 1, ne = (ehi - elo) / 2 + 1;
-    for (int J = wJlo; J <= wJhi; J += 2) {
-      if (J < Jlo || J > Jhi) continue;
-      float sd = 0.0f, se = 0.0f;
-      {
-        const float* row = sjd + ((J - d3) >> 1) * dn6 + ((dlo - d6) >> 1);
-        for (int m = 0; m < nd; ++m) sd += row[m] * zd[m];
-      }
-      {
-        const float* row = sje + ((J - e3) >> 1) * en6 + ((elo - e6) >> 1);
-        for (int m = 0; m < ne; ++m) se += row[m] * ze[m];
-      }
-      const float sm = (-(((jl + jk + J) & 2) ? -1.0f : 1.0f) * sd + se) * pre;
-      const int q = 3 * J + (T + 2) + P;
-      const int kk = q * 6 + g;
-      const int IX = D.pairpos_t[(i * NJ + (J >> 1)) * N + j], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
-      double* X = RES + D.goff[kk] + IX + (int64_t)JX * D.gn1[kk];
-      *X = f32_to_f64(f64_to_f32(*X) + sm);
-    }
-  }
-}
-
-
-void launch_recouple_y(int min_blocks, int grid, cudaStream_t st, const DevLayout& D, const uint64_t* quads,
-                       int64_t nquads, const float* Z, const float* Y, double* RES, int pm) {
-  switch (min_blocks) {
-    case 5: k_recouple_y<5><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
-    case 6: k_recouple_y<6><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
-    case 8: k_recouple_y<8><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
-    default: k_recouple_y<4><<<grid, 256, 0, st>>>(D, quads, nquads, Z, Y, RES, pm); break;
   }
 }
 

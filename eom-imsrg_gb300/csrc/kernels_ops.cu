@@ -174,4 +174,23 @@ __global__ void k_sum(const double* __restrict__ partial, int n, double* __restr
   if (threadIdx.x == 0) *out = red[0];
 }
 
+// Self-check of the integer conversions of dev.cuh against the GPU's conversion
+// instructions: out_f32 = [f64_to_f32(x) | __double2float_rn(x)], out_f64 = [f32_to_f64(y) |
+// (double)y], n entries each.
+__global__ void k_convert_check(const double* __restrict__ x, const float* __restrict__ y, int64_t n,
+                                float* __restrict__ out_f32, double* __restrict__ out_f64) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    out_f32[t] = f64_to_f32(x[t]);
+    out_f32[n + t] = __double2float_rn(x[t]);
+    out_f64[t] = f32_to_f64(y[t]);
+    out_f64[n + t] = (double)y[t];
+  }
+}
+
+// zero the (start, length) run blockIdx.x of a slab
+__global__ void k_zero_runs(double* __restrict__ x, const int64_t* __restrict__ runs) {
+  const int64_t a = runs[2 * blockIdx.x], n = runs[2 * blockIdx.x + 1];
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) x[a + e] = 0.0;
+}
+
 }  // namespace imsrg

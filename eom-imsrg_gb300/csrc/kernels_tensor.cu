@@ -759,7 +759,7 @@ __global__ void k_ts212f(DevLayout D, DevTLayout T, const double* __restrict__ L
     const float f = sqrtf((float)((J1 + 1) * (J2 + 1))) * ((a == b) ? 0.70710678f : 1.0f) *
                     ((c == d) ? 0.70710678f : 1.0f) * sg(rank >> 1);
     double* X = RES + T.goff[0] + e;
-    *X = f32_to_f64(f64_to_f32(*X) + sm * f);
+    *X += f32_to_f64(sm * f);
   }
 }
 

@@ -26,16 +26,27 @@ struct TcTermDesc {
   int sign;            // TcSign
 };
 
+// C = sum over nterm (<= 4) terms of sign * A_t B_t^T, all terms with the same K blocks
 struct TcProb {
   int64_t c_off;
   int M, N, nkb, nterm;
   int out_f32, c_id, ldc, pad;
-  TcTermDesc t[2];
+  TcTermDesc t[4];
 };
 
+// one output tile: rows m0 .. m0+127, columns n0 .. n0+w-1 of problem prob (n0 a multiple of
+// 128, w a multiple of 16, 16 <= w <= the kernel's widest tile)
 struct TcTile {
-  int prob, m0, n0, pad;
+  int prob, m0, n0, w;
 };
+
+// width of the tile at column n0 of an N-column problem: the widest tile, or with narrow
+// tiles the columns left rounded up to a multiple of 16
+inline int tc_tile_width(int N, int n0, int wmax, bool narrow) {
+  if (!narrow) return wmax;
+  const int left = N - n0;
+  return left >= wmax ? wmax : ((left + 15) / 16) * 16;
+}
 
 // split chunk: a contiguous run of rows of one split operand
 struct SplitChunk {

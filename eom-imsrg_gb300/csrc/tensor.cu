@@ -271,11 +271,11 @@ void Ctx::tensor_release() {
 // products through hh pairs keep their FP64 problems.
 imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
   if (!tc_slices()) return fail(IMSRG_ERR_UNSUPPORTED, "tensor-core ladder needs a mixed-precision context");
-  if (S.tc_S == tc_slices()) return IMSRG_OK;
+  if (S.tc_S == tc_slices() && S.tc_kind == tc_kind()) return IMSRG_OK;
   for (void* p : {(void*)S.tc_buf, S.tc_tables, (void*)S.w3})
     if (p) cudaFree(p);
   S.tc_buf = nullptr; S.tc_tables = nullptr; S.w3 = nullptr; S.tc_S = 0;
-  const int BMr = kTcTileRows, BKk = kTcTileK;
+  const int BMr = kTcTileRows, BKk = tc_tile_k();
   const auto P = build_tensor_pphh_problems(S.T, L);
   std::vector<TcSplitOp> ops;
   std::map<std::tuple<int, int64_t, int, int, int, int>, int> seen;  // operand -> tile base
@@ -313,7 +313,7 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
   std::vector<TcTile> tl;
   for (int i = 0; i < (int)probs.size(); ++i)
     for (int m0 = 0; m0 < probs[i].M; m0 += BMr)
-      for (int n0 = 0; n0 < probs[i].N; n0 += BMr) tl.push_back(TcTile{i, m0, n0, 0});
+      for (int n0 = 0; n0 < probs[i].N; n0 += BMr) tl.push_back(TcTile{i, m0, n0, BMr});
   std::stable_sort(tl.begin(), tl.end(), [&](const TcTile& a, const TcTile& b) { return probs[a.prob].nkb > probs[b.prob].nkb; });
   std::vector<SplitChunk> chunks;
   auto add_chunks = [&](int op) {
@@ -360,7 +360,7 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
       probs.push_back(q);
       const int pi = (int)probs.size() - 1;
       for (int m0 = 0; m0 < r1; m0 += BMr)
-        for (int n0 = 0; n0 < r2; n0 += BMr) tph.push_back(TcTile{pi, m0, n0, 0});
+        for (int n0 = 0; n0 < r2; n0 += BMr) tph.push_back(TcTile{pi, m0, n0, BMr});
     };
     if (dox && r1 && r2) {
       TcSplitOp o{};
@@ -389,7 +389,7 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
   S.tc_slice_elems = S.tc_slice_rows * BKk;
   if ((int64_t)Sl * S.tc_slice_rows >= (int64_t)1 << 31)
     return fail(IMSRG_ERR_UNSUPPORTED, "tensor ladder operands too large for 32-bit TMA rows");
-  const size_t bytes = sizeof(__nv_bfloat16) * (size_t)Sl * (size_t)S.tc_slice_elems;
+  const size_t bytes = (size_t)tc_elem_bytes() * (size_t)Sl * (size_t)S.tc_slice_elems;
   CKT(cuda(cudaMalloc(&S.tc_buf, std::max<size_t>(bytes, 256)), "cudaMalloc(tensor ladder operands)"));
   CKT(cuda(cudaMemset(S.tc_buf, 0, std::max<size_t>(bytes, 256)), "memset(tensor ladder operands)"));
   CKT(tc_encode_map(&S.tc_map, S.tc_buf, (int64_t)Sl * S.tc_slice_rows));
@@ -404,6 +404,7 @@ imsrg_status Ctx::tensor_tc_prepare(TensorState& S) {
   S.n_hh_t = (int)hh_tiles.size();
   CKT(cuda(cudaMalloc(&S.w3, sizeof(double) * (size_t)S.T.slab), "cudaMalloc(tensor w3)"));
   S.tc_S = Sl;
+  S.tc_kind = tc_kind();
   return IMSRG_OK;
 }
 

@@ -78,8 +78,8 @@ struct TensorState {
   // split-BF16 tensor-core form of the ladder's products through pp pairs (mixed modes):
   // one single-term problem per product, the first product of a (block, class pair) into
   // w1, the second into w3; the products through hh pairs (K = nhh) stay FP64 into w2
-  int tc_S = 0;
-  __nv_bfloat16* tc_buf = nullptr;
+  int tc_S = 0, tc_kind = 0;  // slices and operand type the tensor-core plan was built for
+  void* tc_buf = nullptr;
   int64_t tc_slice_rows = 0, tc_slice_elems = 0;
   CUtensorMap tc_map;
   void* tc_tables = nullptr;

@@ -14,9 +14,9 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libimsrg_gb300.so")
 IMSRG_OK = 0
 STATUS_NAMES = {
     0: "IMSRG_OK", 1: "IMSRG_ERR_INVALID_ARGUMENT", 2: "IMSRG_ERR_CUDA", 3: "IMSRG_ERR_OUT_OF_MEMORY",
-    4: "IMSRG_ERR_NOT_CONVERGED", 5: "IMSRG_ERR_MISMATCH", 6: "IMSRG_ERR_UNSUPPORTED",
+    4: "IMSRG_ERR_NOT_CONVERGED", 5: "IMSRG_ERR_MISMATCH", 6: "IMSRG_ERR_UNSUPPORTED", 7: "IMSRG_ERR_TIMEOUT",
 }
-PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2}
+PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2, "tf32x3": 3}
 COMM_E0 = 1
 
 
@@ -39,8 +39,9 @@ class HFInfo_t(C.Structure):
 
 class TuneInfo_t(C.Structure):
     _fields_ = [("tiny_cap", C.c_int32), ("small_cap", C.c_int32), ("recouple_ctas", C.c_int32),
-                ("gemm_order", C.c_int32), ("recouple_min_blocks", C.c_int32), ("ms_before", C.c_double),
-                ("ms_after", C.c_double)]
+                ("gemm_order", C.c_int32), ("gemm_wmax", C.c_int32), ("gemm_narrow", C.c_int32),
+                ("ms_before", C.c_double), ("ms_after", C.c_double), ("recouple_kind", C.c_int32),
+                ("recouple_min_blocks", C.c_int32)]
 
 
 class StepInfo_t(C.Structure):
@@ -79,6 +80,7 @@ SIGNATURES = {
     "imsrg_scale_sq_op": [_vp, _vp, _d],
     "imsrg_mat_frob_norm": [_vp, _vp, _pd],
     "imsrg_mbpt2": [_vp, _vp, _pd],
+    "imsrg_check_conversions": [_vp, _vp, _vp, _i64, _vp, _vp],
     "imsrg_cc_create": [_vp, _i32, _pvp],
     "imsrg_cc_destroy": [_vp, _vp],
     "imsrg_cc_download": [_vp, _vp, _vp],
@@ -146,9 +148,12 @@ SIGNATURES = {
     "imsrg_profile_phases": [_vp, _i32],
     "imsrg_profile_read": [_vp, C.POINTER(C.c_float), _pi32],
     "imsrg_mat_frob_norm_noalloc": [_vp, _vp, _vp, _vp],
+    "imsrg_set_wait_limit": [_vp, _i64],
+    "imsrg_recouple_traffic": [_vp, _pi64, _pi64, _pi64, _pi64],
+    "imsrg_test_unarmed_stage": [_vp, _i32],
 }
 PHASES = ["start", "pandya", "one_body", "c122", "pphh_split", "pphh_gemm", "pphh_small", "pphh_update", "c221",
-          "ph_gemm", "recouple"]
+          "ph_gemm", "recouple", "mirror"]
 
 _lib = None
 

@@ -37,11 +37,14 @@ typedef int32_t imsrg_status;
 #define IMSRG_ERR_NOT_CONVERGED 4
 #define IMSRG_ERR_MISMATCH 5
 #define IMSRG_ERR_UNSUPPORTED 6
+#define IMSRG_ERR_TIMEOUT 7 /* a bounded device wait ran out (the kernel stopped, the context stays usable) */
 
 /* arithmetic of the channel contractions (pp/hh ladders and cross-coupled GEMM) */
 #define IMSRG_PREC_FP64 0    /* plain FP64 (DFMA) */
 #define IMSRG_PREC_BF16X3 1  /* 2-slice split-BF16 operands, 3 products, FP32 accumulate (tcgen05) */
 #define IMSRG_PREC_BF16X6 2  /* 3-slice split-BF16 operands, 6 products, FP32 accumulate (tcgen05) */
+#define IMSRG_PREC_TF32X3 3  /* TF32-compensated: each FP32 operand = TF32 hi + TF32 lo, 3 products
+                                (hi.hi, hi.lo, lo.hi), FP32 accumulate (tcgen05 kind::tf32) */
 
 /* flags of imsrg_commutator */
 #define IMSRG_COMM_E0 1      /* also assign RES%E0 = commutator_110 + commutator_220 */
@@ -81,21 +84,45 @@ imsrg_status imsrg_block_pairs(const imsrg_ctx* ctx, int32_t q, int32_t cls, int
 /* per cross-coupled block: rlen, nph, 2J (cc_mat%rlen, %nph, %Jval) */
 imsrg_status imsrg_cc_info(const imsrg_ctx* ctx, int32_t* rlen, int32_t* nph, int32_t* J);
 imsrg_status imsrg_set_precision(imsrg_ctx* ctx, int32_t mode);
+/* Waits for the context's queued work.  Returns IMSRG_ERR_TIMEOUT when a bounded device wait
+ * of a tensor-core kernel ran out since the last call (the reference STOPs where a loop cannot
+ * finish, src/IMSRG_MAGNUS.f90:232; here the kernel records a code, stops its other roles,
+ * waits for its own copies in flight, frees its tensor memory and returns). */
 imsrg_status imsrg_synchronize(imsrg_ctx* ctx);
+/* Limit of every bounded device wait of the tensor-core kernels, in nanoseconds (default
+ * 2 s; 0 restores the default).  No counterpart in the reference. */
+imsrg_status imsrg_set_wait_limit(imsrg_ctx* ctx, int64_t nanoseconds);
+/* Test switch, off by default (no counterpart in the reference): with enable != 0 the next
+ * tensor-core GEMM launch of this context leaves its first pipeline stage unarmed -- no copy
+ * is issued for it and nothing arrives on its barrier -- so the MMA warp's wait on it runs out
+ * after the wait limit and imsrg_synchronize reports IMSRG_ERR_TIMEOUT.  The switch resets
+ * after that one launch.  For testing the failure path only. */
+imsrg_status imsrg_test_unarmed_stage(imsrg_ctx* ctx, int32_t enable);
+/* The traffic of the mixed particle-hole recoupling kernel on this basis, counted exactly
+ * from its orbit quadruples (no counterpart in the reference): X elements read and how many of
+ * them are distinct (FP32), RES elements read-modified-written (FP64), and the bytes of its own
+ * index data and 6j blocks.  For roofline figures.  IMSRG_ERR_UNSUPPORTED in FP64 mode. */
+imsrg_status imsrg_recouple_traffic(imsrg_ctx* ctx, int64_t* x_reads, int64_t* x_distinct, int64_t* res_elems,
+                                    int64_t* aux_bytes);
 /* The library's launch-configuration autotuner (no counterpart in the reference, which has
  * no GPU path).  In a mixed mode it times one commutator [L, R] into RES per candidate on
- * this basis and keeps the fastest, one knob at a time: the size caps that send the
- * commutator_122 sub-blocks to 8-lane groups, warps or CTAs; the CTA count of the
- * particle-hole recoupling and its register / occupancy variant; the tile order of the
- * persistent tcgen05 GEMMs.  The result of a
- * commutator does not depend on these choices.  A captured Magnus-step graph is dropped and
- * re-captured by the next step.  IMSRG_ERR_UNSUPPORTED in FP64 mode. */
+ * this basis and keeps the fastest: the size caps that send the commutator_122 sub-blocks to
+ * 8-lane groups, warps or CTAs; the particle-hole recoupling kernel (by orbit groups, or one
+ * thread per orbit quadruple with its occupancy variant and CTA count); then, jointly, the tile
+ * shape of the persistent tcgen05 GEMM
+ * (widest output tile 128 or 256 columns, and whether the last column tile of a problem is only
+ * as wide as its columns need, in steps of 16) and its tile order.  The result of a commutator
+ * does not depend on these choices.  A captured Magnus-step graph is dropped and re-captured
+ * by the next step.  IMSRG_ERR_UNSUPPORTED in FP64 mode. */
 typedef struct {
   int32_t tiny_cap, small_cap; /* sub-blocks up to tiny_cap elements: 8 lanes; up to small_cap: a warp */
-  int32_t recouple_ctas;       /* CTAs of the recoupling kernel */
+  int32_t recouple_ctas;       /* CTAs of the recoupling kernel (grouped: one per task of its plan) */
   int32_t gemm_order;          /* 0: tiles with the longest K first, 1: problem order */
-  int32_t recouple_min_blocks; /* launch-bounds variant of the recoupling kernel: 4, 5, 6 or 8 CTAs per SM */
+  int32_t gemm_wmax;           /* widest output tile of the tensor-core GEMM: 128 or 256 columns */
+  int32_t gemm_narrow;         /* 1: narrow last column tiles (multiples of 16 columns) */
   double ms_before, ms_after;  /* one commutator before and after tuning */
+  int32_t recouple_kind;       /* 0: recoupling by (i, k, l) groups, 1: one thread per orbit quadruple */
+  int32_t recouple_min_blocks; /* per-quadruple kernel: launch-bounds variant (4, 6 or 8 CTAs per SM) */
 } imsrg_tune_info;
 imsrg_status imsrg_autotune(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES,
                             imsrg_tune_info* info);
@@ -109,8 +136,9 @@ imsrg_status imsrg_timer_begin(imsrg_ctx* ctx);
 imsrg_status imsrg_timer_end(imsrg_ctx* ctx, float* ms);
 /* per-phase event timing of imsrg_commutator; phases: 1 Pandya, 2 one-body (110/220,
  * 111, 121), 3 122, 4 ladder operand split, 5 ladder GEMM, 6 small-K ladder GEMM,
- * 7 ladder accumulation, 8 221, 9 cross-coupled GEMM, 10 6j recoupling */
-#define IMSRG_NUM_PHASES 11
+ * 7 ladder accumulation, 8 221, 9 cross-coupled GEMM, 10 6j recoupling, 11 mirror of the
+ * square arrays' lower triangles */
+#define IMSRG_NUM_PHASES 12
 imsrg_status imsrg_profile_phases(imsrg_ctx* ctx, int32_t enable);
 imsrg_status imsrg_profile_read(imsrg_ctx* ctx, float* ms_per_phase, int32_t* count_per_phase);
 
@@ -142,6 +170,14 @@ imsrg_status imsrg_add_sq_op(imsrg_ctx* ctx, const imsrg_op* A, double ax, const
 imsrg_status imsrg_scale_sq_op(imsrg_ctx* ctx, imsrg_op* A, double ax);                               /* :3610 */
 imsrg_status imsrg_mat_frob_norm(imsrg_ctx* ctx, const imsrg_op* op, double* out);                    /* :4056 */
 imsrg_status imsrg_mbpt2(imsrg_ctx* ctx, const imsrg_op* H, double* out);                             /* :4165 */
+/* Self-check of the integer FP64 <-> FP32 conversions that the mixed-precision kernels use
+ * (round to nearest even; NaN, Inf, overflow and FP32 subnormals as IEEE 754 defines them),
+ * against the GPU's own conversion instructions.  No counterpart in the reference (its
+ * path is FP64 throughout).  For n inputs: out_f32 = [integer(host_x) | hardware(host_x)]
+ * (2n floats), out_f64 = [integer(host_y) | hardware(host_y)] (2n doubles).  Synchronous;
+ * allocates device scratch for the call. */
+imsrg_status imsrg_check_conversions(imsrg_ctx* ctx, const double* host_x, const float* host_y, int64_t n,
+                                     float* out_f32, double* out_f64);
 
 /* Frobenius norm for callers that cannot allocate GPU memory.  No counterpart in the
  * reference.  Same value as imsrg_mat_frob_norm, but for code that must not call
@@ -149,13 +185,16 @@ imsrg_status imsrg_mbpt2(imsrg_ctx* ctx, const imsrg_op* H, double* out);       
  * callback or pool that forbids new allocations, a host driver that only passes its own
  * buffers): the call allocates nothing and frees nothing.  dev_slab is any device sq_op
  * slab of this context's layout, dev_out one device double, stream a cudaStream_t
- * (NULL = legacy default stream); the call is asynchronous on that stream.
+ * (NULL = legacy default stream); the call is asynchronous on that stream.  It is ordered
+ * after every call already queued on the context (which may still be writing dev_slab),
+ * and the context's later calls wait for it.
  * Scratch is one static device array of IMSRG_NOALLOC_MAX_SEGMENTS doubles (64 KiB) that
  * every GPU loading the library keeps until exit; operators with more norm segments
- * (one per 65536 elements of each array) get IMSRG_ERR_UNSUPPORTED.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the array: calls that overlap on the GPU
- * (different streams, no ordering between them) race on it. */
+ * (one per 65536 elements of each array) get IMSRG_ERR_UNSUPPORTED.  Each call looks up
+ * the array's device address (cudaGetSymbolAddress); the first call on a device also loads
+ * the library's device code there and should come before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (on streams with no ordering between
+ * them, from several contexts or threads) race on it. */
 #define IMSRG_NOALLOC_MAX_SEGMENTS 8192
 imsrg_status imsrg_mat_frob_norm_noalloc(imsrg_ctx* ctx, const double* dev_slab, double* dev_out, void* stream);
 

@@ -1726,6 +1726,7 @@ namespace {
 #include "oracle_eom.inc"
 #include "oracle_triples.inc"
 #include "oracle_quads.inc"
+#include "oracle_input.inc"
 }  // namespace
 
 // ====================================================================== C interface
@@ -1785,6 +1786,9 @@ double orc_v_elem(void* b, const double* op, int herm, int a, int bb, int c, int
 double orc_f_elem(void* b, const double* op, int herm, int a, int bb) { return f_elem(*(Basis*)b, op, herm, a, bb); }
 
 void orc_random_op(void* b, uint64_t seed, int herm, double* op) { random_op(*(Basis*)b, seed, herm, op); }
+void orc_synthetic_bare(void* b, uint64_t seed, double v_scale, double* H) {
+  synthetic_bare(*(Basis*)b, seed, v_scale, H);
+}
 
 double orc_commutator_110(void* b, const double* L, int hL, const double* R, int hR) {
   return comm110(*(Basis*)b, L, hL, R, hR);

@@ -56,6 +56,7 @@ def lib():
         "orc_v_elem": (d, [vp, _dp, i, i, i, i, i, i]),
         "orc_f_elem": (d, [vp, _dp, i, i, i]),
         "orc_random_op": (None, [vp, u64, i, _dp]),
+        "orc_synthetic_bare": (None, [vp, u64, d, _dp]),
         "orc_commutator_110": (d, [vp, _dp, i, _dp, i]),
         "orc_commutator_220": (d, [vp, _dp, i, _dp, i]),
         "orc_commutator_111": (None, [vp, _dp, i, _dp, i, _dp, i]),
@@ -190,6 +191,13 @@ class Oracle:
         return x
 
     # pieces ---------------------------------------------------------------
+    def synthetic_bare_hamiltonian(self, seed: int = 1, v_scale: float = 1.0) -> np.ndarray:
+        """The seeded synthetic bare Hamiltonian (me2j-layout records converted to the pn
+        J-scheme, HO kinetic energy, E0 = 0): the oracle's own restatement of the input."""
+        x = self.new()
+        self.L.orc_synthetic_bare(self.h, seed, v_scale, x)
+        return x
+
     def v_elem(self, op, herm, a, b, c, d, J):
         return self.L.orc_v_elem(self.h, op, herm, a, b, c, d, J)
 

@@ -1,8 +1,8 @@
 """The launch-configuration autotuner of the mixed commutator (imsrg_autotune).
 
-Every candidate configuration computes the same commutator: the 122 sub-block partition,
-the recoupling grid and the GEMM tile order change how work is spread over the GPU, not
-what any output element sums.  So the result after tuning is bit-identical to the one
+Every candidate configuration computes the same commutator: the 122 sub-block partition
+and the GEMM tile shape and order change how work is spread over the GPU, not what any
+output element sums (each output tile accumulates its K blocks in the same order).  So the result after tuning is bit-identical to the one
 before, and a Magnus step replayed from the re-captured graph still equals the eager step.
 """
 import numpy as np
@@ -22,7 +22,9 @@ def test_autotune_keeps_results_and_reports_choice(built_lib, oracles):
     before = dR.download()
     info = eng.autotune(dA, dB, dR)
     assert (info["tiny_cap"], info["small_cap"]) in {(16, 256), (32, 128), (32, 256), (64, 256), (64, 512)}
-    assert info["gemm_order"] in (0, 1) and info["recouple_ctas"] > 0 and info["recouple_min_blocks"] in (4, 5, 6, 8)
+    assert info["gemm_order"] in (0, 1) and info["recouple_ctas"] > 0
+    assert info["gemm_wmax"] in (128, 256) and info["gemm_narrow"] in (0, 1)
+    assert info["recouple_kind"] in (0, 1) and info["recouple_min_blocks"] in (0, 4, 6, 8)
     assert info["ms_before"] > 0 and info["ms_after"] > 0
     eng.commutator(dA, dB, dR)
     assert np.array_equal(dR.download(), before)

@@ -1,7 +1,10 @@
-"""Mixed-precision (split-BF16 on tcgen05, FP32 gathers) against the FP64 oracle.
+"""Mixed-precision (split operands on tcgen05, FP32 gathers) against the FP64 oracle.
 
-The mixed path is held to FP32-level agreement: 3-slice BF16 (6 products) to 2e-5
-relative per array group, 2-slice (3 products) to 2e-3.
+The mixed path is held to FP32-level agreement.  The tolerances (largest error per array
+group relative to that group's largest element) are about ten times the errors observed on
+GB300 at each eMax: 3-slice BF16 (6 products) and TF32-compensated (3 products) carry ~24 and
+~22 operand bits and end up at the FP32 level of the gathers; 2-slice BF16 (3 products)
+carries ~16 bits in the ladder products.
 """
 import numpy as np
 import pytest
@@ -9,7 +12,10 @@ import pytest
 from helpers import rel_err, sections
 
 pytestmark = pytest.mark.gpu
-TOL = {"bf16x6": 2e-5, "bf16x3": 2e-3}
+TOL = {("bf16x6", 2): 6e-6, ("bf16x6", 4): 5e-6, ("bf16x6", 6): 2e-5,
+       ("bf16x3", 2): 9e-5, ("bf16x3", 4): 6e-5, ("bf16x3", 6): 5e-5,
+       ("tf32x3", 2): 6e-6, ("tf32x3", 4): 5e-6, ("tf32x3", 6): 2e-5}
+MODES = ["bf16x6", "bf16x3", "tf32x3"]
 
 
 @pytest.fixture(scope="module")
@@ -25,7 +31,7 @@ def mixed_engines(built_lib):
     return get
 
 
-@pytest.mark.parametrize("mode", ["bf16x6", "bf16x3"])
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("emax", [2, 4])
 def test_tc_pphh_intermediates(oracles, mixed_engines, emax, mode):
     o, eng = oracles(emax), mixed_engines(emax, mode)
@@ -36,12 +42,14 @@ def test_tc_pphh_intermediates(oracles, mixed_engines, emax, mode):
     dw1, dw2, dRES = eng.new_op(1), eng.new_op(1), eng.new_op(1)
     eng.commutator_222_pp_hh(dL, dR, dRES, dw1, dw2)
     eng.synchronize()
-    assert rel_err(dw1.download(), w1) <= TOL[mode]
-    assert rel_err(dw2.download(), w2) <= TOL[mode]
-    assert rel_err(dRES.download(), ref) <= TOL[mode]
+    print(f"eMax={emax} {mode} pphh: w1 {rel_err(dw1.download(), w1):.2e} w2 {rel_err(dw2.download(), w2):.2e} "
+          f"RES {rel_err(dRES.download(), ref):.2e}")
+    assert rel_err(dw1.download(), w1) <= TOL[mode, emax]
+    assert rel_err(dw2.download(), w2) <= TOL[mode, emax]
+    assert rel_err(dRES.download(), ref) <= TOL[mode, emax]
 
 
-@pytest.mark.parametrize("mode", ["bf16x6", "bf16x3"])
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("emax", [2, 4, 6])
 def test_mixed_full_commutator(oracles, mixed_engines, emax, mode):
     o, eng = oracles(emax), mixed_engines(emax, mode)
@@ -53,6 +61,8 @@ def test_mixed_full_commutator(oracles, mixed_engines, emax, mode):
     got = dRES.download()
     e0, ob, tb = sections(o, got)
     r0, rob, rtb = sections(o, ref)
-    assert abs(e0 - r0) <= TOL[mode] * max(1.0, abs(r0))
-    assert rel_err(ob, rob) <= TOL[mode]
-    assert rel_err(tb, rtb) <= TOL[mode]
+    print(f"eMax={emax} {mode} mixed [L,R]: E0 {abs(e0 - r0) / max(1.0, abs(r0)):.2e} 1b {rel_err(ob, rob):.2e} "
+          f"2b {rel_err(tb, rtb):.2e}")
+    assert abs(e0 - r0) <= TOL[mode, emax] * max(1.0, abs(r0))
+    assert rel_err(ob, rob) <= TOL[mode, emax]
+    assert rel_err(tb, rtb) <= TOL[mode, emax]

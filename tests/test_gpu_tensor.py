@@ -43,12 +43,12 @@ def test_bch_tensor_matches_oracle(oracles, engines):
     assert abs(dQ.frob() - t.frob(ref)) <= 1e-12 * t.frob(ref)
 
 
-@pytest.mark.parametrize("mode,tol", [("bf16x6", 2e-6), ("bf16x3", 2e-5)])
+@pytest.mark.parametrize("mode,tol", [("bf16x6", 2e-6), ("bf16x3", 2e-5), ("tf32x3", 2e-6)])
 @pytest.mark.parametrize("emax,rank", [(4, 4), (4, 2)])
 def test_tensor_ladder_on_tensor_cores(oracles, emax, rank, mode, tol):
     """In a mixed mode the ladder's products through pp pairs and the cross-coupled products of
-    the particle-hole term run as split-BF16 tcgen05 GEMMs (FP32 accumulate); the rest of the
-    tensor commutator stays FP64."""
+    the particle-hole term run as split-BF16 or TF32-compensated tcgen05 GEMMs (FP32
+    accumulate); the rest of the tensor commutator stays FP64."""
     from imsrg_gb300 import Engine, make_basis
     from oracle.oracle import TensorOracle
     o = oracles(emax)
