@@ -322,6 +322,43 @@ def reference_arm(args):
     }), flush=True)
 
 
+def commutator_workload(args, local: int):
+    """K eager [eta, H] commutators at eMax (default 10) on the HF state, after W warm-up ones, in the
+    mixed mode with a given launch configuration (--tuning) or the autotuner's: the unit of the
+    metric on its own, for profiling (an ncu launch list then holds one commutator's kernels per
+    K)."""
+    from imsrg_gb300 import Engine, make_basis
+    emax = args.emax if args.emax is not None else 10
+    b = make_basis(emax)
+    eng = Engine(b, device=local, precision=args.mode)
+    H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1)
+    dH, dE, dR = eng.new_op(1, H), eng.new_op(-1), eng.new_op(1)
+    eng.build_gs_white(dH, dE)
+    if args.tuning:
+        tune = json.loads(args.tuning)
+        eng.set_tuning(tune)
+    else:
+        tune = eng.autotune(dE, dH, dR)
+    for _ in range(max(args.warmup, 1)):
+        eng.commutator(dE, dH, dR)
+    eng.synchronize()
+    l0 = eng.launch_count()
+    eng.timer_begin()
+    for _ in range(args.steps):
+        eng.commutator(dE, dH, dR)
+    ms = eng.timer_end()
+    print(json.dumps({
+        "metric": f"IMSRG(2) commutators/s at eMax={emax}, eager [eta,H]", "value": args.steps / (ms * 1e-3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "tf32" if args.mode == "tf32x3" else "bf16", "data": "synthetic",
+        "config": {"workload": f"eager [eta,H] commutators at eMax={emax} ({b.norbits} orbits) on the "
+                               f"{args.reference.upper()} state, {args.mode}", "reference_state": hf_rec,
+                   "autotune": tune},
+        "gpu_launches": eng.launch_count() - l0,
+    }), flush=True)
+
+
 def adjoint_workload(args, local: int):
     """dE0/dtheta through a FP64 Magnus flow by the device adjoint, checked against central
     finite differences of the same flow: H(theta) = H0 + sum_k theta_k V_k with K seeded
@@ -791,8 +828,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--emax", type=int, default=None, help="default 10 (flow), 6 (adjoint)")
-    ap.add_argument("--workload", default="flow", choices=["flow", "adjoint", "observables", "precision", "hf-flow", "eom",
-                                                     "triples", "ode"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "commutator", "adjoint", "observables", "precision",
+                                                         "hf-flow", "eom", "triples", "ode"])
     ap.add_argument("--precision-flow-steps", type=int, default=20)
     ap.add_argument("--obs-bch-max-terms", type=int, default=40)
     ap.add_argument("--adjoint-k", type=int, default=16)
@@ -810,12 +847,14 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--tuning", default=None,
+                    help="apply this launch configuration (JSON, as config.autotune reports it) instead of tuning")
     ap.add_argument("--reference", default="hf", choices=["hf", "ho"],
                     help="reference state of the flow: calc_HF (default) or calc_HO")
     args = ap.parse_args()
     args.e2e_steps = max(1, args.e2e_steps)
     if args.mode is None:
-        args.mode = "bf16x3" if args.workload == "flow" else "bf16x6"
+        args.mode = "bf16x3" if args.workload in ("flow", "commutator") else "bf16x6"
     world, rank, local, pg = dist_setup()
 
     if args.emax is None and args.workload == "flow":
@@ -829,6 +868,10 @@ def main():
     if args.workload == "adjoint":
         if rank == 0:
             adjoint_workload(args, local)
+        return
+    if args.workload == "commutator":
+        if rank == 0:
+            commutator_workload(args, local)
         return
     if args.workload == "hf-flow":
         if rank == 0:
@@ -876,7 +919,10 @@ def main():
     H, _, hf_rec = prepared_hamiltonian(eng, args.reference, seed=1, time_transform=True)
     # the library's autotuner picks the launch configuration on [eta, H] of this basis
     tune = None
-    if not args.no_autotune:
+    if args.tuning:
+        tune = json.loads(args.tuning)
+        eng.set_tuning(tune)
+    elif not args.no_autotune:
         tH, tE, tR = eng.new_op(1, H), eng.new_op(-1), eng.new_op(1)
         eng.build_gs_white(tH, tE)
         tune = eng.autotune(tE, tH, tR)

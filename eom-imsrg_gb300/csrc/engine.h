@@ -183,7 +183,7 @@ struct Ctx {
   imsrg_status tc_pphh(const double* L, int hL, const double* R, int hR, double* w1, double* w2);
   imsrg_status tc_wcc(const double* lcc, const double* rcc, double* wcc);
   imsrg_status tc_gemm(const imsrg::TcProb* probs, const imsrg::TcTile* tiles, int ntiles, imsrg::TcOut out, int hL,
-                       int hR);
+                       int hR, int wmax);
   imsrg_status tc_error();
   imsrg_status tc_commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
   void tc_release();
@@ -197,7 +197,7 @@ struct Ctx {
   int tc_elem_bytes() const;  // bytes per operand value (2 BF16, 4 TF32)
   int tc_kind() const;        // operand type of the slices (0 BF16, 1 TF32)
   imsrg_status tc_g122_partition(int tiny_cap, int small_cap);
-  imsrg_status tc_set_tiles(int wmax, bool narrow, int order);
+  imsrg_status tc_set_tiles(const int* wmax, const bool* narrow, int order);
   imsrg_status tc_autotune(const double* L, int hL, const double* R, int hR, double* RES, imsrg_tune_info* info);
 };
 

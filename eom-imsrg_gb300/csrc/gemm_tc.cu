@@ -532,8 +532,11 @@ struct TcState {
   int g122_tiny_cap = 64, g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
   // tuned launch parameters (imsrg_autotune): GEMM tile order and shape
   int gemm_order = 0;  // 0: longest K first, 1: problem order
-  int wmax = 128;      // widest output tile of the persistent GEMM (128 or 256 columns)
-  bool narrow = true;  // last column tile of a problem only as wide as needed (multiple of 16)
+  // tile shape of each list: widest output tile (128 or 256 columns) and narrow last column
+  // tiles (only as wide as needed, a multiple of 16): [0] ladder, [1] X, [2] merged
+  int wmax[3] = {128, 128, 128};
+  bool narrow[3] = {true, true, true};
+  bool merged = true;  // ladder and X products in one launch (else two launches)
   // the merged list of one commutator: the K = npp ladder problems, then the X problems, in one
   // persistent launch (tile lists in device memory sized for the largest tile count)
   std::vector<TcProb> all_probs;
@@ -838,8 +841,8 @@ imsrg_status Ctx::tc_prepare(int mode) {
   return IMSRG_OK;
 }
 
-imsrg_status Ctx::tc_gemm(const TcProb* probs, const TcTile* tiles, int ntiles, TcOut out, int hL, int hR) {
-  return tc_gemm_on(tc->tmap, tc->slice_rows, probs, tiles, ntiles, out, hL, hR, tc->wmax);
+imsrg_status Ctx::tc_gemm(const TcProb* probs, const TcTile* tiles, int ntiles, TcOut out, int hL, int hR, int wmax) {
+  return tc_gemm_on(tc->tmap, tc->slice_rows, probs, tiles, ntiles, out, hL, hR, wmax);
 }
 
 int Ctx::tc_slices() const { return tc ? tc->S : 0; }
@@ -939,7 +942,7 @@ imsrg_status Ctx::tc_pphh(const double* Lp, int hL, const double* Rp, int hR, do
   TcOut out{};
   out.f64[kOpW1] = w1;
   out.f64[kOpW2] = w2;
-  CK_TC(tc_gemm(tc->d_pphh_probs, tc->d_pphh_tiles, (int)tc->pphh_tiles.size(), out, hL, hR));
+  CK_TC(tc_gemm(tc->d_pphh_probs, tc->d_pphh_tiles, (int)tc->pphh_tiles.size(), out, hL, hR, tc->wmax[0]));
   mark(kPhasePphhGemm);
   if (!tc->small_tiles.empty()) {
     GemmOperands ops{};
@@ -994,13 +997,15 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   if (!tc->chunks.empty()) CK_TC(tc_split_on(tc->d_split_ops, tc->d_chunks, (int)tc->chunks.size(), Lp, Rp, tc->buf,
                                              tc->slice_elems));
   mark(kPhasePphhSplit);
-  {
-    TcOut out{};
-    out.f64[kOpW1] = d_w1;
-    out.f64[kOpW2] = d_w2;
-    out.f32 = tc->zbuf;
-    CK_TC(tc_gemm(tc->d_all_probs, tc->d_tile_mem + tc->tile_cap_all, (int)tc->all_tiles.size(), out, hL, hR));
-  }
+  TcOut gout{};
+  gout.f64[kOpW1] = d_w1;
+  gout.f64[kOpW2] = d_w2;
+  gout.f32 = tc->zbuf;
+  if (tc->merged)
+    CK_TC(tc_gemm(tc->d_all_probs, tc->d_tile_mem + tc->tile_cap_all, (int)tc->all_tiles.size(), gout, hL, hR,
+                  tc->wmax[2]));
+  else
+    CK_TC(tc_gemm(tc->d_pphh_probs, tc->d_pphh_tiles, (int)tc->pphh_tiles.size(), gout, hL, hR, tc->wmax[0]));
   mark(kPhasePphhGemm);
   if (with_e0) CK_TC(e0(Lp, hL, Rp, hR, RES, nullptr));
   CK_TC(c111(Lp, hL, Rp, hR, RES));
@@ -1047,6 +1052,10 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   CK_TC(pphh_accumulate(hL, hR, RES, d_w1, d_w2, true));
   CK_TC(c221(hL, hR, RES, hRES, d_w1, d_w2, true));
   mark(kPhase221);
+  if (!tc->merged) {
+    CK_TC(tc_gemm(tc->d_z_probs, tc->d_z_tiles, (int)tc->z_tiles.size(), gout, hL, hR, tc->wmax[1]));
+    mark(kPhasePhGemm);
+  }
   if (!tc->quads.empty()) {
     if (tc->recouple_kind == 0) {
       launch_recouple_g(tc->rc, stream, D, tc->d_rc_tasks, tc->d_rc_groups, tc->d_rc_triples, tc->d_rc_table,
@@ -1104,22 +1113,24 @@ imsrg_status Ctx::tc_g122_partition(int tiny_cap, int small_cap) {
   return IMSRG_OK;
 }
 
-// Tile lists of the persistent GEMMs for a tile shape and order: widest tile wmax (128, or 256
-// with two slices), narrow last column tiles or not, and order 0 = longest K first (LPT),
-// 1 = problem order.  No output element depends on these choices.
-imsrg_status Ctx::tc_set_tiles(int wmax, bool narrow, int order) {
-  if (wmax != 128 && !(wmax == 256 && tc->S == 2)) return fail(IMSRG_ERR_INVALID_ARGUMENT, "unsupported tile width");
-  auto build = [&](const std::vector<TcProb>& probs) {
-    std::vector<TcTile> t = make_tiles(probs, wmax, narrow);
+// Tile lists of the persistent GEMMs for their tile shapes and an order: per list ([0] ladder,
+// [1] X, [2] the merged list) the widest tile wmax (128, or 256 with two slices) and narrow last
+// column tiles or not; order 0 = longest K first (LPT), 1 = problem order.  No output element
+// depends on these choices.
+imsrg_status Ctx::tc_set_tiles(const int* wmax, const bool* narrow, int order) {
+  for (int x = 0; x < 3; ++x)
+    if (wmax[x] != 128 && !(wmax[x] == 256 && tc->S == 2)) return fail(IMSRG_ERR_INVALID_ARGUMENT, "unsupported tile width");
+  auto build = [&](const std::vector<TcProb>& probs, int x) {
+    std::vector<TcTile> t = make_tiles(probs, wmax[x], narrow[x]);
     if (order == 1)
       std::stable_sort(t.begin(), t.end(), [](const TcTile& a, const TcTile& b) {
         return a.prob != b.prob ? a.prob < b.prob : (a.m0 != b.m0 ? a.m0 < b.m0 : a.n0 < b.n0);
       });
     return t;
   };
-  tc->pphh_tiles = build(tc->pphh_probs);
-  tc->z_tiles = build(tc->z_probs);
-  tc->all_tiles = build(tc->all_probs);
+  tc->pphh_tiles = build(tc->pphh_probs, 0);
+  tc->z_tiles = build(tc->z_probs, 1);
+  tc->all_tiles = build(tc->all_probs, 2);
   if (tc->pphh_tiles.size() > tc->tile_cap_pphh || tc->z_tiles.size() > tc->tile_cap_z ||
       tc->all_tiles.size() > tc->tile_cap_all)
     return fail(IMSRG_ERR_MISMATCH, "GEMM tile list larger than its allocation");
@@ -1133,8 +1144,10 @@ imsrg_status Ctx::tc_set_tiles(int wmax, bool narrow, int order) {
   CK_TC(put(tc->d_tile_mem + tc->tile_cap_pphh, tc->z_tiles));
   CK_TC(put(d_all, tc->all_tiles));
   CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize(GEMM tiles)"));
-  tc->wmax = wmax;
-  tc->narrow = narrow;
+  for (int x = 0; x < 3; ++x) {
+    tc->wmax[x] = wmax[x];
+    tc->narrow[x] = narrow[x];
+  }
   tc->gemm_order = order;
   return IMSRG_OK;
 }
@@ -1198,22 +1211,47 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
       tc->recouple_minb = bm;
       tc->recouple_ctas = bc;
     }
-    // tensor-core GEMM: tile shape (widest tile, narrow last tiles) and tile order, jointly
+    // tensor-core GEMM: one merged launch with its tile shape, or two launches with a tile shape
+    // each (the ladder's first, then X's), and the tile order
     {
-      int bw = tc->wmax, bo = tc->gemm_order;
-      bool bn = tc->narrow;
-      for (int wmax : {128, 256}) {
-        if (wmax == 256 && tc->S != 2) continue;
-        for (int narrow = 0; narrow < 2 && st == IMSRG_OK; ++narrow)
-          for (int order : {0, 1}) {
-            if ((st = tc_set_tiles(wmax, narrow != 0, order)) != IMSRG_OK) break;
-            float ms;
-            if ((st = time_one(&ms)) != IMSRG_OK) break;
-            if (ms < best) { best = ms; bw = wmax; bn = narrow != 0; bo = order; }
+      std::vector<std::pair<int, bool>> shapes = {{128, false}, {128, true}};
+      if (tc->S == 2) { shapes.push_back({256, false}); shapes.push_back({256, true}); }
+      int bw[3], bo = tc->gemm_order;
+      bool bn[3], bmg = tc->merged;
+      for (int x = 0; x < 3; ++x) { bw[x] = tc->wmax[x]; bn[x] = tc->narrow[x]; }
+      auto trial = [&](bool merged, const int* w, const bool* n, int order) -> imsrg_status {
+        tc->merged = merged;
+        CK_TC(tc_set_tiles(w, n, order));
+        float ms;
+        CK_TC(time_one(&ms));
+        if (ms < best) {
+          best = ms;
+          bmg = merged;
+          bo = order;
+          for (int x = 0; x < 3; ++x) { bw[x] = w[x]; bn[x] = n[x]; }
+        }
+        return IMSRG_OK;
+      };
+      for (int order : {0, 1}) {
+        for (const auto& sh : shapes) {  // merged
+          int w[3] = {bw[0], bw[1], sh.first};
+          bool n[3] = {bn[0], bn[1], sh.second};
+          if ((st = trial(true, w, n, order)) != IMSRG_OK) break;
+        }
+        if (st != IMSRG_OK) break;
+        for (int list = 0; list < 2 && st == IMSRG_OK; ++list)  // separate: ladder shape, then X shape
+          for (const auto& sh : shapes) {
+            int w[3] = {bw[0], bw[1], bw[2]};
+            bool n[3] = {bn[0], bn[1], bn[2]};
+            w[list] = sh.first;
+            n[list] = sh.second;
+            if ((st = trial(false, w, n, order)) != IMSRG_OK) break;
           }
         if (st != IMSRG_OK) break;
       }
-      if (st != IMSRG_OK || (st = tc_set_tiles(bw, bn, bo)) != IMSRG_OK) break;
+      if (st != IMSRG_OK) break;
+      tc->merged = bmg;
+      if ((st = tc_set_tiles(bw, bn, bo)) != IMSRG_OK) break;
     }
     float after = 0.0f;
     if ((st = time_one(&after)) != IMSRG_OK) break;
@@ -1223,8 +1261,12 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
       info->recouple_kind = tc->recouple_kind;
       info->recouple_min_blocks = tc->recouple_kind ? tc->recouple_minb : 0;
       info->recouple_ctas = tc->recouple_kind ? tc->recouple_ctas : (int32_t)tc->rc.tasks.size();
-      info->gemm_wmax = tc->wmax;
-      info->gemm_narrow = tc->narrow ? 1 : 0;
+      const int gl = tc->merged ? 2 : 0;
+      info->gemm_wmax = tc->wmax[gl];
+      info->gemm_narrow = tc->narrow[gl] ? 1 : 0;
+      info->gemm_wmax_x = tc->wmax[1];
+      info->gemm_narrow_x = tc->narrow[1] ? 1 : 0;
+      info->gemm_merged = tc->merged ? 1 : 0;
       info->gemm_order = tc->gemm_order;
       info->ms_before = base;
       info->ms_after = after;
@@ -1249,6 +1291,39 @@ extern "C" imsrg_status imsrg_recouple_traffic(imsrg_ctx* ctx, int64_t* x_reads,
   *x_distinct = t.x_distinct;
   *res_elems = t.res_elems;
   *aux_bytes = t.aux_bytes;
+  return IMSRG_OK;
+}
+
+extern "C" imsrg_status imsrg_set_tuning(imsrg_ctx* ctx, const imsrg_tune_info* cfg) {
+  if (!ctx || !cfg) return IMSRG_ERR_INVALID_ARGUMENT;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  if (c->device < 0) return c->fail(IMSRG_ERR_UNSUPPORTED, "host-only context (device < 0)");
+  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(IMSRG_ERR_CUDA, "cudaSetDevice");
+  if (c->precision == IMSRG_PREC_FP64) return c->fail(IMSRG_ERR_UNSUPPORTED, "tuning applies to the mixed modes");
+  if (cfg->recouple_kind < 0 || cfg->recouple_kind > 1 || cfg->gemm_order < 0 || cfg->gemm_order > 1 ||
+      (cfg->recouple_kind == 1 && (cfg->recouple_ctas < 1 || (cfg->recouple_min_blocks != 4 &&
+                                                              cfg->recouple_min_blocks != 6 &&
+                                                              cfg->recouple_min_blocks != 8))))
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_set_tuning: value out of range");
+  CK_TC(c->ensure_workspace());
+  CK_TC(c->tc_prepare(c->precision));
+  CK_TC(c->tc_g122_partition(cfg->tiny_cap, cfg->small_cap));
+  {
+    const bool m = cfg->gemm_merged != 0;
+    const int wx = cfg->gemm_wmax_x ? cfg->gemm_wmax_x : cfg->gemm_wmax;
+    int w[3] = {cfg->gemm_wmax, wx, cfg->gemm_wmax};
+    bool n[3] = {cfg->gemm_narrow != 0, (cfg->gemm_wmax_x ? cfg->gemm_narrow_x : cfg->gemm_narrow) != 0,
+                 cfg->gemm_narrow != 0};
+    if (m) { w[0] = c->tc->wmax[0]; n[0] = c->tc->narrow[0]; w[1] = c->tc->wmax[1]; n[1] = c->tc->narrow[1]; }
+    CK_TC(c->tc_set_tiles(w, n, cfg->gemm_order));
+    c->tc->merged = m;
+  }
+  c->tc->recouple_kind = cfg->recouple_kind;
+  if (cfg->recouple_kind == 1) {
+    c->tc->recouple_minb = cfg->recouple_min_blocks;
+    c->tc->recouple_ctas = cfg->recouple_ctas;
+  }
+  c->graph_release();
   return IMSRG_OK;
 }
 

@@ -41,7 +41,8 @@ class TuneInfo_t(C.Structure):
     _fields_ = [("tiny_cap", C.c_int32), ("small_cap", C.c_int32), ("recouple_ctas", C.c_int32),
                 ("gemm_order", C.c_int32), ("gemm_wmax", C.c_int32), ("gemm_narrow", C.c_int32),
                 ("ms_before", C.c_double), ("ms_after", C.c_double), ("recouple_kind", C.c_int32),
-                ("recouple_min_blocks", C.c_int32)]
+                ("recouple_min_blocks", C.c_int32), ("gemm_merged", C.c_int32), ("gemm_wmax_x", C.c_int32),
+                ("gemm_narrow_x", C.c_int32)]
 
 
 class StepInfo_t(C.Structure):
@@ -149,6 +150,7 @@ SIGNATURES = {
     "imsrg_profile_read": [_vp, C.POINTER(C.c_float), _pi32],
     "imsrg_mat_frob_norm_noalloc": [_vp, _vp, _vp, _vp],
     "imsrg_set_wait_limit": [_vp, _i64],
+    "imsrg_set_tuning": [_vp, _vp],
     "imsrg_recouple_traffic": [_vp, _pi64, _pi64, _pi64, _pi64],
     "imsrg_test_unarmed_stage": [_vp, _i32],
 }

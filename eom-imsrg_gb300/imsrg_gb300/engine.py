@@ -212,6 +212,14 @@ class Engine:
         self._ck(self.L.imsrg_autotune(self.h, L.h, R.h, RES.h, C.byref(info)))
         return {k: getattr(info, k) for k, _ in _lib.TuneInfo_t._fields_}
 
+    def set_tuning(self, cfg: dict):
+        """Apply a launch configuration (a dict as autotune() returns; imsrg_set_tuning)."""
+        info = _lib.TuneInfo_t()
+        for k, _ in _lib.TuneInfo_t._fields_:
+            if k in cfg:
+                setattr(info, k, cfg[k])
+        self._ck(self.L.imsrg_set_tuning(self.h, C.byref(info)))
+
     def synchronize(self):
         self._ck(self.L.imsrg_synchronize(self.h))
 

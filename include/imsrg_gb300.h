@@ -111,21 +111,28 @@ imsrg_status imsrg_recouple_traffic(imsrg_ctx* ctx, int64_t* x_reads, int64_t* x
  * thread per orbit quadruple with its occupancy variant and CTA count); then, jointly, the tile
  * shape of the persistent tcgen05 GEMM
  * (widest output tile 128 or 256 columns, and whether the last column tile of a problem is only
- * as wide as its columns need, in steps of 16) and its tile order.  The result of a commutator
+ * as wide as its columns need, in steps of 16), its tile order, and whether the ladder and the
+ * particle-hole products share one launch.  The result of a commutator
  * does not depend on these choices.  A captured Magnus-step graph is dropped and re-captured
  * by the next step.  IMSRG_ERR_UNSUPPORTED in FP64 mode. */
 typedef struct {
   int32_t tiny_cap, small_cap; /* sub-blocks up to tiny_cap elements: 8 lanes; up to small_cap: a warp */
   int32_t recouple_ctas;       /* CTAs of the recoupling kernel (grouped: one per task of its plan) */
   int32_t gemm_order;          /* 0: tiles with the longest K first, 1: problem order */
-  int32_t gemm_wmax;           /* widest output tile of the tensor-core GEMM: 128 or 256 columns */
-  int32_t gemm_narrow;         /* 1: narrow last column tiles (multiples of 16 columns) */
+  int32_t gemm_wmax;           /* widest output tile of the ladder launch (of the merged launch): 128 or 256 */
+  int32_t gemm_narrow;         /* 1: narrow last column tiles (multiples of 16 columns) in that launch */
   double ms_before, ms_after;  /* one commutator before and after tuning */
   int32_t recouple_kind;       /* 0: recoupling by (i, k, l) groups, 1: one thread per orbit quadruple */
   int32_t recouple_min_blocks; /* per-quadruple kernel: launch-bounds variant (4, 6 or 8 CTAs per SM) */
+  int32_t gemm_merged;         /* 1: ladder and particle-hole products in one launch, 0: two launches */
+  int32_t gemm_wmax_x;         /* two launches: widest tile of the particle-hole (X) launch (0: as gemm_wmax) */
+  int32_t gemm_narrow_x;       /* two launches: narrow last tiles in the X launch */
 } imsrg_tune_info;
 imsrg_status imsrg_autotune(imsrg_ctx* ctx, const imsrg_op* L, const imsrg_op* R, imsrg_op* RES,
                             imsrg_tune_info* info);
+/* Applies a configuration (for instance one that imsrg_autotune reported on an earlier run of
+ * this basis) without timing anything; ms_before / ms_after are ignored.  Mixed modes only. */
+imsrg_status imsrg_set_tuning(imsrg_ctx* ctx, const imsrg_tune_info* cfg);
 
 /* ---- instrumentation (no reference counterpart: the reference only prints wall time,
  *      print_time, src/basic_IMSRG.f90:152-169) */

@@ -11,11 +11,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_autotune_keeps_results_and_reports_choice(built_lib, oracles):
+@pytest.mark.parametrize("mode", ["bf16x6", "bf16x3"])
+def test_autotune_keeps_results_and_reports_choice(built_lib, oracles, mode):
     from imsrg_gb300 import Engine, make_basis
     from imsrg_gb300._lib import ImsrgError
     o = oracles(4)
-    eng = Engine(make_basis(4), device=0, precision="bf16x6")
+    eng = Engine(make_basis(4), device=0, precision=mode)
     A, B = o.random(21, -1), o.random(22, 1)
     dA, dB, dR = eng.new_op(-1, A), eng.new_op(1, B), eng.new_op(1)
     eng.commutator(dA, dB, dR)
@@ -25,9 +26,24 @@ def test_autotune_keeps_results_and_reports_choice(built_lib, oracles):
     assert info["gemm_order"] in (0, 1) and info["recouple_ctas"] > 0
     assert info["gemm_wmax"] in (128, 256) and info["gemm_narrow"] in (0, 1)
     assert info["recouple_kind"] in (0, 1) and info["recouple_min_blocks"] in (0, 4, 6, 8)
+    assert info["gemm_merged"] in (0, 1)
     assert info["ms_before"] > 0 and info["ms_after"] > 0
     eng.commutator(dA, dB, dR)
     assert np.array_equal(dR.download(), before)
+    # every other choice of each knob, applied with imsrg_set_tuning, still gives the same bits
+    for change in ({"recouple_kind": 1 - info["recouple_kind"], "recouple_min_blocks": 6, "recouple_ctas": 152 * 8},
+                   {"gemm_merged": 1 - info["gemm_merged"]}, {"gemm_narrow": 1 - info["gemm_narrow"]},
+                   {"gemm_order": 1 - info["gemm_order"]},
+                   {"gemm_wmax": 384 - info["gemm_wmax"]} if mode == "bf16x3" else {},
+                   {"gemm_merged": 0, "gemm_wmax_x": 384 - max(info["gemm_wmax_x"], 128),
+                    "gemm_narrow_x": 1 - info["gemm_narrow_x"]} if mode == "bf16x3" else {},
+                   {"tiny_cap": 16, "small_cap": 128}):
+        cfg = dict(info)
+        cfg.update(change)
+        eng.set_tuning(cfg)
+        eng.commutator(dA, dB, dR)
+        assert np.array_equal(dR.download(), before), change
+    eng.set_tuning(info)
     # graph replay after tuning equals the eager step
     H = eng.synthetic_hamiltonian(seed=3)
     states = []
