@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include")]
 SOURCES = ["layout.cpp", "gemm_plan.cpp", "hamiltonian.cpp", "engine.cu", "kernels_fp64.cu", "kernels_ops.cu",
-           "gemm_fp64.cu", "gemm_tc.cu", "kernels_mixed.cu", "recouple.cu", "noalloc.cu", "graph.cu", "adjoint.cu", "kernels_adjoint.cu", "tensor_layout.cpp", "tensor.cu", "hf.cu", "pair_groups.cpp", "checkpoint.cpp",
+           "gemm_fp64.cu", "gemm_tc.cu", "kernels_mixed.cu", "recouple.cu", "comm122.cu", "noalloc.cu", "graph.cu", "adjoint.cu", "kernels_adjoint.cu", "tensor_layout.cpp", "tensor.cu", "hf.cu", "pair_groups.cpp", "checkpoint.cpp",
            "kernels_tensor.cu", "eom.cu", "triples.cu", "quads.cu"]
 
 

@@ -192,7 +192,7 @@ __device__ __forceinline__ bool d_vref_f(const DevLayout& D, int a, int b, int c
 //   - magnitudes that round above FLT_MAX become +-Inf (the rounding carry runs from the
 //     mantissa into the exponent, and exponent field 255 with a zero mantissa is Inf);
 //   - magnitudes below FP32's normal range round to FP32 subnormals k * 2^-149, or +-0.
-__device__ __forceinline__ float f64_to_f32(double x) {
+__device__ __forceinline__ float f64_to_f32_any(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned int sign = (unsigned int)(b >> 63) << 31;
   const int e = (int)((b >> 52) & 0x7FF);
@@ -216,9 +216,24 @@ __device__ __forceinline__ float f64_to_f32(double x) {
   return __uint_as_float(sign | k);
 }
 
+// The same on FP32's normal range, inline: the FP64 exponent 897..1150 is rebiased, the top
+// 23 mantissa bits kept and the 29 below rounded off (round up above half, and at exactly
+// half when the kept value is odd: (rest + 2^28 - 1 + odd) >> 29).  Everything else (zeros,
+// subnormals, overflow, Inf, NaN) takes f64_to_f32_any.
+__device__ __forceinline__ float f64_to_f32(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned ah = hi & 0x7FFFFFFFu;
+  if (ah - (897u << 20) < (254u << 20)) {
+    unsigned v = ((ah - (896u << 20)) << 3) | (lo >> 29);
+    v += ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (v & 1u)) >> 29;
+    return __uint_as_float((hi & 0x80000000u) | v);
+  }
+  return f64_to_f32_any(x);
+}
+
 // FP32 -> FP64 (exact) with integer instructions only: zeros keep their sign, subnormals
 // are normalised, Inf and NaN (with its payload) carry over.
-__device__ __forceinline__ double f32_to_f64(float f) {
+__device__ __forceinline__ double f32_to_f64_any(float f) {
   const unsigned int u = __float_as_uint(f);
   const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
   const unsigned int e = (u >> 23) & 0xFF;
@@ -233,6 +248,14 @@ __device__ __forceinline__ double f32_to_f64(float f) {
   }
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023 - 127) << 52) |
                                           ((unsigned long long)m << 29)));
+}
+
+// The same for FP32 normal numbers, inline: exponent rebiased by 896, mantissa shifted up 29.
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  if ((u & 0x7F800000u) - 0x00800000u < 0x7F000000u)
+    return __hiloint2double((int)((u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + (896u << 20))), (int)(u << 29));
+  return f32_to_f64_any(f);
 }
 
 __device__ __forceinline__ float d_f_elem_f(const DevLayout& D, const double* op, int herm, int a, int b) {

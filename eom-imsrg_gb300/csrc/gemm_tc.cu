@@ -22,6 +22,7 @@
 #include "dev.cuh"
 #include "engine.h"
 #include "kernels.h"
+#include "comm122.h"
 #include "pair_groups.h"
 #include "recouple.h"
 #include "split.cuh"
@@ -519,17 +520,15 @@ struct TcState {
   const float* d_rc_table = nullptr;
   std::vector<SplitChunk> chunks;
   const SplitChunk* d_chunks = nullptr;
-  // commutator_122 by pair groups: sub-blocks of at most g122_small elements go one per warp,
-  // the larger ones one per CTA (tasks in channel order, so a channel's L and R stay in L2)
-  // (tiny sub-blocks, up to g122_tiny elements, go to 8-lane groups, four per warp)
-  // All tasks in channel order with their sizes; the device list holds them partitioned into
-  // [tiny | warp | cta] runs by the current caps (tc_g122_partition).
-  std::vector<int4> g122_all;
-  std::vector<int64_t> g122_elems;
-  int4* d_g122_tasks = nullptr;
-  int g122_ntiny = 0, g122_nwarp = 0, g122_ncta = 0;
-  PairGroupsDev g122_t{}, g122_w{}, g122_c{};
-  int g122_tiny_cap = 64, g122_small = 256, g122_nmax2 = 1, g122_nmax4 = 1, g122_nspb = 0, g122_nblk2 = 0;
+  // commutator_122 by pair-group sub-blocks (comm122.cu): the plan, its launch order for the
+  // current caps (tc_g122_partition) and its device copies (tasks and runs sized for all tasks)
+  G122Plan g122;
+  G122Task* d_g122_tasks = nullptr;
+  int2* d_g122_items = nullptr;
+  const int2* d_g122_pairs = nullptr;
+  int* d_g122_counter = nullptr;
+  PairGroupsDev g122_w{};
+  int g122_nspb = 0, g122_nblk2 = 0, g122_per_sm = 1;
   // tuned launch parameters (imsrg_autotune): GEMM tile order and shape
   int gemm_order = 0;  // 0: longest K first, 1: problem order
   // tile shape of each list: widest output tile (128 or 256 columns) and narrow last column
@@ -545,7 +544,7 @@ struct TcState {
   TcTile* d_tile_mem = nullptr;  // [pphh tiles | X tiles | merged tiles]
   size_t tile_cap_pphh = 0, tile_cap_z = 0, tile_cap_all = 0;
   std::vector<int> g_start, g_n, g_orb, g_b1, g_b2, g_blk_off;
-  float* g122_fb = nullptr;  // f(x, y) of L and R on every (l, j, tz) block
+  float2* g122_fb = nullptr;  // (fL, fR)(x, y) on every (l, j, tz) block
   int num_sms = 148;
 };
 
@@ -595,6 +594,8 @@ void Ctx::tc_release() {
   if (tc->d_err) cudaFree(tc->d_err);
   if (tc->g122_fb) cudaFree(tc->g122_fb);
   if (tc->d_g122_tasks) cudaFree(tc->d_g122_tasks);
+  if (tc->d_g122_items) cudaFree(tc->d_g122_items);
+  if (tc->d_g122_counter) cudaFree(tc->d_g122_counter);
   if (tc->d_tile_mem) cudaFree(tc->d_tile_mem);
   delete tc;
   tc = nullptr;
@@ -733,15 +734,8 @@ imsrg_status Ctx::tc_prepare(int mode) {
     tc->g_b1 = pg.grp_b1; tc->g_b2 = pg.grp_b2; tc->g_blk_off = pg.blk_off;
     tc->g122_nspb = pg.nspb;
     tc->g122_nblk2 = pg.nblk2;
-    tc->g122_nmax2 = pg.nmax * pg.nmax;
-    tc->g122_nmax4 = tc->g122_nmax2 * tc->g122_nmax2;
-    for (int q = 0; q < l.nblocks; ++q)
-      for (int G2 = pg.grp_first[q]; G2 < pg.grp_first[q + 1]; ++G2)
-        for (int G1 = pg.grp_first[q]; G1 <= G2; ++G1) {
-          const int4 t = make_int4(q, G1, G2, 0);
-          tc->g122_all.push_back(t);
-          tc->g122_elems.push_back(pg.elems(G1, G2));
-        }
+    const std::string e = build_g122_plan(l, pg, tc->g122);
+    if (!e.empty()) return fail(IMSRG_ERR_UNSUPPORTED, e);
   }
   // ---- recoupling quadruples: bra (i<=j) of class c1, ket (k<=l) of class c2, with
   //      c1 < c2, or c1 == c2 and (i,j) <= (k,l) (the unique stored elements), matching
@@ -783,7 +777,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   CK_TC(cuda(cudaMalloc(&tc->zbuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(X)"));
   CK_TC(cuda(cudaMemset(tc->zbuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(X)"));
   CK_TC(cuda(cudaMalloc(&tc->d_err, sizeof(int)), "cudaMalloc(err)"));
-  CK_TC(cuda(cudaMalloc(&tc->g122_fb, sizeof(float) * 2 * std::max(tc->g122_nblk2, 1)), "cudaMalloc(122 blocks)"));
+  CK_TC(cuda(cudaMalloc(&tc->g122_fb, sizeof(float2) * std::max(tc->g122_nblk2, 1)), "cudaMalloc(122 blocks)"));
   CK_TC(cuda(cudaMemset(tc->d_err, 0, sizeof(int)), "memset(err)"));
   DevPacker pk;
   pk.add(tc->split_ops, &tc->d_split_ops);
@@ -815,14 +809,18 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->g_b1, &tc->g122_w.grp_b1);
   pk.add(tc->g_b2, &tc->g122_w.grp_b2);
   pk.add(tc->g_blk_off, &tc->g122_w.blk_off);
+  pk.add(tc->g122.pairs, &tc->d_g122_pairs);
 
   CK_TC(cuda(cudaMalloc(&tc->d_mem, pk.buf.size()), "cudaMalloc(tc tables)"));
   CK_TC(cuda(cudaMemcpy(tc->d_mem, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tc tables)"));
   for (auto& f : pk.fix) *f.second = static_cast<const char*>(tc->d_mem) + f.first;
-  CK_TC(cuda(cudaMalloc(&tc->d_g122_tasks, sizeof(int4) * std::max<size_t>(tc->g122_all.size(), 1)),
+  CK_TC(cuda(cudaMalloc(&tc->d_g122_tasks, sizeof(G122Task) * std::max<size_t>(tc->g122.all.size(), 1)),
              "cudaMalloc(122 tasks)"));
-  tc->g122_t = tc->g122_c = tc->g122_w;
-  CK_TC(tc_g122_partition(tc->g122_tiny_cap, tc->g122_small));
+  CK_TC(cuda(cudaMalloc(&tc->d_g122_items, sizeof(int2) * std::max<size_t>(tc->g122.all.size(), 1)),
+             "cudaMalloc(122 runs)"));
+  CK_TC(cuda(cudaMalloc(&tc->d_g122_counter, sizeof(int)), "cudaMalloc(122 counter)"));
+  CK_TC(cuda(cudaMemset(tc->d_g122_counter, 0, sizeof(int)), "cudaMemset(122 counter)"));
+  CK_TC(tc_g122_partition(tc->g122.tiny_cap, tc->g122.warp_cap));
   tc->recouple_ctas = tc->num_sms * 32;
   // tile lists: the most tiles come with 128-wide tiles
   tc->tile_cap_pphh = make_tiles(tc->pphh_probs, 128, false).size();
@@ -1012,32 +1010,17 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   CK_TC(c121(Lp, hL, Rp, hR, RES, hRES));
   mark(kPhaseOneBody);
   if (L.n_unique) {
-    k_comm122_fblocks<<<tc->g122_nspb, 64, 0, stream>>>(D, tc->g122_w, tc->g122_nspb, tc->g122_nblk2, Lp, hL, Rp, hR,
-                                                         tc->g122_fb);
-    CK_TC(launched("k_comm122_fblocks"));
-    if (tc->g122_ntiny) {  // 8 lanes per task, 32 tasks per CTA
-      const int nt = tc->g122_ntiny;
-      const int grid = std::min((nt + 31) / 32, tc->num_sms * 8);
-      const size_t smem = sizeof(float) * 32 * (size_t)(2 * tc->g122_tiny_cap + 4 * tc->g122_nmax2);
-      launch_comm122_lanes(8, grid, smem, stream, D, tc->g122_t, nt, tc->g122_tiny_cap, tc->g122_nmax2, Lp, hL, Rp, hR,
-                           RES, hRES, tc->g122_fb, tc->g122_nblk2);
-      CK_TC(launched("k_comm122_groups_lanes<8>"));
-    }
-    if (tc->g122_nwarp) {  // a warp per task, 8 tasks per CTA
-      const int nt = tc->g122_nwarp;
-      const int grid = std::min((nt + 7) / 8, tc->num_sms * 8);
-      const size_t smem = sizeof(float) * 8 * (size_t)(2 * tc->g122_small + 4 * tc->g122_nmax2);
-      launch_comm122_lanes(32, grid, smem, stream, D, tc->g122_w, nt, tc->g122_small, tc->g122_nmax2, Lp, hL, Rp, hR,
-                           RES, hRES, tc->g122_fb, tc->g122_nblk2);
-      CK_TC(launched("k_comm122_groups_lanes<32>"));
-    }
-    if (tc->g122_ncta) {
-      const size_t smem = sizeof(float) * (size_t)(2 * tc->g122_nmax4 + 4 * tc->g122_nmax2);
-      k_comm122_groups_cta<<<tc->g122_ncta, 256, smem, stream>>>(D, tc->g122_c, tc->g122_nmax4,
-                                                                             tc->g122_nmax2, Lp, hL, Rp, hR, RES, hRES,
-                                                                             tc->g122_fb, tc->g122_nblk2);
-      CK_TC(launched("k_comm122_groups_cta"));
-    }
+    k_comm122_fb2<<<tc->g122_nspb, 64, 0, stream>>>(D, tc->g122_w, tc->g122_nspb, Lp, hL, Rp, hR, tc->g122_fb,
+                                                     tc->d_g122_counter);
+    CK_TC(launched("k_comm122_fb2"));
+    const G122Plan& P = tc->g122;
+    // the big tasks, then enough eight-warp CTAs to fill the GPU at the occupancy the shared
+    // memory allows (the warps take the runs from the counter)
+    const int grid = P.nbig + tc->num_sms * std::max(1, tc->g122_per_sm);
+    launch_comm122(grid, P.smem_bytes, stream, D, tc->d_g122_tasks, tc->d_g122_items, (int)P.items.size(), P.nbig,
+                   tc->d_g122_counter, tc->d_g122_pairs, std::max(P.warp_cap, 4 * P.tiny_cap), P.tiny_cap, Lp, hL,
+                   Rp, hR, RES, hRES, tc->g122_fb);
+    CK_TC(launched("k_comm122_sub"));
   }
   mark(kPhase122);
   if (!tc->small_tiles.empty()) {  // the K = nhh products (W2) on FP32 SIMT
@@ -1082,34 +1065,23 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
 // each run, and uploads the list.  The caps must keep the per-CTA shared memory of the
 // 8-lane and warp kernels within the 48 KiB default.
 imsrg_status Ctx::tc_g122_partition(int tiny_cap, int small_cap) {
-  const size_t lim = 48 * 1024;
-  if (tiny_cap < 1 || small_cap < tiny_cap ||
-      sizeof(float) * 32 * (size_t)(2 * tiny_cap + 4 * tc->g122_nmax2) > lim ||
-      sizeof(float) * 8 * (size_t)(2 * small_cap + 4 * tc->g122_nmax2) > lim)
-    return fail(IMSRG_ERR_INVALID_ARGUMENT, "122 task caps out of range");
-  const size_t n = tc->g122_all.size();
-  std::vector<int4> v;
-  v.reserve(n);
-  int nt = 0, nw = 0;
-  for (size_t i = 0; i < n; ++i)
-    if (tc->g122_elems[i] <= tiny_cap) { v.push_back(tc->g122_all[i]); ++nt; }
-  for (size_t i = 0; i < n; ++i)
-    if (tc->g122_elems[i] > tiny_cap && tc->g122_elems[i] <= small_cap) { v.push_back(tc->g122_all[i]); ++nw; }
-  for (size_t i = 0; i < n; ++i)
-    if (tc->g122_elems[i] > small_cap) v.push_back(tc->g122_all[i]);
-  if (n) {
-    CK_TC(cuda(cudaMemcpyAsync(tc->d_g122_tasks, v.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, stream),
-               "cudaMemcpyAsync(122 tasks)"));
+  G122Plan& P = tc->g122;
+  const int bt = P.tiny_cap, bw = P.warp_cap;
+  const std::string e = g122_partition(P, tiny_cap, small_cap);
+  if (!e.empty()) {
+    g122_partition(P, bt, bw);  // keep the previous caps
+    return fail(IMSRG_ERR_INVALID_ARGUMENT, e);
+  }
+  if (!P.tasks.empty()) {
+    CK_TC(cuda(cudaMemcpyAsync(tc->d_g122_tasks, P.tasks.data(), sizeof(G122Task) * P.tasks.size(),
+                               cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync(122 tasks)"));
+    if (!P.items.empty())
+      CK_TC(cuda(cudaMemcpyAsync(tc->d_g122_items, P.items.data(), sizeof(int2) * P.items.size(),
+                                 cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync(122 runs)"));
     CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize(122 tasks)"));
   }
-  tc->g122_ntiny = nt;
-  tc->g122_nwarp = nw;
-  tc->g122_ncta = (int)n - nt - nw;
-  tc->g122_t.tasks = tc->d_g122_tasks;
-  tc->g122_w.tasks = tc->d_g122_tasks + nt;
-  tc->g122_c.tasks = tc->d_g122_tasks + nt + nw;
-  tc->g122_tiny_cap = tiny_cap;
-  tc->g122_small = small_cap;
+  CK_TC(cuda(g122_smem_attr(P.smem_bytes), "smem attr (122)"));
+  CK_TC(cuda(g122_blocks_per_sm(P.smem_bytes, &tc->g122_per_sm), "occupancy (122)"));
   return IMSRG_OK;
 }
 
@@ -1179,8 +1151,8 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
     if ((st = time_one(&base)) != IMSRG_OK) break;
     best = base;
     // 122 caps
-    static const int caps[][2] = {{16, 256}, {32, 128}, {32, 256}, {64, 256}, {64, 512}};
-    int bt = tc->g122_tiny_cap, bs = tc->g122_small;
+    static const int caps[][2] = {{32, 256}, {64, 256}, {32, 512}, {64, 512}, {64, 1024}};
+    int bt = tc->g122.tiny_cap, bs = tc->g122.warp_cap;
     for (const auto& c : caps) {
       if ((st = tc_g122_partition(c[0], c[1])) != IMSRG_OK) break;
       float ms;
@@ -1256,8 +1228,8 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
     float after = 0.0f;
     if ((st = time_one(&after)) != IMSRG_OK) break;
     if (info) {
-      info->tiny_cap = tc->g122_tiny_cap;
-      info->small_cap = tc->g122_small;
+      info->tiny_cap = tc->g122.tiny_cap;
+      info->small_cap = tc->g122.warp_cap;
       info->recouple_kind = tc->recouple_kind;
       info->recouple_min_blocks = tc->recouple_kind ? tc->recouple_minb : 0;
       info->recouple_ctas = tc->recouple_kind ? tc->recouple_ctas : (int32_t)tc->rc.tasks.size();

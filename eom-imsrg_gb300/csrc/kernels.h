@@ -45,15 +45,6 @@ __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOp
 void launch_pandya_tc(int S, int kind, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
                       void* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s, const int* nkb,
                       const int* swap_row);
-__global__ void k_comm122f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES, int hRES);
-__global__ void k_comm122_fblocks(DevLayout D, PairGroupsDev G, int nspb, int nblk2, const double* L, int hL,
-                                  const double* R, int hR, float* FB);
-// k_comm122_groups_lanes<lanes> (lanes 8 or 32) on stream st
-void launch_comm122_lanes(int lanes, int grid, size_t smem, cudaStream_t st, const DevLayout& D,
-                          const PairGroupsDev& G, int ntasks, int cap, int nmax2, const double* L, int hL,
-                          const double* R, int hR, double* RES, int hRES, const float* FB, int nblk2);
-__global__ void k_comm122_groups_cta(DevLayout D, PairGroupsDev G, int nmax4, int nmax2, const double* L, int hL,
-                                     const double* R, int hR, double* RES, int hRES, const float* FB, int nblk2);
 __global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
                                 float pm);
 __global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);

@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(kRcThreads) k_recouple_g(DevLayout D, const Rc
         const int kk = (3 * J + (T + 2) + P) * 6 + g;
         const int IX = D.pairpos_t[(i * NJ + (J >> 1)) * N + jt], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
         double* out = RES + D.goff[kk] + IX + (int64_t)JX * D.gn1[kk];
-        *out += f32_to_f64(sm * pre);
+        atomicAdd(out, f32_to_f64(sm * pre));  // the only add to this element: a reduction at L2, no read here
       }
     }
   }
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_recouple_q(DevLayout D, con
       const int kk = (3 * J + (T + 2) + P) * 6 + g;
       const int IX = D.pairpos_t[(i * NJ + (J >> 1)) * N + j], JX = D.pairpos[(k * N + l) * NJ + (J >> 1)];
       double* out = RES + D.goff[kk] + IX + (int64_t)JX * D.gn1[kk];
-      *out += f32_to_f64(sm * pre);
+      atomicAdd(out, f32_to_f64(sm * pre));  // the only add to this element: a reduction at L2, no read here
     }
   }
 }

@@ -22,7 +22,7 @@ def test_autotune_keeps_results_and_reports_choice(built_lib, oracles, mode):
     eng.commutator(dA, dB, dR)
     before = dR.download()
     info = eng.autotune(dA, dB, dR)
-    assert (info["tiny_cap"], info["small_cap"]) in {(16, 256), (32, 128), (32, 256), (64, 256), (64, 512)}
+    assert (info["tiny_cap"], info["small_cap"]) in {(32, 256), (64, 256), (32, 512), (64, 512), (64, 1024)}
     assert info["gemm_order"] in (0, 1) and info["recouple_ctas"] > 0
     assert info["gemm_wmax"] in (128, 256) and info["gemm_narrow"] in (0, 1)
     assert info["recouple_kind"] in (0, 1) and info["recouple_min_blocks"] in (0, 4, 6, 8)
