@@ -496,6 +496,8 @@ struct TcState {
   const GemmTile* d_small_tiles = nullptr;
   const TcProb* d_z_probs = nullptr;
   const TcTile* d_z_tiles = nullptr;
+  std::vector<PandyaChunk> pandya_chunks;  // chunks of the cross-coupled channels for k_pandya_tc
+  const PandyaChunk* d_pandya_chunks = nullptr;
   const int* d_cc_tile_L = nullptr;
   const int* d_cc_tile_R = nullptr;
   const int* d_cc_nkb = nullptr;
@@ -726,6 +728,16 @@ imsrg_status Ctx::tc_prepare(int mode) {
   }
   tc->total_tiles = tiles;
   if (l.JM + 1 > 26) return fail(IMSRG_ERR_UNSUPPORTED, "mixed recoupling supports 2j <= 25 (eMax <= 12)");
+  // ---- Pandya chunks: at most 2048 elements of one cross-coupled channel each
+  for (int q = 0; q < l.ncc; ++q) {
+    const int64_t n = l.cc_off[q + 1] - l.cc_off[q];
+    const int nph = l.cc_nph[q];
+    if (n <= 0) continue;
+    if (n * (int64_t)nph >= (1ll << 32)) return fail(IMSRG_ERR_UNSUPPORTED, "cross-coupled channel too large");
+    const unsigned m = (unsigned)(((1ull << 32) + (unsigned)nph - 1) / (unsigned)nph);
+    for (int64_t e0 = 0; e0 < n; e0 += 2048)
+      tc->pandya_chunks.push_back(PandyaChunk{q, (int)e0, (int)std::min<int64_t>(2048, n - e0), m});
+  }
   // ---- commutator_122 tasks: the group pairs G1 <= G2 of each channel
   {
     PairGroups pg;
@@ -790,6 +802,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   for (TcProb p : tc->z_probs) tc->all_probs.push_back(p);
   pk.add(tc->all_probs, &tc->d_all_probs);
   pk.add(tc->cc_tile_L, &tc->d_cc_tile_L);
+  pk.add(tc->pandya_chunks, &tc->d_pandya_chunks);
   pk.add(tc->cc_tile_R, &tc->d_cc_tile_R);
   pk.add(tc->cc_nkb, &tc->d_cc_nkb);
   pk.add(tc->cc_tile_Ls, &tc->d_cc_tile_Ls);
@@ -983,11 +996,9 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   // columns of the ladder arrays; then one persistent launch computes the K = npp ladder
   // products W1 and the recoupling input X over the merged tile list
   if (ncc) {
-    const int grid = (int)std::min<int64_t>((ncc + 255) / 256, 152 * 16);
-    launch_pandya_tc(tc->S, tc->kind, grid, stream, D, Rp, hR, tc->buf, tc->slice_elems, tc->d_cc_tile_R, tc->d_cc_tile_Rs,
-                     tc->d_cc_nkb, tc->d_swap_row);
-    launch_pandya_tc(tc->S, tc->kind, grid, stream, D, Lp, hL, tc->buf, tc->slice_elems, tc->d_cc_tile_L, tc->d_cc_tile_Ls,
-                     tc->d_cc_nkb, tc->d_swap_row);
+    const PandyaOps ops{{Rp, Lp}, {hR, hL}, {tc->d_cc_tile_R, tc->d_cc_tile_L}, {tc->d_cc_tile_Rs, tc->d_cc_tile_Ls}};
+    launch_pandya_tc(tc->S, tc->kind, (int)tc->pandya_chunks.size(), stream, D, tc->d_pandya_chunks, ops, tc->buf,
+                     tc->slice_elems, tc->d_cc_nkb, tc->d_swap_row);
     CK_TC(launched("k_pandya_tc"));
   }
   mark(kPhasePandya);

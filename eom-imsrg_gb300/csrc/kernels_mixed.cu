@@ -19,49 +19,74 @@ __device__ __forceinline__ float d_sixjf(const DevLayout& D, int j1, int j2, int
 
 // Pandya transform (calculate_cross_coupled, src/cross_coupled.f90:1190-1300) in FP32,
 // written straight into the K-major split operand tiles (BF16 or TF32, split.cuh) of the
-// cross-coupled GEMM:
-// row r of the tile block of channel q, column ph.  Threads run along ph so the writes
-// into each 128-byte tile row are contiguous.
+// cross-coupled GEMM: element (r, ph) of channel q,
+//   X(ab, ph) = (-1)^((jh+jb+JC)/2) sqrt(JC+1) sum_JT (-1)^(JT/2) (JT+1) {jp jh JC; ja jb JT} V(ha, pb; JT).
+// Each CTA takes one chunk of a channel's elements (pandya_chunks: no search over channels),
+// threads run along ph so the writes into each 128-byte tile row are contiguous.  What does
+// not depend on JT is set up once per element: the 6j row, the pair classes and array, the
+// stored order of (h, a) and (p, b) and their sqrt 2 factors; per JT the loop loads the two
+// pair positions (adjacent in JT), the array offset, the operator element and the 6j value.
 // Each element is written twice: at row r of the operand tiles, times the row sign
 // phi(r(a,b)) = (-1)^((ja+jb)/2), and unsigned at row s(r) of the row-swapped copy,
 // s(r(a,b)) = r(b,a).  The recoupling input X (gemm_tc.cu) is built from both.
+// blockIdx.y selects the operator: 0 = R (first), 1 = L.
 template <int S, typename T>
-__global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm, void* __restrict__ bufv,
-                            int64_t slice_elems, const int* __restrict__ tile_base, const int* __restrict__ tile_base_s,
-                            const int* __restrict__ nkb, const int* __restrict__ swap_row) {
+__global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChunk* __restrict__ chunks,
+                                                   PandyaOps ops, void* __restrict__ bufv, int64_t slice_elems,
+                                                   const int* __restrict__ nkb, const int* __restrict__ swap_row) {
   T* buf = static_cast<T*>(bufv);
-  const int64_t total = D.cc_size;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = D.ncc;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (D.cc_off[mid] <= e) lo = mid; else hi = mid;
-    }
-    while (D.cc_off[lo + 1] <= e) ++lo;
-    const int q = lo;
-    const int nph = D.cc_nph[q];
-    const int64_t loc = e - D.cc_off[q];
-    const int r = (int)(loc / nph);
-    const int nbx = (int)(loc - (int64_t)r * nph);
-    const int JC = D.cc_J[q];
-    const int p = D.cc_cp[D.cc_col_off[q] + nbx], h = D.cc_ch[D.cc_col_off[q] + nbx];
-    const int a = D.cc_ra[D.cc_row_off[q] + r], b = D.cc_rb[D.cc_row_off[q] + r];
+  const bool w = blockIdx.y != 0;  // selected with conditionals, not an index (no local copy of ops)
+  const double* __restrict__ op = w ? ops.op[1] : ops.op[0];
+  const int herm = w ? ops.herm[1] : ops.herm[0];
+  const PandyaChunk c = chunks[blockIdx.x];
+  const int q = c.q, nph = D.cc_nph[q], JC = D.cc_J[q];
+  const int col0 = D.cc_col_off[q], row0 = D.cc_row_off[q];
+  const int tb = (w ? ops.tile_base[1] : ops.tile_base[0])[q], tbs = (w ? ops.tile_base_s[1] : ops.tile_base_s[0])[q];
+  const int nk = nkb[q];
+  const int N = D.N, NJ = D.NJ, nh = D.sj_nh;
+  for (int x = threadIdx.x; x < c.n; x += blockDim.x) {
+    const int loc = c.e0 + x;
+    const int r = (int)__umulhi((unsigned)loc, c.mnph), nbx = loc - r * nph;
+    const int p = D.cc_cp[col0 + nbx], h = D.cc_ch[col0 + nbx];
+    const int a = D.cc_ra[row0 + r], b = D.cc_rb[row0 + r];
     const int jp = D.jj[p], jh = D.jj[h], ja = D.jj[a], jb = D.jj[b];
     float val = 0.0f;
     if (((D.ll[a] + D.ll[h]) & 1) == ((D.ll[b] + D.ll[p]) & 1) && D.tz[a] + D.tz[h] == D.tz[b] + D.tz[p]) {
       const int Jmin = max(abs(jp - jb), abs(ja - jh)), Jmax = min(jp + jb, ja + jh);
+      // 6j {jp jh JC; ja jb JT} as srow[JT / 2] (zero unless both JC triads hold)
+      const int ks = (((jp >> 1) * nh + (jh >> 1)) * nh + (ja >> 1)) * nh + (jb >> 1);
+      const bool ok6 = d_tri(jp, jh, JC) && d_tri(ja, jb, JC);
+      const float* srow = D.sj_valf + D.sj_off[ks] + ((JC - D.sj_j3min[ks]) >> 1) * D.sj_n6[ks] - (D.sj_j6min[ks] >> 1);
+      // V(ha, pb; JT): stored order, classes and array of both pairs
+      const bool s1 = h > a, s2 = p > b;
+      const int* pp1 = D.pairpos + ((s1 ? a : h) * N + (s1 ? h : a)) * NJ;
+      const int* pp2 = D.pairpos + ((s2 ? b : p) * N + (s2 ? p : b)) * NJ;
+      const int nsq = (!s1 && h == a) + (!s2 && p == b);
+      const float m = nsq == 0 ? 1.0f : (nsq == 1 ? 1.41421356f : 2.0f);
+      const int C1 = D.con[h] + D.con[a], C2 = D.con[p] + D.con[b];
+      const int lo = min(C1, C2), hi = max(C1, C2);
+      const int g = (lo == 0) ? hi : (lo == 1 ? (hi == 1 ? 3 : 5) : 4);
+      const bool tr = C1 > C2;
+      const int qb = (D.tz[h] + D.tz[a] + 2) + ((D.ll[h] + D.ll[a]) & 1);  // channel of JT: 3 JT + qb
       float sm = 0.0f;
-      VRefF rf;
       for (int JT = Jmin; JT <= Jmax; JT += 2) {
-        if (!d_vref_f(D, h, a, p, b, JT, rf)) continue;
-        const float v = f64_to_f32(op[rf.idx]) * rf.scale(herm);
-        sm += ((JT & 2) ? -1.0f : 1.0f) * (float)(JT + 1) * d_sixjf(D, jp, jh, JC, ja, jb, JT) * v;
+        int neg = 0;
+        if (s1) neg ^= (1 + ((jh + ja - JT) >> 1)) & 1;
+        if (s2) neg ^= (1 + ((jp + jb - JT) >> 1)) & 1;
+        const int i1 = __ldg(pp1 + (JT >> 1)), i2 = __ldg(pp2 + (JT >> 1));
+        const int k = (3 * JT + qb) * 6 + g;
+        const int n1 = __ldg(D.gn1 + k);
+        const int64_t idx = __ldg(D.goff + k) + (tr ? i2 + (int64_t)i1 * n1 : i1 + (int64_t)i2 * n1);
+        const float pre = neg ? -m : m;
+        const float v = f64_to_f32(__ldg(op + idx)) * ((tr && herm < 0) ? -pre : pre);
+        const float sj = ok6 ? __ldg(srow + (JT >> 1)) : 0.0f;
+        sm += ((JT & 2) ? -1.0f : 1.0f) * (float)(JT + 1) * sj * v;
       }
       val = sm * (((jh + jb + JC) & 2) ? -1.0f : 1.0f) * sqrtf((float)(JC + 1));
     }
-    const int rs = swap_row[D.cc_row_off[q] + r];
-    const int64_t dst = split_offset<T>(tile_base[q], nkb[q], r, nbx);
-    const int64_t dsts = split_offset<T>(tile_base_s[q], nkb[q], rs, nbx);
+    const int rs = swap_row[row0 + r];
+    const int64_t dst = split_offset<T>(tb, nk, r, nbx);
+    const int64_t dsts = split_offset<T>(tbs, nk, rs, nbx);
     const bool flip = ((ja + jb) & 2) != 0;  // phi(r) = -1
     float rem = val;
 #pragma unroll
@@ -72,18 +97,15 @@ __global__ void k_pandya_tc(DevLayout D, const double* __restrict__ op, int herm
     }
   }
 }
-void launch_pandya_tc(int S, int kind, int grid, cudaStream_t stream, const DevLayout& D, const double* op, int herm,
-                      void* buf, int64_t slice_elems, const int* tile_base, const int* tile_base_s, const int* nkb,
-                      const int* swap_row) {
+void launch_pandya_tc(int S, int kind, int nchunks, cudaStream_t stream, const DevLayout& D, const PandyaChunk* chunks,
+                      const PandyaOps& ops, void* buf, int64_t slice_elems, const int* nkb, const int* swap_row) {
+  const dim3 grid(nchunks, 2);
   if (kind == 1)
-    k_pandya_tc<2, float><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s, nkb,
-                                                     swap_row);
+    k_pandya_tc<2, float><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, nkb, swap_row);
   else if (S == 2)
-    k_pandya_tc<2, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s,
-                                                             nkb, swap_row);
+    k_pandya_tc<2, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, nkb, swap_row);
   else
-    k_pandya_tc<3, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, op, herm, buf, slice_elems, tile_base, tile_base_s,
-                                                             nkb, swap_row);
+    k_pandya_tc<3, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, nkb, swap_row);
 }
 
 // commutator_221 (src/commutators.f90:435-578) with FP32 arithmetic: one warp per

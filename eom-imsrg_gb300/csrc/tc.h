@@ -48,6 +48,20 @@ inline int tc_tile_width(int N, int n0, int wmax, bool narrow) {
   return left >= wmax ? wmax : ((left + 15) / 16) * 16;
 }
 
+// Pandya chunk: elements [e0, e0 + n) of cross-coupled channel q (row-major, nph columns),
+// with mnph = ceil(2^32 / nph) so that row = umulhi(e, mnph) (exact for e * nph < 2^32)
+struct PandyaChunk {
+  int q, e0, n;
+  unsigned mnph;
+};
+// the two operators of one Pandya launch ([0] R, [1] L) and their operand tile bases
+struct PandyaOps {
+  const double* op[2];
+  int herm[2];
+  const int* tile_base[2];
+  const int* tile_base_s[2];
+};
+
 // split chunk: a contiguous run of rows of one split operand
 struct SplitChunk {
   int op;
