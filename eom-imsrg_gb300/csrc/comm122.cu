@@ -7,7 +7,8 @@
 //                - sum_c' fL(c',c) R_A[a,b,c',d] - fR(c',c) L_A[a,b,c',d]   (and d)
 // Each element of L and R is gathered once per sub-block into shared memory as an (L, R)
 // pair, and every stored element of the sub-block is written once (ASSIGNS), mirrored with
-// hRES when G1 != G2.
+// hRES when G1 != G2, except the lower triangles of the square arrays (pppp, phph, hhhh):
+// the mirror pass at the end of the commutator writes those from the upper triangles.
 //
 // Everything that depends on the basis alone is on the host: per group the stored position,
 // class and factor of each ordered pair (V_A = pre x stored: sqrt 2 for identical orbits,
@@ -72,6 +73,15 @@ __device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, 
     const int x1 = g122_div(eb, t.m0), x0 = eb - x1 * n0;
     const int x3 = g122_div(ek, t.m2), x2 = ek - x3 * n2;
     if (((t.flags & 2) && x0 > x1) || ((t.flags & 4) && x2 > x3)) continue;  // the other order is stored
+    // where the element goes: rectangular arrays (C1 < C2) at (r, c); C1 > C2 at (c, r) with
+    // hRES (G1 != G2; for G1 == G2 the element (ek, eb) of this sub-block writes it); square
+    // arrays (C1 == C2) only in their upper triangle, at (min, max) with hRES when swapped (the
+    // pass after the recoupling writes every lower triangle from the upper one)
+    const int2 cb = __ldg(PB + eb), ck = __ldg(PK + ek);
+    const int C1 = cb.x & 3, C2 = ck.x & 3;
+    const int r = cb.x >> 2, c = ck.x >> 2;
+    const bool swap = C1 > C2 || (C1 == C2 && r > c);
+    if (swap && !(t.flags & 1)) continue;
     float out = 0.0f;
     {  // sum_a' f(a, a') X[a', ...]
       const float2* f = F0 + x0 * n0;
@@ -109,14 +119,12 @@ __device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, 
         out = fmaf(fv.y, xv.x, out);
       }
     }
-    const int2 cb = __ldg(PB + eb), ck = __ldg(PK + ek);
-    const int C1 = cb.x & 3, C2 = ck.x & 3, g = g122_array(C1, C2);
-    const int r = cb.x >> 2, c = ck.x >> 2;
+    const int g = g122_array(C1, C2);
     const float w = out * g122_inv(__int_as_float(cb.y)) * g122_inv(__int_as_float(ck.y));  // stored = V_A / pre
     const int64_t base = __ldg(go + g);
     const int ld = __ldg(gn + g);
-    if (C1 <= C2) RES[base + r + (int64_t)c * ld] = f32_to_f64(w);
-    if ((t.flags & 1) && C2 <= C1) RES[base + c + (int64_t)r * ld] = f32_to_f64(hRES < 0 ? -w : w);
+    if (!swap) RES[base + r + (int64_t)c * ld] = f32_to_f64(w);
+    else RES[base + c + (int64_t)r * ld] = f32_to_f64(hRES < 0 ? -w : w);
   }
   g122_sync(cta, mask);
 }
