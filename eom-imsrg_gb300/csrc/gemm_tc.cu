@@ -288,9 +288,31 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         tc_fence_after();
         const uint32_t d_tmem = tmem_base + (uint32_t)(acc * WMAX);
         bool first = true;
-        for (int term = 0; term < P.nterm && ok; ++term) {
+        // the problem's fields in registers (the MMA asm clobbers memory); for a segmented K the
+        // instruction descriptor of each segment, stepped by a counter of K steps (an MMA takes
+        // 16 BF16 or 8 TF32 elements of K)
+        constexpr int KSTEP = (KIND == kKindTF32) ? 8 : 16;
+        const int nkb = P.nkb, nterm = P.nterm, seg_steps = P.kseg / KSTEP;
+        uint32_t sd0 = 0, sd1 = 0, sd2 = 0, sd3 = 0;
+        if (seg_steps) {
+          sd0 = umma_idesc<KIND>(term_negated(P.t[0].sign, hL, hR), tile.w);
+          sd1 = umma_idesc<KIND>(term_negated(P.t[1].sign, hL, hR), tile.w);
+          sd2 = umma_idesc<KIND>(term_negated(P.t[2].sign, hL, hR), tile.w);
+          sd3 = umma_idesc<KIND>(term_negated(P.t[3].sign, hL, hR), tile.w);
+        }
+        for (int term = 0; term < nterm && ok; ++term) {
           const uint32_t idesc = umma_idesc<KIND>(term_negated(P.t[term].sign, hL, hR), tile.w);
-          for (int kb = 0; kb < P.nkb; ++kb, ++it) {
+          int segi = 0, left = seg_steps;
+          for (int kb = 0; kb < nkb; ++kb, ++it) {
+            uint32_t idk[kMmaPerRow];
+#pragma unroll
+            for (int ks = 0; ks < kMmaPerRow; ++ks) {
+              idk[ks] = seg_steps ? (segi == 0 ? sd0 : segi == 1 ? sd1 : segi == 2 ? sd2 : sd3) : idesc;
+              if (seg_steps && --left == 0) {  // K past the fourth segment is zero padding
+                segi = min(segi + 1, 3);
+                left = seg_steps;
+              }
+            }
             const int s = it % ST;
             if (!mbar_wait(&full[s], (it / ST) & 1, abort_flag, err, 3, wait_ns)) { ok = false; break; }
             tc_fence_after();
@@ -301,7 +323,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               const uint32_t b0 = stage + (uint32_t)(S * TILE_BYTES + SliceProducts<S>::b(p) * BBYTES);
 #pragma unroll
               for (int ks = 0; ks < kMmaPerRow; ++ks) {
-                umma<KIND>(d_tmem, umma_desc(a0 + ks * 32), umma_desc(b0 + ks * 32), idesc, first ? 0u : 1u);
+                umma<KIND>(d_tmem, umma_desc(a0 + ks * 32), umma_desc(b0 + ks * 32), idk[ks], first ? 0u : 1u);
                 first = false;
               }
             }
@@ -484,7 +506,7 @@ struct TcState {
   std::vector<GemmProb> small_probs;
   std::vector<GemmTile> small_tiles;
   // particle-hole: X(q) = phi phi Z - pm Zs with Z(q) = hL LCC RCC^T - hR RCC LCC^T (recouple.cu)
-  std::vector<int> cc_tile_L, cc_tile_R, cc_tile_Ls, cc_tile_Rs, cc_nkb, swap_row;
+  std::vector<int> cc_tile_A, cc_tile_B, cc_nkb, cc_seg, swap_row;
   std::vector<TcProb> z_probs;
   std::vector<TcTile> z_tiles;
   void* d_mem = nullptr;
@@ -498,11 +520,10 @@ struct TcState {
   const TcTile* d_z_tiles = nullptr;
   std::vector<PandyaChunk> pandya_chunks;  // chunks of the cross-coupled channels for k_pandya_tc
   const PandyaChunk* d_pandya_chunks = nullptr;
-  const int* d_cc_tile_L = nullptr;
-  const int* d_cc_tile_R = nullptr;
+  const int* d_cc_tile_A = nullptr;
+  const int* d_cc_tile_B = nullptr;
   const int* d_cc_nkb = nullptr;
-  const int* d_cc_tile_Ls = nullptr;
-  const int* d_cc_tile_Rs = nullptr;
+  const int* d_cc_seg = nullptr;
   const int* d_swap_row = nullptr;
   float* zbuf = nullptr;  // X, the recoupling input (FP32, wcc layout)
   int* d_err = nullptr;
@@ -692,12 +713,14 @@ imsrg_status Ctx::tc_prepare(int mode) {
   //      row r(b,a)): phiL, phiR, Ls, Rs.  One FP32 product per channel,
   //        X = hL phiL phiR^T - hR phiR phiL^T - hR Ls Rs^T + hL Rs Ls^T
   //          = phi phi Z - pm Z(s, s),   Z = hL LCC RCC^T - hR RCC LCC^T, pm = hL hR,
-  //      is the input of the recoupling (recouple.cu).
-  tc->cc_tile_L.assign(l.ncc, 0);
-  tc->cc_tile_R.assign(l.ncc, 0);
-  tc->cc_tile_Ls.assign(l.ncc, 0);
-  tc->cc_tile_Rs.assign(l.ncc, 0);
+  //      is the input of the recoupling (recouple.cu).  The four terms are one product over a
+  //      K of four segments, each nph rounded up to 16: A = [phiL | phiR | Ls | Rs] and
+  //      B = [phiR | phiL | Rs | Ls], the segment signs (hL, -hR, -hR, hL) in the MMAs, so K is
+  //      padded to whole tiles once instead of once per term.
+  tc->cc_tile_A.assign(l.ncc, 0);
+  tc->cc_tile_B.assign(l.ncc, 0);
   tc->cc_nkb.assign(l.ncc, 0);
+  tc->cc_seg.assign(l.ncc, 0);
   tc->swap_row.assign(std::max<size_t>(l.cc_ra.size(), 1), 0);
   for (int q = 0; q < l.ncc; ++q)
     for (int r = 0; r < l.cc_rlen[q]; ++r) {
@@ -709,19 +732,19 @@ imsrg_status Ctx::tc_prepare(int mode) {
   for (int q = 0; q < l.ncc; ++q) {
     const int r = l.cc_rlen[q], nb = l.cc_nph[q];
     if (r == 0 || nb == 0) continue;
-    const int nkb = ceil_div(nb, BK);
+    const int seg = ceil_div(nb, 16) * 16;
+    const int nkb = ceil_div(4 * seg, BK);
     const int blk = ceil_div(r, BM) * nkb;
     tc->cc_nkb[q] = nkb;
-    tc->cc_tile_L[q] = tiles; tiles += blk;
-    tc->cc_tile_R[q] = tiles; tiles += blk;
-    tc->cc_tile_Ls[q] = tiles; tiles += blk;
-    tc->cc_tile_Rs[q] = tiles; tiles += blk;
+    tc->cc_seg[q] = seg;
+    tc->cc_tile_A[q] = tiles; tiles += blk;
+    tc->cc_tile_B[q] = tiles; tiles += blk;
     TcProb p{};
-    p.M = r; p.N = r; p.nkb = nkb; p.nterm = 4;
-    p.t[0] = TcTermDesc{tc->cc_tile_L[q], tc->cc_tile_R[q], hl};
-    p.t[1] = TcTermDesc{tc->cc_tile_R[q], tc->cc_tile_L[q], ng | hr};
-    p.t[2] = TcTermDesc{tc->cc_tile_Ls[q], tc->cc_tile_Rs[q], ng | hr};
-    p.t[3] = TcTermDesc{tc->cc_tile_Rs[q], tc->cc_tile_Ls[q], hl};
+    p.M = r; p.N = r; p.nkb = nkb; p.nterm = 1; p.kseg = seg;
+    p.t[0] = TcTermDesc{tc->cc_tile_A[q], tc->cc_tile_B[q], hl};
+    p.t[1] = TcTermDesc{0, 0, ng | hr};
+    p.t[2] = TcTermDesc{0, 0, ng | hr};
+    p.t[3] = TcTermDesc{0, 0, hl};
     p.out_f32 = 1;
     p.c_id = 0; p.c_off = l.wcc_off[q]; p.ldc = r;
     tc->z_probs.push_back(p);
@@ -801,12 +824,11 @@ imsrg_status Ctx::tc_prepare(int mode) {
   tc->all_probs = tc->pphh_probs;
   for (TcProb p : tc->z_probs) tc->all_probs.push_back(p);
   pk.add(tc->all_probs, &tc->d_all_probs);
-  pk.add(tc->cc_tile_L, &tc->d_cc_tile_L);
+  pk.add(tc->cc_tile_A, &tc->d_cc_tile_A);
   pk.add(tc->pandya_chunks, &tc->d_pandya_chunks);
-  pk.add(tc->cc_tile_R, &tc->d_cc_tile_R);
+  pk.add(tc->cc_tile_B, &tc->d_cc_tile_B);
   pk.add(tc->cc_nkb, &tc->d_cc_nkb);
-  pk.add(tc->cc_tile_Ls, &tc->d_cc_tile_Ls);
-  pk.add(tc->cc_tile_Rs, &tc->d_cc_tile_Rs);
+  pk.add(tc->cc_seg, &tc->d_cc_seg);
   pk.add(tc->swap_row, &tc->d_swap_row);
   pk.add(tc->quads, &tc->d_quads);
   tc->xcol = build_xcol(l);
@@ -996,9 +1018,9 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   // columns of the ladder arrays; then one persistent launch computes the K = npp ladder
   // products W1 and the recoupling input X over the merged tile list
   if (ncc) {
-    const PandyaOps ops{{Rp, Lp}, {hR, hL}, {tc->d_cc_tile_R, tc->d_cc_tile_L}, {tc->d_cc_tile_Rs, tc->d_cc_tile_Ls}};
+    const PandyaOps ops{{Rp, Lp}, {hR, hL}, tc->d_cc_tile_A, tc->d_cc_tile_B, tc->d_cc_nkb, tc->d_cc_seg};
     launch_pandya_tc(tc->S, tc->kind, (int)tc->pandya_chunks.size(), stream, D, tc->d_pandya_chunks, ops, tc->buf,
-                     tc->slice_elems, tc->d_cc_nkb, tc->d_swap_row);
+                     tc->slice_elems, tc->d_swap_row);
     CK_TC(launched("k_pandya_tc"));
   }
   mark(kPhasePandya);

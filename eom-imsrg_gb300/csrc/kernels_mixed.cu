@@ -26,14 +26,16 @@ __device__ __forceinline__ float d_sixjf(const DevLayout& D, int j1, int j2, int
 // not depend on JT is set up once per element: the 6j row, the pair classes and array, the
 // stored order of (h, a) and (p, b) and their sqrt 2 factors; per JT the loop loads the two
 // pair positions (adjacent in JT), the array offset, the operator element and the 6j value.
-// Each element is written twice: at row r of the operand tiles, times the row sign
-// phi(r(a,b)) = (-1)^((ja+jb)/2), and unsigned at row s(r) of the row-swapped copy,
-// s(r(a,b)) = r(b,a).  The recoupling input X (gemm_tc.cu) is built from both.
+// The recoupling input X (gemm_tc.cu) is one product A B^T over a K of four segments of seg
+// columns, A = [phiL | phiR | Ls | Rs], B = [phiR | phiL | Rs | Ls]: phiO is O with row r
+// times phi(r(a,b)) = (-1)^((ja+jb)/2), Os is O with row r(b,a) at row s(r) = r(a,b).  So
+// each element of L goes to A and B signed at row r (segments 0 and 1) and unsigned at row
+// s(r) (segments 2 and 3); R's to segments 1, 0 and 3, 2.
 // blockIdx.y selects the operator: 0 = R (first), 1 = L.
 template <int S, typename T>
 __global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChunk* __restrict__ chunks,
                                                    PandyaOps ops, void* __restrict__ bufv, int64_t slice_elems,
-                                                   const int* __restrict__ nkb, const int* __restrict__ swap_row) {
+                                                   const int* __restrict__ swap_row) {
   T* buf = static_cast<T*>(bufv);
   const bool w = blockIdx.y != 0;  // selected with conditionals, not an index (no local copy of ops)
   const double* __restrict__ op = w ? ops.op[1] : ops.op[0];
@@ -41,8 +43,9 @@ __global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChun
   const PandyaChunk c = chunks[blockIdx.x];
   const int q = c.q, nph = D.cc_nph[q], JC = D.cc_J[q];
   const int col0 = D.cc_col_off[q], row0 = D.cc_row_off[q];
-  const int tb = (w ? ops.tile_base[1] : ops.tile_base[0])[q], tbs = (w ? ops.tile_base_s[1] : ops.tile_base_s[0])[q];
-  const int nk = nkb[q];
+  const int ta = ops.tile_a[q], tbb = ops.tile_b[q], nk = ops.nkb[q], seg = ops.seg[q];
+  // K offsets of this operator's signed rows in A and B, and of its swapped rows
+  const int ka = w ? 0 : seg, kb = w ? seg : 0, ksa = w ? 2 * seg : 3 * seg, ksb = w ? 3 * seg : 2 * seg;
   const int N = D.N, NJ = D.NJ, nh = D.sj_nh;
   for (int x = threadIdx.x; x < c.n; x += blockDim.x) {
     const int loc = c.e0 + x;
@@ -85,27 +88,31 @@ __global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChun
       val = sm * (((jh + jb + JC) & 2) ? -1.0f : 1.0f) * sqrtf((float)(JC + 1));
     }
     const int rs = swap_row[row0 + r];
-    const int64_t dst = split_offset<T>(tb, nk, r, nbx);
-    const int64_t dsts = split_offset<T>(tbs, nk, rs, nbx);
+    const int64_t da = split_offset<T>(ta, nk, r, ka + nbx), db = split_offset<T>(tbb, nk, r, kb + nbx);
+    const int64_t dsa = split_offset<T>(ta, nk, rs, ksa + nbx), dsb = split_offset<T>(tbb, nk, rs, ksb + nbx);
     const bool flip = ((ja + jb) & 2) != 0;  // phi(r) = -1
     float rem = val;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const T hv = SplitElem<T>::take(rem);
-      buf[s * slice_elems + dst] = flip ? SplitElem<T>::neg(hv) : hv;
-      buf[s * slice_elems + dsts] = hv;
+      const T sv = flip ? SplitElem<T>::neg(hv) : hv;
+      T* b = buf + s * slice_elems;
+      b[da] = sv;
+      b[db] = sv;
+      b[dsa] = hv;
+      b[dsb] = hv;
     }
   }
 }
 void launch_pandya_tc(int S, int kind, int nchunks, cudaStream_t stream, const DevLayout& D, const PandyaChunk* chunks,
-                      const PandyaOps& ops, void* buf, int64_t slice_elems, const int* nkb, const int* swap_row) {
+                      const PandyaOps& ops, void* buf, int64_t slice_elems, const int* swap_row) {
   const dim3 grid(nchunks, 2);
   if (kind == 1)
-    k_pandya_tc<2, float><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, nkb, swap_row);
+    k_pandya_tc<2, float><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
   else if (S == 2)
-    k_pandya_tc<2, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, nkb, swap_row);
+    k_pandya_tc<2, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
   else
-    k_pandya_tc<3, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, nkb, swap_row);
+    k_pandya_tc<3, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
 }
 
 // commutator_221 (src/commutators.f90:435-578) with FP32 arithmetic: one warp per

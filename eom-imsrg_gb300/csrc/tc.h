@@ -26,11 +26,13 @@ struct TcTermDesc {
   int sign;            // TcSign
 };
 
-// C = sum over nterm (<= 4) terms of sign * A_t B_t^T, all terms with the same K blocks
+// C = sum over nterm (<= 4) terms of sign * A_t B_t^T, all terms with the same K blocks.
+// With kseg > 0 the problem is one term whose K holds four segments of kseg elements (a
+// multiple of 16): the products of segment j carry the sign t[j].sign.
 struct TcProb {
   int64_t c_off;
   int M, N, nkb, nterm;
-  int out_f32, c_id, ldc, pad;
+  int out_f32, c_id, ldc, kseg;
   TcTermDesc t[4];
 };
 
@@ -54,12 +56,16 @@ struct PandyaChunk {
   int q, e0, n;
   unsigned mnph;
 };
-// the two operators of one Pandya launch ([0] R, [1] L) and their operand tile bases
+// the two operators of one Pandya launch ([0] R, [1] L); per channel the first tiles of the
+// K-concatenated operands A = [phiL | phiR | Ls | Rs] and B = [phiR | phiL | Rs | Ls] of the
+// recoupling input, their K blocks and the segment length
 struct PandyaOps {
   const double* op[2];
   int herm[2];
-  const int* tile_base[2];
-  const int* tile_base_s[2];
+  const int* tile_a;
+  const int* tile_b;
+  const int* nkb;
+  const int* seg;
 };
 
 // split chunk: a contiguous run of rows of one split operand
