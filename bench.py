@@ -233,21 +233,20 @@ def prepared_hamiltonian(eng, reference: str, seed: int = 1, time_transform: boo
 
 
 # ---------------------------------------------------------------- roofline bookkeeping
-def algorithmic_work(eng, mode: str, phase: str):
+def algorithmic_work(eng, mode: str, phase: str, merged: bool = False):
     """Algorithmic bytes (or FLOPs) of one launch of a phase at this basis.
 
     Bytes count each array the phase must touch once: FP64 operators (8 B), the FP32
     recoupling input X (4 B, wcc_size elements; for the recoupling itself the distinct
     elements it reads, counted by the library), the split operand slices (2 B BF16, 4 B TF32
-    per slice).  FLOPs are 2 M N K of the products times the number of slice products."""
+    per slice).  FLOPs are 2 M N K of the products times the number of slice products.
+    merged: the ladder and X products run as one launch (phase pphh_gemm) or two (pphh_gemm,
+    ph_gemm)."""
     import numpy as np
     S = {"bf16x3": 3, "bf16x6": 6, "tf32x3": 3, "fp64": 1}[mode]  # slice products per GEMM
     slices = {"bf16x3": 2, "bf16x6": 3, "tf32x3": 2, "fp64": 1}[mode]
     esize = 4 if mode == "tf32x3" else 2                           # bytes per operand value
     info = eng.block_info()
-    A = eng.basis.nholes
-    P = eng.basis.norbits - A
-    n2b = eng.slab - (1 + A * A + P * P + P * A)
     cc = eng.cc_info()
     if phase == "recouple":   # counted exactly from the quadruples: distinct X reads (FP32), the
         #                        RES elements read and written (FP64), the kernel's index data
@@ -258,15 +257,18 @@ def algorithmic_work(eng, mode: str, phase: str):
     if phase == "mirror":     # the upper triangle of every square array read, the lower written
         sq = sum(n * (n - 1) // 2 for g in ("npp", "nph", "nhh") for n in (int(x) for x in info[g]))
         return "hbm", 16 * sq
-    if phase == "c122":       # read L and R once, write the 2b part of RES
-        return "hbm", 2 * 8 * eng.slab + 8 * n2b
-    if phase == "ph_gemm":    # X written once in FP32 (one product of four terms per channel, K = nph),
-        #                       its split operands (row-signed and row-swapped LCC, RCC) read once
-        return "hbm", 4 * eng.wcc_size + 2 * 2 * esize * slices * int((cc["rlen"] * cc["nph"]).sum())
-    if phase == "pphh_gemm":  # the merged tensor-core launch: sum 2 M N K over the K = npp ladder
-        #                       products and the four K = nph products of X per cross-coupled
-        #                       channel, times the slice products
-        f = 4 * 2 * int((cc["rlen"].astype(np.int64) ** 2 * cc["nph"]).sum()) if mode != "fp64" else 0
+    if phase == "c122":       # read L and R once, write every unique 2b element of RES once (the
+        #                       lower triangles of the square arrays come from the mirror pass)
+        npp, nph_, nhh = (info[k].astype(np.int64) for k in ("npp", "nph", "nhh"))
+        n_unique = int((npp * (npp + 1) // 2 + nph_ * (nph_ + 1) // 2 + nhh * (nhh + 1) // 2
+                        + npp * nph_ + npp * nhh + nph_ * nhh).sum())
+        return "hbm", 2 * 8 * eng.slab + 8 * n_unique
+    x_flops = 4 * 2 * int((cc["rlen"].astype(np.int64) ** 2 * cc["nph"]).sum()) if mode != "fp64" else 0
+    if phase == "ph_gemm":    # X: per cross-coupled channel one product over a K of four nph segments
+        return "tensor", x_flops * S
+    if phase == "pphh_gemm":  # sum 2 M N K over the K = npp ladder products (and X's when merged),
+        #                       times the slice products
+        f = x_flops if merged else 0
         for q in range(eng.nblocks):
             np_, nb, nh = int(info["npp"][q]), int(info["nph"][q]), int(info["nhh"][q])
             if np_ == 0:
@@ -274,8 +276,8 @@ def algorithmic_work(eng, mode: str, phase: str):
             f += 2 * np_ * np_ * np_ + 2 * nh * nh * np_ + 2 * 2 * np_ * nh * np_
             f += 2 * nb * nb * np_ + 2 * 2 * np_ * nb * np_ + 2 * 2 * nb * nh * np_
         return "tensor", f * S
-    if phase == "pandya":     # two operators read, their CC slices written (standard and row-swapped)
-        return "hbm", 2 * 8 * eng.slab + 2 * 2 * esize * slices * int((cc["rlen"] * cc["nph"]).sum())
+    if phase == "pandya":     # two operators read, each value written to four K segments of the X operands
+        return "hbm", 2 * 8 * eng.slab + 2 * 4 * esize * slices * int((cc["rlen"] * cc["nph"]).sum())
     return None, None
 
 
@@ -1052,7 +1054,7 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    bound, work = algorithmic_work(eng, args.mode, dom)
+    bound, work = algorithmic_work(eng, args.mode, dom, bool((tune or {}).get("gemm_merged", 0)))
     traffic = None
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
@@ -1093,7 +1095,7 @@ def main():
                 "precision": f"{args.mode}: " + ("TF32-compensated" if args.mode == "tf32x3" else "split-BF16") +
                              " tcgen05 channel GEMMs, FP32 accumulate, FP32 gathers, FP64 operators, E0 and norms",
                 "parallelism": f"replicas x{world}",
-                "l2": "inputs larger than L2 (0.27 GiB per operator, 0.78 GiB Z and Y each)",
+                "l2": "inputs larger than L2 (0.27 GiB per operator; the recoupling input X 0.14 GiB)",
                 "reference_state": hf_rec, "autotune": tune,
                 "timed": timed, "warmup_E0": e0_steps,
                 "fp64_commutators_per_s": fp64_rate * world if fp64_rate else None,
