@@ -349,6 +349,12 @@ def commutator_workload(args, local: int):
     for _ in range(args.steps):
         eng.commutator(dE, dH, dR)
     ms = eng.timer_end()
+    l1 = eng.launch_count()
+    eng.profile_phases(True)  # per-phase event times of further commutators (after the timed ones)
+    for _ in range(3):
+        eng.commutator(dE, dH, dR)
+    phases = eng.profile_read()
+    eng.profile_phases(False)
     print(json.dumps({
         "metric": f"IMSRG(2) commutators/s at eMax={emax}, eager [eta,H]", "value": args.steps / (ms * 1e-3),
         "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -356,8 +362,9 @@ def commutator_workload(args, local: int):
         "dtype": "tf32" if args.mode == "tf32x3" else "bf16", "data": "synthetic",
         "config": {"workload": f"eager [eta,H] commutators at eMax={emax} ({b.norbits} orbits) on the "
                                f"{args.reference.upper()} state, {args.mode}", "reference_state": hf_rec,
-                   "autotune": tune},
-        "gpu_launches": eng.launch_count() - l0,
+                   "autotune": tune,
+                   "phases_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in phases.items() if v[1]}},
+        "gpu_launches": l1 - l0,
     }), flush=True)
 
 
@@ -1095,7 +1102,7 @@ def main():
                 "precision": f"{args.mode}: " + ("TF32-compensated" if args.mode == "tf32x3" else "split-BF16") +
                              " tcgen05 channel GEMMs, FP32 accumulate, FP32 gathers, FP64 operators, E0 and norms",
                 "parallelism": f"replicas x{world}",
-                "l2": "inputs larger than L2 (0.27 GiB per operator; the recoupling input X 0.14 GiB)",
+                "l2": "inputs larger than L2 (0.27 GiB per operator; the recoupling input X 0.73 GiB)",
                 "reference_state": hf_rec, "autotune": tune,
                 "timed": timed, "warmup_E0": e0_steps,
                 "fp64_commutators_per_s": fp64_rate * world if fp64_rate else None,

@@ -527,20 +527,13 @@ struct TcState {
   const int* d_swap_row = nullptr;
   float* zbuf = nullptr;  // X, the recoupling input (FP32, wcc layout)
   int* d_err = nullptr;
-  // orbit quadruples (i<=j, k<=l) of the particle-hole recoupling, j fastest, and the
-  // recoupling's groups / tasks / staged 6j blocks
+  // orbit quadruples (i<=j, k<=l) of the particle-hole recoupling, j fastest
   std::vector<uint64_t> quads;
   const uint64_t* d_quads = nullptr;
-  RecouplePlan rc;
   std::vector<int> xcol;              // X column offset of every pair and J' (recouple.cu)
   const int* d_xcol = nullptr;
-  int recouple_kind = 0;              // 0: by (i, k, l) groups (k_recouple_g), 1: per quadruple (k_recouple_q)
   int recouple_minb = 6;              // launch-bounds variant of k_recouple_q
   int recouple_ctas = 0;              // CTAs of k_recouple_q
-  const RcTask* d_rc_tasks = nullptr;
-  const RcGroup* d_rc_groups = nullptr;
-  const RcTriple* d_rc_triples = nullptr;
-  const float* d_rc_table = nullptr;
   std::vector<SplitChunk> chunks;
   const SplitChunk* d_chunks = nullptr;
   // commutator_122 by pair-group sub-blocks (comm122.cu): the plan, its launch order for the
@@ -805,10 +798,6 @@ imsrg_status Ctx::tc_prepare(int mode) {
   const size_t bytes = (size_t)tc_elem_bytes() * (size_t)S * tc->slice_elems;
   CK_TC(cuda(cudaMalloc(&tc->buf, std::max<size_t>(bytes, 256)), "cudaMalloc(tc operands)"));
   CK_TC(cuda(cudaMemset(tc->buf, 0, std::max<size_t>(bytes, 256)), "memset(tc operands)"));
-  {
-    const std::string e = build_recouple_plan(l, tc->quads, tc->rc);
-    if (!e.empty()) return fail(IMSRG_ERR_UNSUPPORTED, e);
-  }
   CK_TC(cuda(cudaMalloc(&tc->zbuf, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "cudaMalloc(X)"));
   CK_TC(cuda(cudaMemset(tc->zbuf, 0, sizeof(float) * std::max<int64_t>(l.wcc_size, 1)), "memset(X)"));
   CK_TC(cuda(cudaMalloc(&tc->d_err, sizeof(int)), "cudaMalloc(err)"));
@@ -833,10 +822,6 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->quads, &tc->d_quads);
   tc->xcol = build_xcol(l);
   pk.add(tc->xcol, &tc->d_xcol);
-  pk.add(tc->rc.tasks, &tc->d_rc_tasks);
-  pk.add(tc->rc.groups, &tc->d_rc_groups);
-  pk.add(tc->rc.triples, &tc->d_rc_triples);
-  pk.add(tc->rc.table, &tc->d_rc_table);
   pk.add(tc->chunks, &tc->d_chunks);
   pk.add(tc->g_start, &tc->g122_w.spb_start);
   pk.add(tc->g_n, &tc->g122_w.spb_n);
@@ -869,7 +854,6 @@ imsrg_status Ctx::tc_prepare(int mode) {
 
   // tensor map over the whole operand buffer: rows of 64 bf16 (128 bytes), box 64 x 128
   CK_TC(tc_encode_map(&tc->tmap, tc->buf, (int64_t)S * tc->slice_rows));
-  CK_TC(cuda(recouple_g_smem_attr(tc->rc.smem_bytes), "smem attr (recoupling)"));
   CK_TC(cuda(tc_gemm_smem_attrs(S, kind), "smem attr (tensor-core GEMM)"));
   return IMSRG_OK;
 }
@@ -1073,16 +1057,10 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     mark(kPhasePhGemm);
   }
   if (!tc->quads.empty()) {
-    if (tc->recouple_kind == 0) {
-      launch_recouple_g(tc->rc, stream, D, tc->d_rc_tasks, tc->d_rc_groups, tc->d_rc_triples, tc->d_rc_table,
-                        tc->d_quads, tc->d_xcol, tc->zbuf, RES);
-      CK_TC(launched("k_recouple_g"));
-    } else {
-      const int64_t nq = (int64_t)tc->quads.size();
-      const int grid = (int)std::min<int64_t>((nq + 255) / 256, tc->recouple_ctas);
-      launch_recouple_q(tc->recouple_minb, grid, stream, D, tc->d_quads, nq, tc->d_xcol, tc->zbuf, RES);
-      CK_TC(launched("k_recouple_q"));
-    }
+    const int64_t nq = (int64_t)tc->quads.size();
+    const int grid = (int)std::min<int64_t>((nq + 255) / 256, tc->recouple_ctas);
+    launch_recouple_q(tc->recouple_minb, grid, stream, D, tc->d_quads, nq, tc->d_xcol, tc->zbuf, RES);
+    CK_TC(launched("k_recouple_q"));
   }
   mark(kPhaseRecouple);
   if (!upd_tiles.empty()) {
@@ -1193,26 +1171,20 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
       if (ms < best) { best = ms; bt = c[0]; bs = c[1]; }
     }
     if (st != IMSRG_OK || (st = tc_g122_partition(bt, bs)) != IMSRG_OK) break;
-    // recoupling: by groups, or per quadruple with its launch-bounds variant and CTA count (the
-    // kernels sum every output in the same order, so the choice leaves the result unchanged)
+    // recoupling: the launch-bounds variant and the CTA count (no output depends on them)
     {
-      int bk = tc->recouple_kind, bm = tc->recouple_minb, bc = tc->recouple_ctas;
-      tc->recouple_kind = 0;
+      int bm = tc->recouple_minb, bc = tc->recouple_ctas;
       float ms;
-      if ((st = time_one(&ms)) != IMSRG_OK) break;
-      if (ms < best) { best = ms; bk = 0; }
-      tc->recouple_kind = 1;
       for (int minb : {4, 6, 8}) {
         for (int mult : {16, 32, 64}) {
           tc->recouple_minb = minb;
           tc->recouple_ctas = tc->num_sms * mult;
           if ((st = time_one(&ms)) != IMSRG_OK) break;
-          if (ms < best) { best = ms; bk = 1; bm = minb; bc = tc->recouple_ctas; }
+          if (ms < best) { best = ms; bm = minb; bc = tc->recouple_ctas; }
         }
         if (st != IMSRG_OK) break;
       }
       if (st != IMSRG_OK) break;
-      tc->recouple_kind = bk;
       tc->recouple_minb = bm;
       tc->recouple_ctas = bc;
     }
@@ -1263,9 +1235,9 @@ imsrg_status Ctx::tc_autotune(const double* Lp, int hL, const double* Rp, int hR
     if (info) {
       info->tiny_cap = tc->g122.tiny_cap;
       info->small_cap = tc->g122.warp_cap;
-      info->recouple_kind = tc->recouple_kind;
-      info->recouple_min_blocks = tc->recouple_kind ? tc->recouple_minb : 0;
-      info->recouple_ctas = tc->recouple_kind ? tc->recouple_ctas : (int32_t)tc->rc.tasks.size();
+      info->recouple_kind = 1;
+      info->recouple_min_blocks = tc->recouple_minb;
+      info->recouple_ctas = tc->recouple_ctas;
       const int gl = tc->merged ? 2 : 0;
       info->gemm_wmax = tc->wmax[gl];
       info->gemm_narrow = tc->narrow[gl] ? 1 : 0;
@@ -1291,7 +1263,7 @@ extern "C" imsrg_status imsrg_recouple_traffic(imsrg_ctx* ctx, int64_t* x_reads,
   if (c->precision == IMSRG_PREC_FP64) return c->fail(IMSRG_ERR_UNSUPPORTED, "the recoupling kernel runs in the mixed modes");
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(IMSRG_ERR_CUDA, "cudaSetDevice");
   CK_TC(c->tc_prepare(c->precision));
-  const RecoupleTraffic t = recouple_traffic(c->L, c->tc->quads, c->tc->rc);
+  const RecoupleTraffic t = recouple_traffic(c->L, c->tc->quads);
   *x_reads = t.x_reads;
   *x_distinct = t.x_distinct;
   *res_elems = t.res_elems;
@@ -1305,10 +1277,9 @@ extern "C" imsrg_status imsrg_set_tuning(imsrg_ctx* ctx, const imsrg_tune_info* 
   if (c->device < 0) return c->fail(IMSRG_ERR_UNSUPPORTED, "host-only context (device < 0)");
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(IMSRG_ERR_CUDA, "cudaSetDevice");
   if (c->precision == IMSRG_PREC_FP64) return c->fail(IMSRG_ERR_UNSUPPORTED, "tuning applies to the mixed modes");
-  if (cfg->recouple_kind < 0 || cfg->recouple_kind > 1 || cfg->gemm_order < 0 || cfg->gemm_order > 1 ||
-      (cfg->recouple_kind == 1 && (cfg->recouple_ctas < 1 || (cfg->recouple_min_blocks != 4 &&
-                                                              cfg->recouple_min_blocks != 6 &&
-                                                              cfg->recouple_min_blocks != 8))))
+  // recouple_kind 1 (one thread per quadruple) is the only recoupling kernel
+  if (cfg->recouple_kind != 1 || cfg->gemm_order < 0 || cfg->gemm_order > 1 || cfg->recouple_ctas < 1 ||
+      (cfg->recouple_min_blocks != 4 && cfg->recouple_min_blocks != 6 && cfg->recouple_min_blocks != 8))
     return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_set_tuning: value out of range");
   CK_TC(c->ensure_workspace());
   CK_TC(c->tc_prepare(c->precision));
@@ -1323,11 +1294,8 @@ extern "C" imsrg_status imsrg_set_tuning(imsrg_ctx* ctx, const imsrg_tune_info* 
     CK_TC(c->tc_set_tiles(w, n, cfg->gemm_order));
     c->tc->merged = m;
   }
-  c->tc->recouple_kind = cfg->recouple_kind;
-  if (cfg->recouple_kind == 1) {
-    c->tc->recouple_minb = cfg->recouple_min_blocks;
-    c->tc->recouple_ctas = cfg->recouple_ctas;
-  }
+  c->tc->recouple_minb = cfg->recouple_min_blocks;
+  c->tc->recouple_ctas = cfg->recouple_ctas;
   c->graph_release();
   return IMSRG_OK;
 }

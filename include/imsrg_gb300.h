@@ -117,13 +117,13 @@ imsrg_status imsrg_recouple_traffic(imsrg_ctx* ctx, int64_t* x_reads, int64_t* x
  * by the next step.  IMSRG_ERR_UNSUPPORTED in FP64 mode. */
 typedef struct {
   int32_t tiny_cap, small_cap; /* sub-blocks up to tiny_cap elements: 8 lanes; up to small_cap: a warp */
-  int32_t recouple_ctas;       /* CTAs of the recoupling kernel (grouped: one per task of its plan) */
+  int32_t recouple_ctas;       /* CTAs of the recoupling kernel */
   int32_t gemm_order;          /* 0: tiles with the longest K first, 1: problem order */
   int32_t gemm_wmax;           /* widest output tile of the ladder launch (of the merged launch): 128 or 256 */
   int32_t gemm_narrow;         /* 1: narrow last column tiles (multiples of 16 columns) in that launch */
   double ms_before, ms_after;  /* one commutator before and after tuning */
-  int32_t recouple_kind;       /* 0: recoupling by (i, k, l) groups, 1: one thread per orbit quadruple */
-  int32_t recouple_min_blocks; /* per-quadruple kernel: launch-bounds variant (4, 6 or 8 CTAs per SM) */
+  int32_t recouple_kind;       /* 1: one thread per orbit quadruple (the only recoupling kernel; other values are rejected) */
+  int32_t recouple_min_blocks; /* launch-bounds variant of the recoupling kernel (4, 6 or 8 CTAs per SM) */
   int32_t gemm_merged;         /* 1: ladder and particle-hole products in one launch, 0: two launches */
   int32_t gemm_wmax_x;         /* two launches: widest tile of the particle-hole (X) launch (0: as gemm_wmax) */
   int32_t gemm_narrow_x;       /* two launches: narrow last tiles in the X launch */

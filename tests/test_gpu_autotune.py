@@ -25,13 +25,13 @@ def test_autotune_keeps_results_and_reports_choice(built_lib, oracles, mode):
     assert (info["tiny_cap"], info["small_cap"]) in {(32, 256), (64, 256), (32, 512), (64, 512), (64, 1024)}
     assert info["gemm_order"] in (0, 1) and info["recouple_ctas"] > 0
     assert info["gemm_wmax"] in (128, 256) and info["gemm_narrow"] in (0, 1)
-    assert info["recouple_kind"] in (0, 1) and info["recouple_min_blocks"] in (0, 4, 6, 8)
+    assert info["recouple_kind"] == 1 and info["recouple_min_blocks"] in (4, 6, 8)
     assert info["gemm_merged"] in (0, 1)
     assert info["ms_before"] > 0 and info["ms_after"] > 0
     eng.commutator(dA, dB, dR)
     assert np.array_equal(dR.download(), before)
     # every other choice of each knob, applied with imsrg_set_tuning, still gives the same bits
-    for change in ({"recouple_kind": 1 - info["recouple_kind"], "recouple_min_blocks": 6, "recouple_ctas": 152 * 8},
+    for change in ({"recouple_min_blocks": 4 if info["recouple_min_blocks"] != 4 else 8, "recouple_ctas": 152 * 8},
                    {"gemm_merged": 1 - info["gemm_merged"]}, {"gemm_narrow": 1 - info["gemm_narrow"]},
                    {"gemm_order": 1 - info["gemm_order"]},
                    {"gemm_wmax": 384 - info["gemm_wmax"]} if mode == "bf16x3" else {},
