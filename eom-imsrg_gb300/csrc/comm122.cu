@@ -10,10 +10,14 @@
 // hRES when G1 != G2, except the lower triangles of the square arrays (pppp, phph, hhhh):
 // the mirror pass at the end of the commutator writes those from the upper triangles.
 //
-// Everything that depends on the basis alone is on the host: per group the stored position,
-// class and factor of each ordered pair (V_A = pre x stored: sqrt 2 for identical orbits,
-// the exchange phase when the stored order is swapped), per task the block sizes, the
-// offsets of the f blocks and the constants of the index divisions.  One launch covers every
+// Everything that depends on the basis alone is on the host: per element of every sub-block
+// one code word (comm122.h) with its storage position, swap flag and factor (V_A = pre x
+// stored: sqrt 2 per pair of identical orbits, the exchange phase when a pair's stored order is
+// swapped), per task the block sizes, the offsets of the f blocks and the constants of the
+// index divisions.  Every element is read from, and written to, the same place: the
+// rectangular array of its class pair, or the upper triangle of a square array (the operators'
+// lower triangles are herm times the upper ones, and the pass after the recoupling writes
+// RES's lower triangles).  One launch covers every
 // task: the largest sub-blocks one per CTA at the front of the grid, the rest as runs of tasks
 // that the warps take in channel order from a counter, so the tasks of one channel (which
 // read the same arrays of L and R) run close together in time.
@@ -27,13 +31,19 @@ namespace imsrg {
 
 namespace {
 
-// gam array of the class pair (C1, C2), C = 0 pp, 1 ph, 2 hh: 3 bits at 3 (3 C1 + C2)
-__device__ __forceinline__ int g122_array(int C1, int C2) { return (0x4aab288 >> (3 * (C1 * 3 + C2))) & 7; }
-
 __device__ __forceinline__ int g122_div(int e, int m) { return (int)(((unsigned)e * (unsigned)m) >> 20); }
 
-// 1 / pre for pre in {1, -1, sqrt 2}
-__device__ __forceinline__ float g122_inv(float pre) { return fabsf(pre) > 1.2f ? 0.70710678f : pre; }
+// pre and 1 / pre of a code word
+__device__ __forceinline__ float g122_pre(unsigned w) {
+  const unsigned m = w >> 30;
+  const float v = m == 0 ? 1.0f : (m == 1 ? 1.41421356f : 2.0f);
+  return (w >> 29) & 1u ? -v : v;
+}
+__device__ __forceinline__ float g122_ipre(unsigned w) {
+  const unsigned m = w >> 30;
+  const float v = m == 0 ? 1.0f : (m == 1 ? 0.70710678f : 0.5f);
+  return (w >> 29) & 1u ? -v : v;
+}
 
 __device__ __forceinline__ void g122_sync(bool cta, unsigned mask) {
   if (cta) __syncthreads(); else __syncwarp(mask);
@@ -41,26 +51,21 @@ __device__ __forceinline__ void g122_sync(bool cta, unsigned mask) {
 
 // One task on nth threads: 8 or 32 lanes of a warp (under mask), or the whole CTA (cta).  One
 // copy of this code serves all three, so the warps of a CTA share their instructions.
-__device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, const int2* __restrict__ PT,
+__device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, const unsigned* __restrict__ EC,
                                          const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
                                          double* __restrict__ RES, int hRES, const float2* __restrict__ FB,
                                          float2* __restrict__ X, int tid, int nth, bool cta, unsigned mask) {
   const int n0 = t.nn & 255, n1 = (t.nn >> 8) & 255, n2 = (t.nn >> 16) & 255, n3 = t.nn >> 24;
   const int nb = n0 * n1, ntot = nb * n2 * n3;
-  const int64_t* go = D.goff + t.q * 6;
-  const int* gn = D.gn1 + t.q * 6;
-  const int2* PB = PT + t.pb;
-  const int2* PK = PT + t.pk;
+  const unsigned* C = EC + t.eoff;
+  constexpr unsigned kIdx = (1u << kG122IdxBits) - 1u, kSwap = 1u << kG122IdxBits;
   for (int e = tid; e < ntot; e += nth) {  // gather V_A of L and R
-    const int ek = g122_div(e, t.mb), eb = e - ek * nb;
-    const int2 cb = __ldg(PB + eb), ck = __ldg(PK + ek);
-    const int C1 = cb.x & 3, C2 = ck.x & 3, g = g122_array(C1, C2);
-    const int r = cb.x >> 2, c = ck.x >> 2;
-    const bool tr = C1 > C2;
-    const int64_t idx = __ldg(go + g) + (tr ? c + (int64_t)r * __ldg(gn + g) : r + (int64_t)c * __ldg(gn + g));
-    const float pre = __int_as_float(cb.y) * __int_as_float(ck.y);
+    const unsigned w = __ldg(C + e);
+    const unsigned idx = w & kIdx;
+    const bool sw = (w & kSwap) != 0;
+    const float pre = g122_pre(w);
     const float vl = f64_to_f32(__ldg(L + idx)), vr = f64_to_f32(__ldg(R + idx));
-    X[e] = make_float2(vl * ((tr && hL < 0) ? -pre : pre), vr * ((tr && hR < 0) ? -pre : pre));
+    X[e] = make_float2(vl * ((sw && hL < 0) ? -pre : pre), vr * ((sw && hR < 0) ? -pre : pre));
   }
   g122_sync(cta, mask);
   const int s1 = n0, s2 = nb, s3 = nb * n2;
@@ -73,15 +78,11 @@ __device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, 
     const int x1 = g122_div(eb, t.m0), x0 = eb - x1 * n0;
     const int x3 = g122_div(ek, t.m2), x2 = ek - x3 * n2;
     if (((t.flags & 2) && x0 > x1) || ((t.flags & 4) && x2 > x3)) continue;  // the other order is stored
-    // where the element goes: rectangular arrays (C1 < C2) at (r, c); C1 > C2 at (c, r) with
-    // hRES (G1 != G2; for G1 == G2 the element (ek, eb) of this sub-block writes it); square
-    // arrays (C1 == C2) only in their upper triangle, at (min, max) with hRES when swapped (the
-    // pass after the recoupling writes every lower triangle from the upper one)
-    const int2 cb = __ldg(PB + eb), ck = __ldg(PK + ek);
-    const int C1 = cb.x & 3, C2 = ck.x & 3;
-    const int r = cb.x >> 2, c = ck.x >> 2;
-    const bool swap = C1 > C2 || (C1 == C2 && r > c);
-    if (swap && !(t.flags & 1)) continue;
+    // written at the code word's position, times hRES when swapped; for G1 == G2 a swapped
+    // element's transposed twin of this sub-block writes it
+    const unsigned w = __ldg(C + e);
+    const bool sw = (w & kSwap) != 0;
+    if (sw && !(t.flags & 1)) continue;
     float out = 0.0f;
     {  // sum_a' f(a, a') X[a', ...]
       const float2* f = F0 + x0 * n0;
@@ -119,12 +120,8 @@ __device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, 
         out = fmaf(fv.y, xv.x, out);
       }
     }
-    const int g = g122_array(C1, C2);
-    const float w = out * g122_inv(__int_as_float(cb.y)) * g122_inv(__int_as_float(ck.y));  // stored = V_A / pre
-    const int64_t base = __ldg(go + g);
-    const int ld = __ldg(gn + g);
-    if (!swap) RES[base + r + (int64_t)c * ld] = f32_to_f64(w);
-    else RES[base + c + (int64_t)r * ld] = f32_to_f64(hRES < 0 ? -w : w);
+    const float v = out * g122_ipre(w);  // stored = V_A / pre
+    RES[w & kIdx] = f32_to_f64((sw && hRES < 0) ? -v : v);
   }
   g122_sync(cta, mask);
 }
@@ -134,7 +131,7 @@ __device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, 
 // runs of tasks from the counter until none is left
 __global__ void __launch_bounds__(kG122Threads, 5) k_comm122_sub(DevLayout D, const G122Task* __restrict__ tasks,
                                                               const int2* __restrict__ items, int nitems, int nbig,
-                                                              int* counter, const int2* __restrict__ PT,
+                                                              int* counter, const unsigned* __restrict__ EC,
                                                               int slice_f2, int sub_f2, const double* __restrict__ L,
                                                               int hL, const double* __restrict__ R, int hR,
                                                               double* __restrict__ RES, int hRES,
@@ -142,7 +139,7 @@ __global__ void __launch_bounds__(kG122Threads, 5) k_comm122_sub(DevLayout D, co
   extern __shared__ float2 g122_x[];
   if ((int)blockIdx.x < nbig) {
     const G122Task t = tasks[blockIdx.x];
-    g122_run(D, t, PT, L, hL, R, hR, RES, hRES, FB, g122_x, threadIdx.x, kG122Threads, true, 0u);
+    g122_run(D, t, EC, L, hL, R, hR, RES, hRES, FB, g122_x, threadIdx.x, kG122Threads, true, 0u);
     return;
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -160,7 +157,7 @@ __global__ void __launch_bounds__(kG122Threads, 5) k_comm122_sub(DevLayout D, co
     const unsigned mask = quad ? 0xFFu << (grp * 8) : 0xffffffffu;
     for (int k = grp; k < cnt; k += step) {
       const G122Task t = tasks[w.x + k];
-      g122_run(D, t, PT, L, hL, R, hR, RES, hRES, FB, slice + grp * sub_f2, lane & (nth - 1), nth, false, mask);
+      g122_run(D, t, EC, L, hL, R, hR, RES, hRES, FB, slice + grp * sub_f2, lane & (nth - 1), nth, false, mask);
     }
     __syncwarp();
   }
@@ -182,9 +179,9 @@ __global__ void k_comm122_fb2(DevLayout D, PairGroupsDev G, int nspb, const doub
 }
 
 void launch_comm122(int grid, size_t smem, cudaStream_t st, const DevLayout& D, const G122Task* tasks,
-                    const int2* items, int nitems, int nbig, int* counter, const int2* pairs, int slice_f2, int sub_f2,
+                    const int2* items, int nitems, int nbig, int* counter, const unsigned* codes, int slice_f2, int sub_f2,
                     const double* L, int hL, const double* R, int hR, double* RES, int hRES, const float2* FB) {
-  k_comm122_sub<<<grid, kG122Threads, smem, st>>>(D, tasks, items, nitems, nbig, counter, pairs, slice_f2, sub_f2, L,
+  k_comm122_sub<<<grid, kG122Threads, smem, st>>>(D, tasks, items, nitems, nbig, counter, codes, slice_f2, sub_f2, L,
                                                   hL, R, hR, RES, hRES, FB);
 }
 
@@ -204,30 +201,37 @@ size_t g122_smem_bytes(int tiny_cap, int warp_cap, int nmax4) {
 std::string build_g122_plan(const Layout& L, const PairGroups& G, G122Plan& P) {
   P = G122Plan();
   const int N = L.N, NJ = L.NJ;
-  // the ordered pairs of every group, in the channel's J
+  if (L.slab >= (int64_t)1 << kG122IdxBits) return "122 plan: operator slab too large for 28-bit positions";
+  // the ordered pairs of every group, in the channel's J: stored position, class, and the
+  // factor pre (sqrt 2 for identical orbits, the exchange phase when the stored order is swapped)
+  struct PairInfo {
+    int pos, cls;
+    int sign, sq;  // pre = (sign ? -1 : 1) * (sq ? sqrt 2 : 1)
+  };
   const int ngrp = (int)G.grp_b1.size();
-  P.grp_pair_off.assign(ngrp, 0);
+  std::vector<int> grp_off(ngrp, 0);
+  std::vector<PairInfo> pairs;
   for (int q = 0; q < L.nblocks; ++q) {
     const int J = L.lamJ[q];
     for (int g = G.grp_first[q]; g < G.grp_first[q + 1]; ++g) {
-      P.grp_pair_off[g] = (int)P.pairs.size();
+      grp_off[g] = (int)pairs.size();
       const int B1 = G.grp_b1[g], B2 = G.grp_b2[g], na = G.spb_n[B1], nb = G.spb_n[B2];
       for (int y = 0; y < na * nb; ++y) {
         const int oa = G.spb_orb[G.spb_start[B1] + y % na], ob = G.spb_orb[G.spb_start[B2] + y / na];
         const int lo = std::min(oa, ob), hi = std::max(oa, ob);
-        float pre = 1.0f;
-        if (oa == ob) pre = 1.41421356f;
-        else if (oa > ob && ((1 + ((L.jj[oa] + L.jj[ob] - J) >> 1)) & 1)) pre = -1.0f;
-        const int pos = L.pairpos[((size_t)lo * N + hi) * NJ + J / 2];
-        if (pos < 0) return "122 plan: a group pair is not in its channel";
-        int bits;
-        std::memcpy(&bits, &pre, sizeof(float));
-        P.pairs.push_back(make_int2((pos << 2) | (L.con[lo] + L.con[hi]), bits));
+        PairInfo pi{};
+        pi.sq = oa == ob;
+        pi.sign = oa > ob && ((1 + ((L.jj[oa] + L.jj[ob] - J) >> 1)) & 1);
+        pi.pos = L.pairpos[((size_t)lo * N + hi) * NJ + J / 2];
+        pi.cls = L.con[lo] + L.con[hi];
+        if (pi.pos < 0) return "122 plan: a group pair is not in its channel";
+        pairs.push_back(pi);
       }
     }
   }
-  // the group-pair tasks G1 <= G2 of every channel
+  // the group-pair tasks G1 <= G2 of every channel, and the code words of their elements
   auto magic = [](int n) { return (int)(((1u << 20) + (unsigned)n - 1u) / (unsigned)n); };
+  static const int kArray[3][3] = {{0, 1, 2}, {1, 3, 5}, {2, 5, 4}};  // gam array of a class pair
   for (int q = 0; q < L.nblocks; ++q)
     for (int G2 = G.grp_first[q]; G2 < G.grp_first[q + 1]; ++G2)
       for (int G1 = G.grp_first[q]; G1 <= G2; ++G1) {
@@ -236,9 +240,9 @@ std::string build_g122_plan(const Layout& L, const PairGroups& G, G122Plan& P) {
         const int64_t el = (int64_t)n[0] * n[1] * n[2] * n[3];
         if (el > kG122MaxElems || n[0] * n[1] > 255 || n[2] * n[3] > 255)
           return "122 plan: a sub-block exceeds 4095 elements (eMax too large)";
+        if (P.codes.size() + (size_t)el >= ((size_t)1 << 31)) return "122 plan: element table too large";
         G122Task t{};
-        t.pb = P.grp_pair_off[G1];
-        t.pk = P.grp_pair_off[G2];
+        t.eoff = (int)P.codes.size();
         t.q = q;
         t.nn = (unsigned)n[0] | (unsigned)n[1] << 8 | (unsigned)n[2] << 16 | (unsigned)n[3] << 24;
         for (int x = 0; x < 4; ++x) t.fb[x] = G.blk_off[b[x]];
@@ -246,6 +250,20 @@ std::string build_g122_plan(const Layout& L, const PairGroups& G, G122Plan& P) {
         t.m2 = magic(n[2]);
         t.mb = magic(n[0] * n[1]);
         t.flags = (G1 != G2 ? 1 : 0) | (b[0] == b[1] ? 2 : 0) | (b[2] == b[3] ? 4 : 0);
+        const int nbra = n[0] * n[1];
+        for (int64_t e = 0; e < el; ++e) {
+          const PairInfo& pb = pairs[grp_off[G1] + (int)(e % nbra)];
+          const PairInfo& pk = pairs[grp_off[G2] + (int)(e / nbra)];
+          // the stored element: rectangular array of the class pair, or a square array's upper
+          // triangle; swapped when the element is herm times it
+          const bool sw = pb.cls > pk.cls || (pb.cls == pk.cls && pb.pos > pk.pos);
+          const int row = sw ? pk.pos : pb.pos, col = sw ? pb.pos : pk.pos;
+          const int k = q * 6 + kArray[pb.cls][pk.cls];
+          const int64_t idx = L.goff[k] + row + (int64_t)col * L.gn1[k];
+          const int sq = pb.sq + pk.sq;  // pre = (-1)^sign x sqrt 2^sq
+          P.codes.push_back((unsigned)idx | (sw ? 1u : 0u) << kG122IdxBits | (unsigned)(pb.sign ^ pk.sign) << 29 |
+                            (unsigned)sq << 30);
+        }
         P.all.push_back(t);
         P.elems.push_back(el);
         P.nmax4 = std::max<int>(P.nmax4, (int)el);

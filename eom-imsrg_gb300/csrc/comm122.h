@@ -18,7 +18,7 @@ constexpr int kG122MaxElems = 4095;  // elements of one sub-block (the 20-bit di
 
 // One group-pair sub-block (G1 <= G2) of channel q, everything the kernel needs about it.
 struct __align__(16) G122Task {
-  int pb, pk;          // first pair-table entries of the bra group G1 and the ket group G2
+  int eoff, pad;       // first code word of its elements in the element table
   int q;               // channel
   unsigned nn;         // block sizes n0 | n1 << 8 | n2 << 16 | n3 << 24 (bra: n0 n1, ket: n2 n3)
   int fb[4];           // offsets of the four blocks' f matrices in the (fL, fR) table
@@ -28,9 +28,14 @@ struct __align__(16) G122Task {
 
 // A run of tasks for one warp: x = first task, y = count | lanes << 16 (lanes 0: four 8-lane
 // groups, task k on group k mod 4; 1: the whole warp, one task after another).
+// Code word of one element (x0 + n0 (x1 + n1 (x2 + n2 x3))) of a sub-block: its storage position
+// in the upper triangle or rectangular array where the stored operators keep it (bits 0-27),
+// swapped (bit 28: the element is herm times the stored one, and for G1 == G2 the element of
+// the transposed position stores the result), the sign (bit 29) and size (bits 30-31: 1, sqrt 2,
+// 2) of pre, V_A = pre x stored.
+constexpr unsigned kG122IdxBits = 28;
 struct G122Plan {
-  std::vector<int2> pairs;       // per group, its n(B1) n(B2) ordered pairs: {pos << 2 | class, bits of pre}
-  std::vector<int> grp_pair_off; // per group: first entry in pairs
+  std::vector<unsigned> codes;   // the element table: per task of `all`, its elements' code words
   std::vector<int64_t> elems;    // per task of `all`: elements of its sub-block
   std::vector<G122Task> all;     // every task, channel by channel
   // launch order for the current caps: the big tasks (one CTA each) first, then the warp tasks
@@ -55,7 +60,7 @@ cudaError_t g122_blocks_per_sm(size_t smem, int* n);  // resident CTAs of the 12
 __global__ void k_comm122_fb2(DevLayout D, PairGroupsDev G, int nspb, const double* L, int hL, const double* R, int hR,
                               float2* FB, int* counter);
 void launch_comm122(int grid, size_t smem, cudaStream_t st, const DevLayout& D, const G122Task* tasks,
-                    const int2* items, int nitems, int nbig, int* counter, const int2* pairs, int slice_f2, int sub_f2,
+                    const int2* items, int nitems, int nbig, int* counter, const unsigned* codes, int slice_f2, int sub_f2,
                     const double* L, int hL, const double* R, int hR, double* RES, int hRES, const float2* FB);
 
 }  // namespace imsrg

@@ -541,7 +541,7 @@ struct TcState {
   G122Plan g122;
   G122Task* d_g122_tasks = nullptr;
   int2* d_g122_items = nullptr;
-  const int2* d_g122_pairs = nullptr;
+  const unsigned* d_g122_codes = nullptr;
   int* d_g122_counter = nullptr;
   PairGroupsDev g122_w{};
   int g122_nspb = 0, g122_nblk2 = 0, g122_per_sm = 1;
@@ -829,7 +829,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->g_b1, &tc->g122_w.grp_b1);
   pk.add(tc->g_b2, &tc->g122_w.grp_b2);
   pk.add(tc->g_blk_off, &tc->g122_w.blk_off);
-  pk.add(tc->g122.pairs, &tc->d_g122_pairs);
+  pk.add(tc->g122.codes, &tc->d_g122_codes);
 
   CK_TC(cuda(cudaMalloc(&tc->d_mem, pk.buf.size()), "cudaMalloc(tc tables)"));
   CK_TC(cuda(cudaMemcpy(tc->d_mem, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice), "cudaMemcpy(tc tables)"));
@@ -1035,7 +1035,7 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     // memory allows (the warps take the runs from the counter)
     const int grid = P.nbig + tc->num_sms * std::max(1, tc->g122_per_sm);
     launch_comm122(grid, P.smem_bytes, stream, D, tc->d_g122_tasks, tc->d_g122_items, (int)P.items.size(), P.nbig,
-                   tc->d_g122_counter, tc->d_g122_pairs, std::max(P.warp_cap, 4 * P.tiny_cap), P.tiny_cap, Lp, hL,
+                   tc->d_g122_counter, tc->d_g122_codes, std::max(P.warp_cap, 4 * P.tiny_cap), P.tiny_cap, Lp, hL,
                    Rp, hR, RES, hRES, tc->g122_fb);
     CK_TC(launched("k_comm122_sub"));
   }
