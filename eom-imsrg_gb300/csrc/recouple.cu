@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_recouple_q(DevLayout D, con
       const int* rows = D.ccr_t + l * NJ * N + j;
       for (int m = 0; m < nd; ++m) {
         const int h = (dlo >> 1) + m;
-        zd[m] = __ldg(X + __ldg(col + h) + __ldg(rows + h * N));
+        zd[m] = __ldg(X + col[h] + __ldg(rows + h * N));
       }
     }
     {  // exchange: row pair (k, j), column pair (i, l)
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_recouple_q(DevLayout D, con
       const int* rows = D.ccr_t + k * NJ * N + j;
       for (int m = 0; m < ne; ++m) {
         const int h = (elo >> 1) + m;
-        ze[m] = __ldg(X + __ldg(col + h) + __ldg(rows + h * N));
+        ze[m] = __ldg(X + col[h] + __ldg(rows + h * N));
       }
     }
     const int nh = D.sj_nh;
