@@ -338,7 +338,7 @@ imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, doubl
 imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2, bool f32) {
   if (D.n_ob == 0) return IMSRG_OK;
   if (f32) {
-    k_comm221f<<<(D.n_ob * 32 + kThreads - 1) / kThreads, kThreads, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);
+    k_comm221f<<<D.n_ob, 256, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);
     return launched("k_comm221f");
   }
   k_comm221<<<(D.n_ob * 32 + kThreads - 1) / kThreads, kThreads, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);

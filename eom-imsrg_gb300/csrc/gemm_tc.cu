@@ -1023,7 +1023,11 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     CK_TC(tc_gemm(tc->d_pphh_probs, tc->d_pphh_tiles, (int)tc->pphh_tiles.size(), gout, hL, hR, tc->wmax[0]));
   mark(kPhasePphhGemm);
   if (with_e0) CK_TC(e0(Lp, hL, Rp, hR, RES, nullptr));
-  CK_TC(c111(Lp, hL, Rp, hR, RES));
+  {  // commutator_111 block by block (one-body operators only couple orbits of one (l, j, tz) block)
+    const int n = L.A * L.A + L.P * L.A + L.P * L.P;
+    k_comm111f<<<(n + 255) / 256, 256, 0, stream>>>(D, Lp, hL, Rp, hR, RES);
+    CK_TC(launched("k_comm111f"));
+  }
   CK_TC(c121(Lp, hL, Rp, hR, RES, hRES));
   mark(kPhaseOneBody);
   if (L.n_unique) {

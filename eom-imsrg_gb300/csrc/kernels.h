@@ -22,6 +22,7 @@ __global__ void k_e0_partial(DevLayout D, const double* L, int hL, const double*
 __global__ void k_e0_final(DevLayout D, const double* partial, double* RES, double* out);
 __global__ void k_pphh_update_tiled(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
                                     double pm);
+__global__ void k_comm111f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES);
 __global__ void k_comm221f(DevLayout D, int pm, double* RES, int hRES, const double* w1, const double* w2);
 
 __global__ void k_monopole(DevLayout D, const double* H, int hH, double* mono);

@@ -115,35 +115,75 @@ void launch_pandya_tc(int S, int kind, int nchunks, cudaStream_t stream, const D
     k_pandya_tc<3, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
 }
 
-// commutator_221 (src/commutators.f90:435-578) with FP32 arithmetic: one warp per
-// one-body output, ACCUMULATES into RES (FP64)
-__global__ void k_comm221f(DevLayout D, int pm, double* __restrict__ RES, int hRES, const double* __restrict__ w1,
-                           const double* __restrict__ w2) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= D.n_ob) return;
-  const int kind = D.ob_kind[warp], p = D.ob_p[warp], q = D.ob_q[warp], ik = D.ob_pk[warp], jk = D.ob_qk[warp];
+// commutator_221 (src/commutators.f90:435-578) with FP32 arithmetic, ACCUMULATES into RES
+// (FP64).  About a thousand one-body outputs at eMax=10, so one 256-thread CTA per output: the
+// threads take the (orbit c, JT) terms of its sum, (2JT+1) w(c p, c q; JT) with w = W1 for a
+// hole c and W2 for a particle, all independent, and a block reduction adds them up.
+__global__ void __launch_bounds__(256) k_comm221f(DevLayout D, int pm, double* __restrict__ RES, int hRES,
+                                                  const double* __restrict__ w1, const double* __restrict__ w2) {
+  __shared__ float red[8];
+  const int o = blockIdx.x;
+  if (o >= D.n_ob) return;
+  const int kind = D.ob_kind[o], p = D.ob_p[o], q = D.ob_q[o], ik = D.ob_pk[o], jk = D.ob_qk[o];
   const int ji = D.jj[ik];
   float sm = 0.0f;
   VRefF r;
-  for (int ck = lane; ck < D.N; ck += 32) {
-    const double* w = D.con[ck] ? w1 : w2;
+  for (int t = threadIdx.x; t < D.N * D.NJ; t += blockDim.x) {
+    const int ck = t % D.N, m = t / D.N;
     const int jc = D.jj[ck];
-    for (int JT = abs(jc - ji); JT <= jc + ji; JT += 2) {
-      float v = d_vref_f(D, ck, ik, ck, jk, JT, r) ? f64_to_f32(w[r.idx]) * r.pre : 0.0f;
-      if (kind < 2 && d_vref_f(D, ck, jk, ck, ik, JT, r)) v -= (float)pm * f64_to_f32(w[r.idx]) * r.pre;
-      sm += v * (float)(JT + 1);
-    }
+    const int JT = abs(jc - ji) + 2 * m;
+    if (JT > jc + ji) continue;
+    const double* w = D.con[ck] ? w1 : w2;
+    float v = d_vref_f(D, ck, ik, ck, jk, JT, r) ? f64_to_f32(w[r.idx]) * r.pre : 0.0f;
+    if (kind < 2 && d_vref_f(D, ck, jk, ck, ik, JT, r)) v -= (float)pm * f64_to_f32(w[r.idx]) * r.pre;
+    sm += v * (float)(JT + 1);
   }
-  for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
-  if (lane == 0) {
+  for (int s = 16; s > 0; s >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sm;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float tot = 0.0f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += red[k];
     double* f = (kind == 0) ? RES + D.off_fhh + p + (int64_t)q * D.A
                             : (kind == 1 ? RES + D.off_fpp + p + (int64_t)q * D.P : RES + D.off_fph + p + (int64_t)q * D.P);
-    const double v = *f + (double)(sm / (float)(ji + 1));
+    const double v = *f + (double)(tot / (float)(ji + 1));
     *f = v;
     if (kind < 2) {
       double* g = (kind == 0) ? RES + D.off_fhh + q + (int64_t)p * D.A : RES + D.off_fpp + q + (int64_t)p * D.P;
       *g = v * hRES;
     }
+  }
+}
+
+// commutator_111 (src/commutators.f90:36-80) of the mixed path, FP64, ASSIGNS the one-body part:
+// one thread per element of fhh, fph and fpp.  One-body operators only couple orbits of one
+// (l, j, tz) block, so (L R - R L)(a, b) sums over the at most six orbits of that block and is
+// zero between blocks.
+__global__ void k_comm111f(DevLayout D, const double* __restrict__ L, int hL, const double* __restrict__ R, int hR,
+                           double* __restrict__ RES) {
+  const int A = D.A, P = D.P;
+  const int total = A * A + P * A + P * P;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int a, b;
+    int64_t off;
+    if (t < A * A) {
+      a = D.holes[t % A]; b = D.holes[t / A]; off = D.off_fhh + t;
+    } else if (t < A * A + P * A) {
+      const int s = t - A * A;
+      a = D.parts[s % P]; b = D.holes[s / P]; off = D.off_fph + s;
+    } else {
+      const int s = t - A * A - P * A;
+      a = D.parts[s % P]; b = D.parts[s / P]; off = D.off_fpp + s;
+    }
+    double v = 0.0;
+    if (D.jj[a] == D.jj[b] && D.ll[a] == D.ll[b] && D.tz[a] == D.tz[b]) {
+      const int* blk = D.same_list + D.same_start[a];
+      for (int x = 0; x < D.same_count[a]; ++x) {
+        const int k = blk[x];
+        v += d_f_elem(D, L, hL, a, k) * d_f_elem(D, R, hR, k, b) - d_f_elem(D, R, hR, a, k) * d_f_elem(D, L, hL, k, b);
+      }
+    }
+    RES[off] = v;
   }
 }
 
