@@ -303,23 +303,38 @@ imsrg_status Ctx::pphh_clear(double* w1, double* w2) {
   return IMSRG_OK;
 }
 
+imsrg_status Ctx::pphh_clear_f(float* w1, float* w2) {
+  if (!zero_runs_w1.empty()) {
+    k_zero_runs_f<<<(int)zero_runs_w1.size() / 2, 256, 0, stream>>>(w1, d_zero_runs_w1);
+    CK(launched("k_zero_runs_f"));
+  }
+  if (!zero_runs_w2.empty()) {
+    k_zero_runs_f<<<(int)zero_runs_w2.size() / 2, 256, 0, stream>>>(w2, d_zero_runs_w2);
+    CK(launched("k_zero_runs_f"));
+  }
+  return IMSRG_OK;
+}
+
 // RES += W1 - W2 - pm (W1 - W2)^T on the square arrays, RES += W1 - W2 on the others
-imsrg_status Ctx::pphh_accumulate(int hL, int hR, double* RES, const double* w1, const double* w2, bool upper_f32) {
+imsrg_status Ctx::pphh_accumulate(int hL, int hR, double* RES, const double* w1, const double* w2) {
   if (!upd_tiles.empty()) {
-    if (upper_f32) {
-      k_pphh_update_f<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (float)(hL * hR));
-      CK(launched("k_pphh_update_f"));
-    } else {
-      k_pphh_update_tiled<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (double)(hL * hR));
-      CK(launched("k_pphh_update_tiled"));
-    }
+    k_pphh_update_tiled<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (double)(hL * hR));
+    CK(launched("k_pphh_update_tiled"));
   }
   mark(kPhasePphhUpdate);
   return IMSRG_OK;
 }
 
-imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* w1, double* w2,
-                       bool upper_f32) {
+imsrg_status Ctx::pphh_accumulate_f(int hL, int hR, double* RES, const float* w1, const float* w2) {
+  if (!upd_tiles.empty()) {
+    k_pphh_update_f<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (float)(hL * hR));
+    CK(launched("k_pphh_update_f"));
+  }
+  mark(kPhasePphhUpdate);
+  return IMSRG_OK;
+}
+
+imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* w1, double* w2) {
   CK(pphh_clear(w1, w2));
   if (precision != IMSRG_PREC_FP64) {
     CK(tc_pphh(Lp, hL, Rp, hR, w1, w2));
@@ -332,15 +347,17 @@ imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, doubl
     CK(launched("k_gemm_fp64(pphh)"));
   }
   mark(kPhasePphhGemm);
-  return pphh_accumulate(hL, hR, RES, w1, w2, upper_f32);
+  return pphh_accumulate(hL, hR, RES, w1, w2);
 }
 
-imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2, bool f32) {
+imsrg_status Ctx::c221_f(int hL, int hR, double* RES, int hRES, const float* w1, const float* w2) {
   if (D.n_ob == 0) return IMSRG_OK;
-  if (f32) {
-    k_comm221f<<<D.n_ob, 256, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);
-    return launched("k_comm221f");
-  }
+  k_comm221f<<<D.n_ob, 256, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);
+  return launched("k_comm221f");
+}
+
+imsrg_status Ctx::c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2) {
+  if (D.n_ob == 0) return IMSRG_OK;
   k_comm221<<<(D.n_ob * 32 + kThreads - 1) / kThreads, kThreads, 0, stream>>>(D, hL * hR, RES, hRES, w1, w2);
   return launched("k_comm221");
 }
@@ -378,7 +395,7 @@ imsrg_status Ctx::commutator(const double* Lp, int hL, const double* Rp, int hR,
   CK(c122(Lp, hL, Rp, hR, RES, hRES));
   mark(kPhase122);
   CK(pphh(Lp, hL, Rp, hR, RES, d_w1, d_w2));
-  CK(c221(hL, hR, RES, hRES, d_w1, d_w2, false));
+  CK(c221(hL, hR, RES, hRES, d_w1, d_w2));
   mark(kPhase221);
   CK(ensure_wcc());
   CK(ph(d_lcc, hL, d_rcc, hR, RES, hRES, d_wcc));
@@ -1046,7 +1063,7 @@ imsrg_status imsrg_commutator_221(imsrg_ctx* ctx, const imsrg_op* L, const imsrg
   THREE_OPS("imsrg_commutator_221");
   CK(check_op(c, w1, "imsrg_commutator_221"));
   CK(check_op(c, w2, "imsrg_commutator_221"));
-  return c->c221(L->herm, R->herm, RES->d, RES->herm, w1->d, w2->d, false);
+  return c->c221(L->herm, R->herm, RES->d, RES->herm, w1->d, w2->d);
 }
 
 imsrg_status imsrg_commutator_222_ph(imsrg_ctx* ctx, const imsrg_cc* LCC, const imsrg_cc* RCC, imsrg_op* RES,

@@ -357,6 +357,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               const int n = tile.n0 + c0 + j;
               if (n < P.N) C[m + (int64_t)n * P.ldc] = __uint_as_float(r[j]);
             }
+          } else if (out.w1f && P.c_id == kOpW1) {
+            float* C = out.w1f + P.c_off;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const int n = tile.n0 + c0 + j;
+              if (n < P.N) C[m + (int64_t)n * P.ldc] = __uint_as_float(r[j]);
+            }
           } else {
             double* C = out.f64[P.c_id] + P.c_off;
 #pragma unroll
@@ -422,8 +429,11 @@ __global__ void __launch_bounds__(256) k_split_chunks(const TcSplitOp* __restric
 
 // ---------------------------------------------------------------- small-K FP32 GEMM
 // The K = nhh problems of 222_pp_hh (every W2 product): FP32 SIMT, FP64 in and out.
-__global__ void __launch_bounds__(256) k_gemm_f32(const GemmProb* __restrict__ probs, const GemmTile* __restrict__ tiles,
-                                                  GemmOperands ops) {
+// C = sum of alpha op(A) op(B) in FP32 on the SIMT cores, stored as TO (double, or float at
+// the same element offsets of the output buffer)
+template <typename TO>
+__device__ __forceinline__ void gemm_f32_tile(const GemmProb* __restrict__ probs, const GemmTile* __restrict__ tiles,
+                                              const GemmOperands& ops) {
   __shared__ float As[16][65];
   __shared__ float Bs[16][65];
   const GemmTile tile = tiles[blockIdx.x];
@@ -471,14 +481,23 @@ __global__ void __launch_bounds__(256) k_gemm_f32(const GemmProb* __restrict__ p
       __syncthreads();
     }
   }
-  double* C = ops.out[P.c_id] + P.c_off;
+  TO* C = reinterpret_cast<TO*>(ops.out[P.c_id]) + P.c_off;
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int gm = tile.m0 + tx + 16 * i, gn = tile.n0 + ty + 16 * j;
-      if (gm < P.M && gn < P.N) C[gm + (int64_t)gn * P.ldc] = (double)acc[i][j];
+      if (gm < P.M && gn < P.N) C[gm + (int64_t)gn * P.ldc] = (TO)acc[i][j];
     }
+}
+__global__ void __launch_bounds__(256) k_gemm_f32(const GemmProb* __restrict__ probs, const GemmTile* __restrict__ tiles,
+                                                  GemmOperands ops) {
+  gemm_f32_tile<double>(probs, tiles, ops);
+}
+// the same with FP32 outputs (the mixed commutator's W2)
+__global__ void __launch_bounds__(256) k_gemm_f32_w(const GemmProb* __restrict__ probs,
+                                                    const GemmTile* __restrict__ tiles, GemmOperands ops) {
+  gemm_f32_tile<float>(probs, tiles, ops);
 }
 
 }  // namespace imsrg
@@ -1008,13 +1027,15 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     CK_TC(launched("k_pandya_tc"));
   }
   mark(kPhasePandya);
-  CK_TC(pphh_clear(d_w1, d_w2));
+  // W1 and W2 of the ladder in FP32, in the first half of the FP64 workspaces
+  float* w1f = reinterpret_cast<float*>(d_w1);
+  float* w2f = reinterpret_cast<float*>(d_w2);
+  CK_TC(pphh_clear_f(w1f, w2f));
   if (!tc->chunks.empty()) CK_TC(tc_split_on(tc->d_split_ops, tc->d_chunks, (int)tc->chunks.size(), Lp, Rp, tc->buf,
                                              tc->slice_elems));
   mark(kPhasePphhSplit);
   TcOut gout{};
-  gout.f64[kOpW1] = d_w1;
-  gout.f64[kOpW2] = d_w2;
+  gout.w1f = w1f;
   gout.f32 = tc->zbuf;
   if (tc->merged)
     CK_TC(tc_gemm(tc->d_all_probs, tc->d_tile_mem + tc->tile_cap_all, (int)tc->all_tiles.size(), gout, hL, hR,
@@ -1047,14 +1068,14 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   if (!tc->small_tiles.empty()) {  // the K = nhh products (W2) on FP32 SIMT
     GemmOperands ops{};
     ops.in[kOpL] = Lp; ops.in[kOpR] = Rp;
-    ops.out[kOpW1] = d_w1; ops.out[kOpW2] = d_w2;
+    ops.out[kOpW1] = d_w1; ops.out[kOpW2] = d_w2;  // FP32 stores at the same element offsets
     ops.hL = hL; ops.hR = hR;
-    k_gemm_f32<<<(int)tc->small_tiles.size(), 256, 0, stream>>>(tc->d_small_probs, tc->d_small_tiles, ops);
-    CK_TC(launched("k_gemm_f32"));
+    k_gemm_f32_w<<<(int)tc->small_tiles.size(), 256, 0, stream>>>(tc->d_small_probs, tc->d_small_tiles, ops);
+    CK_TC(launched("k_gemm_f32_w"));
   }
   mark(kPhasePphhSmall);
-  CK_TC(pphh_accumulate(hL, hR, RES, d_w1, d_w2, true));
-  CK_TC(c221(hL, hR, RES, hRES, d_w1, d_w2, true));
+  CK_TC(pphh_accumulate_f(hL, hR, RES, w1f, w2f));
+  CK_TC(c221_f(hL, hR, RES, hRES, w1f, w2f));
   mark(kPhase221);
   if (!tc->merged) {
     CK_TC(tc_gemm(tc->d_z_probs, tc->d_z_tiles, (int)tc->z_tiles.size(), gout, hL, hR, tc->wmax[1]));

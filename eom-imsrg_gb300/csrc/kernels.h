@@ -23,7 +23,7 @@ __global__ void k_e0_final(DevLayout D, const double* partial, double* RES, doub
 __global__ void k_pphh_update_tiled(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
                                     double pm);
 __global__ void k_comm111f(DevLayout D, const double* L, int hL, const double* R, int hR, double* RES);
-__global__ void k_comm221f(DevLayout D, int pm, double* RES, int hRES, const double* w1, const double* w2);
+__global__ void k_comm221f(DevLayout D, int pm, double* RES, int hRES, const float* w1, const float* w2);
 
 __global__ void k_monopole(DevLayout D, const double* H, int hH, double* mono);
 __global__ void k_white_1b(DevLayout D, const double* H, int hH, double* ETA);
@@ -38,6 +38,7 @@ __global__ void k_sum_sqrt(const double* partial, int n, double scale, double* o
 __global__ void k_mbpt2_partial(DevLayout D, const double* H, int hH, double* partial);
 __global__ void k_sum(const double* partial, int n, double* out);
 __global__ void k_zero_runs(double* x, const int64_t* runs);
+__global__ void k_zero_runs_f(float* x, const int64_t* runs);
 __global__ void k_convert_check(const double* x, const float* y, int64_t n, float* out_f32, double* out_f64);
 
 __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOperands ops);
@@ -45,7 +46,7 @@ __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOp
 // mixed-precision companions (kernels_mixed.cu)
 void launch_pandya_tc(int S, int kind, int nchunks, cudaStream_t stream, const DevLayout& D, const PandyaChunk* chunks,
                       const PandyaOps& ops, void* buf, int64_t slice_elems, const int* swap_row);
-__global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const double* w1, const double* w2,
+__global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const float* w1, const float* w2,
                                 float pm);
 __global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);
 

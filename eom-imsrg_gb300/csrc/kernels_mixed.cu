@@ -120,7 +120,7 @@ void launch_pandya_tc(int S, int kind, int nchunks, cudaStream_t stream, const D
 // threads take the (orbit c, JT) terms of its sum, (2JT+1) w(c p, c q; JT) with w = W1 for a
 // hole c and W2 for a particle, all independent, and a block reduction adds them up.
 __global__ void __launch_bounds__(256) k_comm221f(DevLayout D, int pm, double* __restrict__ RES, int hRES,
-                                                  const double* __restrict__ w1, const double* __restrict__ w2) {
+                                                  const float* __restrict__ w1, const float* __restrict__ w2) {
   __shared__ float red[8];
   const int o = blockIdx.x;
   if (o >= D.n_ob) return;
@@ -133,9 +133,9 @@ __global__ void __launch_bounds__(256) k_comm221f(DevLayout D, int pm, double* _
     const int jc = D.jj[ck];
     const int JT = abs(jc - ji) + 2 * m;
     if (JT > jc + ji) continue;
-    const double* w = D.con[ck] ? w1 : w2;
-    float v = d_vref_f(D, ck, ik, ck, jk, JT, r) ? f64_to_f32(w[r.idx]) * r.pre : 0.0f;
-    if (kind < 2 && d_vref_f(D, ck, jk, ck, ik, JT, r)) v -= (float)pm * f64_to_f32(w[r.idx]) * r.pre;
+    const float* w = D.con[ck] ? w1 : w2;
+    float v = d_vref_f(D, ck, ik, ck, jk, JT, r) ? __ldg(w + r.idx) * r.pre : 0.0f;
+    if (kind < 2 && d_vref_f(D, ck, jk, ck, ik, JT, r)) v -= (float)pm * __ldg(w + r.idx) * r.pre;
     sm += v * (float)(JT + 1);
   }
   for (int s = 16; s > 0; s >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, s);
@@ -190,8 +190,8 @@ __global__ void k_comm111f(DevLayout D, const double* __restrict__ L, int hL, co
 // 222_pp_hh accumulation for the mixed path: FP32 arithmetic, upper triangles of the
 // square arrays only (a final mirror pass restores the lower triangles).
 __global__ void __launch_bounds__(256) k_pphh_update_f(DevLayout D, const int4* __restrict__ tiles,
-                                                       double* __restrict__ RES, const double* __restrict__ w1,
-                                                       const double* __restrict__ w2, float pm) {
+                                                       double* __restrict__ RES, const float* __restrict__ w1,
+                                                       const float* __restrict__ w2, float pm) {
   __shared__ float Xa[32][33];
   __shared__ float Xb[32][33];
   const int4 t = tiles[blockIdx.x];
@@ -204,18 +204,17 @@ __global__ void __launch_bounds__(256) k_pphh_update_f(DevLayout D, const int4* 
       const int i = i0 + tx, j = j0 + r;
       if (i < n1 && j < n2) {
         const int64_t e = base + i + (int64_t)j * n1;
-        RES[e] += f32_to_f64(f64_to_f32(w1[e]) - f64_to_f32(w2[e]));
+        RES[e] += f32_to_f64(w1[e] - w2[e]);
       }
     }
     return;
   }
   for (int r = ty; r < 32; r += 8) {
     const int i = i0 + tx, j = j0 + r;
-    Xa[r][tx] = (i < n1 && j < n1) ? f64_to_f32(w1[base + i + (int64_t)j * n1]) - f64_to_f32(w2[base + i + (int64_t)j * n1])
+    Xa[r][tx] = (i < n1 && j < n1) ? w1[base + i + (int64_t)j * n1] - w2[base + i + (int64_t)j * n1]
                                    : 0.0f;
     const int ib = j0 + tx, jb = i0 + r;
-    Xb[r][tx] = (ib < n1 && jb < n1) ? f64_to_f32(w1[base + ib + (int64_t)jb * n1]) -
-                                           f64_to_f32(w2[base + ib + (int64_t)jb * n1])
+    Xb[r][tx] = (ib < n1 && jb < n1) ? w1[base + ib + (int64_t)jb * n1] - w2[base + ib + (int64_t)jb * n1]
                                      : 0.0f;
   }
   __syncthreads();

@@ -192,5 +192,9 @@ __global__ void k_zero_runs(double* __restrict__ x, const int64_t* __restrict__ 
   const int64_t a = runs[2 * blockIdx.x], n = runs[2 * blockIdx.x + 1];
   for (int64_t e = threadIdx.x; e < n; e += blockDim.x) x[a + e] = 0.0;
 }
+__global__ void k_zero_runs_f(float* __restrict__ x, const int64_t* __restrict__ runs) {
+  const int64_t a = runs[2 * blockIdx.x], n = runs[2 * blockIdx.x + 1];
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) x[a + e] = 0.0f;
+}
 
 }  // namespace imsrg

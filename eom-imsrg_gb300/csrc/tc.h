@@ -78,6 +78,7 @@ struct TcOut {
   double* f64[8];
   float* f32;   // out_f32 == 1
   float* f32b;  // out_f32 == 2
+  float* w1f;   // when set: the W1 problems (c_id kOpW1) store FP32 here, same element offsets
 };
 
 }  // namespace imsrg
