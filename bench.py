@@ -254,9 +254,13 @@ def algorithmic_work(eng, mode: str, phase: str, merged: bool = False):
         eng._ck(eng.L.imsrg_recouple_traffic(eng.h, *[C.byref(x) for x in v]))
         x_reads, x_distinct, res_elems, aux = (x.value for x in v)
         return "hbm", 4 * x_distinct + 16 * res_elems + aux
-    if phase == "mirror":     # the upper triangle of every square array read, the lower written
-        sq = sum(n * (n - 1) // 2 for g in ("npp", "nph", "nhh") for n in (int(x) for x in info[g]))
-        return "hbm", 16 * sq
+    if phase == "pphh_update":  # W1 and W2 (FP32) read where RES is updated, RES's upper triangles and
+        #                         rectangular arrays read and written, the lower triangles written
+        npp, nph_, nhh = (info[k].astype(np.int64) for k in ("npp", "nph", "nhh"))
+        sq_up = int((npp * (npp + 1) // 2 + nph_ * (nph_ + 1) // 2 + nhh * (nhh + 1) // 2).sum())
+        rect = int((npp * nph_ + npp * nhh + nph_ * nhh).sum())
+        sq_low = int((npp * (npp - 1) // 2 + nph_ * (nph_ - 1) // 2 + nhh * (nhh - 1) // 2).sum())
+        return "hbm", (2 * 4 + 16) * (sq_up + rect) + 2 * 4 * sq_low + 8 * sq_low
     if phase == "c122":       # read L and R once, write every unique 2b element of RES once (the
         #                       lower triangles of the square arrays come from the mirror pass)
         npp, nph_, nhh = (info[k].astype(np.int64) for k in ("npp", "nph", "nhh"))

@@ -325,14 +325,7 @@ imsrg_status Ctx::pphh_accumulate(int hL, int hR, double* RES, const double* w1,
   return IMSRG_OK;
 }
 
-imsrg_status Ctx::pphh_accumulate_f(int hL, int hR, double* RES, const float* w1, const float* w2) {
-  if (!upd_tiles.empty()) {
-    k_pphh_update_f<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1, w2, (float)(hL * hR));
-    CK(launched("k_pphh_update_f"));
-  }
-  mark(kPhasePphhUpdate);
-  return IMSRG_OK;
-}
+
 
 imsrg_status Ctx::pphh(const double* Lp, int hL, const double* Rp, int hR, double* RES, double* w1, double* w2) {
   CK(pphh_clear(w1, w2));

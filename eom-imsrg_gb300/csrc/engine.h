@@ -115,10 +115,8 @@ struct Ctx {
   imsrg_status pphh_clear(double* w1, double* w2);
   imsrg_status pphh_accumulate(int hL, int hR, double* RES, const double* w1, const double* w2);
   imsrg_status c221(int hL, int hR, double* RES, int hRES, const double* w1, const double* w2);
-  // the same on FP32 W1 / W2 (the mixed commutator's own workspaces, same element offsets);
-  // the update writes the upper triangles of the square arrays only (a mirror pass follows)
+  // the same on FP32 W1 / W2 (the mixed commutator's own workspaces, same element offsets)
   imsrg_status pphh_clear_f(float* w1, float* w2);
-  imsrg_status pphh_accumulate_f(int hL, int hR, double* RES, const float* w1, const float* w2);
   imsrg_status c221_f(int hL, int hR, double* RES, int hRES, const float* w1, const float* w2);
   imsrg_status ensure_wcc();
   imsrg_status ph(const double* lcc, int hL, const double* rcc, int hR, double* RES, int hRES, double* wcc);

@@ -1074,7 +1074,6 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     CK_TC(launched("k_gemm_f32_w"));
   }
   mark(kPhasePphhSmall);
-  CK_TC(pphh_accumulate_f(hL, hR, RES, w1f, w2f));
   CK_TC(c221_f(hL, hR, RES, hRES, w1f, w2f));
   mark(kPhase221);
   if (!tc->merged) {
@@ -1088,11 +1087,14 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
     CK_TC(launched("k_recouple_q"));
   }
   mark(kPhaseRecouple);
+  // the ladder's contribution last (additions commute), with the lower triangles of the square
+  // arrays written from the updated upper ones in the same pass
   if (!upd_tiles.empty()) {
-    k_mirror_square<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, hRES);
-    CK_TC(launched("k_mirror_square"));
+    k_pphh_update_mirror_f<<<(int)upd_tiles.size(), 256, 0, stream>>>(D, d_upd_tiles, RES, w1f, w2f,
+                                                                     (float)(hL * hR), hRES);
+    CK_TC(launched("k_pphh_update_mirror_f"));
   }
-  mark(kPhaseMirror);
+  mark(kPhasePphhUpdate);
   return IMSRG_OK;
 }
 

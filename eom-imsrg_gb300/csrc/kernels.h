@@ -46,8 +46,7 @@ __global__ void k_gemm_fp64(const GemmProb* probs, const GemmTile* tiles, GemmOp
 // mixed-precision companions (kernels_mixed.cu)
 void launch_pandya_tc(int S, int kind, int nchunks, cudaStream_t stream, const DevLayout& D, const PandyaChunk* chunks,
                       const PandyaOps& ops, void* buf, int64_t slice_elems, const int* swap_row);
-__global__ void k_pphh_update_f(DevLayout D, const int4* tiles, double* RES, const float* w1, const float* w2,
-                                float pm);
-__global__ void k_mirror_square(DevLayout D, const int4* tiles, double* RES, int herm);
+__global__ void k_pphh_update_mirror_f(DevLayout D, const int4* tiles, double* RES, const float* w1, const float* w2,
+                                       float pm, int herm);
 
 }  // namespace imsrg

@@ -187,13 +187,19 @@ __global__ void k_comm111f(DevLayout D, const double* __restrict__ L, int hL, co
   }
 }
 
-// 222_pp_hh accumulation for the mixed path: FP32 arithmetic, upper triangles of the
-// square arrays only (a final mirror pass restores the lower triangles).
-__global__ void __launch_bounds__(256) k_pphh_update_f(DevLayout D, const int4* __restrict__ tiles,
-                                                       double* __restrict__ RES, const float* __restrict__ w1,
-                                                       const float* __restrict__ w2, float pm) {
+
+// lower triangle of every square array (pppp, phph, hhhh) = herm * upper triangle
+// The ladder update and the mirror pass in one: RES += W1 - W2 on the rectangular arrays and,
+// on the square arrays, RES(i, j) += W(i, j) - pm W(j, i) for i <= j (W = W1 - W2, FP32) with
+// the lower triangle then written from the updated upper one, RES(j, i) = herm RES(i, j).  It
+// runs after every other contribution to RES's two-body part (122 assigns it, the recoupling
+// adds to the upper triangles; additions commute), so RES's upper triangles are read once.
+__global__ void __launch_bounds__(256) k_pphh_update_mirror_f(DevLayout D, const int4* __restrict__ tiles,
+                                                              double* __restrict__ RES, const float* __restrict__ w1,
+                                                              const float* __restrict__ w2, float pm, int herm) {
   __shared__ float Xa[32][33];
   __shared__ float Xb[32][33];
+  __shared__ double V[32][33];
   const int4 t = tiles[blockIdx.x];
   const int k = t.x, i0 = t.y, j0 = t.z;
   const int64_t base = D.goff[k];
@@ -211,46 +217,29 @@ __global__ void __launch_bounds__(256) k_pphh_update_f(DevLayout D, const int4* 
   }
   for (int r = ty; r < 32; r += 8) {
     const int i = i0 + tx, j = j0 + r;
-    Xa[r][tx] = (i < n1 && j < n1) ? w1[base + i + (int64_t)j * n1] - w2[base + i + (int64_t)j * n1]
-                                   : 0.0f;
+    Xa[r][tx] = (i < n1 && j < n1) ? w1[base + i + (int64_t)j * n1] - w2[base + i + (int64_t)j * n1] : 0.0f;
     const int ib = j0 + tx, jb = i0 + r;
-    Xb[r][tx] = (ib < n1 && jb < n1) ? w1[base + ib + (int64_t)jb * n1] - w2[base + ib + (int64_t)jb * n1]
-                                     : 0.0f;
+    Xb[r][tx] = (ib < n1 && jb < n1) ? w1[base + ib + (int64_t)jb * n1] - w2[base + ib + (int64_t)jb * n1] : 0.0f;
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
     const int i = i0 + tx, j = j0 + r;
     if (i < n1 && j < n1 && i <= j) {
       const int64_t e = base + i + (int64_t)j * n1;
-      RES[e] += f32_to_f64(Xa[r][tx] - Xb[tx][r] * pm);
+      const double v = RES[e] + f32_to_f64(Xa[r][tx] - Xb[tx][r] * pm);
+      RES[e] = v;
+      V[r][tx] = v;
     }
+  }
+  __syncthreads();
+  const unsigned long long flip = herm < 0 ? (1ull << 63) : 0ull;
+  for (int r = ty; r < 32; r += 8) {
+    // destination (j0 + tx, i0 + r) = herm * source (i0 + r, j0 + tx) = V[tx][r]
+    const int i = j0 + tx, j = i0 + r;
+    if (i < n1 && j < n1 && i > j)
+      RES[base + i + (int64_t)j * n1] = __longlong_as_double(__double_as_longlong(V[tx][r]) ^ (long long)flip);
   }
 }
 
-// lower triangle of every square array (pppp, phph, hhhh) = herm * upper triangle
-__global__ void __launch_bounds__(256) k_mirror_square(DevLayout D, const int4* __restrict__ tiles,
-                                                       double* __restrict__ RES, int herm) {
-  __shared__ double T[32][33];
-  const int4 t = tiles[blockIdx.x];
-  if (!t.w) return;
-  const int k = t.x, i0 = t.y, j0 = t.z;  // i0 <= j0: source tile (upper), destination (j0, i0)
-  const int64_t base = D.goff[k];
-  const int n1 = D.gn1[k];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const unsigned long long flip = herm < 0 ? (1ull << 63) : 0ull;
-  for (int r = ty; r < 32; r += 8) {
-    const int i = i0 + tx, j = j0 + r;
-    T[r][tx] = (i < n1 && j < n1) ? RES[base + i + (int64_t)j * n1] : 0.0;
-  }
-  __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    // destination element (j0 + tx, i0 + r) = herm * source (i0 + r, j0 + tx) = T[tx][r]
-    const int i = j0 + tx, j = i0 + r;
-    if (i < n1 && j < n1 && i > j) {
-      const double v = T[tx][r];
-      RES[base + i + (int64_t)j * n1] = __longlong_as_double(__double_as_longlong(v) ^ (long long)flip);
-    }
-  }
-}
 
 }  // namespace imsrg

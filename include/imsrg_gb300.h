@@ -143,8 +143,9 @@ imsrg_status imsrg_timer_begin(imsrg_ctx* ctx);
 imsrg_status imsrg_timer_end(imsrg_ctx* ctx, float* ms);
 /* per-phase event timing of imsrg_commutator; phases: 1 Pandya, 2 one-body (110/220,
  * 111, 121), 3 122, 4 ladder operand split, 5 ladder GEMM, 6 small-K ladder GEMM,
- * 7 ladder accumulation, 8 221, 9 cross-coupled GEMM, 10 6j recoupling, 11 mirror of the
- * square arrays' lower triangles */
+ * 7 ladder accumulation (in a mixed mode it runs last and also writes the square arrays'
+ * lower triangles), 8 221, 9 cross-coupled GEMM, 10 6j recoupling, 11 mirror of the square
+ * arrays' lower triangles (no longer a separate pass; kept for the index layout) */
 #define IMSRG_NUM_PHASES 12
 imsrg_status imsrg_profile_phases(imsrg_ctx* ctx, int32_t enable);
 imsrg_status imsrg_profile_read(imsrg_ctx* ctx, float* ms_per_phase, int32_t* count_per_phase);
