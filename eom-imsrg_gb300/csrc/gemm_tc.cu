@@ -352,10 +352,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         if (m < P.M) {
           if (P.out_f32) {
             float* C = (P.out_f32 == 1 ? out.f32 : out.f32b) + P.c_off;
+            // the columns of this warp's 32-row segment that anything reads (one bit each)
+            // (m < M here; a chunk at or past column N stores nothing and reads no mask word)
+            unsigned keep = 0xffffffffu;
+            if (P.xmask)
+              keep = tile.n0 + c0 < P.N ? __ldg(out.xmask + (P.xmask - 1) + ((tile.m0 >> 5) + quad) * ((P.N + 31) >> 5) +
+                                                ((tile.n0 + c0) >> 5))
+                                        : 0u;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const int n = tile.n0 + c0 + j;
-              if (n < P.N) C[m + (int64_t)n * P.ldc] = __uint_as_float(r[j]);
+              if (n < P.N && ((keep >> j) & 1u)) C[m + (int64_t)n * P.ldc] = __uint_as_float(r[j]);
             }
           } else if (out.w1f && P.c_id == kOpW1) {
             float* C = out.w1f + P.c_off;
@@ -550,6 +557,8 @@ struct TcState {
   std::vector<uint64_t> quads;
   const uint64_t* d_quads = nullptr;
   std::vector<int> xcol;              // X column offset of every pair and J' (recouple.cu)
+  std::vector<unsigned> xmask;        // the X elements the recoupling reads (store masks, recouple.cu)
+  const unsigned* d_xmask = nullptr;
   const int* d_xcol = nullptr;
   int recouple_minb = 6;              // launch-bounds variant of k_recouple_q
   int recouple_ctas = 0;              // CTAs of k_recouple_q
@@ -810,6 +819,14 @@ imsrg_status Ctx::tc_prepare(int mode) {
           }
         }
   }
+  // X stores only where the recoupling reads: the masks of the 32-row column segments
+  {
+    std::vector<int> moff;
+    tc->xmask = build_x_read_mask(l, tc->quads, moff);
+    for (TcProb& p : tc->z_probs)
+      for (int q = 0; q < l.ncc; ++q)
+        if (l.cc_rlen[q] == p.M && l.wcc_off[q] == p.c_off && moff[q] >= 0) p.xmask = moff[q] + 1;
+  }
   tc->slice_rows = (int64_t)tiles * BM;
   tc->slice_elems = tc->slice_rows * BK;
   if ((int64_t)S * tc->slice_rows >= (int64_t)1 << 31) return fail(IMSRG_ERR_UNSUPPORTED, "operand buffer too large for 32-bit TMA rows");
@@ -841,6 +858,7 @@ imsrg_status Ctx::tc_prepare(int mode) {
   pk.add(tc->quads, &tc->d_quads);
   tc->xcol = build_xcol(l);
   pk.add(tc->xcol, &tc->d_xcol);
+  pk.add(tc->xmask, &tc->d_xmask);
   pk.add(tc->chunks, &tc->d_chunks);
   pk.add(tc->g_start, &tc->g122_w.spb_start);
   pk.add(tc->g_n, &tc->g122_w.spb_n);
@@ -1036,6 +1054,7 @@ imsrg_status Ctx::tc_commutator(const double* Lp, int hL, const double* Rp, int 
   mark(kPhasePphhSplit);
   TcOut gout{};
   gout.w1f = w1f;
+  gout.xmask = tc->d_xmask;
   gout.f32 = tc->zbuf;
   if (tc->merged)
     CK_TC(tc_gemm(tc->d_all_probs, tc->d_tile_mem + tc->tile_cap_all, (int)tc->all_tiles.size(), gout, hL, hR,

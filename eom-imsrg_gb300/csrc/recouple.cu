@@ -117,6 +117,35 @@ std::vector<int> build_xcol(const Layout& L) {
   return x;
 }
 
+std::vector<unsigned> build_x_read_mask(const Layout& L, const std::vector<uint64_t>& quads, std::vector<int>& mask_off) {
+  const int N = L.N, NJ = L.NJ, JM = L.JM;
+  mask_off.assign(L.ncc, -1);
+  size_t words = 0;
+  for (int q = 0; q < L.ncc; ++q) {
+    const int r = L.cc_rlen[q];
+    if (r == 0) continue;
+    mask_off[q] = (int)words;
+    words += (size_t)((r + 31) / 32) * ((r + 31) / 32);
+  }
+  std::vector<unsigned> m(std::max<size_t>(words, 1), 0u);
+  auto mark = [&](int a, int b, int r0, int r1, int h) {  // column pair (a, b), row pair (r0, r1) at J' = 2h
+    const int q = h + (std::abs(L.tz[a] - L.tz[b]) >> 1) * (JM + 1) + ((L.ll[a] + L.ll[b]) & 1) * 2 * (JM + 1);
+    const int col = L.ccr[((size_t)a * N + b) * NJ + h], row = L.ccr[((size_t)r0 * N + r1) * NJ + h];
+    const int nwc = (L.cc_rlen[q] + 31) / 32;
+    m[(size_t)mask_off[q] + (size_t)(row >> 5) * nwc + (col >> 5)] |= 1u << (col & 31);
+  };
+  for (uint64_t qd : quads) {
+    const int i = (int)(qd & 0xFFFF), j = (int)((qd >> 16) & 0xFFFF), k = (int)((qd >> 32) & 0xFFFF),
+              l = (int)((qd >> 48) & 0xFFFF);
+    const int ji = L.jj[i], jj = L.jj[j], jk = L.jj[k], jl = L.jj[l];
+    const int dlo = std::max(std::abs(jj - jl), std::abs(ji - jk)), dhi = std::min(jj + jl, ji + jk);
+    for (int JP = dlo; JP <= dhi; JP += 2) mark(i, k, l, j, JP >> 1);  // direct: X[(l,j),(i,k)]
+    const int elo = std::max(std::abs(ji - jl), std::abs(jj - jk)), ehi = std::min(ji + jl, jj + jk);
+    for (int JP = elo; JP <= ehi; JP += 2) mark(i, l, k, j, JP >> 1);  // exchange: X[(k,j),(i,l)]
+  }
+  return m;
+}
+
 RecoupleTraffic recouple_traffic(const Layout& L, const std::vector<uint64_t>& quads) {
   RecoupleTraffic t{};
   const int N = L.N, NJ = L.NJ, JM = L.JM;

@@ -15,6 +15,11 @@ namespace imsrg {
 // (-1 where (a, b) is not in the cross-coupled channel of J')
 std::vector<int> build_xcol(const Layout& L);
 
+// The X elements the recoupling reads, as store masks for the X product's epilogue: per
+// cross-coupled channel q (rlen rows and columns) and 32-row block b, one bit per column,
+// word mask_off[q] + b * ceil(rlen / 32) + column / 32 (mask_off[q] = -1 for an empty channel).
+std::vector<unsigned> build_x_read_mask(const Layout& L, const std::vector<uint64_t>& quads, std::vector<int>& mask_off);
+
 struct RecoupleTraffic {
   int64_t x_reads, x_distinct, res_elems, aux_bytes;
 };

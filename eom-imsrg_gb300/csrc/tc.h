@@ -28,11 +28,14 @@ struct TcTermDesc {
 
 // C = sum over nterm (<= 4) terms of sign * A_t B_t^T, all terms with the same K blocks.
 // With kseg > 0 the problem is one term whose K holds four segments of kseg elements (a
-// multiple of 16): the products of segment j carry the sign t[j].sign.
+// multiple of 16): the products of segment j carry the sign t[j].sign.  xmask > 0 (FP32
+// outputs): only the 32-row column segments whose bit is set in TcOut::xmask are stored, the
+// bits of row block b (32 rows) at word xmask - 1 + b * ceil(N / 32) + column / 32.
 struct TcProb {
   int64_t c_off;
   int M, N, nkb, nterm;
   int out_f32, c_id, ldc, kseg;
+  int xmask, pad;
   TcTermDesc t[4];
 };
 
@@ -79,6 +82,7 @@ struct TcOut {
   float* f32;   // out_f32 == 1
   float* f32b;  // out_f32 == 2
   float* w1f;   // when set: the W1 problems (c_id kOpW1) store FP32 here, same element offsets
+  const unsigned* xmask;  // store masks of the problems with xmask > 0
 };
 
 }  // namespace imsrg
