@@ -604,12 +604,26 @@ int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
 // the output tiles of a problem list: 128 rows by up to wmax columns (narrow: the last
 // column tile only as wide as its columns need, in steps of 16), longest K first
-std::vector<TcTile> make_tiles(const std::vector<TcProb>& probs, int wmax, bool narrow) {
+// whether any element of the tile (rows m0.., columns n0.. n0 + w - 1) is to be stored: always,
+// unless the problem has a store mask (TcProb::xmask) with no bit set in the tile
+bool tile_stored(const TcProb& P, const std::vector<unsigned>* mask, int m0, int n0, int w) {
+  if (!P.xmask || !mask) return true;
+  const int nwc = (P.N + 31) >> 5;
+  for (int b = m0 >> 5; b < std::min((m0 + BM + 31) >> 5, (P.M + 31) >> 5); ++b)
+    for (int c = n0 >> 5; c < std::min((n0 + w + 31) >> 5, nwc); ++c)
+      if ((*mask)[(size_t)(P.xmask - 1) + (size_t)b * nwc + c]) return true;
+  return false;
+}
+
+std::vector<TcTile> make_tiles(const std::vector<TcProb>& probs, int wmax, bool narrow,
+                               const std::vector<unsigned>* mask = nullptr) {
   std::vector<TcTile> t;
   for (int p = 0; p < (int)probs.size(); ++p)
     for (int m0 = 0; m0 < probs[p].M; m0 += BM)
-      for (int n0 = 0; n0 < probs[p].N; n0 += wmax)
-        t.push_back(TcTile{p, m0, n0, tc_tile_width(probs[p].N, n0, wmax, narrow)});
+      for (int n0 = 0; n0 < probs[p].N; n0 += wmax) {
+        const int w = tc_tile_width(probs[p].N, n0, wmax, narrow);
+        if (tile_stored(probs[p], mask, m0, n0, w)) t.push_back(TcTile{p, m0, n0, w});
+      }
   std::stable_sort(t.begin(), t.end(), [&](const TcTile& a, const TcTile& b) {
     return probs[a.prob].nkb * probs[a.prob].nterm > probs[b.prob].nkb * probs[b.prob].nterm;
   });
@@ -1150,7 +1164,7 @@ imsrg_status Ctx::tc_set_tiles(const int* wmax, const bool* narrow, int order) {
   for (int x = 0; x < 3; ++x)
     if (wmax[x] != 128 && !(wmax[x] == 256 && tc->S == 2)) return fail(IMSRG_ERR_INVALID_ARGUMENT, "unsupported tile width");
   auto build = [&](const std::vector<TcProb>& probs, int x) {
-    std::vector<TcTile> t = make_tiles(probs, wmax[x], narrow[x]);
+    std::vector<TcTile> t = make_tiles(probs, wmax[x], narrow[x], &tc->xmask);
     if (order == 1)
       std::stable_sort(t.begin(), t.end(), [](const TcTile& a, const TcTile& b) {
         return a.prob != b.prob ? a.prob < b.prob : (a.m0 != b.m0 ? a.m0 < b.m0 : a.n0 < b.n0);
