@@ -400,6 +400,19 @@ imsrg_status Ctx::axpby(const double* A, double ax, const double* B, double bx, 
   return launched("k_axpby");
 }
 
+// Y += a X and the Frobenius norm of X times scale into d_scalars[slot], in one pass (E0 of Y
+// updated only with with_e0); no synchronization
+imsrg_status Ctx::axpy_frob_async(double* Y, double a, const double* X, double scale, int slot, bool with_e0) {
+  if (nseg == 0) {
+    CK(axpby(Y, 1.0, X, a, Y));
+    return frob_async(X, scale, slot);
+  }
+  k_axpy_frob<<<nseg, 256, 0, stream>>>(Y, a, X, d_seg_start, d_seg_len, d_seg_w, d_partial, with_e0 ? 1 : 0);
+  CK(launched("k_axpy_frob"));
+  k_sum_sqrt<<<1, 1024, 0, stream>>>(d_partial, nseg, scale, d_scalars + slot);
+  return launched("k_sum_sqrt");
+}
+
 // Frobenius norm times scale into d_scalars[slot] (device); no synchronization
 imsrg_status Ctx::frob_async(const double* op, double scale, int slot) {
   if (nseg == 0) return cuda(cudaMemsetAsync(d_scalars + slot, 0, sizeof(double), stream), "memset(norm)");
@@ -464,10 +477,8 @@ imsrg_status Ctx::magnus_expand(double* DG, int hDG, const double* G, int hG, in
   CK(ensure_flow_workspace());
   const double conv = (double)1e-6f;
   const double* cof = kMagnusCof;
-  const size_t sb = sizeof(double) * (size_t)L.slab;
   double advals[8] = {0};
-  CK(cuda(cudaMemcpyAsync(d_int2, DG, sb, cudaMemcpyDeviceToDevice, stream), "copy INT2"));
-  CK(frob_async(d_int2, 1.0, 0));
+  CK(frob_async(DG, 1.0, 0));
   CK(frob_async(G, 1.0, 1));
   CK(read_scalars(2));
   advals[1] = h_scalars[0];
@@ -475,16 +486,18 @@ imsrg_status Ctx::magnus_expand(double* DG, int hDG, const double* G, int hG, in
   *used = 0;
   if (fullnorm < (double)1e-9f) return IMSRG_OK;
   int qq = 1;
+  // ad^(i-1) and ad^i alternate between two buffers (the first input is DG itself, read before
+  // DG is updated); DG += cof ad^i with the norm of ad^i in the same pass (E0 of DG kept: the
+  // nested commutators do not form one)
   for (int i = 2; i <= 7; ++i) {
-    CK(cuda(cudaMemcpyAsync(d_int1, DG, sb, cudaMemcpyDeviceToDevice, stream), "copy INT1"));
-    CK(cuda(cudaMemcpyAsync(d_ad, d_int2, sb, cudaMemcpyDeviceToDevice, stream), "copy AD"));
     const double adnorm = advals[i - qq];
     qq = (std::fabs(cof[i - 1]) > (double)1e-6f) ? 1 : 2;
     if (std::fabs(adnorm / fullnorm) < conv) break;
-    CK(commutator(G, hG, d_ad, hDG, d_int2, hDG, false));
+    const double* ad = (i == 2) ? DG : ((i & 1) ? d_int2 : d_ad);
+    double* out = (i & 1) ? d_ad : d_int2;
+    CK(commutator(G, hG, ad, hDG, out, hDG, false));
     ++*used;
-    CK(axpby(d_int1, 1.0, d_int2, cof[i - 1], DG));
-    CK(frob_async(d_int2, std::fabs(cof[i - 1]), 0));
+    CK(axpy_frob_async(DG, cof[i - 1], out, std::fabs(cof[i - 1]), 0, false));
     CK(read_scalars(1));
     advals[i] = h_scalars[0];
   }
@@ -517,8 +530,7 @@ imsrg_status Ctx::bch_expand(double* HS, const double* G, int hG, const double* 
       CK(axpby(out, 1.0, int3, 1.0, out));
       CK(restore_quadrupoles(ad, hH, G, hG, int3));
     }
-    CK(axpby(HS, 1.0, out, coef, HS));
-    CK(frob_async(out, coef, 0));
+    CK(axpy_frob_async(HS, coef, out, coef, 0, true));
     CK(read_scalars(1));
     if (h_scalars[0] < conv) break;
   }

@@ -122,6 +122,7 @@ struct Ctx {
   imsrg_status ph(const double* lcc, int hL, const double* rcc, int hR, double* RES, int hRES, double* wcc);
   imsrg_status commutator(const double* L, int hL, const double* R, int hR, double* RES, int hRES, bool with_e0);
   imsrg_status axpby(const double* A, double ax, const double* B, double bx, double* C);
+  imsrg_status axpy_frob_async(double* Y, double a, const double* X, double scale, int slot, bool with_e0);
   imsrg_status frob_async(const double* op, double scale, int slot);
   imsrg_status read_scalars(int n);
   imsrg_status white(const double* H, int hH, double* ETA);

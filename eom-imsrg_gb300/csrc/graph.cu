@@ -183,21 +183,20 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
   auto run = [&]() -> imsrg_status {
     // ---- MAGNUS_EXPAND
     int64_t l0 = launches;
-    CK_TC(cuda(cudaMemcpyAsync(d_int2, DG, sb, cudaMemcpyDeviceToDevice, stream), "copy INT2"));
-    CK_TC(frob_async(d_int2, 1.0, 0));
+    CK_TC(frob_async(DG, 1.0, 0));
     CK_TC(frob_async(G, 1.0, 1));
     k_magnus_begin<<<1, 1, 0, stream>>>(d_scalars, sg->d_state, hm[0], mconv, kMagnusCof[1]);
     CK_TC(launched("k_magnus_begin"));
     fixed += launches - l0;
     for (int i = 2; i <= 7; ++i) {
       const double cof = kMagnusCof[i - 1];
+      // the same alternating buffers as Ctx::magnus_expand
+      const double* ad = (i == 2) ? DG : ((i & 1) ? d_int2 : d_ad);
+      double* out = (i & 1) ? d_ad : d_int2;
       CK_TC(capture_if(hm[i - 2], [&]() -> imsrg_status {
         const int64_t b0 = launches;
-        CK_TC(cuda(cudaMemcpyAsync(d_int1, DG, sb, cudaMemcpyDeviceToDevice, stream), "copy INT1"));
-        CK_TC(cuda(cudaMemcpyAsync(d_ad, d_int2, sb, cudaMemcpyDeviceToDevice, stream), "copy AD"));
-        CK_TC(commutator(G, hG, d_ad, hDG, d_int2, hDG, false));
-        CK_TC(axpby(d_int1, 1.0, d_int2, cof, DG));
-        CK_TC(frob_async(d_int2, std::fabs(cof), 0));
+        CK_TC(commutator(G, hG, ad, hDG, out, hDG, false));
+        CK_TC(axpy_frob_async(DG, cof, out, std::fabs(cof), 0, false));
         const int body = (int)(launches - b0) + 1;
         const bool has_next = i < 7;
         k_magnus_next<<<1, 1, 0, stream>>>(i, d_scalars, sg->d_state, has_next ? hm[i - 1] : hm[0], has_next ? 1 : 0,
@@ -221,8 +220,7 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
       CK_TC(capture_if(hb[iw - 2], [&]() -> imsrg_status {
         const int64_t b0 = launches;
         CK_TC(commutator(G, hG, ad, hH, out, hH, true));
-        CK_TC(axpby(HS, 1.0, out, c, HS));
-        CK_TC(frob_async(out, c, 0));
+        CK_TC(axpy_frob_async(HS, c, out, c, 0, true));
         const int body = (int)(launches - b0) + 1;
         const bool has_next = iw < max_terms;
         k_bch_next<<<1, 1, 0, stream>>>(iw, d_scalars, sg->d_state, has_next ? hb[iw - 1] : hb[0], has_next ? 1 : 0,

@@ -34,6 +34,8 @@ __global__ void k_atan_2b(DevLayout D, const double* Hden, int hden, const doubl
 __global__ void k_axpby(int64_t n, const double* A, double ax, const double* B, double bx, double* C);
 __global__ void k_frob_partial(const double* op, const int64_t* seg_start, const int* seg_len, const int8_t* seg_w,
                                double* partial);
+__global__ void k_axpy_frob(double* Y, double a, const double* X, const int64_t* seg_start, const int* seg_len,
+                            const int8_t* seg_w, double* partial, int with_e0);
 __global__ void k_sum_sqrt(const double* partial, int n, double scale, double* out);
 __global__ void k_mbpt2_partial(DevLayout D, const double* H, int hH, double* partial);
 __global__ void k_sum(const double* partial, int n, double* out);

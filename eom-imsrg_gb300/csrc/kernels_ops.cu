@@ -123,6 +123,30 @@ __global__ void k_frob_partial(const double* __restrict__ op, const int64_t* __r
 }
 
 // stage 2: out = sqrt(sum of partials) (fixed order); optional scale (|cof| or coef)
+// Y += a X over the norm segments (every element but E0; E0 too when with_e0) and the
+// segments' weighted sums of X^2 (as k_frob_partial on X): one pass instead of two
+__global__ void k_axpy_frob(double* __restrict__ Y, double a, const double* __restrict__ X,
+                            const int64_t* __restrict__ seg_start, const int* __restrict__ seg_len,
+                            const int8_t* __restrict__ seg_w, double* __restrict__ partial, int with_e0) {
+  __shared__ double red[256];
+  const int s = blockIdx.x;
+  const int64_t o = seg_start[s];
+  const int n = seg_len[s];
+  if (s == 0 && threadIdx.x == 0 && with_e0) Y[0] += a * X[0];
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const double x = X[o + t];
+    Y[o + t] += a * x;
+    acc += x * x;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int k = blockDim.x >> 1; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[s] = red[0] * seg_w[s];
+}
 __global__ void k_sum_sqrt(const double* __restrict__ partial, int n, double scale, double* __restrict__ out) {
   __shared__ double red[1024];
   double acc = 0.0;
