@@ -1017,7 +1017,7 @@ def main():
         del st64, dR64, dE64, dHs64, eng64, dR, dEm, dHm
 
     # ---- end to end through the C ABI: the flow kept in pinned host memory; every step
-    # uploads H, Omega, eta and downloads H(s), Omega, eta around imsrg_magnus_step
+    # uploads H, Omega, eta and downloads H(s), Omega, eta (imsrg_magnus_step_host)
     nbytes = 8 * eng.slab
     st = flow_state(eng, H)
     hb = []
@@ -1033,11 +1033,10 @@ def main():
         if it == 1:
             barrier(pg)
             t0 = time.perf_counter()
-        for op, p in ((H_, hb[3]), (G_, hb[1]), (DG_, hb[2])):
-            eng._ck(eng.L.imsrg_op_upload_slab(eng.h, op.h, p))
-        info = eng.magnus_step(*st, args.ds, allow_unconverged=True, **step_kw)
-        for op, p in ((HS_, hb[0]), (G_, hb[1]), (DG_, hb[2])):
-            eng._ck(eng.L.imsrg_op_download_slab(eng.h, op.h, p))
+        # imsrg_magnus_step_host: uploads H, Omega and eta, runs the step (the graph replay) and
+        # downloads H(s), Omega and eta, with H's upload and Omega's download inside the step
+        info = eng.magnus_step_host(HS_, G_, DG_, H_, hb[0], hb[1], hb[2], hb[3], args.ds, allow_unconverged=True,
+                                    **step_kw)
         if it >= 1:
             e2e_comm += info["magnus_terms"] + info["bch_terms"]
     e2e_s = allreduce_max(pg, time.perf_counter() - t0)

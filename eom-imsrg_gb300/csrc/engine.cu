@@ -1205,6 +1205,30 @@ imsrg_status imsrg_magnus_step(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_
                         info);
 }
 
+imsrg_status imsrg_magnus_step_host(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_op* DG, imsrg_op* H,
+                                    double* hs_host, double* g_host, double* dg_host, const double* h_host, double ds,
+                                    int32_t bch_max_terms, double bch_conv, int32_t use_graph, imsrg_step_info* info) {
+  CTX(ctx);
+  CK(check_op(c, HS, "imsrg_magnus_step_host"));
+  CK(check_op(c, G, "imsrg_magnus_step_host"));
+  CK(check_op(c, DG, "imsrg_magnus_step_host"));
+  CK(check_op(c, H, "imsrg_magnus_step_host"));
+  if (HS == G || HS == H || HS == DG || G == DG || G == H || DG == H)
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "HS, G, DG and H must be distinct operators");
+  if (!hs_host || !g_host || !dg_host || !h_host)
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_magnus_step_host: null host buffer");
+  if (hs_host == g_host || hs_host == dg_host || g_host == dg_host)
+    return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_magnus_step_host: the output buffers must be distinct");
+  if (bch_max_terms < 2) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "max_terms must be >= 2");
+  if (!info) return c->fail(IMSRG_ERR_INVALID_ARGUMENT, "imsrg_magnus_step_host needs info (it waits for the step)");
+  HS->herm = H->herm;
+  G->herm = -1;
+  DG->herm = -1;
+  const StepHostIO io{hs_host, g_host, dg_host, h_host};
+  return c->magnus_step(HS->d, G->d, G->herm, DG->d, H->d, H->herm, ds, bch_max_terms, bch_conv, use_graph != 0,
+                        info, &io);
+}
+
 imsrg_status imsrg_magnus_step_counters(imsrg_ctx* ctx, int64_t* commutators, int64_t* kernels, int64_t* steps,
                                         int64_t* unconverged) {
   CTX(ctx);

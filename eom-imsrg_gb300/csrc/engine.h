@@ -17,6 +17,14 @@ namespace imsrg {
 struct TcState;
 }
 struct StepGraph;
+// The flow state of a step in the caller's pinned host memory (slab format): inputs G (Omega),
+// DG (eta) and H, outputs HS, G and DG
+struct StepHostIO {
+  double* hs;
+  double* g;
+  double* dg;
+  const double* h;
+};
 struct AdjointState;
 struct TensorState;
 struct imsrg_eom;
@@ -140,9 +148,10 @@ struct Ctx {
 
   // one Magnus step, eager or replayed from a CUDA graph (graph.cu)
   imsrg_status magnus_step(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,
-                           int max_terms, double conv, bool use_graph, imsrg_step_info* info);
+                           int max_terms, double conv, bool use_graph, imsrg_step_info* info,
+                           const StepHostIO* hio = nullptr);
   imsrg_status graph_capture(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,
-                             int max_terms, double conv);
+                             int max_terms, double conv, const StepHostIO* hio);
   template <class F>
   imsrg_status capture_if(cudaGraphConditionalHandle h, F&& body);
   imsrg_status step_counters(int64_t* commutators, int64_t* kernels, int64_t* steps, int64_t* unconverged);

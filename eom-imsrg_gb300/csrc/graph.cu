@@ -44,6 +44,10 @@ struct StepGraph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t side = nullptr;
+  // copy branches of a step with host I/O (captured into the graph) and their fork / join events
+  cudaStream_t cp[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  StepHostIO hio{};
   StepState* d_state = nullptr;
   StepState* h_state = nullptr;
   // key of the captured step
@@ -120,6 +124,10 @@ imsrg_status Ctx::graph_release() {
   if (sg->exec) cudaGraphExecDestroy(sg->exec);
   if (sg->graph) cudaGraphDestroy(sg->graph);
   if (sg->side) cudaStreamDestroy(sg->side);
+  for (cudaStream_t c : sg->cp)
+    if (c) cudaStreamDestroy(c);
+  for (cudaEvent_t e : sg->ev)
+    if (e) cudaEventDestroy(e);
   if (sg->d_state) cudaFree(sg->d_state);
   if (sg->h_state) cudaFreeHost(sg->h_state);
   delete sg;
@@ -160,7 +168,7 @@ imsrg_status Ctx::capture_if(cudaGraphConditionalHandle h, F&& body) {
 // Captures the whole step (see the file comment); the eager drivers are
 // Ctx::magnus_expand, Ctx::axpby (euler_step), Ctx::bch_expand, Ctx::white and imsrg_mbpt2.
 imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,
-                                int max_terms, double conv) {
+                                int max_terms, double conv, const StepHostIO* hio) {
   const size_t sb = sizeof(double) * (size_t)L.slab;
   const double mconv = (double)1e-6f;
   const int hDG = -1;
@@ -180,7 +188,24 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
   imsrg_status s = cuda(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
                         "cudaStreamBeginCaptureToGraph");
   int64_t fixed = 0;
+  // with host I/O the copies are nodes of the graph: Omega and eta up first; H0 up on a side
+  // branch joined before BCH_EXPAND (it overlaps MAGNUS_EXPAND); Omega down on a side branch
+  // once euler_step has finished it (it overlaps BCH_EXPAND); H(s) down beside the generator
+  // and MBPT(2); eta down last
+  cudaStream_t* cp = sg->cp;
+  cudaEvent_t* ev = sg->ev;
+  auto fork = [&](cudaEvent_t e, cudaStream_t to) -> imsrg_status {
+    CK_TC(cuda(cudaEventRecord(e, stream), "cudaEventRecord(fork)"));
+    return cuda(cudaStreamWaitEvent(to, e, 0), "cudaStreamWaitEvent(fork)");
+  };
   auto run = [&]() -> imsrg_status {
+    if (hio) {
+      CK_TC(cuda(cudaMemcpyAsync(G, hio->g, sb, cudaMemcpyHostToDevice, stream), "H2D Omega"));
+      CK_TC(cuda(cudaMemcpyAsync(DG, hio->dg, sb, cudaMemcpyHostToDevice, stream), "H2D eta"));
+      CK_TC(fork(ev[0], cp[0]));
+      CK_TC(cuda(cudaMemcpyAsync(const_cast<double*>(H), hio->h, sb, cudaMemcpyHostToDevice, cp[0]), "H2D H"));
+      CK_TC(cuda(cudaEventRecord(ev[1], cp[0]), "cudaEventRecord(H up)"));
+    }
     // ---- MAGNUS_EXPAND
     int64_t l0 = launches;
     CK_TC(frob_async(DG, 1.0, 0));
@@ -207,6 +232,12 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
     // ---- euler_step
     l0 = launches;
     CK_TC(axpby(G, 1.0, DG, ds, G));
+    if (hio) {
+      CK_TC(fork(ev[2], cp[1]));
+      CK_TC(cuda(cudaMemcpyAsync(hio->g, G, sb, cudaMemcpyDeviceToHost, cp[1]), "D2H Omega"));
+      CK_TC(cuda(cudaEventRecord(ev[3], cp[1]), "cudaEventRecord(Omega down)"));
+      CK_TC(cuda(cudaStreamWaitEvent(stream, ev[1], 0), "cudaStreamWaitEvent(H up)"));
+    }
     // ---- BCH_EXPAND
     CK_TC(cuda(cudaMemcpyAsync(HS, H, sb, cudaMemcpyDeviceToDevice, stream), "copy HS"));
     fixed += launches - l0;
@@ -228,6 +259,11 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
         return launched("k_bch_next");
       }));
     }
+    if (hio) {
+      CK_TC(fork(ev[4], cp[2]));
+      CK_TC(cuda(cudaMemcpyAsync(hio->hs, HS, sb, cudaMemcpyDeviceToHost, cp[2]), "D2H H(s)"));
+      CK_TC(cuda(cudaEventRecord(ev[5], cp[2]), "cudaEventRecord(H(s) down)"));
+    }
     // ---- generator and MBPT(2) of the new H(s)
     l0 = launches;
     CK_TC(white(HS, hH, DG));
@@ -237,7 +273,13 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
     CK_TC(launched("k_sum"));
     fixed += launches - l0 + 1;
     k_step_end<<<1, 1, 0, stream>>>(HS, sg->d_state, (int)fixed);
-    return launched("k_step_end");
+    CK_TC(launched("k_step_end"));
+    if (hio) {
+      CK_TC(cuda(cudaMemcpyAsync(hio->dg, DG, sb, cudaMemcpyDeviceToHost, stream), "D2H eta"));
+      CK_TC(cuda(cudaStreamWaitEvent(stream, ev[3], 0), "cudaStreamWaitEvent(Omega down)"));
+      CK_TC(cuda(cudaStreamWaitEvent(stream, ev[5], 0), "cudaStreamWaitEvent(H(s) down)"));
+    }
+    return IMSRG_OK;
   };
   if (s == IMSRG_OK) s = run();
   cudaGraph_t out = nullptr;
@@ -257,7 +299,8 @@ imsrg_status Ctx::graph_capture(double* HS, double* G, int hG, double* DG, const
 }
 
 imsrg_status Ctx::magnus_step(double* HS, double* G, int hG, double* DG, const double* H, int hH, double ds,
-                              int max_terms, double conv, bool use_graph, imsrg_step_info* info) {
+                              int max_terms, double conv, bool use_graph, imsrg_step_info* info,
+                              const StepHostIO* hio) {
   CK_TC(ensure_workspace());
   CK_TC(ensure_flow_workspace());
   if (precision == IMSRG_PREC_FP64 && L.cc_size) CK_TC(ensure_wcc());
@@ -267,10 +310,18 @@ imsrg_status Ctx::magnus_step(double* HS, double* G, int hG, double* DG, const d
     CK_TC(cuda(cudaMemsetAsync(sg->d_state, 0, sizeof(StepState), stream), "memset(step state)"));
     CK_TC(cuda(cudaMallocHost(&sg->h_state, sizeof(StepState)), "cudaMallocHost(step state)"));
     CK_TC(cuda(cudaStreamCreateWithFlags(&sg->side, cudaStreamNonBlocking), "cudaStreamCreate(side)"));
+    for (cudaStream_t& c : sg->cp) CK_TC(cuda(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), "cudaStreamCreate(copy)"));
+    for (cudaEvent_t& e : sg->ev) CK_TC(cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate"));
   }
+  const size_t sbytes = sizeof(double) * (size_t)L.slab;
   int rebuilt = 0;
   if (!use_graph) {
-    // the eager drivers, with the reference's host-side tests
+    // the eager drivers, with the reference's host-side tests (host I/O as plain copies)
+    if (hio) {
+      CK_TC(cuda(cudaMemcpyAsync(G, hio->g, sbytes, cudaMemcpyHostToDevice, stream), "H2D Omega"));
+      CK_TC(cuda(cudaMemcpyAsync(DG, hio->dg, sbytes, cudaMemcpyHostToDevice, stream), "H2D eta"));
+      CK_TC(cuda(cudaMemcpyAsync(const_cast<double*>(H), hio->h, sbytes, cudaMemcpyHostToDevice, stream), "H2D H"));
+    }
     int used = 0, terms = 0;
     CK_TC(magnus_expand(DG, -1, G, hG, &used));
     CK_TC(axpby(G, 1.0, DG, ds, G));
@@ -283,6 +334,11 @@ imsrg_status Ctx::magnus_step(double* HS, double* G, int hG, double* DG, const d
     CK_TC(launched("k_sum"));
     CK_TC(read_scalars(1));
     const double e2 = h_scalars[0];
+    if (hio) {
+      CK_TC(cuda(cudaMemcpyAsync(hio->hs, HS, sbytes, cudaMemcpyDeviceToHost, stream), "D2H H(s)"));
+      CK_TC(cuda(cudaMemcpyAsync(hio->g, G, sbytes, cudaMemcpyDeviceToHost, stream), "D2H Omega"));
+      CK_TC(cuda(cudaMemcpyAsync(hio->dg, DG, sbytes, cudaMemcpyDeviceToHost, stream), "D2H eta"));
+    }
     double e0 = 0;
     CK_TC(cuda(cudaMemcpyAsync(h_scalars, HS, sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H E0"));
     CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize"));
@@ -299,17 +355,20 @@ imsrg_status Ctx::magnus_step(double* HS, double* G, int hG, double* DG, const d
     if (sb != IMSRG_OK) return fail(IMSRG_ERR_NOT_CONVERGED, "BCH series did not converge within max_terms");
     return IMSRG_OK;
   }
+  const StepHostIO none{};
+  const StepHostIO& io = hio ? *hio : none;
   const bool same = sg->exec && sg->HS == HS && sg->G == G && sg->DG == DG && sg->H == H && sg->hH == hH &&
                     sg->hG == hG && sg->ds == ds && sg->max_terms == max_terms && sg->conv == conv &&
-                    sg->precision == precision;
+                    sg->precision == precision && sg->hio.hs == io.hs && sg->hio.g == io.g && sg->hio.dg == io.dg &&
+                    sg->hio.h == io.h;
   if (!same) {
     if (sg->exec) cudaGraphExecDestroy(sg->exec);
     if (sg->graph) cudaGraphDestroy(sg->graph);
     sg->exec = nullptr;
     sg->graph = nullptr;
     CK_TC(cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize"));
-    CK_TC(graph_capture(HS, G, hG, DG, H, hH, ds, max_terms, conv));
-    sg->HS = HS; sg->G = G; sg->DG = DG; sg->H = H; sg->hH = hH; sg->hG = hG;
+    CK_TC(graph_capture(HS, G, hG, DG, H, hH, ds, max_terms, conv, hio));
+    sg->HS = HS; sg->G = G; sg->DG = DG; sg->H = H; sg->hH = hH; sg->hG = hG; sg->hio = io;
     sg->ds = ds; sg->max_terms = max_terms; sg->conv = conv; sg->precision = precision;
     rebuilt = 1;
   }

@@ -106,6 +106,7 @@ SIGNATURES = {
     "imsrg_bch_expand_quads": [_vp, _vp, _vp, _vp, _i32, _d, _pi32],
     "imsrg_restore_quadrupoles": [_vp, _vp, _vp, _vp],
     "imsrg_magnus_step": [_vp, _vp, _vp, _vp, _vp, _d, _i32, _d, _i32, C.POINTER(StepInfo_t)],
+    "imsrg_magnus_step_host": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i32, _d, _i32, C.POINTER(StepInfo_t)],
     "imsrg_magnus_step_counters": [_vp, _pi64, _pi64, _pi64, _pi64],
     "imsrg_tensor_sizes": [_vp, _i32, _i32, _pi64, _pi32],
     "imsrg_tensor_block_info": [_vp, _i32, _i32, _pi32, _pi32, _pi32, _pi32],

@@ -481,6 +481,19 @@ class Engine:
         return {"E0": info.E0, "mbpt2": info.mbpt2, "magnus_terms": info.magnus_terms, "bch_terms": info.bch_terms,
                 "bch_converged": bool(info.bch_converged), "graph_rebuilt": bool(info.graph_rebuilt)}
 
+    def magnus_step_host(self, HS: SqOp, G: SqOp, DG: SqOp, H: SqOp, hs_host, g_host, dg_host, h_host, ds: float,
+                         max_terms: int = 40, conv: float = CONV, graph: bool = True, allow_unconverged: bool = False):
+        """One step of magnus_decouple with the flow state in pinned host slabs (pointers from
+        imsrg_pinned_alloc): uploads Omega (g_host), eta (dg_host) and H (h_host), runs the step
+        and downloads H(s), Omega and eta.  HS, G, DG and H are the device workspaces."""
+        info = _lib.StepInfo_t()
+        st = self.L.imsrg_magnus_step_host(self.h, HS.h, G.h, DG.h, H.h, hs_host, g_host, dg_host, h_host, float(ds),
+                                           int(max_terms), float(conv), 1 if graph else 0, C.byref(info))
+        if st != 0 and not (allow_unconverged and st == 4):
+            self._ck(st)
+        return {"E0": info.E0, "mbpt2": info.mbpt2, "magnus_terms": info.magnus_terms, "bch_terms": info.bch_terms,
+                "bch_converged": bool(info.bch_converged), "graph_rebuilt": bool(info.graph_rebuilt)}
+
     # ---------------------------------------------------------------- reverse mode (FP64)
     def commutator_vjp(self, L: SqOp, R: SqOp, RESb: SqOp, Lb: SqOp, Rb: SqOp, e0: bool = True):
         """Lb += d<RESb,[L,R]>/dL, Rb += d<RESb,[L,R]>/dR (RESb.herm = herm of [L,R])."""

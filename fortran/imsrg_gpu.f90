@@ -261,6 +261,18 @@ module imsrg_gpu
        type(imsrg_step_info) :: info
        integer(c_int32_t) :: imsrg_magnus_step
      end function imsrg_magnus_step
+
+     ! the same step with the flow state in pinned host slabs (inputs omega, eta, H; outputs
+     ! H(s), omega, eta); some copies overlap the step inside the captured graph
+     function imsrg_magnus_step_host(ctx, HS, G, DG, H, hs_host, g_host, dg_host, h_host, ds, max_terms, conv, &
+          use_graph, info) bind(C, name='imsrg_magnus_step_host')
+       import :: c_int32_t, c_ptr, c_double, imsrg_step_info
+       type(c_ptr), value :: ctx, HS, G, DG, H, hs_host, g_host, dg_host, h_host
+       real(c_double), value :: ds, conv
+       integer(c_int32_t), value :: max_terms, use_graph
+       type(imsrg_step_info) :: info
+       integer(c_int32_t) :: imsrg_magnus_step_host
+     end function imsrg_magnus_step_host
   end interface
 
 contains

@@ -284,6 +284,17 @@ typedef struct imsrg_step_info {
 } imsrg_step_info;
 imsrg_status imsrg_magnus_step(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_op* DG, const imsrg_op* H, double ds,
                                int32_t bch_max_terms, double bch_conv, int32_t use_graph, imsrg_step_info* info);
+/* The same step with the flow state in the caller's host memory, for a caller that keeps it there
+ * between steps (a Fortran driver): uploads Omega (g_host), eta (dg_host) and H (h_host), runs the
+ * step and downloads H(s) (hs_host), Omega and eta.  Equal bit for bit to imsrg_op_upload_slab of
+ * the three inputs, imsrg_magnus_step and imsrg_op_download_slab of the three outputs, but in the
+ * captured step H's upload overlaps MAGNUS_EXPAND, Omega's download BCH_EXPAND and H(s)'s download
+ * the generator.  The host buffers are slabs (imsrg_op_upload_slab's format) in pinned memory
+ * (imsrg_pinned_alloc); HS, G, DG and H are device workspaces of the context.  Waits for the step.
+ * No counterpart in the reference. */
+imsrg_status imsrg_magnus_step_host(imsrg_ctx* ctx, imsrg_op* HS, imsrg_op* G, imsrg_op* DG, imsrg_op* H,
+                                    double* hs_host, double* g_host, double* dg_host, const double* h_host, double ds,
+                                    int32_t bch_max_terms, double bch_conv, int32_t use_graph, imsrg_step_info* info);
 /* Totals over all graph-replayed steps of this context (no counterpart in the reference):
  * nested commutators, kernels launched, steps, steps whose BCH series did not converge. */
 imsrg_status imsrg_magnus_step_counters(imsrg_ctx* ctx, int64_t* commutators, int64_t* kernels, int64_t* steps,
