@@ -786,15 +786,15 @@ imsrg_status Ctx::tc_prepare(int mode) {
   }
   tc->total_tiles = tiles;
   if (l.JM + 1 > 26) return fail(IMSRG_ERR_UNSUPPORTED, "mixed recoupling supports 2j <= 25 (eMax <= 12)");
-  // ---- Pandya chunks: at most 2048 elements of one cross-coupled channel each
+  // ---- Pandya chunks: at most 1024 elements of one cross-coupled channel each (both operators)
   for (int q = 0; q < l.ncc; ++q) {
     const int64_t n = l.cc_off[q + 1] - l.cc_off[q];
     const int nph = l.cc_nph[q];
     if (n <= 0) continue;
     if (n * (int64_t)nph >= (1ll << 32)) return fail(IMSRG_ERR_UNSUPPORTED, "cross-coupled channel too large");
     const unsigned m = (unsigned)(((1ull << 32) + (unsigned)nph - 1) / (unsigned)nph);
-    for (int64_t e0 = 0; e0 < n; e0 += 2048)
-      tc->pandya_chunks.push_back(PandyaChunk{q, (int)e0, (int)std::min<int64_t>(2048, n - e0), m});
+    for (int64_t e0 = 0; e0 < n; e0 += 1024)
+      tc->pandya_chunks.push_back(PandyaChunk{q, (int)e0, (int)std::min<int64_t>(1024, n - e0), m});
   }
   // ---- commutator_122 tasks: the group pairs G1 <= G2 of each channel
   {

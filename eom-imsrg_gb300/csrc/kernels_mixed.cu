@@ -22,30 +22,29 @@ __device__ __forceinline__ float d_sixjf(const DevLayout& D, int j1, int j2, int
 // cross-coupled GEMM: element (r, ph) of channel q,
 //   X(ab, ph) = (-1)^((jh+jb+JC)/2) sqrt(JC+1) sum_JT (-1)^(JT/2) (JT+1) {jp jh JC; ja jb JT} V(ha, pb; JT).
 // Each CTA takes one chunk of a channel's elements (pandya_chunks: no search over channels),
-// threads run along ph so the writes into each 128-byte tile row are contiguous.  What does
-// not depend on JT is set up once per element: the 6j row, the pair classes and array, the
-// stored order of (h, a) and (p, b) and their sqrt 2 factors; per JT the loop loads the two
-// pair positions (adjacent in JT), the array offset, the operator element and the 6j value.
+// threads run along ph so the writes into each 128-byte tile row are contiguous.  Both
+// operators (L and R) share every index of an element, so one thread forms both sums: what
+// does not depend on JT is set up once per element (the 6j row, the pair classes and array,
+// the stored order of (h, a) and (p, b) and their sqrt 2 factors), and per JT the loop loads
+// the two pair positions (adjacent in JT), the array offset, the 6j value and the element
+// of each operator.
 // The recoupling input X (gemm_tc.cu) is one product A B^T over a K of four segments of seg
 // columns, A = [phiL | phiR | Ls | Rs], B = [phiR | phiL | Rs | Ls]: phiO is O with row r
 // times phi(r(a,b)) = (-1)^((ja+jb)/2), Os is O with row r(b,a) at row s(r) = r(a,b).  So
 // each element of L goes to A and B signed at row r (segments 0 and 1) and unsigned at row
 // s(r) (segments 2 and 3); R's to segments 1, 0 and 3, 2.
-// blockIdx.y selects the operator: 0 = R (first), 1 = L.
 template <int S, typename T>
 __global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChunk* __restrict__ chunks,
                                                    PandyaOps ops, void* __restrict__ bufv, int64_t slice_elems,
                                                    const int* __restrict__ swap_row) {
   T* buf = static_cast<T*>(bufv);
-  const bool w = blockIdx.y != 0;  // selected with conditionals, not an index (no local copy of ops)
-  const double* __restrict__ op = w ? ops.op[1] : ops.op[0];
-  const int herm = w ? ops.herm[1] : ops.herm[0];
+  const double* __restrict__ opR = ops.op[0];
+  const double* __restrict__ opL = ops.op[1];
+  const int hR = ops.herm[0], hL = ops.herm[1];
   const PandyaChunk c = chunks[blockIdx.x];
   const int q = c.q, nph = D.cc_nph[q], JC = D.cc_J[q];
   const int col0 = D.cc_col_off[q], row0 = D.cc_row_off[q];
   const int ta = ops.tile_a[q], tbb = ops.tile_b[q], nk = ops.nkb[q], seg = ops.seg[q];
-  // K offsets of this operator's signed rows in A and B, and of its swapped rows
-  const int ka = w ? 0 : seg, kb = w ? seg : 0, ksa = w ? 2 * seg : 3 * seg, ksb = w ? 3 * seg : 2 * seg;
   const int N = D.N, NJ = D.NJ, nh = D.sj_nh;
   for (int x = threadIdx.x; x < c.n; x += blockDim.x) {
     const int loc = c.e0 + x;
@@ -53,7 +52,7 @@ __global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChun
     const int p = D.cc_cp[col0 + nbx], h = D.cc_ch[col0 + nbx];
     const int a = D.cc_ra[row0 + r], b = D.cc_rb[row0 + r];
     const int jp = D.jj[p], jh = D.jj[h], ja = D.jj[a], jb = D.jj[b];
-    float val = 0.0f;
+    float valL = 0.0f, valR = 0.0f;
     if (((D.ll[a] + D.ll[h]) & 1) == ((D.ll[b] + D.ll[p]) & 1) && D.tz[a] + D.tz[h] == D.tz[b] + D.tz[p]) {
       const int Jmin = max(abs(jp - jb), abs(ja - jh)), Jmax = min(jp + jb, ja + jh);
       // 6j {jp jh JC; ja jb JT} as srow[JT / 2] (zero unless both JC triads hold)
@@ -70,8 +69,10 @@ __global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChun
       const int lo = min(C1, C2), hi = max(C1, C2);
       const int g = (lo == 0) ? hi : (lo == 1 ? (hi == 1 ? 3 : 5) : 4);
       const bool tr = C1 > C2;
+      // the transposed block is herm times the stored one
+      const float mL = (tr && hL < 0) ? -m : m, mR = (tr && hR < 0) ? -m : m;
       const int qb = (D.tz[h] + D.tz[a] + 2) + ((D.ll[h] + D.ll[a]) & 1);  // channel of JT: 3 JT + qb
-      float sm = 0.0f;
+      float smL = 0.0f, smR = 0.0f;
       for (int JT = Jmin; JT <= Jmax; JT += 2) {
         int neg = 0;
         if (s1) neg ^= (1 + ((jh + ja - JT) >> 1)) & 1;
@@ -80,39 +81,49 @@ __global__ void __launch_bounds__(256) k_pandya_tc(DevLayout D, const PandyaChun
         const int k = (3 * JT + qb) * 6 + g;
         const int n1 = __ldg(D.gn1 + k);
         const int64_t idx = __ldg(D.goff + k) + (tr ? i2 + (int64_t)i1 * n1 : i1 + (int64_t)i2 * n1);
-        const float pre = neg ? -m : m;
-        const float v = f64_to_f32(__ldg(op + idx)) * ((tr && herm < 0) ? -pre : pre);
+        const float vl = f64_to_f32(__ldg(opL + idx)), vr = f64_to_f32(__ldg(opR + idx));
         const float sj = ok6 ? __ldg(srow + (JT >> 1)) : 0.0f;
-        sm += ((JT & 2) ? -1.0f : 1.0f) * (float)(JT + 1) * sj * v;
+        const float cf = (((JT & 2) ^ (neg << 1)) ? -1.0f : 1.0f) * (float)(JT + 1) * sj;
+        smL += cf * (vl * mL);
+        smR += cf * (vr * mR);
       }
-      val = sm * (((jh + jb + JC) & 2) ? -1.0f : 1.0f) * sqrtf((float)(JC + 1));
+      const float f = (((jh + jb + JC) & 2) ? -1.0f : 1.0f) * sqrtf((float)(JC + 1));
+      valL = smL * f;
+      valR = smR * f;
     }
     const int rs = swap_row[row0 + r];
-    const int64_t da = split_offset<T>(ta, nk, r, ka + nbx), db = split_offset<T>(tbb, nk, r, kb + nbx);
-    const int64_t dsa = split_offset<T>(ta, nk, rs, ksa + nbx), dsb = split_offset<T>(tbb, nk, rs, ksb + nbx);
+    // L: A(r, nbx), B(r, seg + nbx), A(s(r), 2 seg + nbx), B(s(r), 3 seg + nbx); R: A(r, seg + nbx),
+    // B(r, nbx), A(s(r), 3 seg + nbx), B(s(r), 2 seg + nbx)
+    const int64_t a0 = split_offset<T>(ta, nk, r, nbx), a1 = split_offset<T>(ta, nk, r, seg + nbx);
+    const int64_t b0 = split_offset<T>(tbb, nk, r, nbx), b1 = split_offset<T>(tbb, nk, r, seg + nbx);
+    const int64_t sa2 = split_offset<T>(ta, nk, rs, 2 * seg + nbx), sa3 = split_offset<T>(ta, nk, rs, 3 * seg + nbx);
+    const int64_t sb2 = split_offset<T>(tbb, nk, rs, 2 * seg + nbx), sb3 = split_offset<T>(tbb, nk, rs, 3 * seg + nbx);
     const bool flip = ((ja + jb) & 2) != 0;  // phi(r) = -1
-    float rem = val;
+    float remL = valL, remR = valR;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      const T hv = SplitElem<T>::take(rem);
-      const T sv = flip ? SplitElem<T>::neg(hv) : hv;
-      T* b = buf + s * slice_elems;
-      b[da] = sv;
-      b[db] = sv;
-      b[dsa] = hv;
-      b[dsb] = hv;
+      const T hl = SplitElem<T>::take(remL), hr = SplitElem<T>::take(remR);
+      const T sl = flip ? SplitElem<T>::neg(hl) : hl, sr = flip ? SplitElem<T>::neg(hr) : hr;
+      T* o = buf + s * slice_elems;
+      o[a0] = sl;
+      o[b1] = sl;
+      o[sa2] = hl;
+      o[sb3] = hl;
+      o[a1] = sr;
+      o[b0] = sr;
+      o[sa3] = hr;
+      o[sb2] = hr;
     }
   }
 }
 void launch_pandya_tc(int S, int kind, int nchunks, cudaStream_t stream, const DevLayout& D, const PandyaChunk* chunks,
                       const PandyaOps& ops, void* buf, int64_t slice_elems, const int* swap_row) {
-  const dim3 grid(nchunks, 2);
   if (kind == 1)
-    k_pandya_tc<2, float><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
+    k_pandya_tc<2, float><<<nchunks, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
   else if (S == 2)
-    k_pandya_tc<2, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
+    k_pandya_tc<2, __nv_bfloat16><<<nchunks, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
   else
-    k_pandya_tc<3, __nv_bfloat16><<<grid, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
+    k_pandya_tc<3, __nv_bfloat16><<<nchunks, 256, 0, stream>>>(D, chunks, ops, buf, slice_elems, swap_row);
 }
 
 // commutator_221 (src/commutators.f90:435-578) with FP32 arithmetic, ACCUMULATES into RES
