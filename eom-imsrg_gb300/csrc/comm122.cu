@@ -45,6 +45,13 @@ __device__ __forceinline__ float g122_ipre(unsigned w) {
   return (w >> 29) & 1u ? -v : v;
 }
 
+// the (L, R) pair of V_A of one element from its code word and stored values
+__device__ __forceinline__ float2 g122_va(unsigned w, double l, double r, int hL, int hR) {
+  const bool sw = (w & (1u << kG122IdxBits)) != 0;
+  const float pre = g122_pre(w);
+  return make_float2(f64_to_f32(l) * ((sw && hL < 0) ? -pre : pre), f64_to_f32(r) * ((sw && hR < 0) ? -pre : pre));
+}
+
 __device__ __forceinline__ void g122_sync(bool cta, unsigned mask) {
   if (cta) __syncthreads(); else __syncwarp(mask);
 }
@@ -59,13 +66,18 @@ __device__ __forceinline__ void g122_run(const DevLayout& D, const G122Task& t, 
   const int nb = n0 * n1, ntot = nb * n2 * n3;
   const unsigned* C = EC + t.eoff;
   constexpr unsigned kIdx = (1u << kG122IdxBits) - 1u, kSwap = 1u << kG122IdxBits;
-  for (int e = tid; e < ntot; e += nth) {  // gather V_A of L and R
+  // gather V_A of L and R, two elements per pass so that two chains of dependent loads are in flight
+  int e = tid;
+  for (; e + nth < ntot; e += 2 * nth) {
+    const unsigned w0 = __ldg(C + e), w1 = __ldg(C + e + nth);
+    const double l0 = __ldg(L + (w0 & kIdx)), r0 = __ldg(R + (w0 & kIdx));
+    const double l1 = __ldg(L + (w1 & kIdx)), r1 = __ldg(R + (w1 & kIdx));
+    X[e] = g122_va(w0, l0, r0, hL, hR);
+    X[e + nth] = g122_va(w1, l1, r1, hL, hR);
+  }
+  if (e < ntot) {
     const unsigned w = __ldg(C + e);
-    const unsigned idx = w & kIdx;
-    const bool sw = (w & kSwap) != 0;
-    const float pre = g122_pre(w);
-    const float vl = f64_to_f32(__ldg(L + idx)), vr = f64_to_f32(__ldg(R + idx));
-    X[e] = make_float2(vl * ((sw && hL < 0) ? -pre : pre), vr * ((sw && hR < 0) ? -pre : pre));
+    X[e] = g122_va(w, __ldg(L + (w & kIdx)), __ldg(R + (w & kIdx)), hL, hR);
   }
   g122_sync(cta, mask);
   const int s1 = n0, s2 = nb, s3 = nb * n2;
