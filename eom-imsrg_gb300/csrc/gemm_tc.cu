@@ -832,6 +832,18 @@ imsrg_status Ctx::tc_prepare(int mode) {
             tc->quads.push_back((uint64_t)i | ((uint64_t)j << 16) | ((uint64_t)k << 32) | ((uint64_t)ll2 << 48));
           }
         }
+    // within the quadruples of one orbit i, by (jj, jk, jl): neighbouring threads then share their J and J' ranges and
+    // 6j rows, so a warp's loops run with its lanes in step (the X rows read for one i are the same in any order)
+    auto shape = [&](uint64_t qd) {
+      return (l.jj[(qd >> 16) & 0xFFFF] * 64 + l.jj[(qd >> 32) & 0xFFFF]) * 64 + l.jj[(qd >> 48) & 0xFFFF];
+    };
+    for (size_t a = 0; a < tc->quads.size();) {
+      size_t b = a;
+      while (b < tc->quads.size() && (tc->quads[b] & 0xFFFF) == (tc->quads[a] & 0xFFFF)) ++b;
+      std::stable_sort(tc->quads.begin() + a, tc->quads.begin() + b,
+                       [&](uint64_t x, uint64_t y) { return shape(x) < shape(y); });
+      a = b;
+    }
   }
   // X stores only where the recoupling reads: the masks of the 32-row column segments
   {

@@ -13,8 +13,8 @@
 // with Sd = -(-1)^((jl+jk+J)/2) {ji jj J; jl jk J'}, Se = {ji jj J; jk jl J'} and
 // pre = 1/sqrt2 per pair of identical orbits.
 //
-// One thread per orbit quadruple (i <= j, k <= l), quadruples in list order (i, k, l, then j),
-// so the X rows a warp reads for one J' are pairs of consecutive j in one column.  A thread
+// One thread per orbit quadruple (i <= j, k <= l).  The quadruples of one orbit i are ordered by
+// (jj, jk, jl), so the threads of a warp mostly share their J and J' ranges and 6j rows.  A thread
 // first issues the X loads of both terms (all independent, so they are in flight together),
 // then forms every output J the pairs share with the 6j rows of the device table.  Each
 // output is the only add the recoupling makes to its element, so it goes out as an FP64
